@@ -1,0 +1,532 @@
+// C ABI of the library (include/cunusht_gb300.h): plans and entry points.
+#include <stdarg.h>
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cunusht {
+
+static thread_local std::string g_err;
+
+void set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+void clear_error() { g_err.clear(); }
+
+static int next_pow2(long long n) {
+    int p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_n.
+static void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+    x.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(PI * (i + 0.75) / (n + 0.5));
+        double dp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int j = 2; j <= n; ++j) {
+                double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        double p0 = 1.0, p1 = z;
+        for (int j = 2; j <= n; ++j) {
+            double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+            p0 = p1;
+            p1 = p2;
+        }
+        dp = n * (z * p1 - p0) / (z * z - 1.0);
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+// ES kernel parameters for oversampling 2 (the FINUFFT rule used by cuFINUFFT
+// for upsampfac 2: width = ceil(log10(10/eps)), beta = 2.30 width).
+static void es_params(double eps, int &w, double &beta) {
+    w = (int)std::ceil(-std::log10(eps / 10.0) - 1e-9);
+    w = std::max(2, std::min(16, w));
+    double bon = 2.30;
+    if (w == 2) bon = 2.20;
+    else if (w == 3) bon = 2.26;
+    else if (w == 4) bon = 2.38;
+    beta = bon * w;
+}
+
+// Fourier transform of the kernel in fine-grid units:
+// Phi(xi) = int_{-w/2}^{w/2} psi(2 t / w) cos(xi t) dt.
+struct EsFT {
+    std::vector<double> z, wz;
+    int w;
+    double beta;
+    EsFT(int w_, double beta_) : w(w_), beta(beta_) { gauss_legendre(400, z, wz); }
+    double operator()(double xi) const {
+        double s = 0.0;
+        for (size_t i = 0; i < z.size(); ++i) {
+            const double q = 1.0 - z[i] * z[i];
+            const double psi = std::exp(beta * (std::sqrt(q) - 1.0));
+            s += wz[i] * psi * std::cos(xi * 0.5 * w * z[i]);
+        }
+        return 0.5 * w * s;
+    }
+};
+
+template <typename T> static int dalloc(cunusht_plan_s *P, T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) return CUNUSHT_OK;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+        *p = nullptr;
+        return CUNUSHT_ERR_ALLOC;
+    }
+    P->ws_bytes += n * sizeof(T);
+    return CUNUSHT_OK;
+}
+
+template <typename T> static int upload(cunusht_plan_s *P, T **p, const std::vector<T> &h) {
+    RC_TRY(dalloc(P, p, h.size()));
+    if (!h.empty()) CU_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return CUNUSHT_OK;
+}
+
+static void free_plan(cunusht_plan_s *P) {
+    if (!P) return;
+    void *ptrs[] = {P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->d_gl_x, P->d_gl_sh,
+                    P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
+                    P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
+                    P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_tw64, P->d_tw32, P->d_chirp, P->d_bker,
+                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete P;
+}
+
+static double lg0_of(int m, int s) {
+    const int l0 = std::max(m, s);
+    const double v = std::log((2.0 * l0 + 1.0) / (4.0 * PI)) + std::lgamma(2.0 * l0 + 1.0) -
+                     std::lgamma(m + s + 1.0) - std::lgamma(std::fabs((double)(m - s)) + 1.0);
+    return 0.5 * v / std::log(2.0);
+}
+
+static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, int max_spin, int nring,
+                      const double *rth, const double *rph0, const int64_t *rnph, const int64_t *rofs) {
+    ARG_CHECK(lmax >= 1 && lmax <= 16383, "lmax must be in [1, 16383], got %d", lmax);
+    ARG_CHECK(eps >= 1e-14 && eps < 1.0, "epsilon must be in [1e-14, 1), got %g", eps);
+    ARG_CHECK(max_spin >= 0 && max_spin <= 2, "max_spin must be 0, 1 or 2, got %d", max_spin);
+    ARG_CHECK(nring >= 1 && rth && rph0 && rnph && rofs, "pointing geometry arrays missing (nring=%d)", nring);
+    ARG_CHECK(precision >= 0 && precision <= 2, "precision must be 0 (auto), 1 (fp64) or 2 (mixed)");
+    P->lmax = lmax;
+    P->eps = eps;
+    P->max_spin = max_spin;
+    P->nalm = (long long)(lmax + 1) * (lmax + 2) / 2;
+    P->prec = precision == CUNUSHT_PREC_AUTO ? (eps > 1e-6 ? CUNUSHT_PREC_MIXED : CUNUSHT_PREC_FP64) : precision;
+    P->grid_fp32 = (P->prec != CUNUSHT_PREC_FP64) && eps > 1e-6;
+
+    // ---- pointing geometry, sorted by first pixel (Geom, geometry.py:47-52)
+    std::vector<int> order(nring);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return rofs[a] < rofs[b]; });
+    P->nring = nring;
+    P->h_theta.resize(nring);
+    P->h_phi0.resize(nring);
+    P->h_nph.resize(nring);
+    P->h_ofs.resize(nring);
+    long long npix = 0;
+    for (int i = 0; i < nring; ++i) {
+        const int o = order[i];
+        ARG_CHECK(rnph[o] >= 1, "ring %d has %lld pixels", o, (long long)rnph[o]);
+        ARG_CHECK(rth[o] >= 0.0 && rth[o] <= PI, "ring %d colatitude %g outside [0, pi]", o, rth[o]);
+        P->h_theta[i] = rth[o];
+        P->h_phi0[i] = rph0[o];
+        P->h_nph[i] = rnph[o];
+        P->h_ofs[i] = rofs[o];
+        npix += rnph[o];
+    }
+    for (int i = 0; i + 1 < nring; ++i)
+        ARG_CHECK(P->h_ofs[i] + P->h_nph[i] <= P->h_ofs[i + 1], "rings overlap (ring starts/counts inconsistent)");
+    P->npix = npix;
+    const long long npix_span = P->h_ofs[nring - 1] + P->h_nph[nring - 1];
+    ARG_CHECK(npix_span == npix && P->h_ofs[0] == 0, "ring pixels must tile [0, npix) contiguously");
+    P->nph_uniform = (int)P->h_nph[0];
+    for (int i = 1; i < nring; ++i)
+        if (P->h_nph[i] != P->h_nph[0]) P->nph_uniform = 0;
+    if (P->nph_uniform == 0) {
+        set_error("rings with different pixel counts are not supported yet");
+        return CUNUSHT_ERR_UNSUPPORTED;
+    }
+    ARG_CHECK(P->nph_uniform >= 2 * lmax + 1, "pixels per ring (%d) must be >= 2 lmax + 1 (%d)",
+              P->nph_uniform, 2 * lmax + 1);
+
+    // ring pairs (theta, pi - theta)
+    {
+        std::vector<int> idx(nring);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::sort(idx.begin(), idx.end(), [&](int a, int b) { return P->h_theta[a] < P->h_theta[b]; });
+        std::vector<double> x, sh, ch;
+        std::vector<int> rn, rs;
+        for (int i = 0, j = nring - 1; i <= j; ++i, --j) {
+            const double tn = P->h_theta[idx[i]], ts = P->h_theta[idx[j]];
+            if (std::fabs(tn + ts - PI) > 1e-9) {
+                set_error("pointing geometry is not north/south symmetric (ring %g vs %g)", tn, ts);
+                return CUNUSHT_ERR_UNSUPPORTED;
+            }
+            x.push_back(std::cos(tn));
+            sh.push_back(std::sin(0.5 * tn));
+            ch.push_back(std::cos(0.5 * tn));
+            rn.push_back(idx[i]);
+            rs.push_back(idx[j]);
+        }
+        P->gl_npairs = (int)x.size();
+        RC_TRY(upload(P, &P->d_gl_x, x));
+        RC_TRY(upload(P, &P->d_gl_sh, sh));
+        RC_TRY(upload(P, &P->d_gl_ch, ch));
+        RC_TRY(upload(P, &P->d_gl_rn, rn));
+        RC_TRY(upload(P, &P->d_gl_rs, rs));
+    }
+    RC_TRY(upload(P, &P->d_ring_theta, P->h_theta));
+    RC_TRY(upload(P, &P->d_ring_phi0, P->h_phi0));
+    RC_TRY(upload(P, &P->d_ring_nph, P->h_nph));
+    RC_TRY(upload(P, &P->d_ring_ofs, P->h_ofs));
+
+    // ---- torus and fine grid
+    P->Nt = std::max(32, next_pow2(2LL * lmax + 2));
+    P->Np = std::max(32, next_pow2(2LL * lmax + 2));
+    P->ncc = P->Nt / 2 + 1;
+    P->Ntf = 2 * P->Nt;
+    P->Npf = 2 * P->Np;
+    es_params(eps, P->w, P->beta);
+    const int hw = (P->w + 1) / 2;
+    P->n_lo = -hw - 1;
+    const int n_hi = P->Ntf / 2 + hw + 1;
+    P->nrows = n_hi - P->n_lo + 1;
+    {
+        const size_t need = fft_smem_bytes(std::max(P->Ntf, P->Npf), P->grid_fp32);
+        if (need > 227 * 1024) {
+            set_error("lmax %d needs a %zu-byte shared-memory FFT in %s; use epsilon > 1e-6 (FP32 grid)", lmax,
+                      need, P->grid_fp32 ? "FP32" : "FP64");
+            return CUNUSHT_ERR_UNSUPPORTED;
+        }
+    }
+    // CC ring pairs: ring k at theta = 2 pi k / Nt, k = 0 .. Nt/2; pair (k, Nt/2 - k)
+    {
+        std::vector<double> x, sh, ch;
+        std::vector<int> rn, rs;
+        for (int k = 0; k <= P->Nt / 4; ++k) {
+            const double t = TWOPI * k / P->Nt;
+            x.push_back(std::cos(t));
+            sh.push_back(std::sin(0.5 * t));
+            ch.push_back(std::cos(0.5 * t));
+            rn.push_back(k);
+            rs.push_back(P->Nt / 2 - k);
+        }
+        P->cc_npairs = (int)x.size();
+        RC_TRY(upload(P, &P->d_cc_x, x));
+        RC_TRY(upload(P, &P->d_cc_sh, sh));
+        RC_TRY(upload(P, &P->d_cc_ch, ch));
+        RC_TRY(upload(P, &P->d_cc_rn, rn));
+        RC_TRY(upload(P, &P->d_cc_rs, rs));
+    }
+    // deconvolution
+    {
+        EsFT ft(P->w, P->beta);
+        std::vector<double> dth(P->Nt, 0.0), dph(2 * lmax + 1, 0.0);
+        for (int k = -P->Nt / 2 + 1; k < P->Nt / 2; ++k)
+            dth[(k + P->Nt) % P->Nt] = 1.0 / (P->Nt * ft(TWOPI * k / P->Ntf));
+        for (int m = -lmax; m <= lmax; ++m) dph[m + lmax] = 1.0 / ft(TWOPI * m / P->Npf);
+        RC_TRY(upload(P, &P->d_Dth, dth));
+        RC_TRY(upload(P, &P->d_Dph, dph));
+    }
+    // recursion tables
+    for (int s = 0; s <= 2; ++s) {
+        RC_TRY(dalloc(P, &P->d_coef[s], 3 * (size_t)P->nalm));
+        std::vector<double> lg(lmax + 1);
+        for (int m = 0; m <= lmax; ++m) lg[m] = lg0_of(m, s);
+        RC_TRY(upload(P, &P->d_lg0[s], lg));
+    }
+    RC_TRY(build_coef_tables(P, 0));
+    {
+        std::vector<double> lf(lmax + 1);
+        for (int l = 0; l <= lmax; ++l) lf[l] = std::sqrt((double)l * (l + 1.0));
+        RC_TRY(upload(P, &P->d_lfac, lf));
+    }
+    // Bluestein data for ring transforms
+    {
+        const int N = P->nph_uniform;
+        P->Mb = next_pow2(2LL * N - 1);
+        if (fft_smem_bytes(P->Mb, false) > 227 * 1024) {
+            set_error("ring length %d needs a Bluestein FFT of %d points, above the FP64 shared-memory limit", N,
+                      P->Mb);
+            return CUNUSHT_ERR_UNSUPPORTED;
+        }
+        std::vector<double2> chirp(N), bk(P->Mb, make_double2(0.0, 0.0));
+        for (int q = 0; q < N; ++q) {
+            const long long qq = ((long long)q * q) % (2LL * N);
+            const double a = PI * (double)qq / N;
+            chirp[q] = make_double2(std::cos(a), std::sin(a));
+        }
+        const double inv = 1.0 / P->Mb;
+        for (int k = 0; k < N; ++k) {
+            const double2 b = make_double2(chirp[k].x * inv, -chirp[k].y * inv);
+            bk[k] = b;
+            if (k > 0) bk[P->Mb - k] = b;
+        }
+        RC_TRY(upload(P, &P->d_chirp, chirp));
+        RC_TRY(upload(P, &P->d_bker, bk));
+    }
+    // twiddles
+    {
+        P->TW = std::max(std::max(P->Ntf, P->Npf), P->Mb);
+        std::vector<double2> tw(P->TW);
+        std::vector<float2> tw32(P->TW);
+        for (int t = 0; t < P->TW; ++t) {
+            const long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)t / (long double)P->TW;
+            tw[t] = make_double2((double)std::cos(a), (double)std::sin(a));
+            tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
+        }
+        RC_TRY(upload(P, &P->d_tw64, tw));
+        RC_TRY(upload(P, &P->d_tw32, tw32));
+    }
+    RC_TRY(fft_global_f64(P->d_bker, P->Mb, -1, P->d_tw64, P->TW, 0));
+    // workspace
+    {
+        const long long ncols = max_spin ? 2LL * lmax + 1 : lmax + 1;
+        const size_t gsz = P->grid_fp32 ? sizeof(float2) : sizeof(double2);
+        const size_t usz = (P->grid_fp32 ? sizeof(float) : sizeof(double)) * (max_spin ? 2 : 1);
+        RC_TRY(dalloc(P, &P->d_H, (size_t)ncols * P->ncc));
+        char *f = nullptr, *u = nullptr;
+        RC_TRY(dalloc(P, &f, gsz * (size_t)ncols * P->nrows));
+        P->d_F = f;
+        RC_TRY(dalloc(P, &u, usz * (size_t)P->nrows * P->Npf));
+        P->d_U = u;
+        RC_TRY(dalloc(P, &P->d_Hgl, (size_t)(2 * lmax + 1) * nring));
+        RC_TRY(dalloc(P, &P->d_glmap, 2 * (size_t)npix));
+        RC_TRY(dalloc(P, &P->d_alm, 2 * (size_t)P->nalm));
+    }
+    CU_TRY(cudaStreamSynchronize(0));
+    CU_TRY(cudaGetLastError());
+    return CUNUSHT_OK;
+}
+
+static int check_plan(const cunusht_plan_s *P) {
+    ARG_CHECK(P != nullptr, "plan is NULL");
+    return CUNUSHT_OK;
+}
+
+static int check_spin(const cunusht_plan_s *P, int spin, int ncomp) {
+    ARG_CHECK(spin >= 0 && spin <= P->max_spin, "spin %d outside [0, max_spin=%d] of the plan", spin,
+              P->max_spin);
+    if (spin == 0) ARG_CHECK(ncomp == 1, "spin 0 takes ncomp = 1, got %d", ncomp);
+    else ARG_CHECK(ncomp == 1 || ncomp == 2, "spin %d takes ncomp 1 (gradient only) or 2, got %d", spin, ncomp);
+    return CUNUSHT_OK;
+}
+
+}  // namespace cunusht
+
+using namespace cunusht;
+
+extern "C" {
+
+const char *cunusht_last_error(void) { return g_err.c_str(); }
+
+int cunusht_version(void) { return 100; }
+
+int cunusht_plan_create(cunusht_plan_t **plan, int lmax, double epsilon, int precision, int max_spin, int nring,
+                        const double *ring_theta, const double *ring_phi0, const int64_t *ring_nph,
+                        const int64_t *ring_ofs) {
+    clear_error();
+    if (!plan) {
+        set_error("plan output pointer is NULL");
+        return CUNUSHT_ERR_ARG;
+    }
+    *plan = nullptr;
+    cunusht_plan_s *P = new cunusht_plan_s();
+    int rc = build_plan(P, lmax, epsilon, precision, max_spin, nring, ring_theta, ring_phi0, ring_nph, ring_ofs);
+    if (rc != CUNUSHT_OK) {
+        std::string keep = g_err;
+        free_plan(P);
+        g_err = keep;
+        return rc;
+    }
+    *plan = P;
+    return CUNUSHT_OK;
+}
+
+int cunusht_plan_destroy(cunusht_plan_t *plan) {
+    clear_error();
+    free_plan(plan);
+    return CUNUSHT_OK;
+}
+
+int cunusht_plan_info(const cunusht_plan_t *P, int64_t *info, int ninfo) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(info != nullptr, "info array is NULL");
+    const int64_t v[10] = {P->npix, P->Nt, P->Np, P->Ntf, P->Npf, P->w, P->nrows, (int64_t)P->ws_bytes,
+                           P->prec, P->nalm};
+    int n = std::min(ninfo, 10);
+    for (int i = 0; i < n; ++i) info[i] = v[i];
+    return n;
+}
+
+int cunusht_nusht2d2(cunusht_plan_t *P, int spin, int ncomp, const void *alm, int alm_dtype, const double *loc,
+                     int64_t npts, int loc_layout, const double *gamma, void *out, int out_dtype, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    RC_TRY(check_spin(P, spin, ncomp));
+    ARG_CHECK(alm && out && (loc || npts == 0), "NULL array argument");
+    ARG_CHECK(npts >= 0, "npts must be >= 0");
+    ARG_CHECK(loc_layout == 0 || loc_layout == 1, "loc_layout must be 0 or 1");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    ARG_CHECK(out_dtype == CUNUSHT_F64 || out_dtype == CUNUSHT_F32, "bad out dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2 *G, *C = nullptr;
+    if (alm_dtype == CUNUSHT_F64) {
+        G = (const double2 *)alm;
+        if (ncomp > 1) C = G + P->nalm;
+    } else {
+        RC_TRY(convert_alm(alm, alm_dtype, ncomp * P->nalm, P->d_alm, st));
+        G = P->d_alm;
+        if (ncomp > 1) C = P->d_alm + P->nalm;
+    }
+    RC_TRY(leg_synth(P, spin, G, C, false, true, P->d_H, st));
+    RC_TRY(theta_fwd(P, spin, P->d_H, P->d_F, st));
+    RC_TRY(phi_fwd(P, spin, P->d_F, P->d_U, st));
+    RC_TRY(nufft_interp(P, spin, loc, npts, loc_layout, spin ? gamma : nullptr, out, out_dtype, st));
+    return CUNUSHT_OK;
+}
+
+int cunusht_nusht2d1(cunusht_plan_t *P, int spin, int ncomp, const void *map, int map_dtype, const double *loc,
+                     int64_t npts, int loc_layout, const double *gamma, void *alm_out, int alm_dtype,
+                     void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    RC_TRY(check_spin(P, spin, ncomp));
+    ARG_CHECK(alm_out && (map || npts == 0) && (loc || npts == 0), "NULL array argument");
+    ARG_CHECK(npts >= 0, "npts must be >= 0");
+    ARG_CHECK(loc_layout == 0 || loc_layout == 1, "loc_layout must be 0 or 1");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    ARG_CHECK(map_dtype == CUNUSHT_F64 || map_dtype == CUNUSHT_F32, "bad map dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    RC_TRY(nufft_spread(P, spin, loc, npts, loc_layout, spin ? gamma : nullptr, map, map_dtype, st));
+    RC_TRY(phi_adj(P, spin, P->d_U, P->d_F, st));
+    RC_TRY(theta_adj(P, spin, P->d_F, P->d_H, st));
+    double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
+    double2 *C = G + P->nalm;
+    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_H, false, true, G, C, st));
+    if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
+    return CUNUSHT_OK;
+}
+
+int cunusht_dlm2pointing(cunusht_plan_t *P, const void *dlm, const void *dclm, int alm_dtype, double *ptg,
+                         double *gamma, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(dlm && ptg, "NULL array argument");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2 *G = (const double2 *)dlm, *C = (const double2 *)dclm;
+    if (alm_dtype != CUNUSHT_F64) {
+        RC_TRY(convert_alm(dlm, alm_dtype, P->nalm, P->d_alm, st));
+        G = P->d_alm;
+        if (dclm) {
+            RC_TRY(convert_alm(dclm, alm_dtype, P->nalm, P->d_alm + P->nalm, st));
+            C = P->d_alm + P->nalm;
+        }
+    }
+    RC_TRY(leg_synth(P, 1, G, C, true, false, P->d_Hgl, st));
+    RC_TRY(ring_synth(P, 1, P->d_Hgl, P->d_glmap, P->d_glmap + P->npix, st));
+    RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->npix,
+                           P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
+    return CUNUSHT_OK;
+}
+
+int cunusht_synthesis(cunusht_plan_t *P, int spin, int ncomp, const void *alm, int alm_dtype, double *map,
+                      void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(spin >= 0 && spin <= 2, "spin must be 0, 1 or 2");
+    if (spin == 0) ARG_CHECK(ncomp == 1, "spin 0 takes ncomp = 1");
+    else ARG_CHECK(ncomp == 1 || ncomp == 2, "spin > 0 takes ncomp 1 or 2");
+    ARG_CHECK(alm && map, "NULL array argument");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2 *G = (const double2 *)alm, *C = nullptr;
+    if (alm_dtype != CUNUSHT_F64) {
+        RC_TRY(convert_alm(alm, alm_dtype, ncomp * P->nalm, P->d_alm, st));
+        G = P->d_alm;
+    }
+    if (ncomp > 1) C = G + P->nalm;
+    RC_TRY(leg_synth(P, spin, G, C, false, false, P->d_Hgl, st));
+    RC_TRY(ring_synth(P, spin, P->d_Hgl, map, spin ? map + P->npix : nullptr, st));
+    return CUNUSHT_OK;
+}
+
+int cunusht_adjoint_synthesis(cunusht_plan_t *P, int spin, int ncomp, const double *map, void *alm_out,
+                              int alm_dtype, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(spin >= 0 && spin <= 2, "spin must be 0, 1 or 2");
+    if (spin == 0) ARG_CHECK(ncomp == 1, "spin 0 takes ncomp = 1");
+    else ARG_CHECK(ncomp == 1 || ncomp == 2, "spin > 0 takes ncomp 1 or 2");
+    ARG_CHECK(alm_out && map, "NULL array argument");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    RC_TRY(ring_adjoint(P, spin, map, spin ? map + P->npix : nullptr, P->d_Hgl, st));
+    double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
+    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st));
+    if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
+    return CUNUSHT_OK;
+}
+
+int cunusht_pointing(int nring, const double *ring_theta, const double *ring_phi0, const int64_t *ring_nph,
+                     const int64_t *ring_ofs, int64_t npix, const double *s1t, const double *s1p, double *ot,
+                     double *op, double *og, void *stream) {
+    clear_error();
+    ARG_CHECK(nring >= 1 && ring_theta && ring_phi0 && ring_nph && ring_ofs, "ring tables missing");
+    ARG_CHECK(s1t && s1p && ot && op, "NULL array argument");
+    ARG_CHECK(npix >= 0, "npix must be >= 0");
+    return pointing_launch(nring, ring_theta, ring_phi0, (const long long *)ring_nph, (const long long *)ring_ofs,
+                           npix, s1t, s1p, ot, op, og, (cudaStream_t)stream);
+}
+
+int cunusht_doubling(const void *cc_map, int64_t ntheta, int64_t nphi, int layout, int spin, int dtype, void *out,
+                     void *stream) {
+    clear_error();
+    ARG_CHECK(cc_map && out, "NULL array argument");
+    ARG_CHECK(ntheta >= 2 && nphi >= 2 && nphi % 2 == 0, "need ntheta >= 2 and even nphi >= 2");
+    ARG_CHECK(layout == 0 || layout == 1, "layout must be 0 (ring-major) or 1 (theta-contiguous)");
+    ARG_CHECK(dtype == CUNUSHT_F64 || dtype == CUNUSHT_F32, "bad dtype");
+    return doubling_launch(cc_map, ntheta, nphi, layout, spin, dtype, out, (cudaStream_t)stream);
+}
+
+int cunusht_adjoint_doubling(const void *dmap, int64_t ntheta, int64_t nphi, int spin, int dtype, void *out,
+                             void *stream) {
+    clear_error();
+    ARG_CHECK(dmap && out, "NULL array argument");
+    ARG_CHECK(ntheta >= 2 && nphi >= 2 && nphi % 2 == 0, "need ntheta >= 2 and even nphi >= 2");
+    ARG_CHECK(dtype == CUNUSHT_F64 || dtype == CUNUSHT_F32, "bad dtype");
+    return adjoint_doubling_launch(dmap, ntheta, nphi, spin, dtype, out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

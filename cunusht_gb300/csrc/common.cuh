@@ -1,0 +1,174 @@
+// Shared definitions of the cunusht_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <vector>
+#include <string>
+
+#include "../../include/cunusht_gb300.h"
+
+namespace cunusht {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+void clear_error();
+
+#define CU_TRY(expr)                                                                     \
+    do {                                                                                 \
+        cudaError_t _e = (expr);                                                         \
+        if (_e != cudaSuccess) {                                                         \
+            ::cunusht::set_error("%s:%d: %s -> %s", __FILE__, __LINE__, #expr,           \
+                                 cudaGetErrorString(_e));                                \
+            return CUNUSHT_ERR_CUDA;                                                     \
+        }                                                                                \
+    } while (0)
+
+#define CU_LAUNCH_CHECK()                                                                \
+    do {                                                                                 \
+        cudaError_t _e = cudaGetLastError();                                             \
+        if (_e != cudaSuccess) {                                                         \
+            ::cunusht::set_error("%s:%d: kernel launch -> %s", __FILE__, __LINE__,       \
+                                 cudaGetErrorString(_e));                                \
+            return CUNUSHT_ERR_CUDA;                                                     \
+        }                                                                                \
+    } while (0)
+
+#define ARG_CHECK(cond, ...)                                                             \
+    do {                                                                                 \
+        if (!(cond)) {                                                                   \
+            ::cunusht::set_error(__VA_ARGS__);                                           \
+            return CUNUSHT_ERR_ARG;                                                      \
+        }                                                                                \
+    } while (0)
+
+#define RC_TRY(expr)                                                                     \
+    do {                                                                                 \
+        int _rc = (expr);                                                                \
+        if (_rc != CUNUSHT_OK) return _rc;                                               \
+    } while (0)
+
+// ---------------------------------------------------------------- complex
+template <typename T> struct cplx_t;
+template <> struct cplx_t<float> { using type = float2; };
+template <> struct cplx_t<double> { using type = double2; };
+template <typename T> using cplx = typename cplx_t<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T re, T im) {
+    cplx<T> r;
+    r.x = re;
+    r.y = im;
+    return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) {
+    C r;
+    r.x = a.x + b.x;
+    r.y = a.y + b.y;
+    return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) {
+    C r;
+    r.x = a.x - b.x;
+    r.y = a.y - b.y;
+    return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename C> __host__ __device__ __forceinline__ C cconj(C a) {
+    C r;
+    r.x = a.x;
+    r.y = -a.y;
+    return r;
+}
+template <typename C, typename S> __host__ __device__ __forceinline__ C cscale(C a, S s) {
+    C r;
+    r.x = a.x * s;
+    r.y = a.y * s;
+    return r;
+}
+// multiply by i*dir (dir = +1 or -1)
+template <typename C> __host__ __device__ __forceinline__ C cmul_idir(C a, int dir) {
+    C r;
+    r.x = -dir * a.y;
+    r.y = dir * a.x;
+    return r;
+}
+template <typename To, typename From> __device__ __forceinline__ cplx<To> ccast(From a) {
+    cplx<To> r;
+    r.x = (To)a.x;
+    r.y = (To)a.y;
+    return r;
+}
+
+__host__ __device__ __forceinline__ long long almidx(int lmax, int l, int m) {
+    return (long long)m * (2 * lmax + 1 - m) / 2 + l;
+}
+
+constexpr double PI = 3.141592653589793238462643383279502884;
+constexpr double TWOPI = 6.283185307179586476925286766559005768;
+
+}  // namespace cunusht
+
+// ---------------------------------------------------------------- plan
+struct cunusht_plan_s {
+    int lmax = 0;
+    int max_spin = 0;
+    int prec = CUNUSHT_PREC_FP64;  // resolved precision
+    bool grid_fp32 = false;        // FFT + nuFFT grids in FP32
+    double eps = 1e-7;
+    long long nalm = 0;
+
+    // pointing (output) geometry
+    int nring = 0;
+    long long npix = 0;
+    int nph_uniform = 0;  // all rings have this many pixels (0 if not uniform)
+    std::vector<double> h_theta, h_phi0;
+    std::vector<long long> h_nph, h_ofs;
+    double *d_ring_theta = nullptr, *d_ring_phi0 = nullptr;
+    long long *d_ring_nph = nullptr, *d_ring_ofs = nullptr;
+    // ring pairs (theta, pi - theta) of the pointing geometry
+    int gl_npairs = 0;
+    double *d_gl_x = nullptr, *d_gl_sh = nullptr, *d_gl_ch = nullptr;
+    int *d_gl_rn = nullptr, *d_gl_rs = nullptr;
+
+    // doubled Clenshaw-Curtis torus and fine (oversampled) nuFFT grid
+    int Nt = 0, Np = 0, ncc = 0;   // torus theta / phi lengths, CC rings = Nt/2+1
+    int Ntf = 0, Npf = 0;          // fine grid lengths
+    int w = 0;                     // ES kernel width
+    double beta = 0.0;
+    int n_lo = 0, nrows = 0;       // fine rows stored: n in [n_lo, n_lo + nrows)
+    int cc_npairs = 0;
+    double *d_cc_x = nullptr, *d_cc_sh = nullptr, *d_cc_ch = nullptr;
+    int *d_cc_rn = nullptr, *d_cc_rs = nullptr;
+    double *d_Dth = nullptr;  // [Nt] deconvolution * 1/Nt, index kappa mod Nt
+    double *d_Dph = nullptr;  // [2L+1] deconvolution, index m+L
+
+    // Legendre recursion tables, per spin s = 0,1,2: alpha, gamma, beta (alm layout)
+    double *d_coef[3] = {nullptr, nullptr, nullptr};
+    double *d_lg0[3] = {nullptr, nullptr, nullptr};  // per m: log2 start normalisation
+    double *d_lfac = nullptr;                        // sqrt(l(l+1)), l = 0..L
+
+    // FFT twiddles e^{-2 pi i t / TW}
+    int TW = 0;
+    double2 *d_tw64 = nullptr;
+    float2 *d_tw32 = nullptr;
+
+    // Bluestein data for the ring (phi) transform of the pointing geometry
+    int Mb = 0;
+    double2 *d_chirp = nullptr;  // [nph] e^{i pi q^2 / nph}
+    double2 *d_bker = nullptr;   // [Mb] FFT_Mb(conj chirp, circular) / Mb
+
+    // workspace
+    double2 *d_H = nullptr;    // Legendre columns on the CC rings  [ncols][ncc]
+    void *d_F = nullptr;       // theta-pass output                 [nrows][ncols]
+    void *d_U = nullptr;       // fine grid                          [nrows][Npf](x2)
+    double2 *d_Hgl = nullptr;  // Legendre columns on pointing rings [ncols][nring]
+    double2 *d_ring = nullptr; // Bluestein buffers (unused: in smem)
+    double *d_glmap = nullptr; // spin-1 maps on pointing grid       [2][npix]
+    double2 *d_alm = nullptr;  // alm staging (dtype conversion)     [2][nalm]
+    size_t ws_bytes = 0;
+};

@@ -1,0 +1,46 @@
+// Host-side launchers shared between the translation units of the library.
+#pragma once
+#include "common.cuh"
+
+namespace cunusht {
+
+constexpr int FFT_TPB = 512;
+
+// legendre.cu
+int build_coef_tables(cunusht_plan_s *P, cudaStream_t st);
+int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C,
+              bool use_lfac, bool cc, double2 *H, cudaStream_t st);
+int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
+                bool cc, double2 *G, double2 *C, cudaStream_t st);
+
+// fft.cu
+int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cudaStream_t st);
+int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cudaStream_t st);
+int phi_fwd(const cunusht_plan_s *P, int spin, const void *F, void *U, cudaStream_t st);
+int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStream_t st);
+int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *out0, double *out1,
+               cudaStream_t st);
+int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
+                 double2 *Hgl, cudaStream_t st);
+int fft_global_f64(double2 *data, int N, int dir, const double2 *tw, int TW, cudaStream_t st);
+size_t fft_smem_bytes(int N, bool f32);
+
+// nufft.cu
+int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long npts,
+                 int layout, const double *gamma, void *out, int out_dtype, cudaStream_t st);
+int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts,
+                 int layout, const double *gamma, const void *in, int in_dtype,
+                 cudaStream_t st);
+
+// pointing.cu
+int pointing_launch(int nring, const double *rth, const double *rph0, const long long *rnph,
+                    const long long *rofs, long long npix, const double *dth, const double *dph,
+                    double *out_th, double *out_ph, double *out_gamma, cudaStream_t st);
+int doubling_launch(const void *in, long long ntheta, long long nphi, int layout, int spin,
+                    int dtype, void *out, cudaStream_t st);
+int adjoint_doubling_launch(const void *in, long long ntheta, long long nphi, int spin, int dtype,
+                            void *out, cudaStream_t st);
+int convert_alm(const void *in, int dtype, long long n, double2 *out, cudaStream_t st);
+int store_alm(const double2 *in, long long n, int dtype, void *out, cudaStream_t st);
+
+}  // namespace cunusht

@@ -1,0 +1,506 @@
+// Legendre stage of the spin-s spherical harmonic transform on iso-latitude
+// ring sets, FP64 (plain path).
+//
+// Replaces the SHTns calls of the reference: ``synth`` on the Clenshaw-Curtis
+// grid (cunusht/sht/GPU_sht_transformer.py:56-62), ``analys(map*iw)`` as the
+// adjoint (:65-73) and ``synth_grad`` on the Gauss-Legendre grid (:88-97).
+//
+// Per order m and ring theta the kernels evaluate
+//     h_m(theta)  = sum_l a_lm  sLambda_lm(theta)             (synthesis)
+//     a'_lm       = sum_rings   sLambda_lm(theta_r) h'_m(r)    (adjoint)
+// with the normalised Wigner-d three-term recursion in l
+//     sLambda_{l+1} = (alpha_l x + gamma_l) sLambda_l - beta_l sLambda_{l-1},
+// started at l0 = max(m, s) from the closed form
+//     sLambda_{l0,m} = (-1)^m 2^{lg0[m]} sin^{m+s}(theta/2) cos^{|m-s|}(theta/2),
+// which is regular at both poles.  The start is kept as mantissa x 2^e with
+// e a non-positive multiple of 512 so that sin^m never underflows; values are
+// accumulated only once e has climbed back to 0 (before that they are below
+// 2^-312 and cannot contribute).
+//
+// Rings come in pairs (theta, pi - theta): spin 0 uses the parity
+// Lambda_lm(pi - theta) = (-1)^{l+m} Lambda_lm(theta) (one recursion per pair);
+// spin s > 0 runs the recursion at both rings and gets the (-s) functions from
+// -sLambda_lm(theta) = (-1)^{l+m} sLambda_lm(pi - theta).
+//
+// Output layout: H[c][ring], c = m (spin 0) or c = m + lmax (spin s, m in
+// [-lmax, lmax]), rings contiguous (ldH = ring count).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cunusht {
+
+__device__ __forceinline__ void rec_start(double lg0, int m, int s, double sh, double ch,
+                                          double &cur, double &prev, int &e) {
+    prev = 0.0;
+    double lg = lg0;
+    bool zero = false;
+    if (m + s > 0) {
+        if (sh <= 0.0) zero = true;
+        else lg += (double)(m + s) * log2(sh);
+    }
+    if (m != s) {
+        if (ch <= 0.0) zero = true;
+        else lg += (double)abs(m - s) * log2(ch);
+    }
+    if (zero) {
+        cur = 0.0;
+        e = 0;
+        return;
+    }
+    int k = 0;
+    if (lg < -400.0) k = (int)ceil((-400.0 - lg) / 512.0);
+    e = -512 * k;
+    cur = exp2(lg + 512.0 * (double)k);
+    if (m & 1) cur = -cur;
+}
+
+#define REC_RESCALE(cur, prev, e)                                                        \
+    if ((e) < 0 && fabs(cur) > 0x1p200) {                                               \
+        (cur) *= 0x1p-512;                                                               \
+        (prev) *= 0x1p-512;                                                              \
+        (e) += 512;                                                                      \
+    }
+
+// ---------------------------------------------------------------- tables
+__global__ void k_build_coef(int L, int s, double *__restrict__ coef, long long nalm) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nalm) return;
+    int lo = 0, hi = L;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) / 2;
+        if (almidx(L, mid, mid) <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    const int m = lo;
+    const int l = m + (int)(idx - almidx(L, m, m));
+    const int l0 = max(m, s);
+    double al = 0.0, ga = 0.0, be = 0.0;
+    if (l >= l0 && l < L) {
+        const double lp = l + 1.0, dm = m, ds = s, dl = l;
+        const double den = sqrt((lp * lp - dm * dm) * (lp * lp - ds * ds));
+        al = lp * sqrt((2.0 * dl + 1.0) * (2.0 * dl + 3.0)) / den;
+        if (l > 0) {
+            ga = al * (dm * ds / (dl * lp));
+            be = (lp / dl) * sqrt((dl * dl - dm * dm) * (dl * dl - ds * ds)) / den *
+                 sqrt((2.0 * dl + 3.0) / (2.0 * dl - 1.0));
+        }
+    }
+    coef[idx] = al;
+    coef[nalm + idx] = ga;
+    coef[2 * nalm + idx] = be;
+}
+
+int build_coef_tables(cunusht_plan_s *P, cudaStream_t st) {
+    for (int s = 0; s <= 2; ++s) {
+        int nb = (int)((P->nalm + 255) / 256);
+        k_build_coef<<<nb, 256, 0, st>>>(P->lmax, s, P->d_coef[s], P->nalm);
+        CU_LAUNCH_CHECK();
+    }
+    return CUNUSHT_OK;
+}
+
+// ---------------------------------------------------------------- synthesis, spin 0
+constexpr int LEG_TPB = 128;
+constexpr int LEG_CH = 128;
+
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_synth_s0(int L, const double2 *__restrict__ alm, const double *__restrict__ lfac,
+                   const double *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
+                   int npairs, const double *__restrict__ px, const double *__restrict__ psh,
+                   const double *__restrict__ pch, const int *__restrict__ prn,
+                   const int *__restrict__ prs, double2 *__restrict__ H, int ldH) {
+    __shared__ double s_al[LEG_CH], s_be[LEG_CH];
+    __shared__ double2 s_a[LEG_CH];
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+    }
+    double cur, prev;
+    int e;
+    rec_start(lg0[m], m, 0, sh, ch, cur, prev, e);
+    double Er = 0.0, Ei = 0.0, Or = 0.0, Oi = 0.0;
+    const double *al = coef, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;  // (l, m) at b + l
+    for (int lb = m; lb <= L; lb += LEG_CH) {
+        const int cnt = min(LEG_CH, L - lb + 1);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += LEG_TPB) {
+            const long long ix = b + lb + i;
+            s_al[i] = al[ix];
+            s_be[i] = be[ix];
+            double2 a = alm[ix];
+            const double f = lfac ? lfac[lb + i] : 1.0;
+            s_a[i] = make_double2(a.x * f, a.y * f);
+        }
+        __syncthreads();
+        for (int i = 0; i < cnt; ++i) {
+            if (e == 0) {
+                const double2 a = s_a[i];
+                if ((lb + i + m) & 1) {
+                    Or = fma(a.x, cur, Or);
+                    Oi = fma(a.y, cur, Oi);
+                } else {
+                    Er = fma(a.x, cur, Er);
+                    Ei = fma(a.y, cur, Ei);
+                }
+            }
+            const double nxt = fma(s_al[i] * x, cur, -s_be[i] * prev);
+            prev = cur;
+            cur = nxt;
+            REC_RESCALE(cur, prev, e);
+        }
+    }
+    if (act) {
+        const int n = prn[p], s = prs[p];
+        H[(long long)m * ldH + n] = make_double2(Er + Or, Ei + Oi);
+        if (s != n) H[(long long)m * ldH + s] = make_double2(Er - Or, Ei - Oi);
+    }
+}
+
+// ---------------------------------------------------------------- synthesis, spin s > 0
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_synth_spin(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
+                     const double *__restrict__ lfac, const double *__restrict__ coef,
+                     long long nalm, const double *__restrict__ lg0, int npairs,
+                     const double *__restrict__ px, const double *__restrict__ psh,
+                     const double *__restrict__ pch, const int *__restrict__ prn,
+                     const int *__restrict__ prs, double2 *__restrict__ H, int ldH) {
+    __shared__ double s_al[LEG_CH], s_ga[LEG_CH], s_be[LEG_CH];
+    __shared__ double2 s_A[LEG_CH], s_B[LEG_CH];
+    const int m = blockIdx.y;
+    const int l0 = max(m, spin);
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+    }
+    double cN, pN, cS, pS;
+    int eN, eS;
+    rec_start(lg0[m], m, spin, sh, ch, cN, pN, eN);  // ring theta
+    rec_start(lg0[m], m, spin, ch, sh, cS, pS, eS);  // ring pi - theta
+    double2 hpn = make_double2(0, 0), hps = hpn, hmn = hpn, hms = hpn;
+    const double *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    for (int lb = l0; lb <= L; lb += LEG_CH) {
+        const int cnt = min(LEG_CH, L - lb + 1);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += LEG_TPB) {
+            const int l = lb + i;
+            const long long ix = b + l;
+            s_al[i] = al[ix];
+            s_ga[i] = ga[ix];
+            s_be[i] = be[ix];
+            const double f = lfac ? lfac[l] : 1.0;
+            const double2 g = G[ix];
+            const double2 c = C ? C[ix] : make_double2(0.0, 0.0);
+            // A = G + iC ; B = (conj G + i conj C) (-1)^{l+m}
+            s_A[i] = make_double2(f * (g.x - c.y), f * (g.y + c.x));
+            const double par = ((l + m) & 1) ? -f : f;
+            s_B[i] = make_double2(par * (g.x + c.y), par * (c.x - g.y));
+        }
+        __syncthreads();
+        for (int i = 0; i < cnt; ++i) {
+            const double2 A = s_A[i], B = s_B[i];
+            if (eN == 0) {
+                hpn.x = fma(A.x, cN, hpn.x);
+                hpn.y = fma(A.y, cN, hpn.y);
+                hms.x = fma(B.x, cN, hms.x);
+                hms.y = fma(B.y, cN, hms.y);
+            }
+            if (eS == 0) {
+                hps.x = fma(A.x, cS, hps.x);
+                hps.y = fma(A.y, cS, hps.y);
+                hmn.x = fma(B.x, cS, hmn.x);
+                hmn.y = fma(B.y, cS, hmn.y);
+            }
+            const double a_ = s_al[i], g_ = s_ga[i], b_ = s_be[i];
+            const double nN = fma(fma(a_, x, g_), cN, -b_ * pN);
+            const double nS = fma(fma(a_, -x, g_), cS, -b_ * pS);
+            pN = cN;
+            cN = nN;
+            pS = cS;
+            cS = nS;
+            REC_RESCALE(cN, pN, eN);
+            REC_RESCALE(cS, pS, eS);
+        }
+    }
+    if (act) {
+        const int n = prn[p], s = prs[p];
+        const double sgs = (spin & 1) ? -1.0 : 1.0;
+        H[(long long)(L + m) * ldH + n] = make_double2(-hpn.x, -hpn.y);
+        if (s != n) H[(long long)(L + m) * ldH + s] = make_double2(-hps.x, -hps.y);
+        if (m > 0) {
+            H[(long long)(L - m) * ldH + n] = make_double2(-sgs * hmn.x, -sgs * hmn.y);
+            if (s != n) H[(long long)(L - m) * ldH + s] = make_double2(-sgs * hms.x, -sgs * hms.y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- adjoint helpers
+// Sum v[16] over the 32 lanes of a warp; afterwards lane k holds the total of
+// index ((k >> 1) & 15) in v[0] (lanes 2j and 2j+1 hold the same value).
+__device__ __forceinline__ void warp_reduce_scatter16(double v[16]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const bool up = lane & 16;
+        const double send = up ? v[i] : v[i + 8];
+        const double keep = up ? v[i + 8] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool up = lane & 8;
+        const double send = up ? v[i] : v[i + 4];
+        const double keep = up ? v[i + 4] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const bool up = lane & 4;
+        const double send = up ? v[i] : v[i + 2];
+        const double keep = up ? v[i + 2] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    {
+        const bool up = lane & 2;
+        const double send = up ? v[0] : v[1];
+        const double keep = up ? v[1] : v[0];
+        v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+// index held by lane after the reduce-scatter: bits (lane>>1) reversed order
+// of the halving steps: step 16 -> bit 3 of index, step 8 -> bit 2, 4 -> 1, 2 -> 0
+__device__ __forceinline__ int rs16_index(int lane) {
+    return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+}
+
+// ---------------------------------------------------------------- adjoint, spin 0
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_adj_s0(int L, const double2 *__restrict__ H, int ldH, const double *__restrict__ lfac,
+                 const double *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
+                 int npairs, const double *__restrict__ px, const double *__restrict__ psh,
+                 const double *__restrict__ pch, const int *__restrict__ prn,
+                 const int *__restrict__ prs, double *__restrict__ alm /* interleaved */) {
+    constexpr int NW = LEG_TPB / 32;
+    __shared__ double red[NW][16];
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    double2 Ep = make_double2(0, 0), Op = Ep;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+        const int n = prn[p], s = prs[p];
+        const double2 hn = H[(long long)m * ldH + n];
+        if (s != n) {
+            const double2 hs = H[(long long)m * ldH + s];
+            Ep = make_double2(hn.x + hs.x, hn.y + hs.y);
+            Op = make_double2(hn.x - hs.x, hn.y - hs.y);
+        } else {
+            Ep = hn;
+            Op = hn;
+        }
+    }
+    double cur, prev;
+    int e;
+    rec_start(lg0[m], m, 0, sh, ch, cur, prev, e);
+    if (!act) {
+        cur = 0.0;
+        e = 0;
+    }
+    const double *al = coef, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int lb = m; lb <= L; lb += 8) {
+        double v[16];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int l = lb + i;
+            const double lam = (e == 0 && l <= L) ? cur : 0.0;
+            const double2 src = ((l + m) & 1) ? Op : Ep;
+            v[2 * i] = lam * src.x;
+            v[2 * i + 1] = lam * src.y;
+            if (l < L) {
+                const double nxt = fma(__ldg(al + b + l) * x, cur, -__ldg(be + b + l) * prev);
+                prev = cur;
+                cur = nxt;
+                REC_RESCALE(cur, prev, e);
+            }
+        }
+        warp_reduce_scatter16(v);
+        if (!(lane & 1)) red[wid][rs16_index(lane)] = v[0];
+        __syncthreads();
+        if (threadIdx.x < 16) {
+            double t = 0.0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) t += red[w][threadIdx.x];
+            const int l = lb + (threadIdx.x >> 1);
+            if (l <= L) {
+                const double f = lfac ? lfac[l] : 1.0;
+                atomicAdd(alm + 2 * (b + l) + (threadIdx.x & 1), t * f);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- adjoint, spin s > 0
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_adj_spin(int L, int spin, int ncomp, const double2 *__restrict__ H, int ldH,
+                   const double *__restrict__ lfac, const double *__restrict__ coef,
+                   long long nalm, const double *__restrict__ lg0, int npairs,
+                   const double *__restrict__ px, const double *__restrict__ psh,
+                   const double *__restrict__ pch, const int *__restrict__ prn,
+                   const int *__restrict__ prs, double *__restrict__ Gout,
+                   double *__restrict__ Cout) {
+    constexpr int NW = LEG_TPB / 32;
+    __shared__ double red[NW][16];
+    __shared__ double tot[16];
+    const int m = blockIdx.y;
+    const int l0 = max(m, spin);
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    double2 hpn = make_double2(0, 0), hps = hpn, hmn = hpn, hms = hpn;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+        const int n = prn[p], s = prs[p];
+        hpn = H[(long long)(L + m) * ldH + n];
+        hmn = H[(long long)(L - m) * ldH + n];
+        if (s != n) {
+            hps = H[(long long)(L + m) * ldH + s];
+            hms = H[(long long)(L - m) * ldH + s];
+        }
+    }
+    double cN, pN, cS, pS;
+    int eN, eS;
+    rec_start(lg0[m], m, spin, sh, ch, cN, pN, eN);
+    rec_start(lg0[m], m, spin, ch, sh, cS, pS, eS);
+    if (!act) {
+        cN = cS = 0.0;
+        eN = eS = 0;
+    }
+    const double *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const double sgs = (spin & 1) ? -1.0 : 1.0;
+    for (int lb = l0; lb <= L; lb += 4) {
+        double v[16];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int l = lb + i;
+            const double lN = (eN == 0 && l <= L) ? cN : 0.0;
+            const double lS = (eS == 0 && l <= L) ? cS : 0.0;
+            const double par = ((l + m) & 1) ? -1.0 : 1.0;
+            // P = lN hpn + lS hps ; Q = par (lS conj(hmn) + lN conj(hms))
+            v[4 * i + 0] = fma(lN, hpn.x, lS * hps.x);
+            v[4 * i + 1] = fma(lN, hpn.y, lS * hps.y);
+            v[4 * i + 2] = par * fma(lS, hmn.x, lN * hms.x);
+            v[4 * i + 3] = -par * fma(lS, hmn.y, lN * hms.y);
+            if (l < L) {
+                const double a_ = __ldg(al + b + l), g_ = __ldg(ga + b + l), b_ = __ldg(be + b + l);
+                const double nN = fma(fma(a_, x, g_), cN, -b_ * pN);
+                const double nS = fma(fma(a_, -x, g_), cS, -b_ * pS);
+                pN = cN;
+                cN = nN;
+                pS = cS;
+                cS = nS;
+                REC_RESCALE(cN, pN, eN);
+                REC_RESCALE(cS, pS, eS);
+            }
+        }
+        warp_reduce_scatter16(v);
+        if (!(lane & 1)) red[wid][rs16_index(lane)] = v[0];
+        __syncthreads();
+        if (threadIdx.x < 16) {
+            double t = 0.0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) t += red[w][threadIdx.x];
+            tot[threadIdx.x] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            const int l = lb + threadIdx.x;
+            if (l <= L) {
+                const double f = lfac ? lfac[l] : 1.0;
+                const double Pr = tot[4 * threadIdx.x], Pi = tot[4 * threadIdx.x + 1];
+                const double Qr = sgs * tot[4 * threadIdx.x + 2], Qi = sgs * tot[4 * threadIdx.x + 3];
+                atomicAdd(Gout + 2 * (b + l), -0.5 * f * (Pr + Qr));
+                atomicAdd(Gout + 2 * (b + l) + 1, -0.5 * f * (Pi + Qi));
+                if (ncomp > 1) {
+                    atomicAdd(Cout + 2 * (b + l), -0.5 * f * (Pi - Qi));
+                    atomicAdd(Cout + 2 * (b + l) + 1, 0.5 * f * (Pr - Qr));
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- host launchers
+struct RingPairs {
+    int npairs;
+    const double *x, *sh, *ch;
+    const int *rn, *rs;
+    int ld;
+};
+
+static RingPairs pairs_of(const cunusht_plan_s *P, bool cc) {
+    if (cc) return {P->cc_npairs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn, P->d_cc_rs, P->ncc};
+    return {P->gl_npairs, P->d_gl_x, P->d_gl_sh, P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->nring};
+}
+
+int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C,
+              bool use_lfac, bool cc, double2 *H, cudaStream_t st) {
+    const RingPairs R = pairs_of(P, cc);
+    const int L = P->lmax;
+    dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
+    const double *lf = use_lfac ? P->d_lfac : nullptr;
+    if (spin == 0) {
+        k_leg_synth_s0<<<grid, LEG_TPB, 0, st>>>(L, G, lf, P->d_coef[0], P->nalm, P->d_lg0[0],
+                                                 R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H, R.ld);
+    } else {
+        k_leg_synth_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, lf, P->d_coef[spin], P->nalm,
+                                                   P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch,
+                                                   R.rn, R.rs, H, R.ld);
+    }
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
+                bool cc, double2 *G, double2 *C, cudaStream_t st) {
+    const RingPairs R = pairs_of(P, cc);
+    const int L = P->lmax;
+    CU_TRY(cudaMemsetAsync(G, 0, sizeof(double2) * P->nalm, st));
+    if (spin > 0 && ncomp > 1) CU_TRY(cudaMemsetAsync(C, 0, sizeof(double2) * P->nalm, st));
+    dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
+    const double *lf = use_lfac ? P->d_lfac : nullptr;
+    if (spin == 0) {
+        k_leg_adj_s0<<<grid, LEG_TPB, 0, st>>>(L, H, R.ld, lf, P->d_coef[0], P->nalm, P->d_lg0[0],
+                                               R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
+                                               (double *)G);
+    } else {
+        k_leg_adj_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, H, R.ld, lf, P->d_coef[spin],
+                                                 P->nalm, P->d_lg0[spin], R.npairs, R.x, R.sh,
+                                                 R.ch, R.rn, R.rs, (double *)G, (double *)C);
+    }
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+}  // namespace cunusht

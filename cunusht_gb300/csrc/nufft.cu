@@ -1,0 +1,408 @@
+// Non-uniform interpolation (type 2) and spreading (type 1) on the oversampled
+// 2 pi torus with the "exponential of semicircle" kernel
+//     psi(z) = exp(beta (sqrt(1 - z^2) - 1)),  |z| <= 1,  z = 2 (x - n) / w,
+// which replaces the cuFINUFFT execute calls of the reference
+// (cunusht/deflection/GPU_nufft_transformer.py:292-310; plan :242-246 with
+// isign +1 for type 2 and -1 for type 1, FFT mode ordering).  The deconvolution
+// by the kernel's Fourier transform is applied in the theta pass (fft.cu).
+//
+// Fine-grid layout: rows n in [n_lo, n_lo + nrows) of the theta torus (row
+// r = n - n_lo), each row Npf longitudes; real (spin 0) or complex (spin s).
+// Points are read in the caller's order; for lensing they are the deflected
+// pixels in ring order, so neighbouring threads touch neighbouring columns.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cunusht {
+
+constexpr int NU_TPB = 256;
+constexpr int MAXW = 16;
+
+template <typename T> __device__ __forceinline__ T es_kernel(T z, T beta) {
+    const T q = (T)1 - z * z;
+    return q > (T)0 ? exp(beta * (sqrt(q) - (T)1)) : (T)0;
+}
+
+struct PointCoords {
+    int r0;  // first fine row (relative to n_lo)
+    int p0;  // first fine column (may be negative / >= Npf: wrap)
+    double ft, fp;  // (n0 - t), (p0 - p): offsets of the first tap
+};
+
+__device__ __forceinline__ PointCoords point_coords(double th, double ph, int Ntf, int Npf, int n_lo,
+                                                    int nrows, int w) {
+    PointCoords pc;
+    // non-finite or far out-of-range coordinates are clamped so every index
+    // below stays inside the grid (the result for such points is garbage-in)
+    if (!isfinite(th)) th = 0.0;
+    if (!isfinite(ph) || fabs(ph) > 1e12) ph = 0.0;
+    double t = th * ((double)Ntf / TWOPI);
+    t = fmin(fmax(t, -1.0), 0.5 * Ntf + 1.0);
+    double p = ph * ((double)Npf / TWOPI);
+    p -= floor(p / (double)Npf) * (double)Npf;
+    p = fmin(fmax(p, 0.0), (double)Npf);
+    const double hw = 0.5 * w;
+    const int n0 = (int)ceil(t - hw);
+    const int p0 = (int)ceil(p - hw);
+    pc.ft = (double)n0 - t;
+    pc.fp = (double)p0 - p;
+    int r0 = n0 - n_lo;
+    r0 = r0 < 0 ? 0 : (r0 > nrows - w ? nrows - w : r0);  // stays in bounds for any input
+    pc.r0 = r0;
+    pc.p0 = p0;
+    return pc;
+}
+
+__device__ __forceinline__ void load_point(const double *loc, long long j, long long npts, int layout,
+                                           double &th, double &ph) {
+    if (layout == 0) {
+        th = loc[2 * j];
+        ph = loc[2 * j + 1];
+    } else {
+        th = loc[j];
+        ph = loc[npts + j];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void weights(const PointCoords &pc, int w, T beta, T *kt, T *kp) {
+    const T s = (T)2 / (T)w;
+#pragma unroll
+    for (int a = 0; a < MAXW; ++a) {
+        if (a < w) {
+            kt[a] = es_kernel<T>(((T)pc.ft + (T)a) * s, beta);
+            kp[a] = es_kernel<T>(((T)pc.fp + (T)a) * s, beta);
+        }
+    }
+}
+
+// ------------------------------------------------------------ interp (type 2)
+template <typename T, bool CPLX>
+__global__ void __launch_bounds__(NU_TPB)
+    k_interp(const T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
+             const double *__restrict__ loc, long long npts, int layout,
+             const double *__restrict__ gamma, int spin, void *__restrict__ out, int out_f32) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npts) return;
+    double th, ph;
+    load_point(loc, j, npts, layout, th, ph);
+    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+    T kt[MAXW], kp[MAXW];
+    weights<T>(pc, w, beta, kt, kp);
+    int cols[MAXW];
+#pragma unroll
+    for (int b = 0; b < MAXW; ++b) {
+        int c = pc.p0 + b;
+        c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+        cols[b] = c;
+    }
+    T ar = 0, ai = 0;
+    for (int a = 0; a < w; ++a) {
+        const long long rowoff = (long long)(pc.r0 + a) * Npf;
+        T rr = 0, ri = 0;
+        if constexpr (CPLX) {
+            const cplx<T> *row = reinterpret_cast<const cplx<T> *>(U) + rowoff;
+#pragma unroll
+            for (int b = 0; b < MAXW; ++b) {
+                if (b < w) {
+                    const cplx<T> v = row[cols[b]];
+                    rr = fma(kp[b], v.x, rr);
+                    ri = fma(kp[b], v.y, ri);
+                }
+            }
+        } else {
+            const T *row = U + rowoff;
+#pragma unroll
+            for (int b = 0; b < MAXW; ++b)
+                if (b < w) rr = fma(kp[b], row[cols[b]], rr);
+        }
+        ar = fma(kt[a], rr, ar);
+        if constexpr (CPLX) ai = fma(kt[a], ri, ai);
+    }
+    if constexpr (CPLX) {
+        double zr = ar, zi = ai;
+        if (gamma) {
+            double s, c;
+            sincos(spin * gamma[j], &s, &c);
+            const double tr = zr * c - zi * s;
+            zi = zr * s + zi * c;
+            zr = tr;
+        }
+        if (out_f32) {
+            ((float *)out)[j] = (float)zr;
+            ((float *)out)[npts + j] = (float)zi;
+        } else {
+            ((double *)out)[j] = zr;
+            ((double *)out)[npts + j] = zi;
+        }
+    } else {
+        if (out_f32) ((float *)out)[j] = (float)ar;
+        else ((double *)out)[j] = (double)ar;
+    }
+}
+
+// ------------------------------------------------------------ spread (type 1)
+template <typename T, bool CPLX>
+__global__ void __launch_bounds__(NU_TPB)
+    k_spread(T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
+             const double *__restrict__ loc, long long npts, int layout,
+             const double *__restrict__ gamma, int spin, const void *__restrict__ in, int in_f32) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npts) return;
+    double th, ph;
+    load_point(loc, j, npts, layout, th, ph);
+    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+    T kt[MAXW], kp[MAXW];
+    weights<T>(pc, w, beta, kt, kp);
+    double vr, vi = 0.0;
+    if (in_f32) {
+        vr = ((const float *)in)[j];
+        if (CPLX) vi = ((const float *)in)[npts + j];
+    } else {
+        vr = ((const double *)in)[j];
+        if (CPLX) vi = ((const double *)in)[npts + j];
+    }
+    if (CPLX && gamma) {
+        double s, c;
+        sincos(spin * gamma[j], &s, &c);  // multiply by e^{-i spin gamma}
+        const double tr = vr * c + vi * s;
+        vi = vi * c - vr * s;
+        vr = tr;
+    }
+    for (int a = 0; a < w; ++a) {
+        const long long rowoff = (long long)(pc.r0 + a) * Npf;
+        const T fr = kt[a] * (T)vr, fi = kt[a] * (T)vi;
+        for (int b = 0; b < w; ++b) {
+            int c = pc.p0 + b;
+            c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+            if constexpr (CPLX) {
+                T *cell = U + 2 * (rowoff + c);
+                atomicAdd(cell, kp[b] * fr);
+                atomicAdd(cell + 1, kp[b] * fi);
+            } else {
+                atomicAdd(U + rowoff + c, kp[b] * fr);
+            }
+        }
+    }
+}
+
+int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
+                 const double *gamma, void *out, int out_dtype, cudaStream_t st) {
+    if (npts == 0) return CUNUSHT_OK;
+    const int nb = (int)((npts + NU_TPB - 1) / NU_TPB);
+    const int f32o = out_dtype == CUNUSHT_F32;
+    if (P->grid_fp32) {
+        if (spin == 0)
+            k_interp<float, false><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                          P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
+                                                          f32o);
+        else
+            k_interp<float, true><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                         P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
+                                                         f32o);
+    } else {
+        if (spin == 0)
+            k_interp<double, false><<<nb, NU_TPB, 0, st>>>((const double *)P->d_U, P->nrows, P->Npf, P->Ntf,
+                                                           P->n_lo, P->w, P->beta, loc, npts, layout, gamma, spin,
+                                                           out, f32o);
+        else
+            k_interp<double, true><<<nb, NU_TPB, 0, st>>>((const double *)P->d_U, P->nrows, P->Npf, P->Ntf,
+                                                          P->n_lo, P->w, P->beta, loc, npts, layout, gamma, spin,
+                                                          out, f32o);
+    }
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
+                 const double *gamma, const void *in, int in_dtype, cudaStream_t st) {
+    const size_t cell = (P->grid_fp32 ? 4 : 8) * (spin ? 2 : 1);
+    CU_TRY(cudaMemsetAsync(P->d_U, 0, cell * (size_t)P->nrows * P->Npf, st));
+    if (npts == 0) return CUNUSHT_OK;
+    const int nb = (int)((npts + NU_TPB - 1) / NU_TPB);
+    const int f32i = in_dtype == CUNUSHT_F32;
+    if (P->grid_fp32) {
+        if (spin == 0)
+            k_spread<float, false><<<nb, NU_TPB, 0, st>>>((float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                          (float)P->beta, loc, npts, layout, gamma, spin, in, f32i);
+        else
+            k_spread<float, true><<<nb, NU_TPB, 0, st>>>((float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                         (float)P->beta, loc, npts, layout, gamma, spin, in, f32i);
+    } else {
+        if (spin == 0)
+            k_spread<double, false><<<nb, NU_TPB, 0, st>>>((double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                           P->w, P->beta, loc, npts, layout, gamma, spin, in, f32i);
+        else
+            k_spread<double, true><<<nb, NU_TPB, 0, st>>>((double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                          P->w, P->beta, loc, npts, layout, gamma, spin, in, f32i);
+    }
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+// ------------------------------------------------------------ pointing
+// Deflected angles per pixel, cunusht/c/pointing.cu:210-222 (one thread per
+// pixel instead of one per ring); the rotation angle gamma of
+// CPU_nufft_transformer.py:160 is computed as a single atan2 of the angle
+// difference (equal modulo 2 pi).
+__global__ void __launch_bounds__(256)
+    k_pointing(int nring, const double *__restrict__ rth, const double *__restrict__ rph0,
+               const long long *__restrict__ rnph, const long long *__restrict__ rofs, long long npix,
+               const double *__restrict__ dth, const double *__restrict__ dph,
+               double *__restrict__ oth, double *__restrict__ oph, double *__restrict__ ogam) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npix) return;
+    int lo = 0, hi = nring - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (rofs[mid] <= j) lo = mid;
+        else hi = mid - 1;
+    }
+    const int ring = lo;
+    const double theta = rth[ring];
+    const long long nph = rnph[ring];
+    const double phi = rph0[ring] + (double)(j - rofs[ring]) * (TWOPI / (double)nph);
+    const double t = dth[j], p = dph[j];
+    const double d2 = t * t + p * p;
+    double sinaoa, cosa;
+    if (d2 > 1e-6) {
+        const double a = sqrt(d2);
+        double sa;
+        sincos(a, &sa, &cosa);
+        sinaoa = sa / a;
+    } else {
+        // sin(a)/a and cos(a) series, error < a^10/10!
+        sinaoa = 1.0 - d2 / 6.0 * (1.0 - d2 / 20.0 * (1.0 - d2 / 42.0 * (1.0 - d2 / 72.0)));
+        cosa = 1.0 - d2 / 2.0 * (1.0 - d2 / 12.0 * (1.0 - d2 / 30.0 * (1.0 - d2 / 56.0)));
+    }
+    double st, ct;
+    sincos(theta, &st, &ct);
+    const double nx = st * cosa + ct * t * sinaoa;
+    const double ny = -p * sinaoa;
+    const double nz = ct * cosa - st * t * sinaoa;
+    oth[j] = atan2(sqrt(nx * nx + ny * ny), nz);
+    double php = phi - atan2(ny, nx);
+    if (php >= TWOPI) php -= TWOPI;
+    oph[j] = php;
+    if (ogam) {
+        // gamma = atan2(p, t) - atan2(p, d sin d cot(theta) + t cos d)
+        //       = atan2(p * x2 - t * p, t * x2 + p * p),  x2 = d^2 (sin d / d) cot + t cos d
+        const double x2 = d2 * sinaoa * (ct / st) + t * cosa;
+        ogam[j] = (d2 > 0.0) ? atan2(p * x2 - t * p, t * x2 + p * p) : 0.0;
+    }
+}
+
+int pointing_launch(int nring, const double *rth, const double *rph0, const long long *rnph,
+                    const long long *rofs, long long npix, const double *dth, const double *dph,
+                    double *out_th, double *out_ph, double *out_gamma, cudaStream_t st) {
+    if (npix == 0) return CUNUSHT_OK;
+    const int nb = (int)((npix + 255) / 256);
+    k_pointing<<<nb, 256, 0, st>>>(nring, rth, rph0, rnph, rofs, npix, dth, dph, out_th, out_ph, out_gamma);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+// ------------------------------------------------------------ doubling
+template <typename T>
+__global__ void k_doubling(const T *__restrict__ in, long long nt, long long np, int layout, T sg,
+                           T *__restrict__ out) {
+    const long long dt = 2 * nt - 2;
+    const long long tot = dt * np;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= tot) return;
+    const long long h = np / 2;
+    long long k, i;  // ring k of the torus, longitude i
+    if (layout == 1) {
+        i = idx / dt;
+        k = idx - i * dt;
+    } else {
+        k = idx / np;
+        i = idx - k * np;
+    }
+    T v;
+    if (k < nt) {
+        v = layout == 1 ? in[i * nt + k] : in[k * np + i];
+    } else {
+        const long long km = dt - k;
+        const long long im = i < h ? i + h : i - h;
+        v = sg * (layout == 1 ? in[im * nt + km] : in[km * np + im]);
+    }
+    out[idx] = v;
+}
+
+template <typename T>
+__global__ void k_adjoint_doubling(const T *__restrict__ in, long long nt, long long np, T sg,
+                                   T *__restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nt * np) return;
+    const long long k = idx / np, i = idx - k * np;
+    const long long h = np / 2;
+    T v = in[idx];
+    if (k > 0 && k < nt - 1) {
+        const long long km = 2 * nt - 2 - k;
+        const long long im = i < h ? i + h : i - h;
+        v += sg * in[km * np + im];
+    }
+    out[idx] = v;
+}
+
+int doubling_launch(const void *in, long long nt, long long np, int layout, int spin, int dtype, void *out,
+                    cudaStream_t st) {
+    const long long tot = (2 * nt - 2) * np;
+    if (tot <= 0) return CUNUSHT_OK;
+    const int nb = (int)((tot + 255) / 256);
+    if (dtype == CUNUSHT_F32)
+        k_doubling<float><<<nb, 256, 0, st>>>((const float *)in, nt, np, layout, (spin & 1) ? -1.f : 1.f, (float *)out);
+    else
+        k_doubling<double><<<nb, 256, 0, st>>>((const double *)in, nt, np, layout, (spin & 1) ? -1.0 : 1.0,
+                                               (double *)out);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+int adjoint_doubling_launch(const void *in, long long nt, long long np, int spin, int dtype, void *out,
+                            cudaStream_t st) {
+    const long long tot = nt * np;
+    if (tot <= 0) return CUNUSHT_OK;
+    const int nb = (int)((tot + 255) / 256);
+    if (dtype == CUNUSHT_F32)
+        k_adjoint_doubling<float><<<nb, 256, 0, st>>>((const float *)in, nt, np, (spin & 1) ? -1.f : 1.f,
+                                                      (float *)out);
+    else
+        k_adjoint_doubling<double><<<nb, 256, 0, st>>>((const double *)in, nt, np, (spin & 1) ? -1.0 : 1.0,
+                                                       (double *)out);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+// ------------------------------------------------------------ alm dtype conversion
+__global__ void k_c64_to_c128(const float2 *__restrict__ in, long long n, double2 *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_double2(in[i].x, in[i].y);
+}
+__global__ void k_c128_to_c64(const double2 *__restrict__ in, long long n, float2 *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+int convert_alm(const void *in, int dtype, long long n, double2 *out, cudaStream_t st) {
+    if (dtype == CUNUSHT_F64) {
+        CU_TRY(cudaMemcpyAsync(out, in, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+    } else {
+        k_c64_to_c128<<<(int)((n + 255) / 256), 256, 0, st>>>((const float2 *)in, n, out);
+        CU_LAUNCH_CHECK();
+    }
+    return CUNUSHT_OK;
+}
+
+int store_alm(const double2 *in, long long n, int dtype, void *out, cudaStream_t st) {
+    if (dtype == CUNUSHT_F64) {
+        CU_TRY(cudaMemcpyAsync(out, in, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+    } else {
+        k_c128_to_c64<<<(int)((n + 255) / 256), 256, 0, st>>>(in, n, (float2 *)out);
+        CU_LAUNCH_CHECK();
+    }
+    return CUNUSHT_OK;
+}
+
+}  // namespace cunusht

@@ -1,0 +1,382 @@
+"""GPU nuSHT / lensing transformer with the surface of the reference's
+``GPU_cufinufft_transformer`` (cunusht/deflection/GPU_nufft_transformer.py:107-680).
+
+Arrays in and out are torch CUDA tensors (cupy arrays and host arrays are
+accepted and moved to the device, with the reference's warning for host
+arrays).  All compute runs in the CUDA library through the C ABI on the current
+torch stream; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import get_geom
+from .utils import Alm
+
+_PREC = {"auto": _lib.PREC_AUTO, "fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def to_device(x, name: str, dtype: torch.dtype | None = None, warn: bool = True) -> torch.Tensor:
+    """Device tensor view of x (torch / cupy / numpy), contiguous, of dtype."""
+    if isinstance(x, torch.Tensor) and x.is_cuda:
+        t = x
+    elif hasattr(x, "__cuda_array_interface__"):
+        t = torch.as_tensor(x, device="cuda")
+    else:
+        if warn:
+            print(f"WARNING: {name} not on the device and has automatically been transferred to device. "
+                  "This may reduce performance. Consider passing a device array instead")
+        t = torch.as_tensor(np.asarray(x), device="cuda")
+    if dtype is not None and t.dtype != dtype:
+        t = t.to(dtype)
+    return t.contiguous()
+
+
+def _loc_args(loc: torch.Tensor, npts_hint: int | None = None):
+    """(pointer tensor, npts, layout) for a point array: (npts, 2) rows of
+    (theta, phi) -> layout 0; (2, npts) or a transposed (npts, 2) view of a
+    planar (2, npts) array -> layout 1."""
+    if loc.dim() != 2:
+        raise ValueError(f"loc must be 2-d, got shape {tuple(loc.shape)}")
+    if loc.shape[1] == 2 and loc.is_contiguous():
+        return loc, loc.shape[0], 0
+    if loc.shape[1] == 2 and loc.t().is_contiguous():
+        return loc.t(), loc.shape[0], 1
+    if loc.shape[0] == 2:
+        t = loc.contiguous()
+        return t, t.shape[1], 1
+    return loc.contiguous(), loc.shape[0], 0
+
+
+class GPU_cufinufft_transformer:
+    """Transformer with the reference's constructor and methods; see the
+    C ABI (include/cunusht_gb300.h) for the math of each call."""
+
+    def __init__(self, geominfo_deflection, shttransformer_desc="shtns", nuFFTtype=None, epsilon=None,
+                 precision: str = "auto", max_spin: int = 2):
+        if nuFFTtype:
+            assert epsilon is not None, "epsilon must be provided if planned is True"
+        if shttransformer_desc not in ("shtns", "ducc", "cunusht"):
+            raise ValueError('shttransformer_desc must be either "ducc" or "shtns" or "cunusht"')
+        self.backend = "GPU"
+        self.shttransformer_desc = shttransformer_desc
+        self.nuFFTtype = nuFFTtype
+        self.geominfo = geominfo_deflection
+        self.geom = get_geom(geominfo_deflection)
+        self.lmax = int(geominfo_deflection[1]["lmax"])
+        self.execmode = "normal"
+        self.dlm_scaled = None
+        self.dclm_scaled = None
+        self.ptg = None
+        self.gamma = None
+        self.ret = {}
+        self.timings = {}
+        self.precision = precision
+        self.max_spin = max_spin
+        self.epsilon = epsilon
+        self.single_prec = bool(epsilon is not None and epsilon > 1e-6)
+        self._plan = None
+        self._lib = _lib.load()
+        if epsilon is not None:
+            self.plan(epsilon, nuFFTtype or 1)
+
+    # -------------------------------------------------------------- plan
+    def plan(self, epsilon, nuFFTtype=1):
+        """Create the device plan (grid sizes, kernel tables, workspace) for
+        this accuracy (GPU_nufft_transformer.py:227-246)."""
+        self._destroy()
+        g = self.geom
+        th = np.ascontiguousarray(g.theta, dtype=np.float64)
+        p0 = np.ascontiguousarray(g.phi0, dtype=np.float64)
+        nph = np.ascontiguousarray(g.nph, dtype=np.int64)
+        ofs = np.ascontiguousarray(g.ofs, dtype=np.int64)
+        h = ctypes.c_void_p()
+        torch.cuda.init()
+        _lib.check(self._lib.cunusht_plan_create(
+            ctypes.byref(h), self.lmax, float(epsilon), _PREC[self.precision], self.max_spin, th.size,
+            th.ctypes.data, p0.ctypes.data, nph.ctypes.data, ofs.ctypes.data))
+        self._plan = h
+        self.epsilon = epsilon
+        self.single_prec = epsilon > 1e-6
+        info = (ctypes.c_int64 * 10)()
+        self._lib.cunusht_plan_info(h, info, 10)
+        self.info = dict(zip(["npix", "ntheta_torus", "nphi_torus", "ntheta_fine", "nphi_fine", "kernel_width",
+                              "fine_rows", "workspace_bytes", "precision", "nalm"], list(info)))
+        self.ptg = None
+        self.dlm_scaled = None
+
+    def _destroy(self):
+        if getattr(self, "_plan", None) is not None:
+            self._lib.cunusht_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self._destroy()
+        except Exception:
+            pass
+
+    def _ensure_plan(self, epsilon):
+        if self.nuFFTtype:
+            assert epsilon is None or epsilon == self.epsilon, \
+                "expected epsilon = {} as set during initialisation of nuFFT plan, but is {}".format(self.epsilon, epsilon)
+            epsilon = self.epsilon
+        else:
+            assert epsilon is not None or self.epsilon is not None, "epsilon must be provided if not planned"
+            epsilon = self.epsilon if epsilon is None else epsilon
+        if self._plan is None or epsilon != self.epsilon:
+            self.plan(epsilon)
+        return epsilon
+
+    def _check_lm(self, lmax, mmax):
+        assert lmax == self.lmax, "Expected lmax={}. lmax must be same as during init, but is {}".format(self.lmax, lmax)
+        assert mmax == self.lmax, "Expected mmax={}. mmax must be same as lmax during init, but is {}".format(self.lmax, mmax)
+
+    @property
+    def nalm(self) -> int:
+        return Alm.getsize(self.lmax, self.lmax)
+
+    def npix(self) -> int:
+        return self.geom.npix()
+
+    def get_grid_uniform(self) -> torch.Tensor:
+        """(2, npix) colatitude / longitude of every pixel of the geometry."""
+        th, ph = self.geom.pixels()
+        return torch.as_tensor(np.stack([th, ph]), device="cuda")
+
+    # -------------------------------------------------------------- alm helpers
+    def _alm_in(self, alm, name, spin):
+        a = to_device(alm, name)
+        if not a.is_complex():
+            raise TypeError(f"{name} must be complex, got {a.dtype}")
+        a = a.reshape(-1, self.nalm) if a.dim() > 1 or a.numel() != self.nalm else a.reshape(1, self.nalm)
+        ncomp = a.shape[0]
+        if spin == 0 and ncomp != 1:
+            raise ValueError(f"spin 0 expects one alm array, got {ncomp}")
+        if ncomp > 2:
+            raise ValueError(f"at most 2 alm components, got {ncomp}")
+        dt = _lib.F32 if a.dtype == torch.complex64 else _lib.F64
+        if a.dtype not in (torch.complex64, torch.complex128):
+            a = a.to(torch.complex128)
+            dt = _lib.F64
+        return a.contiguous(), ncomp, dt
+
+    # -------------------------------------------------------------- transforms
+    def nusht2d2(self, lmax, mmax, alm, loc, pointmap=None, epsilon=None, verbose=0, spin=0, gamma=None,
+                 out_dtype=torch.float64):
+        """alm -> values at loc (npts, 2) [theta, phi]: a new array, spin 0
+        (npts,), spin s (2, npts) = (Q, U) (GPU_nufft_transformer.py:386-435)."""
+        self._check_lm(lmax, mmax)
+        self._ensure_plan(epsilon)
+        a, ncomp, adt = self._alm_in(alm, "alm", spin)
+        assert loc is not None, "loc must be provided"
+        loc_t, npts, layout = _loc_args(to_device(loc, "loc", torch.float64))
+        out = torch.empty((npts,) if spin == 0 else (2, npts), dtype=out_dtype, device="cuda")
+        odt = _lib.F32 if out_dtype == torch.float32 else _lib.F64
+        g = None
+        if gamma is not None and spin:
+            g = to_device(gamma, "gamma", torch.float64)
+        _lib.check(self._lib.cunusht_nusht2d2(
+            self._plan, spin, ncomp, a.data_ptr(), adt, loc_t.data_ptr(), npts, layout,
+            g.data_ptr() if g is not None else None, out.data_ptr(), odt, _stream()))
+        return out
+
+    def nusht2d1(self, lmax, mmax, pointmap, loc, epsilon=None, alm=None, verbose=0, spin=0, ncomp=None,
+                 gamma=None, alm_dtype=torch.complex128):
+        """values at loc -> alm, the exact adjoint of nusht2d2
+        (GPU_nufft_transformer.py:439-484).  Returns a new alm array."""
+        self._check_lm(lmax, mmax)
+        self._ensure_plan(epsilon)
+        m = to_device(pointmap, "pointmap")
+        if m.is_complex():
+            m = m.real.contiguous()
+        if m.dtype not in (torch.float32, torch.float64):
+            m = m.to(torch.float64)
+        mdt = _lib.F32 if m.dtype == torch.float32 else _lib.F64
+        loc_t, npts, layout = _loc_args(to_device(loc, "loc", torch.float64))
+        if spin == 0:
+            m = m.reshape(-1)
+            assert m.numel() == npts, (m.numel(), npts)
+            ncomp = 1
+        else:
+            m = m.reshape(2, -1).contiguous()
+            assert m.shape[1] == npts, (m.shape, npts)
+            ncomp = 2 if ncomp is None else ncomp
+        out = torch.empty((ncomp, self.nalm), dtype=alm_dtype, device="cuda")
+        odt = _lib.F32 if alm_dtype == torch.complex64 else _lib.F64
+        g = to_device(gamma, "gamma", torch.float64) if (gamma is not None and spin) else None
+        _lib.check(self._lib.cunusht_nusht2d1(
+            self._plan, spin, ncomp, m.data_ptr(), mdt, loc_t.data_ptr(), npts, layout,
+            g.data_ptr() if g is not None else None, out.data_ptr(), odt, _stream()))
+        return out[0] if spin == 0 else out
+
+    def dlm2pointing(self, dlm_scaled, mmax_dlm, verbose=0, single_prec=False, dclm_scaled=None):
+        """Deflected (theta', phi') of every pixel, (2, npix) float64
+        (GPU_nufft_transformer.py:344-351); the rotation angle is kept in
+        ``self.gamma``."""
+        assert mmax_dlm == self.lmax, (mmax_dlm, self.lmax)
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        d, _, ddt = self._alm_in(dlm_scaled, "dlm_scaled", 0)
+        c = None
+        if dclm_scaled is not None:
+            c = to_device(dclm_scaled, "dclm_scaled", d.dtype).reshape(-1)
+        npix = self.npix()
+        ptg = torch.empty((2, npix), dtype=torch.float64, device="cuda")
+        gamma = torch.empty((npix,), dtype=torch.float64, device="cuda")
+        _lib.check(self._lib.cunusht_dlm2pointing(
+            self._plan, d.data_ptr(), c.data_ptr() if c is not None else None, ddt, ptg.data_ptr(),
+            gamma.data_ptr(), _stream()))
+        self.gamma = gamma
+        return ptg
+
+    def synthesis(self, alm, out=None, lmax=None, mmax=None, spin=0):
+        """Spin-s synthesis on the pointing geometry (GPU_nufft_transformer.py:356-367)."""
+        lmax = self.lmax if lmax is None else lmax
+        self._check_lm(lmax, self.lmax if mmax is None else mmax)
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        a, ncomp, adt = self._alm_in(alm, "alm", spin)
+        npix = self.npix()
+        res = torch.empty((npix,) if spin == 0 else (2, npix), dtype=torch.float64, device="cuda")
+        _lib.check(self._lib.cunusht_synthesis(self._plan, spin, ncomp, a.data_ptr(), adt, res.data_ptr(), _stream()))
+        return res
+
+    def adjoint_synthesis(self, synthmap, lmax=None, mmax=None, out=None, spin=0, ncomp=None):
+        """Adjoint of ``synthesis`` (no quadrature weights) (GPU_nufft_transformer.py:372-383)."""
+        lmax = self.lmax if lmax is None else lmax
+        self._check_lm(lmax, self.lmax if mmax is None else mmax)
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        m = to_device(synthmap, "synthmap", torch.float64)
+        ncomp = (1 if spin == 0 else 2) if ncomp is None else ncomp
+        res = torch.empty((ncomp, self.nalm), dtype=torch.complex128, device="cuda")
+        _lib.check(self._lib.cunusht_adjoint_synthesis(self._plan, spin, ncomp, m.data_ptr(), res.data_ptr(),
+                                                       _lib.F64, _stream()))
+        return res[0] if spin == 0 else res
+
+    def synthesis_der1(self, alm, out=None):
+        """(d/dtheta, 1/sin(theta) d/dphi) of a scalar field on the pointing
+        geometry, as SHTns synth_grad (GPU_sht_transformer.py:88-97)."""
+        a = to_device(alm, "alm", torch.complex128).reshape(-1)
+        ll = torch.arange(self.lmax + 1, dtype=torch.float64, device="cuda")
+        fl = torch.sqrt(ll * (ll + 1))
+        mi = torch.repeat_interleave(torch.arange(self.lmax + 1, device="cuda"),
+                                     torch.arange(self.lmax + 1, 0, -1, device="cuda"))
+        li = torch.arange(self.nalm, device="cuda") - (mi * (2 * self.lmax + 1 - mi)) // 2
+        return self.synthesis((a * fl[li])[None], spin=1)
+
+    def set_pts(self, ptg):
+        self.ptg = to_device(ptg, "ptg", torch.float64)
+
+    # -------------------------------------------------------------- lensing
+    def _spin_of(self, gclm, spin):
+        if spin is not None:
+            return spin
+        return 0 if (getattr(gclm, "ndim", 1) == 1 or gclm.shape[0] == 1) else 2
+
+    def _pointing(self, ptg, dlm_scaled, dclm_scaled, lmax, verbose):
+        if ptg is not None:
+            ptg = to_device(ptg, "ptg", torch.float64)
+            if ptg.shape[0] != 2 and ptg.shape[-1] == 2:
+                ptg = ptg.t().contiguous()
+            self.ptg = ptg
+            return self.ptg, None
+        assert dlm_scaled is not None or self.dlm_scaled is not None, "Need to provide dlm_scaled if ptg is None"
+        d = to_device(dlm_scaled, "dlm_scaled") if dlm_scaled is not None else self.dlm_scaled
+        c = to_device(dclm_scaled, "dclm_scaled") if dclm_scaled is not None else None
+        same = (self.dlm_scaled is not None and self.ptg is not None and self.gamma is not None
+                and self.dlm_scaled.shape == d.shape and torch.equal(self.dlm_scaled, d)
+                and ((c is None and self.dclm_scaled is None) or
+                     (c is not None and self.dclm_scaled is not None and torch.equal(self.dclm_scaled, c))))
+        if not same:
+            self.dlm_scaled = d.clone()
+            self.dclm_scaled = c.clone() if c is not None else None
+            self.ptg = self.dlm2pointing(d, lmax, verbose, dclm_scaled=c)
+        return self.ptg, self.gamma
+
+    def _timed(self, name, fn):
+        if self.execmode != "timing":
+            return fn()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        r = fn()
+        e.record()
+        e.synchronize()
+        self.timings[name] = s.elapsed_time(e) * 1e-3
+        return r
+
+    def gclm2lenmap(self, gclm, lmax, mmax, ptg=None, dlm_scaled=None, epsilon=None, lenmap=None, verbose=1,
+                    execmode="normal", runid=None, GPUdesc="", spin=None, polrot=True, dclm_scaled=None):
+        """Lensed map from unlensed alm and the deflection
+        (GPU_nufft_transformer.py:487-578; spin-s semantics of
+        CPU_nufft_transformer.py:430-484 incl. the exp(i s gamma) rotation)."""
+        assert execmode in ["normal", "debug", "timing"]
+        self.execmode = execmode
+        self.runid, self.GPUdesc = runid, GPUdesc
+        self._check_lm(lmax, mmax)
+        epsilon = self._ensure_plan(epsilon)
+        spin = self._spin_of(gclm, spin)
+        ptg, gamma = self._timed("dlm2pointing", lambda: self._pointing(ptg, dlm_scaled, dclm_scaled, lmax, verbose))
+        g = gamma if (spin and polrot) else None
+        res = self._timed("nusht2d2", lambda: self.nusht2d2(lmax, mmax, gclm, ptg.t(), epsilon=epsilon, spin=spin,
+                                                            gamma=g))
+        if execmode == "debug":
+            self.ret = {"dlm2pointing": ptg, "gamma": gamma, "nusht2d2": res}
+            return self.ret
+        return res
+
+    def lenmap2gclm(self, lenmap, dlm_scaled, gclm=None, lmax=None, mmax=None, epsilon=None, ptg=None, verbose=1,
+                    execmode="normal", runid=None, GPUdesc="", spin=None, polrot=True, dclm_scaled=None, ncomp=None):
+        """Adjoint lensing, values on the lensed grid -> alm
+        (GPU_nufft_transformer.py:581-673); exact adjoint of gclm2lenmap."""
+        assert execmode in ["normal", "debug", "timing"]
+        self.execmode = execmode
+        self.runid, self.GPUdesc = runid, GPUdesc
+        lmax = self.lmax if lmax is None else lmax
+        mmax = self.lmax if mmax is None else mmax
+        self._check_lm(lmax, mmax)
+        epsilon = self._ensure_plan(epsilon)
+        lm = to_device(lenmap, "lenmap")
+        if gclm is not None and hasattr(gclm, "dtype") and hasattr(lm, "dtype"):
+            real_of = {torch.complex128: torch.float64, torch.complex64: torch.float32}
+            gdt = gclm.dtype if isinstance(gclm, torch.Tensor) else None
+            if gdt in real_of:
+                ldt = lm.real.dtype if lm.is_complex() else lm.dtype
+                assert ldt == real_of[gdt], \
+                    "lenmap and gclm must have same precision, but are {} and {}".format(lm.dtype, gdt)
+        if spin is None:
+            spin = 0 if (lm.dim() == 1 or lm.shape[0] == 1) else 2
+        if spin == 0:
+            lm = lm.reshape(-1) if lm.dim() == 1 else lm[0]
+        ptg_, gamma = self._timed("dlm2pointing", lambda: self._pointing(ptg, dlm_scaled, dclm_scaled, lmax, verbose))
+        g = gamma if (spin and polrot) else None
+        adt = torch.complex64 if (isinstance(gclm, torch.Tensor) and gclm.dtype == torch.complex64) else torch.complex128
+        res = self._timed("nusht2d1", lambda: self.nusht2d1(lmax, mmax, lm, ptg_.t(), epsilon=epsilon, spin=spin,
+                                                            gamma=g, ncomp=ncomp, alm_dtype=adt))
+        if execmode == "debug":
+            self.ret = {"dlm2pointing": ptg_, "gamma": gamma, "nusht2d1": res}
+            return self.ret
+        return res
+
+    @staticmethod
+    def hashdict():
+        """Compatibility with delensalot (GPU_nufft_transformer.py:676-680)."""
+        return "GPU_cufinufft_transformer"
+
+
+class GPU_SHT_transformer(GPU_cufinufft_transformer):
+    """SHT-only mode on the (GL) geometry: synthesis / adjoint_synthesis /
+    synthesis_der1 (cunusht.py:75-76, GPU_sht_transformer.py:11-127)."""
+
+    def __init__(self, geominfo, nthreads=None, max_spin: int = 2):
+        super().__init__(geominfo, nuFFTtype=None, epsilon=1e-7, max_spin=max_spin)

@@ -1,0 +1,153 @@
+/*
+ * cunusht_gb300 -- C ABI of the GB300 (sm_103a) non-uniform spherical harmonic
+ * transform / CMB lensing engine.
+ *
+ * Every entry point returns an int status (CUNUSHT_OK == 0) and never
+ * synchronises the device implicitly: work is enqueued on the caller's
+ * ``stream`` (a cudaStream_t passed as void*, NULL = legacy default stream).
+ * All array arguments are DEVICE pointers unless stated otherwise.  A failed
+ * call leaves a human-readable message in cunusht_last_error().
+ *
+ * Conventions (same as the reference, Sebastian-Belkner/cunuSHT):
+ *   alm      healpy m-major layout, idx(l,m) = m(2 lmax+1-m)/2 + l
+ *            (cunusht/utils.py:58); complex128 or complex64 interleaved.
+ *            A spin-s (s>0) field is ncomp consecutive alm arrays (G[, C]),
+ *            i.e. E[, B] for s = 2; s_a_lm = -(G_lm + i C_lm).
+ *   loc      points; layout 0 = (npts, 2) rows of (theta, phi) as nusht2d2's
+ *            ``loc`` (GPU_nufft_transformer.py:386), layout 1 = (2, npts)
+ *            planar (theta block then phi block) as ``ptg``
+ *            (GPU_nufft_transformer.py:344-351).
+ *   maps     spin 0: npts reals.  spin s>0: (2, npts) planar (Q block, U block).
+ *   dtype    CUNUSHT_F64 (float64 / complex128) or CUNUSHT_F32 (float32 /
+ *            complex64).
+ */
+#ifndef CUNUSHT_GB300_H
+#define CUNUSHT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUNUSHT_OK 0
+#define CUNUSHT_ERR_ARG 1         /* bad argument (sizes, layout, spin ...) */
+#define CUNUSHT_ERR_CUDA 2        /* a CUDA runtime call or kernel launch failed */
+#define CUNUSHT_ERR_ALLOC 3       /* device allocation failed */
+#define CUNUSHT_ERR_UNSUPPORTED 4 /* valid request outside what this build supports */
+
+#define CUNUSHT_F64 0
+#define CUNUSHT_F32 1
+
+#define CUNUSHT_PREC_AUTO 0  /* eps > 1e-6 -> FP32 FFT/nuFFT, else FP64 */
+#define CUNUSHT_PREC_FP64 1  /* plain FP64 everywhere */
+#define CUNUSHT_PREC_MIXED 2 /* split-precision Legendre + FP32/FP64 rest */
+
+typedef struct cunusht_plan_s cunusht_plan_t;
+
+/* Last error message of the calling thread ("" when none). */
+const char *cunusht_last_error(void);
+
+/* ABI version (major*10000 + minor*100 + patch). */
+int cunusht_version(void);
+
+/*
+ * Plan = the transformer state of GPU_cufinufft_transformer.__init__ /
+ * plan (cunusht/deflection/GPU_nufft_transformer.py:108-173, :227-246):
+ * band limit, accuracy, the pointing (output) ring geometry, the doubled
+ * Clenshaw-Curtis torus, nuFFT kernel and all device workspace.  All
+ * device memory of the plan is allocated here, none per call.
+ *   ring_*   host arrays of the pointing geometry (Geom, geometry.py:29-57):
+ *            colatitude, first longitude, pixels per ring, first pixel.
+ *   max_spin largest spin the plan will be asked for (0, 1 or 2).
+ */
+int cunusht_plan_create(cunusht_plan_t **plan, int lmax, double epsilon, int precision,
+                        int max_spin, int nring, const double *ring_theta,
+                        const double *ring_phi0, const int64_t *ring_nph,
+                        const int64_t *ring_ofs);
+int cunusht_plan_destroy(cunusht_plan_t *plan);
+
+/* Plan sizes: info[0]=npix, [1]=torus theta length, [2]=torus phi length,
+ * [3]=fine grid theta length, [4]=fine grid phi length, [5]=kernel width,
+ * [6]=fine rows stored, [7]=workspace bytes, [8]=precision in use,
+ * [9]=nalm.  Returns the number of entries written. */
+int cunusht_plan_info(const cunusht_plan_t *plan, int64_t *info, int ninfo);
+
+/*
+ * nusht2d2: alm -> values at arbitrary points (type-2 direction).
+ * Replaces GPU_cufinufft_transformer.nusht2d2
+ * (cunusht/deflection/GPU_nufft_transformer.py:386-435: SHTns CC synthesis,
+ * doubling, cuFFT fft2, cuFINUFFT type 2).  gamma (may be NULL) is the
+ * polarisation rotation angle per point; when given and spin>0 the output is
+ * multiplied by exp(i spin gamma) (CPU_nufft_transformer.py:356-368).
+ */
+int cunusht_nusht2d2(cunusht_plan_t *plan, int spin, int ncomp, const void *alm, int alm_dtype,
+                     const double *loc, int64_t npts, int loc_layout, const double *gamma,
+                     void *out, int out_dtype, void *stream);
+
+/*
+ * nusht2d1: values at arbitrary points -> alm, the exact adjoint of
+ * cunusht_nusht2d2 (real map inner product, alm inner product with m>0
+ * counted twice).  Replaces GPU_cufinufft_transformer.nusht2d1
+ * (GPU_nufft_transformer.py:439-484: cuFINUFFT type 1, ifft2, adjoint
+ * doubling, SHTns analysis of map*iw).  gamma (may be NULL) applies
+ * exp(-i spin gamma) first.
+ */
+int cunusht_nusht2d1(cunusht_plan_t *plan, int spin, int ncomp, const void *map, int map_dtype,
+                     const double *loc, int64_t npts, int loc_layout, const double *gamma,
+                     void *alm_out, int alm_dtype, void *stream);
+
+/*
+ * dlm2pointing: deflected angles of every pixel of the plan geometry.
+ * Replaces GPU_cufinufft_transformer.dlm2pointing / deflection.dlm2pointing
+ * (GPU_nufft_transformer.py:64-104, :344-351: SHTns synth_grad on the GL
+ * grid + compute_pointing_1Dto1D_lowmem, pointing.cu:197-255).
+ *   dlm_scaled   complex alm of the lensing potential (dlm / sqrt(l(l+1)))
+ *   dclm_scaled  curl potential (may be NULL)
+ *   ptg          out (2, npix) planar: theta' block then phi' block
+ *   gamma        out npix rotation angle (may be NULL), CPU_nufft_transformer.py:158-160
+ */
+int cunusht_dlm2pointing(cunusht_plan_t *plan, const void *dlm_scaled, const void *dclm_scaled,
+                         int alm_dtype, double *ptg, double *gamma, void *stream);
+
+/*
+ * Spin-s synthesis / adjoint synthesis on the plan's ring geometry (SHT-only
+ * mode; GPU_cufinufft_transformer.synthesis / adjoint_synthesis,
+ * GPU_nufft_transformer.py:356-383).  maps as above (npix or 2 x npix, FP64).
+ * The adjoint has no quadrature weights (adjoint, not analysis).
+ */
+int cunusht_synthesis(cunusht_plan_t *plan, int spin, int ncomp, const void *alm, int alm_dtype,
+                      double *map, void *stream);
+int cunusht_adjoint_synthesis(cunusht_plan_t *plan, int spin, int ncomp, const double *map,
+                              void *alm_out, int alm_dtype, void *stream);
+
+/*
+ * Raw pointing rotation (compute_pointing_1Dto1D_lowmem, pointing.cu:197-226):
+ * per pixel of a ring geometry, deflected (theta', phi') from the spin-1
+ * deflection maps (d_theta, d_phi) in ring-major pixel order; gamma optional.
+ * Ring tables are DEVICE arrays here (as the reference binding takes them).
+ */
+int cunusht_pointing(int nring, const double *ring_theta, const double *ring_phi0,
+                     const int64_t *ring_nph, const int64_t *ring_ofs, int64_t npix,
+                     const double *spin1_theta, const double *spin1_phi, double *out_theta,
+                     double *out_phi, double *out_gamma, void *stream);
+
+/*
+ * Map doubling to the 2 pi theta torus and its adjoint.
+ * cunusht_doubling replaces CUdoubling_contig_1D (layout 1, theta-contiguous
+ * (nphi, ntheta) in, (nphi, 2 ntheta - 2) out; doubling.cu:180-220) and
+ * CUdoubling_1D (layout 0, ring-major (ntheta, nphi) in, (2 ntheta - 2, nphi)
+ * out; doubling.cu:137-178).  cunusht_adjoint_doubling replaces
+ * CUadjoint_doubling_1D (ring-major (2 ntheta - 2, nphi) in, (ntheta, nphi)
+ * out; doubling.cu:53-92).  spin odd negates the mirrored half
+ * (CPU_nufft_transformer.py:284-318).  nphi must be even.
+ */
+int cunusht_doubling(const void *cc_map, int64_t ntheta, int64_t nphi, int layout, int spin,
+                     int dtype, void *out, void *stream);
+int cunusht_adjoint_doubling(const void *dmap, int64_t ntheta, int64_t nphi, int spin, int dtype,
+                             void *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CUNUSHT_GB300_H */

@@ -1,0 +1,120 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+symbol include/cunusht_gb300.h declares, and the Python host logic (geometry,
+alm utilities, argument parsing, factory) matches the reference semantics."""
+import os
+import re
+import shutil
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "cunusht_gb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(cunusht_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cunusht_gb300 import _lib, build
+    if not os.path.exists(_lib.LIB_PATH):
+        if shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+            pytest.skip("library not built and nvcc unavailable")
+        build.build()
+    return _lib.load()
+
+
+def test_header_declares_expected_entry_points():
+    syms = declared_symbols()
+    for s in ["cunusht_plan_create", "cunusht_nusht2d2", "cunusht_nusht2d1", "cunusht_dlm2pointing",
+              "cunusht_doubling", "cunusht_adjoint_doubling", "cunusht_pointing", "cunusht_last_error"]:
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from cunusht_gb300 import _lib
+    for s in declared_symbols():
+        assert hasattr(lib, s), f"{s} declared in the header but not exported"
+        assert s in _lib.SIGNATURES, f"{s} has no ctypes signature"
+
+
+def test_library_rejects_bad_arguments_without_touching_the_gpu(lib):
+    """Argument validation happens on the host before any CUDA call."""
+    import ctypes
+    from cunusht_gb300 import _lib
+    h = ctypes.c_void_p()
+    th = np.array([0.5, np.pi - 0.5])
+    p0 = np.zeros(2)
+    nph = np.array([8, 8], dtype=np.int64)
+    ofs = np.array([0, 8], dtype=np.int64)
+    rc = lib.cunusht_plan_create(ctypes.byref(h), 0, 1e-7, 0, 0, 2, th.ctypes.data, p0.ctypes.data,
+                                 nph.ctypes.data, ofs.ctypes.data)
+    assert rc == 1 and b"lmax" in lib.cunusht_last_error()
+    rc = lib.cunusht_plan_create(ctypes.byref(h), 3, 1e-7, 0, 5, 2, th.ctypes.data, p0.ctypes.data,
+                                 nph.ctypes.data, ofs.ctypes.data)
+    assert rc == 1 and b"max_spin" in lib.cunusht_last_error()
+    rc = lib.cunusht_doubling(None, 4, 8, 0, 0, 0, None, None)
+    assert rc == 1
+    rc = lib.cunusht_nusht2d2(None, 0, 1, None, 0, None, 0, 0, None, None, 0, None)
+    assert rc == 1 and b"plan" in lib.cunusht_last_error()
+    with pytest.raises(_lib.CunushtError):
+        _lib.check(rc)
+
+
+def test_gl_geometry_matches_oracle():
+    from cunusht_gb300 import get_geom
+    from oracle import oracle as orc
+    for lmax, nphi in [(31, None), (255, 511), (2047, 4095)]:
+        gi = {"lmax": lmax} if nphi is None else {"lmax": lmax, "nphi": nphi}
+        g = get_geom(("gl", gi))
+        th, p0, nph, ofs, w = orc.gl_geometry(lmax, nphi)
+        np.testing.assert_allclose(g.theta, th, atol=1e-14)
+        assert np.array_equal(g.nph.astype(np.int64), nph) and np.array_equal(g.ofs.astype(np.int64), ofs)
+        np.testing.assert_allclose(g.weight, w, rtol=1e-12)
+        assert abs(g.fsky() - 1.0) < 1e-12
+
+
+def test_alm_utils_match_reference_semantics():
+    from cunusht_gb300 import Alm, almxfl, alm2cl, synalm
+    from oracle import oracle as orc
+    L = 40
+    assert Alm.getsize(L, L) == orc.nalm(L)
+    assert Alm.getidx(L, 5, 3) == orc.almidx(L, 5, 3)
+    assert Alm.getlmax(orc.nalm(L), L) == L
+    cl = orc.cl_unlensed(L)
+    a = synalm(cl, L, L, rng=np.random.default_rng(3))
+    b = orc.synalm(cl, L, np.random.default_rng(3))
+    np.testing.assert_allclose(a, b)
+    np.testing.assert_allclose(alm2cl(a, None, L, L, L), orc.alm2cl(a, L))
+    fl = np.arange(L + 1.0)
+    np.testing.assert_allclose(almxfl(a, fl, L, False), orc.almxfl(a, fl, L))
+
+
+def test_loc_layout_detection():
+    torch = pytest.importorskip("torch")
+    from cunusht_gb300.transformer import _loc_args
+    loc = torch.arange(20, dtype=torch.float64).reshape(10, 2)
+    t, n, lay = _loc_args(loc)
+    assert (n, lay) == (10, 0)
+    ptg = torch.arange(20, dtype=torch.float64).reshape(2, 10)
+    t, n, lay = _loc_args(ptg.t())  # reference passes ptg.T as loc
+    assert (n, lay) == (10, 1) and t.data_ptr() == ptg.data_ptr()
+    t, n, lay = _loc_args(ptg)
+    assert (n, lay) == (10, 1)
+
+
+def test_factory_surface():
+    import cunusht_gb300 as cu
+    from cunusht_gb300.transformer import GPU_cufinufft_transformer, GPU_SHT_transformer
+    assert cu.get_transformer("GPU") is GPU_cufinufft_transformer
+    assert cu.get_transformer("GPU", "cufinufft", "nuFFT") is GPU_cufinufft_transformer
+    assert cu.get_transformer("GPU", "shtns", "SHT") is GPU_SHT_transformer
+    with pytest.raises(ValueError):
+        cu.get_transformer("CPU")
+    with pytest.raises(ValueError):
+        cu.get_transformer("GPU", "nope")
+    with pytest.raises(NotImplementedError):
+        cu.set_transformer(None)
