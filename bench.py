@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Benchmark: lensing solves/s at lmax 2047, spin 2, epsilon 1e-7.
+
+A step is one lensing solve on one request: dlm2pointing (spin-1 synthesis of
+the deflection on the GL 2048 x 4095 grid + pointing rotation) followed by the
+spin-2 nusht2d2 of the E-mode alm at the deflected points with the exp(2 i
+gamma) polarisation rotation -- the reference's gclm2lenmap
+(cunusht/deflection/GPU_nufft_transformer.py:487-578) without its pointing cache
+(a fresh deflection field every step).
+
+  value  inputs resident in HBM, calls through the C ABI (whole job, all ranks)
+  e2e    the public API (GPU_cufinufft_transformer.gclm2lenmap) from pinned host
+         buffers: H2D of gclm + dlm, the solve, D2H of the lensed Q/U map,
+         every step, inside the timed region
+Multi-GPU (torchrun): independent replicas per rank (weak scaling), timed with
+a barrier on both sides, max over ranks.
+
+--impl reference times the reference algorithm's CPU path: the reference's CPU
+backend needs ducc0 / lenspyx, which are absent, so the FP64 CPU oracle port
+(direct summation on all host cores) runs a bounded sample of pixels per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--lmax", type=int, default=2047)
+    p.add_argument("--nphi", type=int, default=None, help="pixels per GL ring (default 2 lmax + 1)")
+    p.add_argument("--spin", type=int, default=2)
+    p.add_argument("--eps", type=float, default=1e-7)
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "auto"])
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the cpu_baseline sample")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        rows = [r for r in self.rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------- workload
+def synth_inputs(lmax: int, spin: int, seed: int):
+    """Seeded synthetic fields of the benchmark configuration (restated from the
+    configuration text, independent of the oracle): gclm E ~ CN(0, 0.1 C_l),
+    B = 0 (spin 2) or T ~ CN(0, C_l) (spin 0), C_l = 1e3/(l+10)^2; lensing
+    potential phi_lm ~ CN(0, 4e-7 (l+20)^-4) rescaled to 2.5' rms deflection;
+    returns gclm (ncomp, nalm), dlm_scaled (nalm,) complex128."""
+    from cunusht_gb300.utils import synalm, alm2cl, almxfl
+    rng = np.random.default_rng(seed)
+    ll = np.arange(lmax + 1, dtype=np.float64)
+    cl = 1e3 / (ll + 10.0) ** 2
+    if spin == 0:
+        g = synalm(cl, lmax, lmax, rng)[None]
+    else:
+        e = synalm(0.1 * cl, lmax, lmax, rng)
+        g = np.stack([e, np.zeros_like(e)])
+    plm = synalm(4e-7 * (ll + 20.0) ** -4, lmax, lmax, rng)
+    dlm = almxfl(plm, np.sqrt(ll * (ll + 1.0)), lmax, False)
+    rms = np.sqrt(np.sum(alm2cl(dlm, None, lmax, lmax, lmax) * (2 * ll + 1)) / (4 * np.pi))
+    plm *= (2.5 / 60.0 * np.pi / 180.0) / rms
+    return g, plm
+
+
+def stage_quantities(info, lmax, spin, nring, npix):
+    """Algorithmic bytes (or flops) per launch of each stage: every array read
+    or written once; Legendre contraction 8 flops per (l, m, ring) per
+    component for spin > 0, 4 for spin 0."""
+    nalm = (lmax + 1) * (lmax + 2) // 2
+    ncc = info["ntheta_torus"] // 2 + 1
+    ncols = 2 * lmax + 1 if spin else lmax + 1
+    nrows, npf = info["fine_rows"], info["nphi_fine"]
+    c = 16  # complex128
+    ncomp = 2 if spin else 1
+    grid_cell = (8 if info.get("grid_fp32") else 16) if spin else (4 if info.get("grid_fp32") else 8)
+    q = {
+        "leg_synth": ("flops", (8 if spin else 4) * ncomp * nalm * ncc),
+        "theta_fwd": ("bytes", ncols * ncc * c + nrows * ncols * c),
+        "phi_fwd": ("bytes", nrows * ncols * c + nrows * npf * grid_cell),
+        "interp": ("bytes", nrows * npf * grid_cell + npix * (16 + (8 if spin else 0) + 8 * ncomp)),
+        "ptg_leg": ("flops", 8 * nalm * nring),
+        "ptg_ring": ("bytes", (2 * lmax + 1) * nring * c + 2 * npix * 8),
+        "ptg_rot": ("bytes", 2 * npix * 8 + 3 * npix * 8),
+    }
+    return q
+
+
+# ----------------------------------------------------------------------------- cpu baseline
+def cpu_sample(lmax, nphi, spin, gclm, plm, npix_target_s: float, threads: int, max_pixels=None, fixed=None):
+    """Time the FP64 oracle port on a sample of pixels of the lensing solve:
+    deflection (spin-1 direct sum) + pointing + spin-s direct sum at the
+    deflected points + rotation.  Returns (seconds, npix_sample, values)."""
+    import oracle
+    from oracle import oracle as orc
+    th, p0, nph, ofs, _ = orc.gl_geometry(lmax, nphi)
+    tpix, ppix = orc.geometry_pixels(th, p0, nph, ofs)
+    ll = np.arange(lmax + 1)
+    dlm = orc.almxfl(plm, np.sqrt(ll * (ll + 1.0)), lmax)
+    rng = np.random.default_rng(123)
+
+    def run(n):
+        idx = np.sort(rng.choice(tpix.size, n, replace=False))
+        t0 = time.perf_counter()
+        d = oracle.synth_points_c(lmax, 1, dlm[None], tpix[idx], ppix[idx], nthreads=threads)
+        rt, rp = orc.pointing(tpix[idx], ppix[idx], d[0], d[1])
+        v = oracle.synth_points_c(lmax, spin, gclm if spin else gclm[0], rt, rp, nthreads=threads)
+        if spin:
+            z = (v[0] + 1j * v[1]) * np.exp(1j * spin * orc.rotation_gamma(tpix[idx], d[0], d[1]))
+            v = np.stack([z.real, z.imag])
+        return time.perf_counter() - t0, idx, v
+
+    if fixed is not None:
+        dt, idx, v = run(fixed)
+        return dt, idx, v, tpix.size
+    n = 16
+    dt, idx, v = run(n)
+    while dt < 0.5 * npix_target_s and (max_pixels is None or n < max_pixels):
+        n = int(min(n * max(2.0, 0.8 * npix_target_s / max(dt, 1e-3)), tpix.size))
+        dt, idx, v = run(n)
+    return dt, idx, v, tpix.size
+
+
+def reference_arm(args):
+    """--impl reference: the reference algorithm's CPU path on host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    lmax, spin = args.lmax, args.spin
+    nphi = args.nphi or 2 * lmax + 1
+    threads = os.cpu_count() or 1
+    gclm, plm = synth_inputs(lmax, spin, seed=1)
+    budget = min(15.0, max(1.0, 120.0 / max(1, args.steps + args.warmup)))
+    # size the sample so that one step is about `budget` seconds, then time K steps
+    _, idx, _, npix = cpu_sample(lmax, nphi, spin, gclm, plm, budget, threads)
+    n = idx.size
+    for _ in range(args.warmup):
+        cpu_sample(lmax, nphi, spin, gclm, plm, 0.0, threads, max_pixels=max(16, n // 10))
+    times = []
+    for _ in range(args.steps):
+        t, idx_k, _, _ = cpu_sample(lmax, nphi, spin, gclm, plm, 0.0, threads, max_pixels=n, fixed=n)
+        times.append(t / idx_k.size * npix)
+    solve_s = float(np.mean(times))
+    val = 1.0 / solve_s
+    line = {"metric": METRIC, "value": val, "unit": "solves/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian alm / deflection, 2.5 arcmin rms)",
+            "config": {"workload": f"lensing solve lmax={lmax} GL {lmax + 1}x{nphi} spin-{spin} eps={args.eps}"},
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{n} of {npix} pixels per step (exact FP64 direct summation: "
+                                       "deflection, pointing, spin-2 synthesis, rotation), extrapolated; "
+                                       "reference CPU backend needs ducc0/lenspyx (absent)"},
+            "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------- main arm
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+
+    from cunusht_gb300 import build as _b
+    _b.build()
+    import cunusht_gb300 as cu
+
+    lmax, spin, eps = args.lmax, args.spin, args.eps
+    nphi = args.nphi or 2 * lmax + 1
+    T = cu.get_transformer("GPU")(("gl", {"lmax": lmax, "nphi": nphi}), nuFFTtype=2, epsilon=eps,
+                                  precision=args.precision, max_spin=max(spin, 1))
+    npix, nring = T.npix(), lmax + 1
+    gclm_h, plm_a = synth_inputs(lmax, spin, seed=1 + 17 * rank)
+    _, plm_b = synth_inputs(lmax, spin, seed=2 + 17 * rank)
+    ncomp = gclm_h.shape[0]
+    G = torch.as_tensor(gclm_h if spin else gclm_h[0], device=dev)
+    D = [torch.as_tensor(plm_a, device=dev), torch.as_tensor(plm_b, device=dev)]
+    out = torch.empty((2, npix) if spin else (npix,), dtype=torch.float64, device=dev)
+    ptg = torch.empty((2, npix), dtype=torch.float64, device=dev)
+    gam = torch.empty((npix,), dtype=torch.float64, device=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def maxall(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---------------- device-resident timing (value)
+    for i in range(args.warmup):
+        T.lensing_solve(G, D[i % 2], out, ptg, gam, spin)
+    torch.cuda.synchronize()
+    T.profile(True)
+    T.stage_times()
+    clk = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if clk:
+        clk.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record()
+    for k in range(args.steps):
+        T.lensing_solve(G, D[k % 2], out, ptg, gam, spin)
+        ev[k + 1].record()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = clk.stop() if clk else None
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_s = ev[0].elapsed_time(ev[-1]) * 1e-3
+    stages = T.stage_times()
+    T.profile(False)
+    total_s = maxall(total_s)
+    value = world * args.steps / total_s
+    launches = int(sum(c for _, c in stages.values()))
+
+    # ---------------- roofline of the dominant stage
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    info = dict(T.info, grid_fp32=bool(T.single_prec and args.precision != "fp64"))
+    q = stage_quantities(info, lmax, spin, nring, npix)
+    dom = max(stages, key=lambda s: stages[s][0])
+    avg_s = stages[dom][0] / stages[dom][1] * 1e-3
+    kind, amount = q.get(dom, ("bytes", 0))
+    if kind == "bytes":
+        ach = amount / avg_s / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": None, "kernel": dom,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    else:
+        ach = amount / avg_s / 1e12
+        peak = 1.25
+        roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": None, "kernel": dom, "peak_source": "nominal GB300 FP64 (no measured FP64 peak)"}
+    stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
+                       "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
+    for s, v in stage_table.items():
+        if s in q:
+            kind, amount = q[s]
+            v["algorithmic_" + kind] = amount
+            v["achieved"] = amount / (v["ms_per_launch"] * 1e-3) / (1e9 if kind == "bytes" else 1e12)
+            v["unit"] = "GB/s" if kind == "bytes" else "TFLOP/s"
+
+    # ---------------- end to end through the public API
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.as_tensor(a).pin_memory()
+        Gh = pin(gclm_h if spin else gclm_h[0])
+        Dh = [pin(plm_a), pin(plm_b)]
+        res_h = torch.empty((2, npix) if spin else (npix,), dtype=torch.float64).pin_memory()
+        for i in range(args.warmup):
+            g = Gh.to(dev, non_blocking=True)
+            d = Dh[i % 2].to(dev, non_blocking=True)
+            r = T.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0)
+            res_h.copy_(r, non_blocking=True)
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for k in range(args.steps):
+            g = Gh.to(dev, non_blocking=True)
+            d = Dh[k % 2].to(dev, non_blocking=True)
+            r = T.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0)
+            res_h.copy_(r, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        barrier()
+        e2e_s = maxall(e0.elapsed_time(e1) * 1e-3)
+        e2e = {"value": world * args.steps / e2e_s, "unit": "solves/s",
+               "h2d_bytes_per_step": int(Gh.numel() * Gh.element_size() + Dh[0].numel() * Dh[0].element_size()),
+               "d2h_bytes_per_step": int(res_h.numel() * res_h.element_size()),
+               "ms_per_step": e2e_s * 1e3 / args.steps}
+
+    # ---------------- CPU baseline (rank 0, N=1 only) + accuracy of the same sample
+    cpu = None
+    acc = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        dt, idx, ref, npix_all = cpu_sample(lmax, nphi, spin, gclm_h, plm_a, args.cpu_seconds, threads)
+        cpu_val = 1.0 / (dt / idx.size * npix_all)
+        cpu = {"value": cpu_val, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"{idx.size} of {npix_all} pixels (exact FP64 direct summation of the solve), "
+                         "extrapolated to the full map"}
+        T.lensing_solve(G, D[0], out, ptg, gam, spin)
+        got = out.cpu().numpy()
+        got = got[:, idx] if spin else got[idx]
+        acc = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+
+    if rank == 0:
+        p50, p99 = np.percentile(step_ms, [50, 99])
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if T.info["precision"] == 1 or not T.single_prec else "f64-legendre+f32-grid",
+                "data": "synthetic (seeded Gaussian alm / deflection, 2.5 arcmin rms)",
+                "config": {"workload": f"lensing solve lmax={lmax} GL {lmax + 1}x{nphi} spin-{spin} eps={eps}",
+                           "precision": args.precision, "requests_per_launch": 1,
+                           "l2": "working set > L2 (fine grid %d MB per solve)" %
+                                 (T.info["fine_rows"] * T.info["nphi_fine"] * (16 if spin else 8) // 2 ** 20)},
+                "p50_ms": float(p50), "p99_ms": float(p99),
+                "roofline": roof, "stages": stage_table, "gpu_launches": launches,
+                "e2e": e2e, "cpu_baseline": cpu, "rel_err_vs_fp64_oracle_sample": acc, "clocks": clocks}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

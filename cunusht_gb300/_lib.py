@@ -13,6 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcunusht_gb300.so")
 
 OK = 0
+NSTAGE = 11
+STAGES = ["leg_synth", "theta_fwd", "phi_fwd", "interp", "spread", "phi_adj", "theta_adj", "leg_adj",
+          "ptg_leg", "ptg_ring", "ptg_rot"]
 F64 = 0
 F32 = 1
 PREC_AUTO, PREC_FP64, PREC_MIXED = 0, 1, 2
@@ -28,6 +31,8 @@ SIGNATURES = {
     "cunusht_plan_create": (_i, [ctypes.POINTER(_vp), _i, _d, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "cunusht_plan_destroy": (_i, [_vp]),
     "cunusht_plan_info": (_i, [_vp, _vp, _i]),
+    "cunusht_plan_set_profiling": (_i, [_vp, _i]),
+    "cunusht_plan_stage_times": (_i, [_vp, _vp, _vp, _i]),
     "cunusht_nusht2d2": (_i, [_vp, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _i, _vp]),
     "cunusht_nusht2d1": (_i, [_vp, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _i, _vp]),
     "cunusht_dlm2pointing": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _vp]),

@@ -119,6 +119,10 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (auto &e : P->evt_pool) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
     delete P;
 }
 
@@ -341,6 +345,37 @@ static int check_spin(const cunusht_plan_s *P, int spin, int ncomp) {
     return CUNUSHT_OK;
 }
 
+
+// Brackets one stage launch with CUDA events when profiling is on.
+struct StageScope {
+    cunusht_plan_s *P;
+    int stage;
+    cudaStream_t st;
+    int slot = -1;
+    StageScope(cunusht_plan_s *P_, int stage_, cudaStream_t st_) : P(P_), stage(stage_), st(st_) {
+        if (!P->profiling) return;
+        if (P->evt_used >= (int)P->evt_pool.size()) flush_events(P);
+        if (P->evt_used >= (int)P->evt_pool.size()) return;
+        slot = P->evt_used++;
+        P->evt_pool[slot].stage = stage;
+        cudaEventRecord(P->evt_pool[slot].a, st);
+    }
+    ~StageScope() {
+        if (slot >= 0) cudaEventRecord(P->evt_pool[slot].b, st);
+    }
+    static void flush_events(cunusht_plan_s *P) {
+        for (int i = 0; i < P->evt_used; ++i) {
+            auto &e = P->evt_pool[i];
+            float ms = 0.f;
+            if (cudaEventSynchronize(e.b) == cudaSuccess && cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+                P->stage_ms[e.stage] += ms;
+                P->stage_cnt[e.stage] += 1;
+            }
+        }
+        P->evt_used = 0;
+    }
+};
+
 }  // namespace cunusht
 
 using namespace cunusht;
@@ -389,6 +424,35 @@ int cunusht_plan_info(const cunusht_plan_t *P, int64_t *info, int ninfo) {
     return n;
 }
 
+int cunusht_plan_set_profiling(cunusht_plan_t *P, int enable) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    if (enable && P->evt_pool.empty()) {
+        P->evt_pool.resize(4096);
+        for (auto &e : P->evt_pool) {
+            CU_TRY(cudaEventCreate(&e.a));
+            CU_TRY(cudaEventCreate(&e.b));
+        }
+    }
+    P->profiling = enable != 0;
+    return CUNUSHT_OK;
+}
+
+int cunusht_plan_stage_times(cunusht_plan_t *P, double *ms, int64_t *count, int nstage) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    StageScope::flush_events(P);
+    for (int i = 0; i < CUNUSHT_NSTAGE; ++i) {
+        if (i < nstage) {
+            if (ms) ms[i] = P->stage_ms[i];
+            if (count) count[i] = P->stage_cnt[i];
+        }
+        P->stage_ms[i] = 0.0;
+        P->stage_cnt[i] = 0;
+    }
+    return CUNUSHT_OK;
+}
+
 int cunusht_nusht2d2(cunusht_plan_t *P, int spin, int ncomp, const void *alm, int alm_dtype, const double *loc,
                      int64_t npts, int loc_layout, const double *gamma, void *out, int out_dtype, void *stream) {
     clear_error();
@@ -409,10 +473,10 @@ int cunusht_nusht2d2(cunusht_plan_t *P, int spin, int ncomp, const void *alm, in
         G = P->d_alm;
         if (ncomp > 1) C = P->d_alm + P->nalm;
     }
-    RC_TRY(leg_synth(P, spin, G, C, false, true, P->d_H, st));
-    RC_TRY(theta_fwd(P, spin, P->d_H, P->d_F, st));
-    RC_TRY(phi_fwd(P, spin, P->d_F, P->d_U, st));
-    RC_TRY(nufft_interp(P, spin, loc, npts, loc_layout, spin ? gamma : nullptr, out, out_dtype, st));
+    { StageScope sc(P, CUNUSHT_STAGE_LEG_SYNTH, st); RC_TRY(leg_synth(P, spin, G, C, false, true, P->d_H, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_THETA_FWD, st); RC_TRY(theta_fwd(P, spin, P->d_H, P->d_F, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_PHI_FWD, st); RC_TRY(phi_fwd(P, spin, P->d_F, P->d_U, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_INTERP, st); RC_TRY(nufft_interp(P, spin, loc, npts, loc_layout, spin ? gamma : nullptr, out, out_dtype, st)); }
     return CUNUSHT_OK;
 }
 
@@ -428,12 +492,12 @@ int cunusht_nusht2d1(cunusht_plan_t *P, int spin, int ncomp, const void *map, in
     ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
     ARG_CHECK(map_dtype == CUNUSHT_F64 || map_dtype == CUNUSHT_F32, "bad map dtype");
     cudaStream_t st = (cudaStream_t)stream;
-    RC_TRY(nufft_spread(P, spin, loc, npts, loc_layout, spin ? gamma : nullptr, map, map_dtype, st));
-    RC_TRY(phi_adj(P, spin, P->d_U, P->d_F, st));
-    RC_TRY(theta_adj(P, spin, P->d_F, P->d_H, st));
+    { StageScope sc(P, CUNUSHT_STAGE_SPREAD, st); RC_TRY(nufft_spread(P, spin, loc, npts, loc_layout, spin ? gamma : nullptr, map, map_dtype, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_PHI_ADJ, st); RC_TRY(phi_adj(P, spin, P->d_U, P->d_F, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_THETA_ADJ, st); RC_TRY(theta_adj(P, spin, P->d_F, P->d_H, st)); }
     double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
     double2 *C = G + P->nalm;
-    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_H, false, true, G, C, st));
+    { StageScope sc(P, CUNUSHT_STAGE_LEG_ADJ, st); RC_TRY(leg_adjoint(P, spin, ncomp, P->d_H, false, true, G, C, st)); }
     if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
     return CUNUSHT_OK;
 }
@@ -454,10 +518,13 @@ int cunusht_dlm2pointing(cunusht_plan_t *P, const void *dlm, const void *dclm, i
             C = P->d_alm + P->nalm;
         }
     }
-    RC_TRY(leg_synth(P, 1, G, C, true, false, P->d_Hgl, st));
-    RC_TRY(ring_synth(P, 1, P->d_Hgl, P->d_glmap, P->d_glmap + P->npix, st));
-    RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->npix,
-                           P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
+    { StageScope sc(P, CUNUSHT_STAGE_PTG_LEG, st); RC_TRY(leg_synth(P, 1, G, C, true, false, P->d_Hgl, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_PTG_RING, st); RC_TRY(ring_synth(P, 1, P->d_Hgl, P->d_glmap, P->d_glmap + P->npix, st)); }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_ROT, st);
+        RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->npix,
+                               P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
+    }
     return CUNUSHT_OK;
 }
 

@@ -171,4 +171,15 @@ struct cunusht_plan_s {
     double *d_glmap = nullptr; // spin-1 maps on pointing grid       [2][npix]
     double2 *d_alm = nullptr;  // alm staging (dtype conversion)     [2][nalm]
     size_t ws_bytes = 0;
+
+    // per-stage CUDA-event timing (cunusht_plan_set_profiling)
+    bool profiling = false;
+    struct StageEvt {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    std::vector<StageEvt> evt_pool;  // created once, reused
+    int evt_used = 0;
+    double stage_ms[CUNUSHT_NSTAGE] = {0};
+    long long stage_cnt[CUNUSHT_NSTAGE] = {0};
 };

@@ -278,6 +278,37 @@ class GPU_cufinufft_transformer:
     def set_pts(self, ptg):
         self.ptg = to_device(ptg, "ptg", torch.float64)
 
+    # -------------------------------------------------------------- profiling
+    def profile(self, enable: bool = True):
+        """Bracket every stage launch with CUDA events on the caller's stream."""
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        _lib.check(self._lib.cunusht_plan_set_profiling(self._plan, int(enable)))
+
+    def stage_times(self) -> dict:
+        """{stage: (total ms, launches)} since the last call (then reset)."""
+        ms = (ctypes.c_double * _lib.NSTAGE)()
+        cnt = (ctypes.c_int64 * _lib.NSTAGE)()
+        _lib.check(self._lib.cunusht_plan_stage_times(self._plan, ms, cnt, _lib.NSTAGE))
+        return {n: (ms[i], cnt[i]) for i, n in enumerate(_lib.STAGES) if cnt[i]}
+
+    def lensing_solve(self, gclm: torch.Tensor, dlm_scaled: torch.Tensor, out: torch.Tensor, ptg: torch.Tensor,
+                      gamma: torch.Tensor, spin: int, dclm_scaled: torch.Tensor | None = None):
+        """One uncached lensing solve on device tensors (dlm2pointing + nusht2d2
+        with rotation), no host synchronisation: the serving / benchmark step."""
+        ncomp = 1 if gclm.dim() == 1 else gclm.shape[0]
+        adt = _lib.F32 if gclm.dtype == torch.complex64 else _lib.F64
+        s = _stream()
+        _lib.check(self._lib.cunusht_dlm2pointing(self._plan, dlm_scaled.data_ptr(),
+                                                  dclm_scaled.data_ptr() if dclm_scaled is not None else None,
+                                                  _lib.F64 if dlm_scaled.dtype == torch.complex128 else _lib.F32,
+                                                  ptg.data_ptr(), gamma.data_ptr(), s))
+        odt = _lib.F32 if out.dtype == torch.float32 else _lib.F64
+        _lib.check(self._lib.cunusht_nusht2d2(self._plan, spin, ncomp, gclm.data_ptr(), adt, ptg.data_ptr(),
+                                              ptg.shape[1], 1, gamma.data_ptr() if spin else None,
+                                              out.data_ptr(), odt, s))
+        return out
+
     # -------------------------------------------------------------- lensing
     def _spin_of(self, gclm, spin):
         if spin is not None:

@@ -67,6 +67,30 @@ int cunusht_plan_create(cunusht_plan_t **plan, int lmax, double epsilon, int pre
                         const int64_t *ring_ofs);
 int cunusht_plan_destroy(cunusht_plan_t *plan);
 
+/*
+ * Per-stage timing.  When enabled, every stage launch of this plan is
+ * bracketed by CUDA events recorded on the caller's stream (no extra
+ * synchronisation); cunusht_plan_stage_times waits for the recorded events,
+ * returns per stage the summed milliseconds and launch counts since the last
+ * query, and resets them.  Replaces the reference's timing_decorator /
+ * execmode='timing' (cunusht/helper_GPU.py:10-51), which synchronised the
+ * device around every stage.
+ */
+#define CUNUSHT_STAGE_LEG_SYNTH 0    /* Legendre synthesis, CC rings      */
+#define CUNUSHT_STAGE_THETA_FWD 1    /* theta pass (FFT, deconv, pad, iFFT) */
+#define CUNUSHT_STAGE_PHI_FWD 2      /* phi pass to the fine grid          */
+#define CUNUSHT_STAGE_INTERP 3       /* nuFFT interpolation (type 2)       */
+#define CUNUSHT_STAGE_SPREAD 4       /* nuFFT spreading (type 1)           */
+#define CUNUSHT_STAGE_PHI_ADJ 5      /* adjoint phi pass                   */
+#define CUNUSHT_STAGE_THETA_ADJ 6    /* adjoint theta pass                 */
+#define CUNUSHT_STAGE_LEG_ADJ 7      /* Legendre adjoint, CC rings         */
+#define CUNUSHT_STAGE_PTG_LEG 8      /* spin-1 Legendre on pointing rings  */
+#define CUNUSHT_STAGE_PTG_RING 9     /* ring (phi) transform, pointing     */
+#define CUNUSHT_STAGE_PTG_ROT 10     /* pointing rotation                  */
+#define CUNUSHT_NSTAGE 11
+int cunusht_plan_set_profiling(cunusht_plan_t *plan, int enable);
+int cunusht_plan_stage_times(cunusht_plan_t *plan, double *ms, int64_t *count, int nstage);
+
 /* Plan sizes: info[0]=npix, [1]=torus theta length, [2]=torus phi length,
  * [3]=fine grid theta length, [4]=fine grid phi length, [5]=kernel width,
  * [6]=fine rows stored, [7]=workspace bytes, [8]=precision in use,
