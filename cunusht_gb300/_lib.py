@@ -41,6 +41,7 @@ SIGNATURES = {
     "cunusht_pointing": (_i, [_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cunusht_doubling": (_i, [_vp, _i64, _i64, _i, _i, _i, _vp, _vp]),
     "cunusht_adjoint_doubling": (_i, [_vp, _i64, _i64, _i, _i, _vp, _vp]),
+    "cunusht_synthesis_noalloc": (_i, [_i, _i, _i, _vp, _i, _vp, _vp, _i, _vp, _vp]),
 }
 
 

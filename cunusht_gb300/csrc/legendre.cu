@@ -99,6 +99,13 @@ int build_coef_tables(cunusht_plan_s *P, cudaStream_t st) {
     return CUNUSHT_OK;
 }
 
+int build_coef_tables_spin(const cunusht_plan_s *P, int spin, double *coef, cudaStream_t st) {
+    const int nb = (int)((P->nalm + 255) / 256);
+    k_build_coef<<<nb, 256, 0, st>>>(P->lmax, spin, coef, P->nalm);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
 // ---------------------------------------------------------------- synthesis, spin 0
 constexpr int LEG_TPB = 128;
 constexpr int LEG_CH = 128;

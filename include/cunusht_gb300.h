@@ -171,6 +171,33 @@ int cunusht_doubling(const void *cc_map, int64_t ntheta, int64_t nphi, int layou
 int cunusht_adjoint_doubling(const void *dmap, int64_t ntheta, int64_t nphi, int spin, int dtype,
                              void *out, void *stream);
 
+/*
+ * Spin-s synthesis on a small ring geometry that allocates no device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- code running inside another framework's memory pool, which
+ * owns all device memory, latency-critical pipelines that forbid allocation
+ * after start-up (cudaMalloc can synchronise the device), and plugin hosts
+ * that give a plugin no allocator.  The caller passes the alm (complex128,
+ * device, ncomp x nalm) and the output map (device, npix or 2 x npix float64,
+ * ring i at pixels [i nphi, (i + 1) nphi)); ring colatitudes and first
+ * longitudes are host arrays and the rings must be north/south symmetric.
+ * Every intermediate lives in one file-scope device array of
+ * CUNUSHT_NOALLOC_SCRATCH_BYTES that each GPU loading the library holds until
+ * the process exits; sizes beyond the CUNUSHT_NOALLOC_MAX_* limits are
+ * rejected with CUNUSHT_ERR_ARG.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture.  All calls share the one array,
+ * so calls that overlap on the GPU (different streams or host threads) race.
+ * Same math as cunusht_synthesis; nothing is allocated and nothing freed.
+ */
+#define CUNUSHT_NOALLOC_SCRATCH_BYTES (4u * 1024u * 1024u)
+#define CUNUSHT_NOALLOC_MAX_LMAX 255
+#define CUNUSHT_NOALLOC_MAX_NRING 256
+#define CUNUSHT_NOALLOC_MAX_NPHI 1024
+int cunusht_synthesis_noalloc(int lmax, int spin, int ncomp, const void *alm, int nring,
+                              const double *ring_theta, const double *ring_phi0, int nphi,
+                              double *map, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
