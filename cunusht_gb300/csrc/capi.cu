@@ -115,7 +115,7 @@ static void free_plan(cunusht_plan_s *P) {
     void *ptrs[] = {P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->d_gl_x, P->d_gl_sh,
                     P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
-                    P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_tw64, P->d_tw32, P->d_chirp, P->d_bker,
+                    P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_chirp, P->d_bker,
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -269,6 +269,10 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         RC_TRY(upload(P, &P->d_lg0[s], lg));
     }
     RC_TRY(build_coef_tables(P, 0));
+    if (P->prec == CUNUSHT_PREC_MIXED) {
+        for (int s = 0; s <= 2; ++s) RC_TRY(dalloc(P, &P->d_coef_df[s], 3 * (size_t)P->nalm));
+        RC_TRY(build_coef_tables_df(P, 0));
+    }
     {
         std::vector<double> lf(lmax + 1);
         for (int l = 0; l <= lmax; ++l) lf[l] = std::sqrt((double)l * (l + 1.0));

@@ -151,6 +151,7 @@ struct cunusht_plan_s {
     double *d_coef[3] = {nullptr, nullptr, nullptr};
     double *d_lg0[3] = {nullptr, nullptr, nullptr};  // per m: log2 start normalisation
     double *d_lfac = nullptr;                        // sqrt(l(l+1)), l = 0..L
+    float2 *d_coef_df[3] = {nullptr, nullptr, nullptr};  // the same tables as (hi, lo) FP32 pairs
 
     // FFT twiddles e^{-2 pi i t / TW}
     int TW = 0;

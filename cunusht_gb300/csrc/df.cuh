@@ -1,0 +1,89 @@
+// Double-float ("df") arithmetic: a value is hi + lo with two FP32 numbers,
+// about 48 significant bits.  Error-free transformations (Knuth TwoSum,
+// FMA-based TwoProduct; Dekker 1971) on the FP32 pipe, which on GB300 runs
+// about 60 times the FP64 instruction rate.  Only additions, subtractions and
+// explicit fmaf are used, so FMA contraction cannot change the error terms.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace cunusht {
+
+struct dfl {
+    float h, l;
+};
+
+__device__ __forceinline__ dfl df_from(double x) {
+    dfl r;
+    r.h = (float)x;
+    r.l = (float)(x - (double)r.h);
+    return r;
+}
+
+__device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
+
+// hi/lo renormalisation, |a| >= |b| assumed (Fast2Sum)
+__device__ __forceinline__ dfl df_fast(float a, float b) {
+    dfl r;
+    r.h = a + b;
+    r.l = b - (r.h - a);
+    return r;
+}
+
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return df_fast(p, e);
+}
+
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    float e = (a.h - (s - bb)) + (b.h - bb);
+    e += a.l + b.l;
+    return df_fast(s, e);
+}
+
+// t * x - b * y in one renormalisation
+__device__ __forceinline__ dfl df_mul_sub(dfl t, dfl x, dfl b, dfl y) {
+    const float p1 = t.h * x.h;
+    float e1 = fmaf(t.h, x.h, -p1);
+    e1 = fmaf(t.h, x.l, e1);
+    e1 = fmaf(t.l, x.h, e1);
+    const float p2 = b.h * y.h;
+    float e2 = fmaf(b.h, y.h, -p2);
+    e2 = fmaf(b.h, y.l, e2);
+    e2 = fmaf(b.l, y.h, e2);
+    const float s = p1 - p2;
+    const float bb = s - p1;
+    float e = (p1 - (s - bb)) + (-p2 - bb);
+    e += e1 - e2;
+    return df_fast(s, e);
+}
+
+__device__ __forceinline__ dfl df_scale(dfl a, float s) {
+    dfl r;
+    r.h = a.h * s;
+    r.l = a.l * s;
+    return r;
+}
+
+// Kahan-compensated FP32 sum: value = s - c
+struct kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float p) {
+        const float y = p - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// a * lam with both operands as df, rounded once to FP32
+__device__ __forceinline__ float df_prod(float ah, float al, dfl lam) {
+    return fmaf(ah, lam.h, fmaf(al, lam.h, ah * lam.l));
+}
+
+}  // namespace cunusht

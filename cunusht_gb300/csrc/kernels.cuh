@@ -8,6 +8,7 @@ constexpr int FFT_TPB = 512;
 
 // legendre.cu
 int build_coef_tables(cunusht_plan_s *P, cudaStream_t st);
+int build_coef_tables_df(cunusht_plan_s *P, cudaStream_t st);
 int build_coef_tables_spin(const cunusht_plan_s *P, int spin, double *coef, cudaStream_t st);
 int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C,
               bool use_lfac, bool cc, double2 *H, cudaStream_t st);

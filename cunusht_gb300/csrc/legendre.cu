@@ -25,6 +25,7 @@
 // Output layout: H[c][ring], c = m (spin 0) or c = m + lmax (spin s, m in
 // [-lmax, lmax]), rings contiguous (ldH = ring count).
 #include "common.cuh"
+#include "df.cuh"
 #include "kernels.cuh"
 
 namespace cunusht {
@@ -247,6 +248,213 @@ __global__ void __launch_bounds__(LEG_TPB)
         if (m > 0) {
             H[(long long)(L - m) * ldH + n] = make_double2(-sgs * hmn.x, -sgs * hmn.y);
             if (s != n) H[(long long)(L - m) * ldH + s] = make_double2(-sgs * hms.x, -sgs * hms.y);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- mixed precision synthesis
+// Same recursion and accumulation pattern as the FP64 kernels, with the
+// recursion in double-float (FP32 hi/lo, ~48 bits) and each product a_lm * lam
+// formed from the hi/lo parts, rounded once to FP32 and added with Kahan
+// compensation.  The start mantissa is kept in FP32 range with an exponent in
+// steps of 96 (values below 2^-56 are not accumulated).
+__device__ __forceinline__ void rec_start_df(double lg0, int m, int s, double sh, double ch, dfl &cur,
+                                             dfl &prev, int &e) {
+    prev.h = prev.l = 0.f;
+    double lg = lg0;
+    bool zero = false;
+    if (m + s > 0) {
+        if (sh <= 0.0) zero = true;
+        else lg += (double)(m + s) * log2(sh);
+    }
+    if (m != s) {
+        if (ch <= 0.0) zero = true;
+        else lg += (double)abs(m - s) * log2(ch);
+    }
+    if (zero) {
+        cur.h = cur.l = 0.f;
+        e = 0;
+        return;
+    }
+    int k = 0;
+    if (lg < -40.0) k = (int)ceil((-40.0 - lg) / 96.0);
+    e = -96 * k;
+    double v = exp2(lg + 96.0 * (double)k);
+    if (m & 1) v = -v;
+    cur = df_from(v);
+}
+
+#define REC_RESCALE_DF(cur, prev, e)                                                     \
+    if ((e) < 0 && fabsf((cur).h) > 0x1p40f) {                                          \
+        (cur) = df_scale((cur), 0x1p-96f);                                               \
+        (prev) = df_scale((prev), 0x1p-96f);                                             \
+        (e) += 96;                                                                       \
+    }
+
+__global__ void k_split_coef(const double *__restrict__ c, long long n, float2 *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = c[i];
+    const float h = (float)v;
+    out[i] = make_float2(h, (float)(v - (double)h));
+}
+
+int build_coef_tables_df(cunusht_plan_s *P, cudaStream_t st) {
+    for (int s = 0; s <= 2; ++s) {
+        const long long n = 3 * P->nalm;
+        k_split_coef<<<(int)((n + 255) / 256), 256, 0, st>>>(P->d_coef[s], n, P->d_coef_df[s]);
+        CU_LAUNCH_CHECK();
+    }
+    return CUNUSHT_OK;
+}
+
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_synth_s0_df(int L, const double2 *__restrict__ alm, const double *__restrict__ lfac,
+                      const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
+                      int npairs, const double *__restrict__ px, const double *__restrict__ psh,
+                      const double *__restrict__ pch, const int *__restrict__ prn,
+                      const int *__restrict__ prs, double2 *__restrict__ H, int ldH) {
+    __shared__ float2 s_al[LEG_CH], s_be[LEG_CH];
+    __shared__ float4 s_a[LEG_CH];
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+    }
+    const dfl xd = df_from(x);
+    dfl cur, prev;
+    int e;
+    rec_start_df(lg0[m], m, 0, sh, ch, cur, prev, e);
+    kahan Er, Ei, Or, Oi;
+    const float2 *al = coef, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    for (int lb = m; lb <= L; lb += LEG_CH) {
+        const int cnt = min(LEG_CH, L - lb + 1);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += LEG_TPB) {
+            const long long ix = b + lb + i;
+            s_al[i] = al[ix];
+            s_be[i] = be[ix];
+            const double2 a = alm[ix];
+            const double f = lfac ? lfac[lb + i] : 1.0;
+            const dfl re = df_from(a.x * f), im = df_from(a.y * f);
+            s_a[i] = make_float4(re.h, re.l, im.h, im.l);
+        }
+        __syncthreads();
+        for (int i = 0; i < cnt; ++i) {
+            if (e == 0) {
+                const float4 a = s_a[i];
+                const float pr = df_prod(a.x, a.y, cur), pi = df_prod(a.z, a.w, cur);
+                if ((lb + i + m) & 1) {
+                    Or.add(pr);
+                    Oi.add(pi);
+                } else {
+                    Er.add(pr);
+                    Ei.add(pi);
+                }
+            }
+            const float2 a2 = s_al[i], b2 = s_be[i];
+            const dfl t = df_mul(dfl{a2.x, a2.y}, xd);
+            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+            prev = cur;
+            cur = nxt;
+            REC_RESCALE_DF(cur, prev, e);
+        }
+    }
+    if (act) {
+        const int n = prn[p], s = prs[p];
+        const double er = Er.value(), ei = Ei.value(), orr = Or.value(), oi = Oi.value();
+        H[(long long)m * ldH + n] = make_double2(er + orr, ei + oi);
+        if (s != n) H[(long long)m * ldH + s] = make_double2(er - orr, ei - oi);
+    }
+}
+
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_synth_spin_df(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
+                        const double *__restrict__ lfac, const float2 *__restrict__ coef, long long nalm,
+                        const double *__restrict__ lg0, int npairs, const double *__restrict__ px,
+                        const double *__restrict__ psh, const double *__restrict__ pch,
+                        const int *__restrict__ prn, const int *__restrict__ prs, double2 *__restrict__ H,
+                        int ldH) {
+    __shared__ float2 s_al[LEG_CH], s_ga[LEG_CH], s_be[LEG_CH];
+    __shared__ float4 s_A[LEG_CH], s_B[LEG_CH];
+    const int m = blockIdx.y;
+    const int l0 = max(m, spin);
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+    }
+    const dfl xN = df_from(x), xS = df_from(-x);
+    dfl cN, pN, cS, pS;
+    int eN, eS;
+    rec_start_df(lg0[m], m, spin, sh, ch, cN, pN, eN);
+    rec_start_df(lg0[m], m, spin, ch, sh, cS, pS, eS);
+    kahan hpn_r, hpn_i, hps_r, hps_i, hmn_r, hmn_i, hms_r, hms_i;
+    const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    for (int lb = l0; lb <= L; lb += LEG_CH) {
+        const int cnt = min(LEG_CH, L - lb + 1);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += LEG_TPB) {
+            const int l = lb + i;
+            const long long ix = b + l;
+            s_al[i] = al[ix];
+            s_ga[i] = ga[ix];
+            s_be[i] = be[ix];
+            const double f = lfac ? lfac[l] : 1.0;
+            const double2 g = G[ix];
+            const double2 c = C ? C[ix] : make_double2(0.0, 0.0);
+            const dfl ar = df_from(f * (g.x - c.y)), ai = df_from(f * (g.y + c.x));
+            const double par = ((l + m) & 1) ? -f : f;
+            const dfl br = df_from(par * (g.x + c.y)), bi = df_from(par * (c.x - g.y));
+            s_A[i] = make_float4(ar.h, ar.l, ai.h, ai.l);
+            s_B[i] = make_float4(br.h, br.l, bi.h, bi.l);
+        }
+        __syncthreads();
+        for (int i = 0; i < cnt; ++i) {
+            const float4 A = s_A[i], B = s_B[i];
+            if (eN == 0) {
+                hpn_r.add(df_prod(A.x, A.y, cN));
+                hpn_i.add(df_prod(A.z, A.w, cN));
+                hms_r.add(df_prod(B.x, B.y, cN));
+                hms_i.add(df_prod(B.z, B.w, cN));
+            }
+            if (eS == 0) {
+                hps_r.add(df_prod(A.x, A.y, cS));
+                hps_i.add(df_prod(A.z, A.w, cS));
+                hmn_r.add(df_prod(B.x, B.y, cS));
+                hmn_i.add(df_prod(B.z, B.w, cS));
+            }
+            const float2 a2 = s_al[i], g2 = s_ga[i], b2 = s_be[i];
+            const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
+            const dfl tN = df_add(df_mul(ad, xN), gd);
+            const dfl tS = df_add(df_mul(ad, xS), gd);
+            const dfl nN = df_mul_sub(tN, cN, bd, pN);
+            const dfl nS = df_mul_sub(tS, cS, bd, pS);
+            pN = cN;
+            cN = nN;
+            pS = cS;
+            cS = nS;
+            REC_RESCALE_DF(cN, pN, eN);
+            REC_RESCALE_DF(cS, pS, eS);
+        }
+    }
+    if (act) {
+        const int n = prn[p], s = prs[p];
+        const double sgs = (spin & 1) ? -1.0 : 1.0;
+        H[(long long)(L + m) * ldH + n] = make_double2(-hpn_r.value(), -hpn_i.value());
+        if (s != n) H[(long long)(L + m) * ldH + s] = make_double2(-hps_r.value(), -hps_i.value());
+        if (m > 0) {
+            H[(long long)(L - m) * ldH + n] = make_double2(-sgs * hmn_r.value(), -sgs * hmn_i.value());
+            if (s != n) H[(long long)(L - m) * ldH + s] = make_double2(-sgs * hms_r.value(), -sgs * hms_i.value());
         }
     }
 }
@@ -477,6 +685,17 @@ int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2
     const int L = P->lmax;
     dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
     const double *lf = use_lfac ? P->d_lfac : nullptr;
+    if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
+        if (spin == 0)
+            k_leg_synth_s0_df<<<grid, LEG_TPB, 0, st>>>(L, G, lf, P->d_coef_df[0], P->nalm, P->d_lg0[0], R.npairs,
+                                                        R.x, R.sh, R.ch, R.rn, R.rs, H, R.ld);
+        else
+            k_leg_synth_spin_df<<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, lf, P->d_coef_df[spin], P->nalm,
+                                                          P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
+                                                          H, R.ld);
+        CU_LAUNCH_CHECK();
+        return CUNUSHT_OK;
+    }
     if (spin == 0) {
         k_leg_synth_s0<<<grid, LEG_TPB, 0, st>>>(L, G, lf, P->d_coef[0], P->nalm, P->d_lg0[0],
                                                  R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H, R.ld);
