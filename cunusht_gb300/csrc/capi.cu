@@ -61,10 +61,12 @@ static void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w
     }
 }
 
-// ES kernel parameters for oversampling 2 (the FINUFFT rule used by cuFINUFFT
-// for upsampfac 2: width = ceil(log10(10/eps)), beta = 2.30 width).
+// ES kernel parameters for oversampling 2: beta = 2.30 width as in the FINUFFT
+// rule behind cuFINUFFT's upsampfac 2, but one tap wider than its
+// width = ceil(log10(10/eps)), which measures 1.5e-7 relative L2 for
+// full-band white spectra at eps = 1e-7; the extra tap keeps results within eps.
 static void es_params(double eps, int &w, double &beta) {
-    w = (int)std::ceil(-std::log10(eps / 10.0) - 1e-9);
+    w = (int)std::ceil(-std::log10(eps / 10.0) - 1e-9) + 1;
     w = std::max(2, std::min(16, w));
     double bon = 2.30;
     if (w == 2) bon = 2.20;
@@ -112,10 +114,10 @@ template <typename T> static int upload(cunusht_plan_s *P, T **p, const std::vec
 
 static void free_plan(cunusht_plan_s *P) {
     if (!P) return;
-    void *ptrs[] = {P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->d_gl_x, P->d_gl_sh,
+    void *ptrs[] = {P->d_ring_sc, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->d_gl_x, P->d_gl_sh,
                     P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
-                    P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_chirp, P->d_bker,
+                    P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -146,6 +148,8 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     P->nalm = (long long)(lmax + 1) * (lmax + 2) / 2;
     P->prec = precision == CUNUSHT_PREC_AUTO ? (eps > 1e-6 ? CUNUSHT_PREC_MIXED : CUNUSHT_PREC_FP64) : precision;
     P->grid_fp32 = (P->prec != CUNUSHT_PREC_FP64) && eps > 1e-6;
+    P->fwd_u32 = (P->prec == CUNUSHT_PREC_MIXED) && !P->grid_fp32;
+    P->fft_df = P->fwd_u32;
 
     // ---- pointing geometry, sorted by first pixel (Geom, geometry.py:47-52)
     std::vector<int> order(nring);
@@ -212,6 +216,14 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     RC_TRY(upload(P, &P->d_ring_phi0, P->h_phi0));
     RC_TRY(upload(P, &P->d_ring_nph, P->h_nph));
     RC_TRY(upload(P, &P->d_ring_ofs, P->h_ofs));
+    {
+        std::vector<float4> sc(nring);
+        for (int i = 0; i < nring; ++i) {
+            const dfl s_ = df_from_host(std::sin(P->h_theta[i])), c_ = df_from_host(std::cos(P->h_theta[i]));
+            sc[i] = make_float4(s_.h, s_.l, c_.h, c_.l);
+        }
+        RC_TRY(upload(P, &P->d_ring_sc, sc));
+    }
 
     // ---- torus and fine grid
     P->Nt = std::max(32, next_pow2(2LL * lmax + 2));
@@ -316,6 +328,18 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         RC_TRY(upload(P, &P->d_tw32, tw32));
     }
     RC_TRY(fft_global_f64(P->d_bker, P->Mb, -1, P->d_tw64, P->TW, 0));
+    if (P->fft_df) {
+        char *t = nullptr, *c = nullptr, *b = nullptr;
+        RC_TRY(dalloc(P, &t, 16 * (size_t)P->TW));
+        RC_TRY(dalloc(P, &c, 16 * (size_t)P->nph_uniform));
+        RC_TRY(dalloc(P, &b, 16 * (size_t)P->Mb));
+        P->d_twdf = t;
+        P->d_chirp_df = c;
+        P->d_bker_df = b;
+        RC_TRY(split_c128_to_df(P->d_tw64, P->TW, P->d_twdf, 0));
+        RC_TRY(split_c128_to_df(P->d_chirp, P->nph_uniform, P->d_chirp_df, 0));
+        RC_TRY(split_c128_to_df(P->d_bker, P->Mb, P->d_bker_df, 0));
+    }
     // workspace
     {
         const long long ncols = max_spin ? 2LL * lmax + 1 : lmax + 1;
@@ -526,8 +550,14 @@ int cunusht_dlm2pointing(cunusht_plan_t *P, const void *dlm, const void *dclm, i
     { StageScope sc(P, CUNUSHT_STAGE_PTG_RING, st); RC_TRY(ring_synth(P, 1, P->d_Hgl, P->d_glmap, P->d_glmap + P->npix, st)); }
     {
         StageScope sc(P, CUNUSHT_STAGE_PTG_ROT, st);
-        RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->npix,
-                               P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
+        if (P->prec == CUNUSHT_PREC_MIXED)
+            RC_TRY(pointing_mixed_launch(P->nring, P->nph_uniform, P->d_ring_theta, P->d_ring_sc, P->d_ring_phi0,
+                                         P->d_ring_nph,
+                                         P->d_ring_ofs, P->npix, P->d_glmap, P->d_glmap + P->npix, ptg,
+                                         ptg + P->npix, gamma, st));
+        else
+            RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs,
+                                   P->npix, P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
     }
     return CUNUSHT_OK;
 }

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "../../include/cunusht_gb300.h"
+#include "df.cuh"
 
 namespace cunusht {
 
@@ -52,6 +53,19 @@ void clear_error();
 template <typename T> struct cplx_t;
 template <> struct cplx_t<float> { using type = float2; };
 template <> struct cplx_t<double> { using type = double2; };
+template <> struct cplx_t<dfl> { using type = dcplx; };
+
+// scalar conversions used by code templated on float / double / dfl
+template <typename T> __device__ __forceinline__ T cvt(double x) { return (T)x; }
+template <> __device__ __forceinline__ dfl cvt<dfl>(double x) { return df_from(x); }
+__device__ __forceinline__ double to_d(float x) { return (double)x; }
+__device__ __forceinline__ double to_d(double x) { return x; }
+__device__ __forceinline__ double to_d(dfl x) { return (double)x.h + (double)x.l; }
+template <typename To> __device__ __forceinline__ To to_t(float x) { return (To)x; }
+template <typename To> __device__ __forceinline__ To to_t(double x) { return (To)x; }
+template <typename To> __device__ __forceinline__ To to_t(dfl x);
+template <> __device__ __forceinline__ float to_t<float>(dfl x) { return x.h + x.l; }
+template <> __device__ __forceinline__ double to_t<double>(dfl x) { return (double)x.h + (double)x.l; }
 template <typename T> using cplx = typename cplx_t<T>::type;
 
 template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T re, T im) {
@@ -99,8 +113,8 @@ template <typename C> __host__ __device__ __forceinline__ C cmul_idir(C a, int d
 }
 template <typename To, typename From> __device__ __forceinline__ cplx<To> ccast(From a) {
     cplx<To> r;
-    r.x = (To)a.x;
-    r.y = (To)a.y;
+    r.x = to_t<To>(a.x);
+    r.y = to_t<To>(a.y);
     return r;
 }
 
@@ -119,6 +133,8 @@ struct cunusht_plan_s {
     int max_spin = 0;
     int prec = CUNUSHT_PREC_FP64;  // resolved precision
     bool grid_fp32 = false;        // FFT + nuFFT grids in FP32
+    bool fwd_u32 = false;          // forward fine grid stored FP32 (FFTs FP64), mixed-precision interp
+    bool fft_df = false;           // forward FFTs (theta, phi, ring) in double-float
     double eps = 1e-7;
     long long nalm = 0;
 
@@ -130,6 +146,7 @@ struct cunusht_plan_s {
     std::vector<long long> h_nph, h_ofs;
     double *d_ring_theta = nullptr, *d_ring_phi0 = nullptr;
     long long *d_ring_nph = nullptr, *d_ring_ofs = nullptr;
+    float4 *d_ring_sc = nullptr;  // (sin theta, cos theta) per ring as hi/lo FP32 pairs
     // ring pairs (theta, pi - theta) of the pointing geometry
     int gl_npairs = 0;
     double *d_gl_x = nullptr, *d_gl_sh = nullptr, *d_gl_ch = nullptr;
@@ -157,6 +174,9 @@ struct cunusht_plan_s {
     int TW = 0;
     double2 *d_tw64 = nullptr;
     float2 *d_tw32 = nullptr;
+    void *d_twdf = nullptr;      // double-float twiddles (dcplx)
+    void *d_chirp_df = nullptr;  // double-float Bluestein tables (dcplx)
+    void *d_bker_df = nullptr;
 
     // Bluestein data for the ring (phi) transform of the pointing geometry
     int Mb = 0;

@@ -86,4 +86,31 @@ __device__ __forceinline__ float df_prod(float ah, float al, dfl lam) {
     return fmaf(ah, lam.h, fmaf(al, lam.h, ah * lam.l));
 }
 
+// operators so that templated complex code (FFT butterflies) runs on dfl
+__host__ __device__ __forceinline__ dfl df_neg(dfl a) {
+    dfl r;
+    r.h = -a.h;
+    r.l = -a.l;
+    return r;
+}
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) { return df_add(a, b); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ dfl operator-(dfl a) { return df_neg(a); }
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) { return df_mul(a, b); }
+// scale by +-1 (FFT direction) or a power of two: exact
+__device__ __forceinline__ dfl operator*(int s, dfl a) { return df_scale(a, (float)s); }
+
+// complex double-float, same 16-byte footprint as double2
+struct dcplx {
+    dfl x, y;
+};
+
+// host-side split of a double into hi + lo floats
+inline dfl df_from_host(double x) {
+    dfl r;
+    r.h = (float)x;
+    r.l = (float)(x - (double)r.h);
+    return r;
+}
+
 }  // namespace cunusht

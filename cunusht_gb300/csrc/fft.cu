@@ -10,6 +10,8 @@
 //   * the ring transform on the pointing geometry via Bluestein's chirp-z
 //     algorithm (any ring length, e.g. 4095 = 3^2*5*7*13 or the prime 8191),
 //     which SHTns performs inside synth_grad (GPU_sht_transformer.py:95).
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -34,7 +36,7 @@ template <typename T> __device__ __forceinline__ void dft8(cplx<T> *v, int dir) 
     using C = cplx<T>;
     dft4(v[0], v[2], v[4], v[6], dir);
     dft4(v[1], v[3], v[5], v[7], dir);
-    const T r = (T)0.70710678118654752440084436210485;
+    const T r = cvt<T>(0.70710678118654752440084436210485);
     C o1 = v[3], o2 = v[5], o3 = v[7];
     // w^1 = (1 + dir i)/sqrt2, w^2 = dir i, w^3 = (-1 + dir i)/sqrt2
     C t1 = mk<T>(r * (o1.x - dir * o1.y), r * (o1.y + dir * o1.x));
@@ -61,22 +63,22 @@ template <typename T> __device__ __forceinline__ void dft16(cplx<T> *v, int dir)
     }
     dft8<T>(e, dir);
     dft8<T>(o, dir);
-    const T cs[8] = {(T)1.0,
-                     (T)0.92387953251128675612818318939679,
-                     (T)0.70710678118654752440084436210485,
-                     (T)0.38268343236508977172845998403040,
-                     (T)0.0,
-                     (T)-0.38268343236508977172845998403040,
-                     (T)-0.70710678118654752440084436210485,
-                     (T)-0.92387953251128675612818318939679};
-    const T sn[8] = {(T)0.0,
-                     (T)0.38268343236508977172845998403040,
-                     (T)0.70710678118654752440084436210485,
-                     (T)0.92387953251128675612818318939679,
-                     (T)1.0,
-                     (T)0.92387953251128675612818318939679,
-                     (T)0.70710678118654752440084436210485,
-                     (T)0.38268343236508977172845998403040};
+    const T cs[8] = {cvt<T>(1.0),
+                     cvt<T>(0.92387953251128675612818318939679),
+                     cvt<T>(0.70710678118654752440084436210485),
+                     cvt<T>(0.38268343236508977172845998403040),
+                     cvt<T>(0.0),
+                     cvt<T>(-0.38268343236508977172845998403040),
+                     cvt<T>(-0.70710678118654752440084436210485),
+                     cvt<T>(-0.92387953251128675612818318939679)};
+    const T sn[8] = {cvt<T>(0.0),
+                     cvt<T>(0.38268343236508977172845998403040),
+                     cvt<T>(0.70710678118654752440084436210485),
+                     cvt<T>(0.92387953251128675612818318939679),
+                     cvt<T>(1.0),
+                     cvt<T>(0.92387953251128675612818318939679),
+                     cvt<T>(0.70710678118654752440084436210485),
+                     cvt<T>(0.38268343236508977172845998403040)};
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         C w = mk<T>(cs[q], dir * sn[q]);
@@ -94,86 +96,104 @@ template <typename T, int RAD> __device__ __forceinline__ void dftR(cplx<T> *v, 
 }
 
 // One Stockham pass (Govindaraju et al. 2008 formulation), in place in shared
-// memory: every thread first loads all of its butterflies, then the block
-// synchronises, then results are written.
-template <typename T, int RAD, int MAXJ>
-__device__ __forceinline__ void fft_pass(cplx<T> *buf, int N, int Ns, int dir,
-                                         const cplx<T> *__restrict__ tw, int twstride) {
+// memory.  Each of the nthr = N / E active threads owns exactly E elements
+// (NB butterflies of R points, E = NB R, all compile-time), so the butterfly
+// data stays in registers: loads, barrier, twiddle + R-point DFT, stores,
+// barrier.
+template <typename T, int R, int NB>
+__device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
+                                           const cplx<T> *__restrict__ tw, int twstride, int nthr) {
     using C = cplx<T>;
-    const int nb = N / RAD;
-    C v[MAXJ][RAD];
+    const int nb = N / R;  // == nthr * NB
+    const bool act = (int)threadIdx.x < nthr;
+    C v[NB][R];
+    if (act) {
 #pragma unroll
-    for (int c = 0; c < MAXJ; ++c) {
-        const int j = threadIdx.x + c * blockDim.x;
-        if (j < nb) {
+        for (int c = 0; c < NB; ++c) {
+            const int j = threadIdx.x + c * nthr;
 #pragma unroll
-            for (int r = 0; r < RAD; ++r) v[c][r] = buf[j + r * nb];
+            for (int r = 0; r < R; ++r) v[c][r] = buf[j + r * nb];
         }
     }
     __syncthreads();
-    const int tstep = (N / (Ns * RAD)) * twstride;
+    if (act) {
+        const int tstep = (N / (Ns * R)) * twstride;
 #pragma unroll
-    for (int c = 0; c < MAXJ; ++c) {
-        const int j = threadIdx.x + c * blockDim.x;
-        if (j < nb) {
+        for (int c = 0; c < NB; ++c) {
+            const int j = threadIdx.x + c * nthr;
             const int k = j & (Ns - 1);
+            if (Ns > 1) {
 #pragma unroll
-            for (int r = 1; r < RAD; ++r) {
-                C w = tw[r * k * tstep];
-                if (dir > 0) w.y = -w.y;
-                v[c][r] = cmul(v[c][r], w);
+                for (int r = 1; r < R; ++r) {
+                    C w = tw[r * k * tstep];
+                    if (dir > 0) w.y = -w.y;
+                    v[c][r] = cmul(v[c][r], w);
+                }
             }
-            dftR<T, RAD>(v[c], dir);
-            const int idxD = (j - k) * RAD + k;
+            dftR<T, R>(v[c], dir);
+            const int idxD = (j - k) * R + k;
 #pragma unroll
-            for (int r = 0; r < RAD; ++r) buf[idxD + r * Ns] = v[c][r];
+            for (int r = 0; r < R; ++r) buf[idxD + r * Ns] = v[c][r];
+            // one butterfly at a time: keeps the twiddle loads and DFT
+            // temporaries of the other butterflies out of the live set
+            asm volatile("" ::: "memory");
         }
     }
     __syncthreads();
 }
 
-template <typename T, int RAD>
-__device__ __forceinline__ void fft_pass_dispatch(cplx<T> *buf, int N, int Ns, int dir,
-                                                  const cplx<T> *tw, int twstride) {
-    const int nb = N / RAD;
-    const int per = (nb + blockDim.x - 1) / blockDim.x;
-    if (per <= 1) fft_pass<T, RAD, 1>(buf, N, Ns, dir, tw, twstride);
-    else if (per <= 2) fft_pass<T, RAD, 2>(buf, N, Ns, dir, tw, twstride);
-    else if (per <= 4) {
-        if constexpr (RAD <= 8) fft_pass<T, RAD, 4>(buf, N, Ns, dir, tw, twstride);
-    } else if (per <= 8) {
-        if constexpr (RAD <= 4) fft_pass<T, RAD, 8>(buf, N, Ns, dir, tw, twstride);
-    } else {
-        if constexpr (RAD == 2) fft_pass<T, RAD, 16>(buf, N, Ns, dir, tw, twstride);
-    }
-}
-
-// In-place FFT of length N (power of two, 2 <= N <= 16 * 16 * blockDim) in
-// shared memory.  dir = -1: X_k = sum_n x_n e^{-2 pi i nk/N}; dir = +1: the
-// unnormalised inverse.  tw[t] = e^{-2 pi i t / TW}, N | TW.
-template <typename T>
-__device__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
+// Whole transform with E elements per thread; radices up to min(E, RMAX) with
+// RMAX = 16 for float and 8 for double / double-float (register budget).
+template <typename T, int E, int LMAX = (std::is_same<T, float>::value ? 4 : 3)>
+__device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
+    constexpr int LE = (E >= 16) ? 4 : (E >= 8) ? 3 : (E >= 4) ? 2 : 1;
+    constexpr int LR = LE < LMAX ? LE : LMAX;
+    const int nthr = N / E;
+    const int twstride = TW / N;
     int rem = __ffs(N) - 1;
     int Ns = 1;
-    const int twstride = TW / N;
     while (rem > 0) {
-        int r;
-        if (rem == 4) r = 4;
-        else if (rem == 2) r = 2;
-        else if (rem == 1) r = 1;
-        else r = 3;
-        if (r == 4) fft_pass_dispatch<T, 16>(buf, N, Ns, dir, tw, twstride);
-        else if (r == 3) fft_pass_dispatch<T, 8>(buf, N, Ns, dir, tw, twstride);
-        else if (r == 2) fft_pass_dispatch<T, 4>(buf, N, Ns, dir, tw, twstride);
-        else fft_pass_dispatch<T, 2>(buf, N, Ns, dir, tw, twstride);
+        const int r = rem < LR ? rem : LR;
+        if (r == 4) {
+            if constexpr (LR >= 4) fft_pass_e<T, 16, E / 16>(buf, N, Ns, dir, tw, twstride, nthr);
+        } else if (r == 3) {
+            if constexpr (LR >= 3) fft_pass_e<T, 8, E / 8>(buf, N, Ns, dir, tw, twstride, nthr);
+        } else if (r == 2) {
+            if constexpr (LR >= 2) fft_pass_e<T, 4, E / 4>(buf, N, Ns, dir, tw, twstride, nthr);
+        } else {
+            fft_pass_e<T, 2, E / 2>(buf, N, Ns, dir, tw, twstride, nthr);
+        }
         Ns <<= r;
         rem -= r;
     }
 }
 
+// In-place FFT of length N (power of two, 2 <= N <= 16 blockDim; 32 blockDim
+// for float) in shared memory.  dir = -1: X_k = sum_n x_n e^{-2 pi i nk/N};
+// dir = +1: the unnormalised inverse.  tw[t] = e^{-2 pi i t / TW}, N | TW.
+template <typename T>
+__device__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
+    const int B = blockDim.x;
+    if (N > 16 * B) {
+        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 32, 3>(buf, N, dir, tw, TW);
+    } else if (N > 8 * B) {
+        // 16 elements per thread: radix <= 8 for float, <= 4 for double and
+        // double-float keeps the pass within the 128-register budget of a
+        // 512-thread block
+        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 16, 3>(buf, N, dir, tw, TW);
+        else fft_smem_e<T, 16, 2>(buf, N, dir, tw, TW);
+    } else if (N > 4 * B) {
+        fft_smem_e<T, 8, 3>(buf, N, dir, tw, TW);
+    } else if (N > 2 * B) {
+        fft_smem_e<T, 4>(buf, N, dir, tw, TW);
+    } else {
+        fft_smem_e<T, 2>(buf, N, dir, tw, TW);
+    }
+}
+
 size_t fft_smem_bytes(int N, bool f32) { return (size_t)N * (f32 ? sizeof(float2) : sizeof(double2)); }
 
-template <typename T> __device__ __forceinline__ cplx<T> czero() { return mk<T>((T)0, (T)0); }
+template <typename T> __device__ __forceinline__ cplx<T> czero() { return mk<T>(cvt<T>(0.0), cvt<T>(0.0)); }
 
 __device__ __forceinline__ int wrapi(int n, int N) {
     n %= N;
@@ -191,23 +211,23 @@ __global__ void __launch_bounds__(FFT_TPB)
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
     const int c = blockIdx.x;
     const int m = c - mofs;
-    const T sgn = ((abs(m) + spin) & 1) ? (T)-1 : (T)1;
+    const double sgn = ((abs(m) + spin) & 1) ? -1.0 : 1.0;
     const double2 *col = H + (long long)c * ldH;
     const int half = Nt / 2;
     for (int k = threadIdx.x; k < Nt; k += blockDim.x) {
         const bool lo = k <= half;
         const double2 v = lo ? col[k] : col[Nt - k];
-        const T s = lo ? (T)1 : sgn;
-        buf[k] = mk<T>((T)v.x * s, (T)v.y * s);
+        const double s = lo ? 1.0 : sgn;
+        buf[k] = mk<T>(cvt<T>(v.x * s), cvt<T>(v.y * s));
     }
     __syncthreads();
     fft_smem<T>(buf, Nt, -1, tw, TW);
     const double dm = Dph[m + L];
     for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
         const int src = Nt - 1 - i;  // kappa = -(i+1)
-        buf[Ntf - 1 - i] = cscale(buf[src], (T)(Dth[src] * dm));
+        buf[Ntf - 1 - i] = cscale(buf[src], cvt<T>(Dth[src] * dm));
     }
-    for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], (T)(Dth[i] * dm));
+    for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
     __syncthreads();
     for (int i = half + threadIdx.x; i <= Ntf - half; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
@@ -226,7 +246,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
     const int c = blockIdx.x;
     const int m = c - mofs;
-    const T sgn = ((abs(m) + spin) & 1) ? (T)-1 : (T)1;
+    const T sgn = cvt<T>(((abs(m) + spin) & 1) ? -1.0 : 1.0);
     for (int i = threadIdx.x; i < Ntf; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
     for (int r = threadIdx.x; r < nrows; r += blockDim.x)
@@ -237,9 +257,9 @@ __global__ void __launch_bounds__(FFT_TPB)
     const double dm = Dph[m + L];
     for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
         const int dst = Nt - 1 - i;  // kappa = -(i+1)
-        buf[dst] = cscale(buf[Ntf - 1 - i], (T)(Dth[dst] * dm));
+        buf[dst] = cscale(buf[Ntf - 1 - i], cvt<T>(Dth[dst] * dm));
     }
-    for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], (T)(Dth[i] * dm));
+    for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
     if (threadIdx.x == 0) buf[half] = czero<T>();
     __syncthreads();
     fft_smem<T>(buf, Nt, +1, tw, TW);
@@ -247,15 +267,15 @@ __global__ void __launch_bounds__(FFT_TPB)
     for (int k = threadIdx.x; k <= half; k += blockDim.x) {
         cplx<T> v = buf[k];
         if (k > 0 && k < half) v = cadd(v, cscale(buf[Nt - k], sgn));
-        col[k] = make_double2((double)v.x, (double)v.y);
+        col[k] = make_double2(to_d(v.x), to_d(v.y));
     }
 }
 
 // ------------------------------------------------------------ phi pass
 // spin 0: two real rows per block packed as one complex transform
-template <typename T>
+template <typename T, typename TU>
 __global__ void __launch_bounds__(FFT_TPB)
-    k_phi_fwd_s0(const cplx<T> *__restrict__ F, int ncols, int nrows, int Npf, T *__restrict__ U,
+    k_phi_fwd_s0(const cplx<T> *__restrict__ F, int ncols, int nrows, int Npf, TU *__restrict__ U,
                  const cplx<T> *__restrict__ tw, int TW) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
@@ -275,12 +295,12 @@ __global__ void __launch_bounds__(FFT_TPB)
     }
     __syncthreads();
     fft_smem<T>(buf, Npf, +1, tw, TW);
-    T *u1 = U + (long long)r1 * Npf;
-    T *u2 = U + (long long)r2 * Npf;
+    TU *u1 = U + (long long)r1 * Npf;
+    TU *u2 = U + (long long)r2 * Npf;
     for (int p = threadIdx.x; p < Npf; p += blockDim.x) {
         const cplx<T> z = buf[p];
-        u1[p] = z.x;
-        if (has2) u2[p] = z.y;
+        u1[p] = to_t<TU>(z.x);
+        if (has2) u2[p] = to_t<TU>(z.y);
     }
 }
 
@@ -294,22 +314,22 @@ __global__ void __launch_bounds__(FFT_TPB)
     const bool has2 = r2 < nrows;
     const T *u1 = U + (long long)r1 * Npf;
     const T *u2 = U + (long long)r2 * Npf;
-    for (int p = threadIdx.x; p < Npf; p += blockDim.x) buf[p] = mk<T>(u1[p], has2 ? u2[p] : (T)0);
+    for (int p = threadIdx.x; p < Npf; p += blockDim.x) buf[p] = mk<T>(u1[p], has2 ? u2[p] : cvt<T>(0.0));
     __syncthreads();
     fft_smem<T>(buf, Npf, -1, tw, TW);
     for (int m = threadIdx.x; m < ncols; m += blockDim.x) {
         const cplx<T> zm = buf[m];
         const cplx<T> zn = buf[m == 0 ? 0 : Npf - m];
         // U1 = (zm + conj zn)/2 ; U2 = (zm - conj zn)/(2i)
-        F[(long long)r1 * ncols + m] = mk<T>((T)0.5 * (zm.x + zn.x), (T)0.5 * (zm.y - zn.y));
-        if (has2) F[(long long)r2 * ncols + m] = mk<T>((T)0.5 * (zm.y + zn.y), (T)-0.5 * (zm.x - zn.x));
+        F[(long long)r1 * ncols + m] = mk<T>(cvt<T>(0.5) * (zm.x + zn.x), cvt<T>(0.5) * (zm.y - zn.y));
+        if (has2) F[(long long)r2 * ncols + m] = mk<T>(cvt<T>(0.5) * (zm.y + zn.y), cvt<T>(-0.5) * (zm.x - zn.x));
     }
 }
 
 // spin s: one complex row per block, columns c = m + L for m in [-L, L]
-template <typename T>
+template <typename T, typename TU>
 __global__ void __launch_bounds__(FFT_TPB)
-    k_phi_fwd_spin(const cplx<T> *__restrict__ F, int L, int Npf, cplx<T> *__restrict__ U,
+    k_phi_fwd_spin(const cplx<T> *__restrict__ F, int L, int Npf, cplx<TU> *__restrict__ U,
                    const cplx<T> *__restrict__ tw, int TW) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
@@ -320,7 +340,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) buf[wrapi(c - L, Npf)] = F[(long long)r * ncols + c];
     __syncthreads();
     fft_smem<T>(buf, Npf, +1, tw, TW);
-    for (int p = threadIdx.x; p < Npf; p += blockDim.x) U[(long long)r * Npf + p] = buf[p];
+    for (int p = threadIdx.x; p < Npf; p += blockDim.x) U[(long long)r * Npf + p] = ccast<TU>(buf[p]);
 }
 
 template <typename T>
@@ -340,53 +360,78 @@ __global__ void __launch_bounds__(FFT_TPB)
 // ------------------------------------------------------------ ring transform (Bluestein)
 // z_p = sum_m h_m e^{i m (phi0 + 2 pi p / N)}, p < N, for one ring per block.
 // spin 0: real output from m in [0, L] (h_{-m} = conj h_m); spin s: complex.
+// T = double (plain path) or dfl (mixed path); tables are given in T.
+template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_ring_synth(const double2 *__restrict__ Hgl, int nring, int L, int spin,
                  const double *__restrict__ phi0, const long long *__restrict__ ofs, int N, int Mb,
-                 const double2 *__restrict__ chirp, const double2 *__restrict__ bker,
+                 const cplx<T> *__restrict__ chirp, const cplx<T> *__restrict__ bker,
                  double *__restrict__ out0, double *__restrict__ out1,
-                 const double2 *__restrict__ tw, int TW) {
+                 const cplx<T> *__restrict__ tw, int TW) {
+    using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double2 *buf = reinterpret_cast<double2 *>(smem_raw);
+    C *buf = reinterpret_cast<C *>(smem_raw);
     const int ring = blockIdx.x;
     const double ph0 = phi0[ring];
-    for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = make_double2(0, 0);
+    for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
     if (spin == 0) {
         for (int m = threadIdx.x; m <= L; m += blockDim.x) {
             double2 h = Hgl[(long long)m * nring + ring];
             if (m == 0) {
-                buf[0] = make_double2(h.x, 0.0);
+                buf[0] = mk<T>(cvt<T>(h.x), cvt<T>(0.0));
             } else {
-                double s, c;
-                sincos(m * ph0, &s, &c);
-                h = cmul(h, make_double2(c, s));
-                buf[m] = cmul(h, chirp[m]);
-                buf[N - m] = cmul(cconj(h), chirp[N - m]);
+                if (ph0 != 0.0) {
+                    double sn, cs;
+                    sincos(m * ph0, &sn, &cs);
+                    h = cmul(h, make_double2(cs, sn));
+                }
+                const C hc = mk<T>(cvt<T>(h.x), cvt<T>(h.y));
+                buf[m] = cmul(hc, chirp[m]);
+                buf[N - m] = cmul(cconj(hc), chirp[N - m]);
             }
         }
     } else {
         for (int cidx = threadIdx.x; cidx < 2 * L + 1; cidx += blockDim.x) {
             const int m = cidx - L;
             double2 h = Hgl[(long long)cidx * nring + ring];
-            double s, c;
-            sincos(m * ph0, &s, &c);
-            h = cmul(h, make_double2(c, s));
+            if (ph0 != 0.0) {
+                double sn, cs;
+                sincos(m * ph0, &sn, &cs);
+                h = cmul(h, make_double2(cs, sn));
+            }
             const int q = wrapi(m, N);
-            buf[q] = cmul(h, chirp[q]);
+            buf[q] = cmul(mk<T>(cvt<T>(h.x), cvt<T>(h.y)), chirp[q]);
         }
     }
     __syncthreads();
-    fft_smem<double>(buf, Mb, -1, tw, TW);
+    fft_smem<T>(buf, Mb, -1, tw, TW);
     for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = cmul(buf[i], bker[i]);
     __syncthreads();
-    fft_smem<double>(buf, Mb, +1, tw, TW);
+    fft_smem<T>(buf, Mb, +1, tw, TW);
     const long long o = ofs[ring];
     for (int p = threadIdx.x; p < N; p += blockDim.x) {
-        const double2 z = cmul(buf[p], chirp[p]);
-        out0[o + p] = z.x;
-        if (spin != 0) out1[o + p] = z.y;
+        const C z = cmul(buf[p], chirp[p]);
+        out0[o + p] = to_d(z.x);
+        if (spin != 0) out1[o + p] = to_d(z.y);
     }
+}
+
+// split FP64 complex tables into double-float ones (plan set-up)
+__global__ void k_split_c128(const double2 *__restrict__ in, long long n, dcplx *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dcplx r;
+    r.x = df_from(in[i].x);
+    r.y = df_from(in[i].y);
+    out[i] = r;
+}
+
+int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st) {
+    if (n == 0) return CUNUSHT_OK;
+    k_split_c128<<<(int)((n + 255) / 256), 256, 0, st>>>(in, n, (dcplx *)out);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
 }
 
 // h'_m = e^{-i m phi0} sum_p z'_p e^{-2 pi i m p / N} (adjoint of k_ring_synth)
@@ -465,6 +510,11 @@ int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cuda
         RC_TRY(set_smem(k_theta_fwd<float>, sm));
         k_theta_fwd<float><<<ncols, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
                                                        (float2 *)F, ncols, P->n_lo, P->nrows, P->d_tw32, P->TW);
+    } else if (P->fft_df) {
+        RC_TRY(set_smem(k_theta_fwd<dfl>, sm));
+        k_theta_fwd<dfl><<<ncols, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
+                                                     (dcplx *)F, ncols, P->n_lo, P->nrows, (const dcplx *)P->d_twdf,
+                                                     P->TW);
     } else {
         RC_TRY(set_smem(k_theta_fwd<double>, sm));
         k_theta_fwd<double><<<ncols, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
@@ -498,23 +548,39 @@ int phi_fwd(const cunusht_plan_s *P, int spin, const void *F, void *U, cudaStrea
     if (spin == 0) {
         const int nb = (P->nrows + 1) / 2;
         if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_fwd_s0<float>, sm));
-            k_phi_fwd_s0<float><<<nb, FFT_TPB, sm, st>>>((const float2 *)F, L + 1, P->nrows, P->Npf, (float *)U,
-                                                         P->d_tw32, P->TW);
+            RC_TRY(set_smem(k_phi_fwd_s0<float, float>, sm));
+            k_phi_fwd_s0<float, float><<<nb, FFT_TPB, sm, st>>>((const float2 *)F, L + 1, P->nrows, P->Npf,
+                                                                (float *)U, P->d_tw32, P->TW);
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_phi_fwd_s0<dfl, float>, sm));
+            k_phi_fwd_s0<dfl, float><<<nb, FFT_TPB, sm, st>>>((const dcplx *)F, L + 1, P->nrows, P->Npf,
+                                                              (float *)U, (const dcplx *)P->d_twdf, P->TW);
+        } else if (P->fwd_u32) {
+            RC_TRY(set_smem(k_phi_fwd_s0<double, float>, sm));
+            k_phi_fwd_s0<double, float><<<nb, FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
+                                                                 (float *)U, P->d_tw64, P->TW);
         } else {
-            RC_TRY(set_smem(k_phi_fwd_s0<double>, sm));
-            k_phi_fwd_s0<double><<<nb, FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf, (double *)U,
-                                                          P->d_tw64, P->TW);
+            RC_TRY(set_smem(k_phi_fwd_s0<double, double>, sm));
+            k_phi_fwd_s0<double, double><<<nb, FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
+                                                                  (double *)U, P->d_tw64, P->TW);
         }
     } else {
         if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_fwd_spin<float>, sm));
-            k_phi_fwd_spin<float><<<P->nrows, FFT_TPB, sm, st>>>((const float2 *)F, L, P->Npf, (float2 *)U,
-                                                                 P->d_tw32, P->TW);
+            RC_TRY(set_smem(k_phi_fwd_spin<float, float>, sm));
+            k_phi_fwd_spin<float, float><<<P->nrows, FFT_TPB, sm, st>>>((const float2 *)F, L, P->Npf,
+                                                                        (float2 *)U, P->d_tw32, P->TW);
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_phi_fwd_spin<dfl, float>, sm));
+            k_phi_fwd_spin<dfl, float><<<P->nrows, FFT_TPB, sm, st>>>((const dcplx *)F, L, P->Npf, (float2 *)U,
+                                                                      (const dcplx *)P->d_twdf, P->TW);
+        } else if (P->fwd_u32) {
+            RC_TRY(set_smem(k_phi_fwd_spin<double, float>, sm));
+            k_phi_fwd_spin<double, float><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
+                                                                         (float2 *)U, P->d_tw64, P->TW);
         } else {
-            RC_TRY(set_smem(k_phi_fwd_spin<double>, sm));
-            k_phi_fwd_spin<double><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf, (double2 *)U,
-                                                                  P->d_tw64, P->TW);
+            RC_TRY(set_smem(k_phi_fwd_spin<double, double>, sm));
+            k_phi_fwd_spin<double, double><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
+                                                                          (double2 *)U, P->d_tw64, P->TW);
         }
     }
     CU_LAUNCH_CHECK();
@@ -553,10 +619,18 @@ int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStrea
 int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *out0, double *out1,
                cudaStream_t st) {
     size_t sm = fft_smem_bytes(P->Mb, false);
-    RC_TRY(set_smem(k_ring_synth, sm));
-    k_ring_synth<<<P->nring, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
-                                                P->nph_uniform, P->Mb, P->d_chirp, P->d_bker, out0, out1,
-                                                P->d_tw64, P->TW);
+    if (P->fft_df && P->d_chirp_df) {
+        RC_TRY(set_smem(k_ring_synth<dfl>, sm));
+        k_ring_synth<dfl><<<P->nring, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0,
+                                                         P->d_ring_ofs, P->nph_uniform, P->Mb,
+                                                         (const dcplx *)P->d_chirp_df, (const dcplx *)P->d_bker_df,
+                                                         out0, out1, (const dcplx *)P->d_twdf, P->TW);
+    } else {
+        RC_TRY(set_smem(k_ring_synth<double>, sm));
+        k_ring_synth<double><<<P->nring, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0,
+                                                            P->d_ring_ofs, P->nph_uniform, P->Mb, P->d_chirp,
+                                                            P->d_bker, out0, out1, P->d_tw64, P->TW);
+    }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }

@@ -24,6 +24,7 @@ int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *ou
                cudaStream_t st);
 int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
                  double2 *Hgl, cudaStream_t st);
+int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st);
 int fft_global_f64(double2 *data, int N, int dir, const double2 *tw, int TW, cudaStream_t st);
 size_t fft_smem_bytes(int N, bool f32);
 
@@ -38,6 +39,9 @@ int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long
 int pointing_launch(int nring, const double *rth, const double *rph0, const long long *rnph,
                     const long long *rofs, long long npix, const double *dth, const double *dph,
                     double *out_th, double *out_ph, double *out_gamma, cudaStream_t st);
+int pointing_mixed_launch(int nring, int nph_uniform, const double *rth, const float4 *rsc, const double *rph0,
+                          const long long *rnph, const long long *rofs, long long npix, const double *dth,
+                          const double *dph, double *out_th, double *out_ph, double *out_gamma, cudaStream_t st);
 int doubling_launch(const void *in, long long ntheta, long long nphi, int layout, int spin,
                     int dtype, void *out, cudaStream_t st);
 int adjoint_doubling_launch(const void *in, long long ntheta, long long nphi, int spin, int dtype,

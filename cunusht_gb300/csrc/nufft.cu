@@ -11,6 +11,7 @@
 // Points are read in the caller's order; for lensing they are the deflected
 // pixels in ring order, so neighbouring threads touch neighbouring columns.
 #include "common.cuh"
+#include "df.cuh"
 #include "kernels.cuh"
 
 namespace cunusht {
@@ -186,11 +187,121 @@ __global__ void __launch_bounds__(NU_TPB)
     }
 }
 
+// ------------------------------------------------------------ interp, mixed precision
+// FP32 fine grid (from FP64 FFTs), FP32 kernel weights from the cancellation-free
+// exponent  beta (sqrt(1 - z^2) - 1) = -beta z^2 / (1 + sqrt(1 - z^2)),
+// Kahan-compensated FP32 sums, and the exp(i s gamma) rotation applied in FP64
+// from d = 1 - cos(x) = 2 sin^2(x/2) and sin(x) evaluated in FP32 (errors
+// relative to the small angle, not to 1).
+__device__ __forceinline__ float es_kernel_acc(float z, float beta) {
+    const float q = 1.f - z * z;
+    if (q <= 0.f) return 0.f;
+    const float r = sqrtf(q);
+    return expf(-beta * (z * z) / (1.f + r));
+}
+
+template <bool CPLX>
+__global__ void __launch_bounds__(NU_TPB)
+    k_interp_mixed(const float *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
+                   const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
+                   int spin, void *__restrict__ out, int out_f32) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npts) return;
+    double th, ph;
+    load_point(loc, j, npts, layout, th, ph);
+    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+    float kt[MAXW], kp[MAXW];
+    // tap offsets (n0 + a - t) from the FP64 offset split into hi + lo floats:
+    // (a + ft_h) is exact in FP32, so each tap argument carries only its own
+    // final rounding (a single FP32 rounding of ft would shift every tap of
+    // the point by up to 2.4e-7 grid cells, a coherent position error)
+    const float sc = 2.f / (float)w;
+    const float fth = (float)pc.ft, ftl = (float)(pc.ft - (double)fth);
+    const float fph = (float)pc.fp, fpl = (float)(pc.fp - (double)fph);
+#pragma unroll
+    for (int a = 0; a < MAXW; ++a) {
+        if (a < w) {
+            kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
+            kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
+        }
+    }
+    int cols[MAXW];
+#pragma unroll
+    for (int b = 0; b < MAXW; ++b) {
+        int c = pc.p0 + b;
+        c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+        cols[b] = c;
+    }
+    kahan zr, zi;
+    for (int a = 0; a < w; ++a) {
+        const long long rowoff = (long long)(pc.r0 + a) * Npf;
+        kahan rr, ri;
+        if constexpr (CPLX) {
+            const float2 *row = reinterpret_cast<const float2 *>(U) + rowoff;
+#pragma unroll
+            for (int b = 0; b < MAXW; ++b) {
+                if (b < w) {
+                    const float2 v = row[cols[b]];
+                    rr.add(kp[b] * v.x);
+                    ri.add(kp[b] * v.y);
+                }
+            }
+        } else {
+            const float *row = U + rowoff;
+#pragma unroll
+            for (int b = 0; b < MAXW; ++b)
+                if (b < w) rr.add(kp[b] * row[cols[b]]);
+        }
+        // row sums carry their compensation into the outer sum
+        zr.add(kt[a] * rr.s);
+        zr.add(-kt[a] * rr.c);
+        if constexpr (CPLX) {
+            zi.add(kt[a] * ri.s);
+            zi.add(-kt[a] * ri.c);
+        }
+    }
+    if constexpr (CPLX) {
+        double vr = zr.value(), vi = zi.value();
+        if (gamma) {
+            const float x = (float)(spin * gamma[j]);
+            const float sh = sinf(0.5f * x);
+            const double d = 2.0 * (double)sh * (double)sh;  // 1 - cos x
+            const double s = (double)sinf(x);
+            const double tr = vr - vr * d - vi * s;
+            vi = vi - vi * d + vr * s;
+            vr = tr;
+        }
+        if (out_f32) {
+            ((float *)out)[j] = (float)vr;
+            ((float *)out)[npts + j] = (float)vi;
+        } else {
+            ((double *)out)[j] = vr;
+            ((double *)out)[npts + j] = vi;
+        }
+    } else {
+        const double v = zr.value();
+        if (out_f32) ((float *)out)[j] = (float)v;
+        else ((double *)out)[j] = v;
+    }
+}
+
 int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
                  const double *gamma, void *out, int out_dtype, cudaStream_t st) {
     if (npts == 0) return CUNUSHT_OK;
     const int nb = (int)((npts + NU_TPB - 1) / NU_TPB);
     const int f32o = out_dtype == CUNUSHT_F32;
+    if (P->fwd_u32) {
+        if (spin == 0)
+            k_interp_mixed<false><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                         P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
+                                                         f32o);
+        else
+            k_interp_mixed<true><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                        P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
+                                                        f32o);
+        CU_LAUNCH_CHECK();
+        return CUNUSHT_OK;
+    }
     if (P->grid_fp32) {
         if (spin == 0)
             k_interp<float, false><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
@@ -290,6 +401,121 @@ __global__ void __launch_bounds__(256)
         const double x2 = d2 * sinaoa * (ct / st) + t * cosa;
         ogam[j] = (d2 > 0.0) ? atan2(p * x2 - t * p, t * x2 + p * p) : 0.0;
     }
+}
+
+// Mixed-precision pointing: the same rotation as k_pointing, written as small
+// increments evaluated in double-float (FP32 hi/lo) and added to the ring
+// angles in FP64:
+//   phi'   = phi + atan(d_p S / nx),  nx = st C + ct d_t S
+//   theta' = theta + asin( ct num / (rho + st C) + st^2 d_t S ),
+//   num = rho^2 - st^2 C^2 = 2 st ct C d_t S + (ct^2 d_t^2 + d_p^2) S^2
+// (sin(theta' - theta) = rho ct - nz st), S = sin(a)/a = 1 + s1,
+// C = cos a = 1 + c1 with the small s1, c1 from their series in FP32;
+// asin / atan of the small increments by x + (x^3/6 + 3x^5/40) and
+// x - x^3/3 + x^5/5 with the correction in FP32 (FP64 atan2 / asin for the
+// few near-pole pixels where the increment is not small).
+// gamma = atan2(d_p (x2 - d_t), d_t x2 + d_p^2), x2 - d_t = a^2 S cot + d_t c1,
+// in FP32 (it only enters through exp(i s gamma)).
+__device__ __forceinline__ dfl df_div(dfl a, dfl b) {
+    const float q0 = a.h / b.h;
+    // r = a - q0 b
+    const float p = q0 * b.h;
+    const float pe = fmaf(q0, b.h, -p);
+    float r = (a.h - p) - pe;
+    r = fmaf(-q0, b.l, r) + a.l;
+    return df_fast(q0, r / b.h);
+}
+
+__device__ __forceinline__ dfl df_sqrt(dfl a) {
+    if (a.h <= 0.f) return dfl{0.f, 0.f};
+    const float r0 = sqrtf(a.h);
+    const float e = fmaf(-r0, r0, a.h) + a.l;
+    return df_fast(r0, e / (2.f * r0));
+}
+
+__global__ void __launch_bounds__(256)
+    k_pointing_mixed(int nring, int nph_uniform, const double *__restrict__ rth,
+                     const float4 *__restrict__ rsc, const double *__restrict__ rph0,
+                     const long long *__restrict__ rnph, const long long *__restrict__ rofs, long long npix,
+                     const double *__restrict__ dth, const double *__restrict__ dph, double *__restrict__ oth,
+                     double *__restrict__ oph, double *__restrict__ ogam) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npix) return;
+    int ring;
+    if (nph_uniform > 0) {
+        ring = (int)(j / nph_uniform);
+    } else {
+        int lo = 0, hi = nring - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (rofs[mid] <= j) lo = mid;
+            else hi = mid - 1;
+        }
+        ring = lo;
+    }
+    const double theta = rth[ring];
+    const long long nph = rnph[ring];
+    const double phi = rph0[ring] + (double)(j - rofs[ring]) * (TWOPI / (double)nph);
+    const double t64 = dth[j], p64 = dph[j];
+    const dfl t = df_from(t64), p = df_from(p64);
+    const float d2 = t.h * t.h + p.h * p.h;
+    float s1, c1;
+    if (d2 < 1e-3f) {
+        s1 = -d2 / 6.f * (1.f - d2 / 20.f * (1.f - d2 / 42.f));
+        c1 = -0.5f * d2 * (1.f - d2 / 12.f * (1.f - d2 / 30.f * (1.f - d2 / 56.f)));
+    } else {
+        const float a = sqrtf(d2);
+        const float sh = sinf(0.5f * a);
+        s1 = sinf(a) / a - 1.f;
+        c1 = -2.f * sh * sh;
+    }
+    const dfl S{1.f, s1}, C{1.f, c1};
+    const float4 sc = rsc[ring];
+    const dfl st{sc.x, sc.y}, ct{sc.z, sc.w};
+    const dfl tS = df_mul(t, S);
+    const dfl stC = df_mul(st, C);
+    const dfl nx = df_add(stC, df_mul(ct, tS));
+    const dfl pS = df_mul(p, S);
+    const dfl rho = df_sqrt(df_add(df_mul(nx, nx), df_mul(pS, pS)));
+    const dfl ctt = df_mul(ct, t), two_st_ct_C = df_scale(df_mul(df_mul(st, ct), C), 2.f);
+    const dfl num = df_add(df_mul(two_st_ct_C, tS), df_mul(df_add(df_mul(ctt, ctt), df_mul(p, p)), df_mul(S, S)));
+    const dfl sdt = df_add(df_mul(ct, df_div(num, df_add(rho, stC))), df_mul(df_mul(st, st), tS));
+    double dtheta;
+    if (fabsf(sdt.h) < 0.02f) {
+        const float x = sdt.h, x2 = x * x;
+        dtheta = df_to(df_add(sdt, dfl{x * x2 * (1.f / 6.f + 0.075f * x2), 0.f}));
+    } else {
+        dtheta = asin(fmin(fmax(df_to(sdt), -1.0), 1.0));
+    }
+    oth[j] = theta + dtheta;
+    double dphi;
+    const dfl q = nx.h > 0.f ? df_div(pS, nx) : dfl{1e30f, 0.f};
+    if (fabsf(q.h) < 0.02f) {
+        const float x = q.h, x2 = x * x;
+        dphi = df_to(df_add(q, dfl{x * x2 * (-1.f / 3.f + 0.2f * x2), 0.f}));
+    } else {
+        dphi = atan2(df_to(pS), df_to(nx));
+    }
+    double php = phi + dphi;
+    if (php >= TWOPI) php -= TWOPI;
+    oph[j] = php;
+    if (ogam) {
+        const float x2m = d2 * (1.f + s1) * (sc.z / sc.x) + t.h * c1;  // x2 - d_t
+        const float x2 = t.h + x2m;
+        ogam[j] = d2 > 0.f ? (double)atan2f(p.h * x2m, t.h * x2 + p.h * p.h) : 0.0;
+    }
+}
+
+int pointing_mixed_launch(int nring, int nph_uniform, const double *rth, const float4 *rsc, const double *rph0,
+                          const long long *rnph,
+                          const long long *rofs, long long npix, const double *dth, const double *dph,
+                          double *out_th, double *out_ph, double *out_gamma, cudaStream_t st) {
+    if (npix == 0) return CUNUSHT_OK;
+    const int nb = (int)((npix + 255) / 256);
+    k_pointing_mixed<<<nb, 256, 0, st>>>(nring, nph_uniform, rth, rsc, rph0, rnph, rofs, npix, dth, dph, out_th, out_ph,
+                                         out_gamma);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
 }
 
 int pointing_launch(int nring, const double *rth, const double *rph0, const long long *rnph,
