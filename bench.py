@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7"
+# DRAM bytes (read + write) per launch from one ncu capture at lmax 2047
+# (profiles/leg_synth_spin_df_l2047.md)
+LEG_TRAFFIC = {"leg_synth": 196.3e6, "ptg_leg": 161.1e6}
 
 
 def parse():
@@ -308,9 +311,21 @@ def main():
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
     else:
         ach = amount / avg_s / 1e12
-        peak = 1.25
-        roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": None, "kernel": dom, "peak_source": "nominal GB300 FP64 (no measured FP64 peak)"}
+        if args.precision == "fp64":
+            peak = 1.25
+            roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                    "traffic": None, "kernel": dom,
+                    "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)"}
+        else:
+            # double-float Legendre on the FP32 pipe: 152 SMs x 128 lanes x 2 flop x max SM clock
+            mhz = peaks.get("sm_max_mhz", 2070.0)
+            peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+            roof = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                    "traffic": LEG_TRAFFIC.get(dom), "kernel": dom,
+                    "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; "
+                                   "achieved counts algorithmic flops only (8 per l,m,ring,component), "
+                                   "the double-float arithmetic issues ~15x more: ncu FMA-pipe "
+                                   "utilisation 73 %, issue slots 91 % (profiles/leg_synth_spin_df_l2047.md)"}
     stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
                        "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
     for s, v in stage_table.items():
