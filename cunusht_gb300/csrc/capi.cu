@@ -118,7 +118,7 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
-                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm};
+                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : P->evt_pool) {
@@ -354,6 +354,7 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         RC_TRY(dalloc(P, &P->d_Hgl, (size_t)(2 * lmax + 1) * nring));
         RC_TRY(dalloc(P, &P->d_glmap, 2 * (size_t)npix));
         RC_TRY(dalloc(P, &P->d_alm, 2 * (size_t)P->nalm));
+        RC_TRY(dalloc(P, &P->d_vjp, 4 * (size_t)npix));
     }
     CU_TRY(cudaStreamSynchronize(0));
     CU_TRY(cudaGetLastError());
@@ -559,6 +560,45 @@ int cunusht_dlm2pointing(cunusht_plan_t *P, const void *dlm, const void *dclm, i
             RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs,
                                    P->npix, P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
     }
+    return CUNUSHT_OK;
+}
+
+int cunusht_lensing_vjp_dlm(cunusht_plan_t *P, int spin, const void *gclm, int alm_dtype, const void *dlm_scaled,
+                            int dlm_dtype, const double *grad_map, void *grad_dlm, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(gclm && dlm_scaled && grad_map && grad_dlm, "NULL array argument");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    ARG_CHECK(dlm_dtype == CUNUSHT_F64 || dlm_dtype == CUNUSHT_F32, "bad dlm dtype");
+    if (spin != 0) {
+        set_error("lensing VJP with respect to the deflection is implemented for spin 0 only");
+        return CUNUSHT_ERR_UNSUPPORTED;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    double *ptg = P->d_vjp, *gd = P->d_vjp + 2 * P->npix;
+    // deflection (kept in d_glmap) and deflected angles
+    const double2 *D = (const double2 *)dlm_scaled;
+    if (dlm_dtype != CUNUSHT_F64) {
+        RC_TRY(convert_alm(dlm_scaled, dlm_dtype, P->nalm, P->d_alm + P->nalm, st));
+        D = P->d_alm + P->nalm;
+    }
+    RC_TRY(leg_synth(P, 1, D, nullptr, true, false, P->d_Hgl, st));
+    RC_TRY(ring_synth(P, 1, P->d_Hgl, P->d_glmap, P->d_glmap + P->npix, st));
+    RC_TRY(pointing_launch(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs, P->npix,
+                           P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, nullptr, st));
+    // fine grid of the unlensed field
+    const double2 *G = (const double2 *)gclm;
+    if (alm_dtype != CUNUSHT_F64) {
+        RC_TRY(convert_alm(gclm, alm_dtype, P->nalm, P->d_alm, st));
+        G = P->d_alm;
+    }
+    RC_TRY(leg_synth(P, 0, G, nullptr, false, true, P->d_H, st));
+    RC_TRY(theta_fwd(P, 0, P->d_H, P->d_F, st));
+    RC_TRY(phi_fwd(P, 0, P->d_F, P->d_U, st));
+    // per-pixel pull-back, then the adjoint spin-1 synthesis (scaled by sqrt(l(l+1)))
+    RC_TRY(lens_vjp_launch(P, ptg, grad_map, gd, st));
+    RC_TRY(ring_adjoint(P, 1, gd, gd + P->npix, P->d_Hgl, st));
+    RC_TRY(leg_adjoint(P, 1, 1, P->d_Hgl, true, false, (double2 *)grad_dlm, nullptr, st));
     return CUNUSHT_OK;
 }
 

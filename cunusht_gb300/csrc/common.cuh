@@ -191,6 +191,7 @@ struct cunusht_plan_s {
     double2 *d_ring = nullptr; // Bluestein buffers (unused: in smem)
     double *d_glmap = nullptr; // spin-1 maps on pointing grid       [2][npix]
     double2 *d_alm = nullptr;  // alm staging (dtype conversion)     [2][nalm]
+    double *d_vjp = nullptr;   // lensing VJP scratch: pointing + deflection gradient [4][npix]
     size_t ws_bytes = 0;
 
     // per-stage CUDA-event timing (cunusht_plan_set_profiling)

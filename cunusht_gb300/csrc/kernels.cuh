@@ -42,6 +42,7 @@ int pointing_launch(int nring, const double *rth, const double *rph0, const long
 int pointing_mixed_launch(int nring, int nph_uniform, const double *rth, const float4 *rsc, const double *rph0,
                           const long long *rnph, const long long *rofs, long long npix, const double *dth,
                           const double *dph, double *out_th, double *out_ph, double *out_gamma, cudaStream_t st);
+int lens_vjp_launch(const cunusht_plan_s *P, const double *ptg, const double *grad, double *gd, cudaStream_t st);
 int doubling_launch(const void *in, long long ntheta, long long nphi, int layout, int spin,
                     int dtype, void *out, cudaStream_t st);
 int adjoint_doubling_launch(const void *in, long long ntheta, long long nphi, int spin, int dtype,

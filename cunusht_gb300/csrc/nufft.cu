@@ -506,6 +506,127 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// ------------------------------------------------------------ lensing VJP (spin 0)
+// Vector-Jacobian product of lenmap_j = f(theta'_j, phi'_j) with respect to
+// the deflection d_j = (d_theta, d_phi) of every pixel:
+//   dL/dd_i = g_j [ f_theta(n') e'_theta . dn'/dd_i + f_phi(n') / sin(theta') e'_phi . dn'/dd_i ],
+//   n' = C n + S (d_theta e_theta + d_phi e_phi),  C = cos a, S = sin(a)/a,
+//   dn'/dd_i = -S d_i n + K d_i (d_theta e_theta + d_phi e_phi) + S e_i,  K = (C - S)/a^2,
+// (the pointing rotation of pointing.cu:210-213 as a vector formula).  The
+// derivatives f_theta, f_phi of the unlensed field at the deflected points
+// are interpolated from the same fine grid with the derivative of the same
+// ES kernel, so this is the exact derivative of the implemented forward map.
+template <typename TU>
+__global__ void __launch_bounds__(256)
+    k_lens_vjp_s0(const TU *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, double beta,
+                  int nring, const double *__restrict__ rth, const double *__restrict__ rph0,
+                  const long long *__restrict__ rnph, const long long *__restrict__ rofs, long long npix,
+                  const double *__restrict__ dth, const double *__restrict__ dph,
+                  const double *__restrict__ ptg, const double *__restrict__ grad, double *__restrict__ gd) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npix) return;
+    int lo = 0, hi = nring - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (rofs[mid] <= j) lo = mid;
+        else hi = mid - 1;
+    }
+    const int ring = lo;
+    const double theta = rth[ring];
+    const double phi = rph0[ring] + (double)(j - rofs[ring]) * (TWOPI / (double)rnph[ring]);
+    const double tp = ptg[j], pp = ptg[npix + j];
+    const PointCoords pc = point_coords(tp, pp, Ntf, Npf, n_lo, nrows, w);
+    double kt[MAXW], dkt[MAXW], kp[MAXW], dkp[MAXW];
+    const double sc = 2.0 / w;
+    const double dzt = -sc * Ntf / TWOPI, dzp = -sc * Npf / TWOPI;  // dz / dtheta, dz / dphi
+#pragma unroll
+    for (int a = 0; a < MAXW; ++a) {
+        if (a < w) {
+            const double zt = (pc.ft + a) * sc, zp = (pc.fp + a) * sc;
+            const double qt = 1.0 - zt * zt, qp = 1.0 - zp * zp;
+            const double rt = qt > 0.0 ? sqrt(qt) : 0.0, rp = qp > 0.0 ? sqrt(qp) : 0.0;
+            kt[a] = qt > 0.0 ? exp(beta * (rt - 1.0)) : 0.0;
+            kp[a] = qp > 0.0 ? exp(beta * (rp - 1.0)) : 0.0;
+            dkt[a] = qt > 1e-24 ? kt[a] * (-beta * zt / rt) * dzt : 0.0;
+            dkp[a] = qp > 1e-24 ? kp[a] * (-beta * zp / rp) * dzp : 0.0;
+        }
+    }
+    double ft = 0.0, fp = 0.0;
+    for (int a = 0; a < w; ++a) {
+        const TU *row = U + (long long)(pc.r0 + a) * Npf;
+        double r0 = 0.0, r1 = 0.0;
+#pragma unroll
+        for (int b = 0; b < MAXW; ++b) {
+            if (b < w) {
+                int c = pc.p0 + b;
+                c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+                const double v = (double)row[c];
+                r0 = fma(kp[b], v, r0);
+                r1 = fma(dkp[b], v, r1);
+            }
+        }
+        ft = fma(dkt[a], r0, ft);
+        fp = fma(kt[a], r1, fp);
+    }
+    const double g = grad[j];
+    const double Gt = g * ft, Gp = g * fp;
+    const double t = dth[j], p = dph[j];
+    const double a2 = t * t + p * p;
+    double S, C, K;
+    if (a2 < 1e-3) {
+        S = 1.0 - a2 / 6.0 * (1.0 - a2 / 20.0 * (1.0 - a2 / 42.0 * (1.0 - a2 / 72.0)));
+        C = 1.0 - a2 / 2.0 * (1.0 - a2 / 12.0 * (1.0 - a2 / 30.0 * (1.0 - a2 / 56.0)));
+        K = -1.0 / 3.0 + a2 / 30.0 - a2 * a2 / 840.0 + a2 * a2 * a2 / 45360.0;
+    } else {
+        const double a = sqrt(a2);
+        double sa;
+        sincos(a, &sa, &C);
+        S = sa / a;
+        K = (C - S) / a2;
+    }
+    double st, ct, sp, cp;
+    sincos(theta, &st, &ct);
+    sincos(phi, &sp, &cp);
+    const double n[3] = {st * cp, st * sp, ct};
+    const double et[3] = {ct * cp, ct * sp, -st};
+    const double ep[3] = {-sp, cp, 0.0};
+    double stq, ctq, spq, cpq;
+    sincos(tp, &stq, &ctq);
+    sincos(pp, &spq, &cpq);
+    const double etq[3] = {ctq * cpq, ctq * spq, -stq};
+    const double epq[3] = {-spq, cpq, 0.0};
+    const double gpq = Gp / fmax(stq, 1e-300);
+    double dt_t = 0.0, dt_p = 0.0, dp_t = 0.0, dp_p = 0.0;  // e'_theta . dn'/dd_t, ...
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double dv = t * et[i] + p * ep[i];
+        const double dnt = -S * t * n[i] + K * t * dv + S * et[i];
+        const double dnp = -S * p * n[i] + K * p * dv + S * ep[i];
+        dt_t += etq[i] * dnt;
+        dp_t += epq[i] * dnt;
+        dt_p += etq[i] * dnp;
+        dp_p += epq[i] * dnp;
+    }
+    gd[j] = Gt * dt_t + gpq * dp_t;
+    gd[npix + j] = Gt * dt_p + gpq * dp_p;
+}
+
+int lens_vjp_launch(const cunusht_plan_s *P, const double *ptg, const double *grad, double *gd, cudaStream_t st) {
+    const int nb = (int)((P->npix + 255) / 256);
+    if (P->fwd_u32 || P->grid_fp32)
+        k_lens_vjp_s0<float><<<nb, 256, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                 P->beta, P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph,
+                                                 P->d_ring_ofs, P->npix, P->d_glmap, P->d_glmap + P->npix, ptg, grad,
+                                                 gd);
+    else
+        k_lens_vjp_s0<double><<<nb, 256, 0, st>>>((const double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                  P->beta, P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph,
+                                                  P->d_ring_ofs, P->npix, P->d_glmap, P->d_glmap + P->npix, ptg,
+                                                  grad, gd);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
 int pointing_mixed_launch(int nring, int nph_uniform, const double *rth, const float4 *rsc, const double *rph0,
                           const long long *rnph,
                           const long long *rofs, long long npix, const double *dth, const double *dph,

@@ -135,6 +135,20 @@ int cunusht_dlm2pointing(cunusht_plan_t *plan, const void *dlm_scaled, const voi
                          int alm_dtype, double *ptg, double *gamma, void *stream);
 
 /*
+ * Vector-Jacobian product of the spin-0 lensing map with respect to the
+ * scaled lensing potential: for lenmap = gclm2lenmap(gclm, dlm_scaled) and a
+ * map gradient g = dL/dlenmap (npix float64), returns grad_dlm (complex128,
+ * nalm) = sqrt(l(l+1)) x spin-1 adjoint synthesis of J^T (g grad f), with f the
+ * unlensed field and J the Jacobian of the pointing rotation
+ * (pointing.cu:210-213).  Same alm inner-product convention as
+ * cunusht_nusht2d1 (m > 0 counted twice).  Backward of the differentiable
+ * gclm2lenmap; the reference has no gradient path.  Spin 0 only.
+ */
+int cunusht_lensing_vjp_dlm(cunusht_plan_t *plan, int spin, const void *gclm, int alm_dtype,
+                            const void *dlm_scaled, int dlm_dtype, const double *grad_map,
+                            void *grad_dlm, void *stream);
+
+/*
  * Spin-s synthesis / adjoint synthesis on the plan's ring geometry (SHT-only
  * mode; GPU_cufinufft_transformer.synthesis / adjoint_synthesis,
  * GPU_nufft_transformer.py:356-383).  maps as above (npix or 2 x npix, FP64).

@@ -290,3 +290,42 @@ def test_mixed_dlm2pointing_matches_oracle(cu):
     assert np.max(np.abs(dt)) < 2e-9 and np.max(np.abs(dp)) < 2e-9
     rg = orc.rotation_gamma(th, d[0], d[1])
     assert np.max(np.abs(np.angle(np.exp(1j * (T.gamma.cpu().numpy() - rg))))) < 1e-8
+
+
+# ------------------------------------------------------------------ curl deflection, spin-2 adjoint lensing
+def test_dlm2pointing_with_curl_matches_oracle(cu):
+    """Gradient + curl deflection (config 2 pattern): spin-1 synthesis of
+    (dlm, dclm) then the pointing rotation."""
+    lmax = 127
+    T = _T(cu, lmax)
+    _, dls = orc.make_inputs(lmax, 0, seed=21, curl=True)
+    ptg = T.dlm2pointing(torch.as_tensor(dls[0], device="cuda"), lmax, 0,
+                         dclm_scaled=torch.as_tensor(dls[1], device="cuda")).cpu().numpy()
+    th, ph = T.geom.pixels()
+    ll = np.arange(lmax + 1)
+    fl = np.sqrt(ll * (ll + 1.0))
+    dd = np.stack([orc.almxfl(dls[0], fl, lmax), orc.almxfl(dls[1], fl, lmax)])
+    d = oracle.synth_points_c(lmax, 1, dd, th, ph)
+    rt, rp = orc.pointing(th, ph, d[0], d[1])
+    assert np.max(np.abs(ptg[0] - rt)) < 1e-13
+    assert np.max(np.abs(np.angle(np.exp(1j * (ptg[1] - rp))))) < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_lensing_adjointness_spin2_with_rotation(cu, precision):
+    """<y, gclm2lenmap(x)> = <lenmap2gclm(y), x> for spin 2 with the exp(2 i gamma)
+    rotation (E and B components)."""
+    lmax = 127
+    T = _T(cu, lmax, eps=1e-8 if precision == "fp64" else 1e-7, precision=precision)
+    rng = np.random.default_rng(31)
+    _, dls = orc.make_inputs(lmax, 0, seed=22)
+    d = torch.as_tensor(dls[0], device="cuda")
+    x = ralm(lmax, 2, rng, 2)
+    Ax = T.gclm2lenmap(torch.as_tensor(x, device="cuda"), lmax, lmax, dlm_scaled=d, spin=2, verbose=0).cpu().numpy()
+    y = rng.standard_normal(Ax.shape)
+    AHy = T.lenmap2gclm(torch.as_tensor(y, device="cuda"), d, None, lmax, lmax, spin=2, verbose=0).cpu().numpy()
+    lhs = float(np.sum(y * Ax))
+    rhs = orc.alm_dot(AHy[0], x[0], lmax) + orc.alm_dot(AHy[1], x[1], lmax)
+    # mixed: the forward carries ~1e-7 arithmetic error (eps 1e-7) while the
+    # adjoint runs in FP64, so the two agree to a few eps, not to FP64 rounding
+    np.testing.assert_allclose(lhs, rhs, rtol=5e-7 if precision == "mixed" else 1e-9)
