@@ -1,16 +1,18 @@
 #!/usr/bin/env python
-"""Benchmark: lensing solves/s at lmax 2047, spin 2, epsilon 1e-7.
+"""Benchmark: lensing solves/s at lmax 2047, spin 2, epsilon 1e-7, served form.
 
-A step is one lensing solve on one request: dlm2pointing (spin-1 synthesis of
-the deflection on the GL 2048 x 4095 grid + pointing rotation) followed by the
-spin-2 nusht2d2 of the E-mode alm at the deflected points with the exp(2 i
-gamma) polarisation rotation -- the reference's gclm2lenmap
-(cunusht/deflection/GPU_nufft_transformer.py:487-578) without its pointing cache
-(a fresh deflection field every step).
+A step is one launch of the served form: B lensing requests (default 4), each
+with its own gclm and deflection, through cunusht_lensing_batch --
+dlm2pointing (spin-1 synthesis of the deflection on the GL 2048 x 4095 grid +
+pointing rotation) followed by the spin-2 nusht2d2 of the E-mode alm at the
+deflected points with the exp(2 i gamma) polarisation rotation: the
+reference's gclm2lenmap (cunusht/deflection/GPU_nufft_transformer.py:487-578)
+without its pointing cache.  Beside it, on the same GPU: the mixed-precision
+single-request form and the plain FP64 single-request form.
 
-  value  inputs resident in HBM, calls through the C ABI (whole job, all ranks)
-  e2e    the public API (GPU_cufinufft_transformer.gclm2lenmap) from pinned host
-         buffers: H2D of gclm + dlm, the solve, D2H of the lensed Q/U map,
+  value  served throughput, inputs resident in HBM (whole job, all ranks)
+  e2e    the same through the public API from pinned host buffers: H2D of the
+         B requests' gclm + dlm, the launch, D2H of the B lensed Q/U maps,
          every step, inside the timed region
 Multi-GPU (torchrun): independent replicas per rank (weak scaling), timed with
 a barrier on both sides, max over ranks.
@@ -34,7 +36,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7"
+METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7 (served mixed vs plain FP64); p99 ms"
 # DRAM bytes (read + write) per launch from one ncu capture at lmax 2047
 # (profiles/leg_synth_spin_df_l2047.md)
 LEG_TRAFFIC = {"leg_synth": 196.3e6, "ptg_leg": 161.1e6}
@@ -54,6 +56,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the cpu_baseline sample")
+    p.add_argument("--batch", type=int, default=4, help="requests per launch of the served form")
+    p.add_argument("--fp64-steps", type=int, default=3, help="timed solves of the plain FP64 single-request form")
     return p.parse_args()
 
 
@@ -242,10 +246,13 @@ def main():
 
     lmax, spin, eps = args.lmax, args.spin, args.eps
     nphi = args.nphi or 2 * lmax + 1
+    B = args.batch
     T = cu.get_transformer("GPU")(("gl", {"lmax": lmax, "nphi": nphi}), nuFFTtype=2, epsilon=eps,
                                   precision=args.precision, max_spin=max(spin, 1))
     npix, nring = T.npix(), lmax + 1
-    gclm_h, plm_a = synth_inputs(lmax, spin, seed=1 + 17 * rank)
+    # B distinct requests (request 0 is the one the CPU baseline samples)
+    reqs = [synth_inputs(lmax, spin, seed=1 + 17 * rank + 1000 * b) for b in range(B)]
+    gclm_h, plm_a = reqs[0]
     _, plm_b = synth_inputs(lmax, spin, seed=2 + 17 * rank)
     ncomp = gclm_h.shape[0]
     G = torch.as_tensor(gclm_h if spin else gclm_h[0], device=dev)
@@ -253,6 +260,10 @@ def main():
     out = torch.empty((2, npix) if spin else (npix,), dtype=torch.float64, device=dev)
     ptg = torch.empty((2, npix), dtype=torch.float64, device=dev)
     gam = torch.empty((npix,), dtype=torch.float64, device=dev)
+    GB = torch.as_tensor(np.stack([r[0] for r in reqs]), device=dev)        # (B, ncomp, nalm)
+    DB = torch.as_tensor(np.stack([r[1] for r in reqs]), device=dev)        # (B, nalm)
+    outB = torch.empty((B, 2, npix) if spin else (B, npix), dtype=torch.float64, device=dev)
+    T.reserve_batch(B)
 
     def barrier():
         if world > 1:
@@ -265,41 +276,68 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    # ---------------- device-resident timing (value)
-    for i in range(args.warmup):
-        T.lensing_solve(G, D[i % 2], out, ptg, gam, spin)
-    torch.cuda.synchronize()
-    T.profile(True)
-    T.stage_times()
-    clk = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
-    if clk:
-        clk.start()
-    barrier()
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    ev[0].record()
-    for k in range(args.steps):
-        T.lensing_solve(G, D[k % 2], out, ptg, gam, spin)
-        ev[k + 1].record()
-    torch.cuda.synchronize()
-    barrier()
-    clocks = clk.stop() if clk else None
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    total_s = ev[0].elapsed_time(ev[-1]) * 1e-3
-    stages = T.stage_times()
-    T.profile(False)
-    total_s = maxall(total_s)
-    value = world * args.steps / total_s
+    def timed(fn, steps, warmup, profile=False, sample_clocks=False):
+        """CUDA-event timing of `steps` calls after `warmup` untimed ones;
+        barrier + synchronize on both sides; returns (total_s max over ranks,
+        per-step ms, stage table or None, clocks or None)."""
+        for i in range(warmup):
+            fn(i)
+        torch.cuda.synchronize()
+        if profile:
+            T.profile(True)
+            T.stage_times()
+        clk = ClockSampler(torch.cuda.current_device()) if (sample_clocks and rank == 0) else None
+        if clk:
+            clk.start()
+        barrier()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record()
+        for k in range(steps):
+            fn(k)
+            ev[k + 1].record()
+        torch.cuda.synchronize()
+        barrier()
+        clocks = clk.stop() if clk else None
+        st = None
+        if profile:
+            st = T.stage_times()
+            T.profile(False)
+        per = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+        return maxall(ev[0].elapsed_time(ev[-1]) * 1e-3), per, st, clocks
+
+    # ---------------- served form: B requests per launch, inputs resident (value)
+    total_s, step_ms, stages, clocks = timed(lambda k: T.lensing_batch(GB, DB, spin, out=outB), args.steps,
+                                             args.warmup, profile=True, sample_clocks=True)
+    value = world * B * args.steps / total_s
     launches = int(sum(c for _, c in stages.values()))
 
-    # ---------------- roofline of the dominant stage
+    # ---------------- single-request forms on the same GPU
+    single_s, single_ms, _, _ = timed(lambda k: T.lensing_solve(G, D[k % 2], out, ptg, gam, spin),
+                                      max(2, args.steps // 2), 1)
+    single = {"value": world * max(2, args.steps // 2) / single_s, "unit": "solves/s",
+              "p50_ms": float(np.percentile(single_ms, 50)), "p99_ms": float(np.percentile(single_ms, 99)),
+              "precision": args.precision}
+    fp64 = None
+    if args.fp64_steps > 0 and args.precision != "fp64":
+        T64 = cu.get_transformer("GPU")(("gl", {"lmax": lmax, "nphi": nphi}), nuFFTtype=2, epsilon=eps,
+                                        precision="fp64", max_spin=max(spin, 1))
+        f_s, f_ms, _, _ = timed(lambda k: T64.lensing_solve(G, D[k % 2], out, ptg, gam, spin), args.fp64_steps, 1)
+        fp64 = {"value": world * args.fp64_steps / f_s, "unit": "solves/s",
+                "p50_ms": float(np.percentile(f_ms, 50)), "p99_ms": float(np.percentile(f_ms, 99)),
+                "precision": "fp64", "requests_per_launch": 1}
+        T64._destroy()
+        del T64
+        torch.cuda.empty_cache()
+
+    # ---------------- roofline of the dominant stage (per launch = B requests)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     info = dict(T.info, grid_fp32=bool(T.single_prec and args.precision != "fp64"))
-    q = stage_quantities(info, lmax, spin, nring, npix)
+    q = {k: (kind, B * amount) for k, (kind, amount) in stage_quantities(info, lmax, spin, nring, npix).items()}
     dom = max(stages, key=lambda s: stages[s][0])
     avg_s = stages[dom][0] / stages[dom][1] * 1e-3
     kind, amount = q.get(dom, ("bytes", 0))
@@ -320,12 +358,14 @@ def main():
             # double-float Legendre on the FP32 pipe: 152 SMs x 128 lanes x 2 flop x max SM clock
             mhz = peaks.get("sm_max_mhz", 2070.0)
             peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+            tr = LEG_TRAFFIC.get(dom)
             roof = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                    "traffic": LEG_TRAFFIC.get(dom), "kernel": dom,
+                    "traffic": tr * B if tr else None, "kernel": dom,
                     "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; "
                                    "achieved counts algorithmic flops only (8 per l,m,ring,component), "
                                    "the double-float arithmetic issues ~15x more: ncu FMA-pipe "
-                                   "utilisation 73 %, issue slots 91 % (profiles/leg_synth_spin_df_l2047.md)"}
+                                   "utilisation 73 %, issue slots 91 % (profiles/leg_synth_spin_df_l2047.md); "
+                                   "traffic scaled from the single-request capture by the requests per launch"}
     stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
                        "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
     for s, v in stage_table.items():
@@ -335,36 +375,42 @@ def main():
             v["achieved"] = amount / (v["ms_per_launch"] * 1e-3) / (1e9 if kind == "bytes" else 1e12)
             v["unit"] = "GB/s" if kind == "bytes" else "TFLOP/s"
 
-    # ---------------- end to end through the public API
+    # ---------------- end to end: host buffers, H2D + served launch + D2H every step
     e2e = None
+    e2e_single = None
     if not args.no_e2e:
         pin = lambda a: torch.as_tensor(a).pin_memory()
+        GBh, DBh = pin(GB.cpu()), pin(DB.cpu())
+        resB = torch.empty(tuple(outB.shape), dtype=torch.float64).pin_memory()
+
+        def e2e_step(k):
+            g = GBh.to(dev, non_blocking=True)
+            d = DBh.to(dev, non_blocking=True)
+            r = T.lensing_batch(g, d, spin, out=outB)
+            resB.copy_(r, non_blocking=True)
+
+        e_s, e_ms, _, _ = timed(e2e_step, args.steps, args.warmup)
+        e2e = {"value": world * B * args.steps / e_s, "unit": "solves/s",
+               "h2d_bytes_per_step": int(GBh.numel() * GBh.element_size() + DBh.numel() * DBh.element_size()),
+               "d2h_bytes_per_step": int(resB.numel() * resB.element_size()),
+               "ms_per_step": e_s * 1e3 / args.steps, "api": "GPU_cufinufft_transformer.lensing_batch",
+               "requests_per_step": B}
+        # the reference's own call, one request per call (gclm2lenmap)
         Gh = pin(gclm_h if spin else gclm_h[0])
         Dh = [pin(plm_a), pin(plm_b)]
         res_h = torch.empty((2, npix) if spin else (npix,), dtype=torch.float64).pin_memory()
-        for i in range(args.warmup):
-            g = Gh.to(dev, non_blocking=True)
-            d = Dh[i % 2].to(dev, non_blocking=True)
-            r = T.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0)
-            res_h.copy_(r, non_blocking=True)
-        torch.cuda.synchronize()
-        barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for k in range(args.steps):
+
+        def e2e_single_step(k):
             g = Gh.to(dev, non_blocking=True)
             d = Dh[k % 2].to(dev, non_blocking=True)
             r = T.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0)
             res_h.copy_(r, non_blocking=True)
-        e1.record()
-        torch.cuda.synchronize()
-        barrier()
-        e2e_s = maxall(e0.elapsed_time(e1) * 1e-3)
-        e2e = {"value": world * args.steps / e2e_s, "unit": "solves/s",
-               "h2d_bytes_per_step": int(Gh.numel() * Gh.element_size() + Dh[0].numel() * Dh[0].element_size()),
-               "d2h_bytes_per_step": int(res_h.numel() * res_h.element_size()),
-               "ms_per_step": e2e_s * 1e3 / args.steps}
+
+        n1 = max(2, args.steps // 2)
+        s1, _, _, _ = timed(e2e_single_step, n1, 1)
+        e2e_single = {"value": world * n1 / s1, "unit": "solves/s", "api": "GPU_cufinufft_transformer.gclm2lenmap",
+                      "h2d_bytes_per_step": int(Gh.numel() * Gh.element_size() + Dh[0].numel() * Dh[0].element_size()),
+                      "d2h_bytes_per_step": int(res_h.numel() * res_h.element_size())}
 
     # ---------------- CPU baseline (rank 0, N=1 only) + accuracy of the same sample
     cpu = None
@@ -376,8 +422,8 @@ def main():
         cpu = {"value": cpu_val, "unit": "solves/s", "cores": threads, "kind": "port",
                "sample": f"{idx.size} of {npix_all} pixels (exact FP64 direct summation of the solve), "
                          "extrapolated to the full map"}
-        T.lensing_solve(G, D[0], out, ptg, gam, spin)
-        got = out.cpu().numpy()
+        T.lensing_batch(GB, DB, spin, out=outB)
+        got = outB[0].cpu().numpy()
         got = got[:, idx] if spin else got[idx]
         acc = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
 
@@ -386,15 +432,20 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64" if T.info["precision"] == 1 or not T.single_prec else "f64-legendre+f32-grid",
+                "dtype": "f64" if T.info["precision"] == 1 else
+                         "mixed: double-float (f32 hi/lo) Legendre + FFTs, f32 fine grid, f64 seeds/pointing",
                 "data": "synthetic (seeded Gaussian alm / deflection, 2.5 arcmin rms)",
-                "config": {"workload": f"lensing solve lmax={lmax} GL {lmax + 1}x{nphi} spin-{spin} eps={eps}",
-                           "precision": args.precision, "requests_per_launch": 1,
-                           "l2": "working set > L2 (fine grid %d MB per solve)" %
+                "config": {"workload": f"served lensing solves lmax={lmax} GL {lmax + 1}x{nphi} spin-{spin} "
+                                       f"eps={eps}, {B} requests per launch",
+                           "precision": args.precision, "requests_per_launch": B,
+                           "l2": "working set > L2 (fine grid %d MB per request)" %
                                  (T.info["fine_rows"] * T.info["nphi_fine"] * (16 if spin else 8) // 2 ** 20)},
                 "p50_ms": float(p50), "p99_ms": float(p99),
+                "latency_note": "closed loop: every request of a launch completes when the launch does",
+                "single_request": single, "fp64_single_request": fp64,
                 "roofline": roof, "stages": stage_table, "gpu_launches": launches,
-                "e2e": e2e, "cpu_baseline": cpu, "rel_err_vs_fp64_oracle_sample": acc, "clocks": clocks}
+                "e2e": e2e, "e2e_single_request": e2e_single, "cpu_baseline": cpu,
+                "rel_err_vs_fp64_oracle_sample": acc, "clocks": clocks}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

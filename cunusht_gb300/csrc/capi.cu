@@ -118,7 +118,8 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
-                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp};
+                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
+                    P->d_glmapb, P->d_ptgb, P->d_gamb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : P->evt_pool) {
@@ -133,6 +134,33 @@ static double lg0_of(int m, int s) {
     const double v = std::log((2.0 * l0 + 1.0) / (4.0 * PI)) + std::lgamma(2.0 * l0 + 1.0) -
                      std::lgamma(m + s + 1.0) - std::lgamma(std::fabs((double)(m - s)) + 1.0);
     return 0.5 * v / std::log(2.0);
+}
+
+// In-place forward DFT X_k = sum_n x_n e^{-2 pi i nk/n} (n a power of two):
+// iterative radix-2 Cooley-Tukey in long double, plan set-up only.
+static void host_fft_forward(std::vector<double2> &a) {
+    const size_t n = a.size();
+    std::vector<std::complex<long double>> x(n);
+    for (size_t i = 0; i < n; ++i) x[i] = {a[i].x, a[i].y};
+    for (size_t i = 1, j = 0; i < n; ++i) {  // bit reversal
+        size_t bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) std::swap(x[i], x[j]);
+    }
+    const long double pi = 3.14159265358979323846264338327950288L;
+    for (size_t len = 2; len <= n; len <<= 1) {
+        for (size_t k = 0; k < len / 2; ++k) {
+            const long double ang = -2.0L * pi * (long double)k / (long double)len;
+            const std::complex<long double> w(std::cos(ang), std::sin(ang));
+            for (size_t i = 0; i < n; i += len) {
+                const std::complex<long double> u = x[i + k], v = x[i + k + len / 2] * w;
+                x[i + k] = u + v;
+                x[i + k + len / 2] = u - v;
+            }
+        }
+    }
+    for (size_t i = 0; i < n; ++i) a[i] = make_double2((double)x[i].real(), (double)x[i].imag());
 }
 
 static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, int max_spin, int nring,
@@ -237,10 +265,14 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     const int n_hi = P->Ntf / 2 + hw + 1;
     P->nrows = n_hi - P->n_lo + 1;
     {
-        const size_t need = fft_smem_bytes(std::max(P->Ntf, P->Npf), P->grid_fp32);
-        if (need > 227 * 1024) {
-            set_error("lmax %d needs a %zu-byte shared-memory FFT in %s; use epsilon > 1e-6 (FP32 grid)", lmax,
-                      need, P->grid_fp32 ? "FP32" : "FP64");
+        // transforms longer than 16 x FFT_TPB points run as two half-length
+        // transforms split by output parity (a half-size shared buffer)
+        const int emax = 16 * FFT_TPB;
+        P->sp_theta = P->Ntf > emax ? 2 : 1;
+        P->sp_phi = P->Npf > emax ? 2 : 1;
+        const int nb = std::max(P->Ntf / P->sp_theta, P->Npf / P->sp_phi);
+        if (nb > emax) {
+            set_error("lmax %d needs %d-point fine-grid transforms; at most lmax 4095 is supported", lmax, nb);
             return CUNUSHT_ERR_UNSUPPORTED;
         }
     }
@@ -294,9 +326,10 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     {
         const int N = P->nph_uniform;
         P->Mb = next_pow2(2LL * N - 1);
-        if (fft_smem_bytes(P->Mb, false) > 227 * 1024) {
-            set_error("ring length %d needs a Bluestein FFT of %d points, above the FP64 shared-memory limit", N,
-                      P->Mb);
+        P->sp_ring = P->Mb > 16 * FFT_TPB ? 2 : 1;
+        if (P->Mb / P->sp_ring > 16 * FFT_TPB) {
+            set_error("ring length %d needs a Bluestein FFT of %d points; at most 8192 pixels per ring are supported",
+                      N, P->Mb);
             return CUNUSHT_ERR_UNSUPPORTED;
         }
         std::vector<double2> chirp(N), bk(P->Mb, make_double2(0.0, 0.0));
@@ -327,7 +360,15 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         RC_TRY(upload(P, &P->d_tw64, tw));
         RC_TRY(upload(P, &P->d_tw32, tw32));
     }
-    RC_TRY(fft_global_f64(P->d_bker, P->Mb, -1, P->d_tw64, P->TW, 0));
+    if (P->sp_ring == 1) {
+        RC_TRY(fft_global_f64(P->d_bker, P->Mb, -1, P->d_tw64, P->TW, 0));
+    } else {
+        // too long for one shared-memory transform: the kernel spectrum on the host
+        std::vector<double2> bk(P->Mb);
+        CU_TRY(cudaMemcpy(bk.data(), P->d_bker, P->Mb * sizeof(double2), cudaMemcpyDeviceToHost));
+        host_fft_forward(bk);
+        CU_TRY(cudaMemcpy(P->d_bker, bk.data(), P->Mb * sizeof(double2), cudaMemcpyHostToDevice));
+    }
     if (P->fft_df) {
         char *t = nullptr, *c = nullptr, *b = nullptr;
         RC_TRY(dalloc(P, &t, 16 * (size_t)P->TW));
@@ -351,6 +392,10 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         P->d_F = f;
         RC_TRY(dalloc(P, &u, usz * (size_t)P->nrows * P->Npf));
         P->d_U = u;
+        if (P->sp_theta == 2 && (size_t)ncols * P->Nt * gsz > usz * (size_t)P->nrows * P->Npf) {
+            set_error("internal: split theta adjoint scratch does not fit the fine-grid workspace");
+            return CUNUSHT_ERR_UNSUPPORTED;
+        }
         RC_TRY(dalloc(P, &P->d_Hgl, (size_t)(2 * lmax + 1) * nring));
         RC_TRY(dalloc(P, &P->d_glmap, 2 * (size_t)npix));
         RC_TRY(dalloc(P, &P->d_alm, 2 * (size_t)P->nalm));
@@ -453,6 +498,16 @@ int cunusht_plan_info(const cunusht_plan_t *P, int64_t *info, int ninfo) {
     return n;
 }
 
+int cunusht_plan_force_split(cunusht_plan_t *P, int force) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    const int emax = 16 * FFT_TPB;
+    P->sp_theta = (force || P->Ntf > emax) ? 2 : 1;
+    P->sp_phi = (force || P->Npf > emax) ? 2 : 1;
+    P->sp_ring = (force || P->Mb > emax) ? 2 : 1;
+    return CUNUSHT_OK;
+}
+
 int cunusht_plan_set_profiling(cunusht_plan_t *P, int enable) {
     clear_error();
     RC_TRY(check_plan(P));
@@ -478,6 +533,97 @@ int cunusht_plan_stage_times(cunusht_plan_t *P, double *ms, int64_t *count, int 
         }
         P->stage_ms[i] = 0.0;
         P->stage_cnt[i] = 0;
+    }
+    return CUNUSHT_OK;
+}
+
+static size_t f_elem(const cunusht_plan_s *P) { return P->grid_fp32 ? sizeof(float2) : 16; }
+static size_t u_scalar(const cunusht_plan_s *P) { return (P->grid_fp32 || P->fwd_u32) ? sizeof(float) : sizeof(double); }
+
+int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(max_batch >= 1 && max_batch <= 64, "max_batch must be in [1, 64], got %d", max_batch);
+    if (max_batch <= P->batch_cap) return CUNUSHT_OK;
+    void *old[] = {P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb, P->d_glmapb, P->d_ptgb, P->d_gamb};
+    CU_TRY(cudaDeviceSynchronize());
+    for (void *q : old)
+        if (q) cudaFree(q);
+    P->d_Hb = nullptr;
+    P->d_Fb = P->d_Ub = nullptr;
+    P->d_Hglb = nullptr;
+    P->d_glmapb = P->d_ptgb = P->d_gamb = nullptr;
+    P->batch_cap = 0;
+    const int L = P->lmax;
+    const size_t B = max_batch;
+    const size_t ncols = P->max_spin ? 2 * (size_t)L + 1 : (size_t)L + 1;
+    char *f = nullptr, *u = nullptr;
+    RC_TRY(dalloc(P, &P->d_Hb, B * ncols * P->ncc));
+    RC_TRY(dalloc(P, &f, B * f_elem(P) * ncols * P->nrows));
+    RC_TRY(dalloc(P, &u, B * u_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf));
+    P->d_Fb = f;
+    P->d_Ub = u;
+    RC_TRY(dalloc(P, &P->d_Hglb, B * (2 * (size_t)L + 1) * P->nring));
+    RC_TRY(dalloc(P, &P->d_glmapb, B * 2 * (size_t)P->npix));
+    RC_TRY(dalloc(P, &P->d_ptgb, B * 2 * (size_t)P->npix));
+    RC_TRY(dalloc(P, &P->d_gamb, B * (size_t)P->npix));
+    P->batch_cap = max_batch;
+    return CUNUSHT_OK;
+}
+
+int cunusht_lensing_batch(cunusht_plan_t *P, int nreq, int spin, int ncomp, const void *gclm,
+                          const void *dlm_scaled, const void *dclm_scaled, double *ptg, double *gamma, void *out,
+                          int out_dtype, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    RC_TRY(check_spin(P, spin, ncomp));
+    ARG_CHECK(nreq >= 1, "nreq must be >= 1");
+    ARG_CHECK(nreq <= P->batch_cap, "nreq %d exceeds the reserved batch capacity %d (cunusht_plan_reserve_batch)",
+              nreq, P->batch_cap);
+    ARG_CHECK(gclm && dlm_scaled && out, "NULL array argument");
+    ARG_CHECK(out_dtype == CUNUSHT_F64 || out_dtype == CUNUSHT_F32, "bad out dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int L = P->lmax;
+    const long long npix = P->npix, nalm = P->nalm;
+    const long long ncols = spin ? 2LL * L + 1 : (long long)L + 1;
+    const long long hgl_s = (2LL * L + 1) * P->nring;
+    double *ptg_b = ptg ? ptg : P->d_ptgb;
+    double *gam_b = gamma ? gamma : (spin ? P->d_gamb : nullptr);
+    // pointing of every request
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_LEG, st);
+        RC_TRY(leg_synth_batch(P, nreq, 1, (const double2 *)dlm_scaled, (const double2 *)dclm_scaled, nalm, true,
+                               false, P->d_Hglb, hgl_s, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_RING, st);
+        RC_TRY(ring_synth_batch(P, nreq, 1, P->d_Hglb, hgl_s, P->d_glmapb, P->d_glmapb + npix, 2 * npix, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_ROT, st);
+        RC_TRY(pointing_batch(P, nreq, P->d_glmapb, 2 * npix, ptg_b, 2 * npix, gam_b, st));
+    }
+    // synthesis at the deflected points
+    const double2 *G = (const double2 *)gclm;
+    const long long fs = (long long)P->nrows * ncols;
+    const long long us = (long long)P->nrows * P->Npf;
+    {
+        StageScope sc(P, CUNUSHT_STAGE_LEG_SYNTH, st);
+        RC_TRY(leg_synth_batch(P, nreq, spin, G, ncomp > 1 ? G + nalm : nullptr, ncomp * nalm, false, true, P->d_Hb,
+                               ncols * P->ncc, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_THETA_FWD, st);
+        RC_TRY(theta_fwd_batch(P, nreq, spin, P->d_Hb, ncols * P->ncc, P->d_Fb, fs, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PHI_FWD, st);
+        RC_TRY(phi_fwd_batch(P, nreq, spin, P->d_Fb, fs, P->d_Ub, us, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_INTERP, st);
+        RC_TRY(nufft_interp_batch(P, nreq, spin, P->d_Ub, (spin ? 2 : 1) * us, ptg_b, 2 * npix, npix, 1, gam_b, out,
+                                  (spin ? 2 : 1) * npix, out_dtype, st));
     }
     return CUNUSHT_OK;
 }

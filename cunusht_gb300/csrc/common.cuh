@@ -155,6 +155,10 @@ struct cunusht_plan_s {
     // doubled Clenshaw-Curtis torus and fine (oversampled) nuFFT grid
     int Nt = 0, Np = 0, ncc = 0;   // torus theta / phi lengths, CC rings = Nt/2+1
     int Ntf = 0, Npf = 0;          // fine grid lengths
+    // parity split of the long transforms: 2 when a transform of more than
+    // 16 x FFT_TPB points is done as two half-length transforms (even / odd
+    // outputs) in a buffer of half the size, else 1
+    int sp_theta = 1, sp_phi = 1, sp_ring = 1;
     int w = 0;                     // ES kernel width
     double beta = 0.0;
     int n_lo = 0, nrows = 0;       // fine rows stored: n in [n_lo, n_lo + nrows)
@@ -192,6 +196,15 @@ struct cunusht_plan_s {
     double *d_glmap = nullptr; // spin-1 maps on pointing grid       [2][npix]
     double2 *d_alm = nullptr;  // alm staging (dtype conversion)     [2][nalm]
     double *d_vjp = nullptr;   // lensing VJP scratch: pointing + deflection gradient [4][npix]
+    // batched-solve workspace (cunusht_plan_reserve_batch), per request:
+    int batch_cap = 0;
+    double2 *d_Hb = nullptr;    // [cap][ncols][ncc]
+    void *d_Fb = nullptr;       // [cap][nrows][ncols]
+    void *d_Ub = nullptr;       // [cap][nrows][Npf] (x2 for spin)
+    double2 *d_Hglb = nullptr;  // [cap][2L+1][nring]
+    double *d_glmapb = nullptr; // [cap][2][npix]
+    double *d_ptgb = nullptr;   // [cap][2][npix]
+    double *d_gamb = nullptr;   // [cap][npix]
     size_t ws_bytes = 0;
 
     // per-stage CUDA-event timing (cunusht_plan_set_profiling)

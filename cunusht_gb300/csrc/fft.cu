@@ -168,15 +168,14 @@ __device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const c
     }
 }
 
-// In-place FFT of length N (power of two, 2 <= N <= 16 blockDim; 32 blockDim
-// for float) in shared memory.  dir = -1: X_k = sum_n x_n e^{-2 pi i nk/N};
-// dir = +1: the unnormalised inverse.  tw[t] = e^{-2 pi i t / TW}, N | TW.
+// In-place FFT of length N (power of two, 2 <= N <= 16 blockDim) in shared
+// memory.  dir = -1: X_k = sum_n x_n e^{-2 pi i nk/N}; dir = +1: the
+// unnormalised inverse.  tw[t] = e^{-2 pi i t / TW}, N | TW.  Longer
+// transforms are split by output parity in the callers (sp_* of the plan).
 template <typename T>
-__device__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
+__device__ __forceinline__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
     const int B = blockDim.x;
-    if (N > 16 * B) {
-        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 32, 3>(buf, N, dir, tw, TW);
-    } else if (N > 8 * B) {
+    if (N > 8 * B) {
         // 16 elements per thread: radix <= 8 for float, <= 4 for double and
         // double-float keeps the pass within the 128-register budget of a
         // 512-thread block
@@ -195,25 +194,44 @@ size_t fft_smem_bytes(int N, bool f32) { return (size_t)N * (f32 ? sizeof(float2
 
 template <typename T> __device__ __forceinline__ cplx<T> czero() { return mk<T>(cvt<T>(0.0), cvt<T>(0.0)); }
 
+// e^{dirsign 2 pi i k / TW'} from the table, tstep = TW / TW' (TW' | TW,
+// |k| < TW'), dirsign = +-1
+template <typename T>
+__device__ __forceinline__ cplx<T> twk(const cplx<T> *__restrict__ tw, int k, int tstep, int dirsign) {
+    cplx<T> w = tw[(k < 0 ? -k : k) * tstep];
+    if ((k < 0) != (dirsign > 0)) w.y = -w.y;
+    return w;
+}
+
 __device__ __forceinline__ int wrapi(int n, int N) {
     n %= N;
     return n < 0 ? n + N : n;
 }
 
 // ------------------------------------------------------------ theta pass
+// SP = 2 (long columns): the 2 Nt-point inverse is done as two Nt-point
+// inverses, one per output parity q = blockIdx.z: y_{2j+q} = sum_k X_k
+// e^{i pi k q / Nt} e^{2 pi i k j / Nt} (X band-limited to |k| < Nt/2), each
+// block repeating the forward Nt-point transform.  (A loop over q inside the
+// block would put the inlined transforms in a loop, which ptxas compiles to a
+// 32-register spilling kernel.)
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_theta_fwd(const double2 *__restrict__ H, int ldH, int Nt, int Ntf, int spin, int mofs, int L,
                 const double *__restrict__ Dth, const double *__restrict__ Dph,
                 cplx<T> *__restrict__ F, int ncols, int n_lo, int nrows,
-                const cplx<T> *__restrict__ tw, int TW) {
+                const cplx<T> *__restrict__ tw, int TW, long long hbs, long long fbs, int SP) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    H += blockIdx.y * hbs;  // request of a batch
+    F += blockIdx.y * fbs;
+    const int q = blockIdx.z;
     const int c = blockIdx.x;
     const int m = c - mofs;
     const double sgn = ((abs(m) + spin) & 1) ? -1.0 : 1.0;
     const double2 *col = H + (long long)c * ldH;
     const int half = Nt / 2;
+    const double dm = Dph[m + L];
     for (int k = threadIdx.x; k < Nt; k += blockDim.x) {
         const bool lo = k <= half;
         const double2 v = lo ? col[k] : col[Nt - k];
@@ -222,45 +240,77 @@ __global__ void __launch_bounds__(FFT_TPB)
     }
     __syncthreads();
     fft_smem<T>(buf, Nt, -1, tw, TW);
-    const double dm = Dph[m + L];
-    for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
-        const int src = Nt - 1 - i;  // kappa = -(i+1)
-        buf[Ntf - 1 - i] = cscale(buf[src], cvt<T>(Dth[src] * dm));
+    if (SP == 1) {
+        for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
+            const int src = Nt - 1 - i;  // kappa = -(i+1)
+            buf[Ntf - 1 - i] = cscale(buf[src], cvt<T>(Dth[src] * dm));
+        }
+        for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
+        __syncthreads();
+        for (int i = half + threadIdx.x; i <= Ntf - half; i += blockDim.x) buf[i] = czero<T>();
+    } else {
+        const int tstep = TW / Ntf;
+        for (int i = threadIdx.x; i < Nt; i += blockDim.x) {
+            // Dth[half] = 0 drops the Nyquist term
+            cplx<T> v = cscale(buf[i], cvt<T>(Dth[i] * dm));
+            if (q) v = cmul(v, twk<T>(tw, i < half ? i : i - Nt, tstep, +1));
+            buf[i] = v;
+        }
     }
-    for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
     __syncthreads();
-    for (int i = half + threadIdx.x; i <= Ntf - half; i += blockDim.x) buf[i] = czero<T>();
-    __syncthreads();
-    fft_smem<T>(buf, Ntf, +1, tw, TW);
-    for (int r = threadIdx.x; r < nrows; r += blockDim.x)
-        F[(long long)r * ncols + c] = buf[wrapi(r + n_lo, Ntf)];
+    fft_smem<T>(buf, Ntf / SP, +1, tw, TW);
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const int n = wrapi(r + n_lo, Ntf);
+        if (SP == 1) F[(long long)r * ncols + c] = buf[n];
+        else if ((n & 1) == q) F[(long long)r * ncols + c] = buf[n >> 1];
+    }
 }
 
+// SP = 2: Z_k = E_k + e^{-i pi k / Nt} O_k with E / O the Nt-point transforms
+// of the even / odd fine rows: launched for q = 1 (odd rows, phase applied,
+// written to the scratch S, Nt values per column), then q = 0 (even rows plus
+// S, deconvolution, inverse transform to the CC column).
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_theta_adj(const cplx<T> *__restrict__ F, int ncols, int n_lo, int nrows, int Nt, int Ntf,
                 int spin, int mofs, int L, const double *__restrict__ Dth,
                 const double *__restrict__ Dph, double2 *__restrict__ H, int ldH,
-                const cplx<T> *__restrict__ tw, int TW) {
+                const cplx<T> *__restrict__ tw, int TW, int SP, int q, cplx<T> *__restrict__ S) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
     const int c = blockIdx.x;
     const int m = c - mofs;
     const T sgn = cvt<T>(((abs(m) + spin) & 1) ? -1.0 : 1.0);
-    for (int i = threadIdx.x; i < Ntf; i += blockDim.x) buf[i] = czero<T>();
-    __syncthreads();
-    for (int r = threadIdx.x; r < nrows; r += blockDim.x)
-        buf[wrapi(r + n_lo, Ntf)] = F[(long long)r * ncols + c];
-    __syncthreads();
-    fft_smem<T>(buf, Ntf, -1, tw, TW);
     const int half = Nt / 2;
     const double dm = Dph[m + L];
-    for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
-        const int dst = Nt - 1 - i;  // kappa = -(i+1)
-        buf[dst] = cscale(buf[Ntf - 1 - i], cvt<T>(Dth[dst] * dm));
+    const int Nb = Ntf / SP;  // forward transform length
+    for (int i = threadIdx.x; i < Nb; i += blockDim.x) buf[i] = czero<T>();
+    __syncthreads();
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const int n = wrapi(r + n_lo, Ntf);
+        if (SP == 1) buf[n] = F[(long long)r * ncols + c];
+        else if ((n & 1) == q) buf[n >> 1] = F[(long long)r * ncols + c];
     }
-    for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
-    if (threadIdx.x == 0) buf[half] = czero<T>();
+    __syncthreads();
+    fft_smem<T>(buf, Nb, -1, tw, TW);
+    if (SP == 1) {
+        for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
+            const int dst = Nt - 1 - i;  // kappa = -(i+1)
+            buf[dst] = cscale(buf[Ntf - 1 - i], cvt<T>(Dth[dst] * dm));
+        }
+        for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
+        if (threadIdx.x == 0) buf[half] = czero<T>();
+    } else {
+        const int tstep = TW / Ntf;
+        cplx<T> *sc = S + (long long)c * Nt;
+        if (q) {
+            for (int i = threadIdx.x; i < Nt; i += blockDim.x)
+                sc[i] = cmul(buf[i], twk<T>(tw, i < half ? i : i - Nt, tstep, -1));
+            return;
+        }
+        for (int i = threadIdx.x; i < Nt; i += blockDim.x)
+            buf[i] = cscale(cadd(buf[i], sc[i]), cvt<T>(Dth[i] * dm));  // Dth[half] = 0
+    }
     __syncthreads();
     fft_smem<T>(buf, Nt, +1, tw, TW);
     double2 *col = H + (long long)c * ldH;
@@ -272,16 +322,25 @@ __global__ void __launch_bounds__(FFT_TPB)
 }
 
 // ------------------------------------------------------------ phi pass
+// SP = 2 (long rows): U_{2j+q} = sum_m X_m e^{i pi m q / Np} e^{2 pi i m j / Np},
+// Np = Npf / 2 >= 2L + 2 (no aliasing): one half-length inverse per parity,
+// q = blockIdx.z in the forward kernels; the adjoint kernels are launched for
+// q = 1 (writes F) and then q = 0 (adds to F).
 // spin 0: two real rows per block packed as one complex transform
 template <typename T, typename TU>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_fwd_s0(const cplx<T> *__restrict__ F, int ncols, int nrows, int Npf, TU *__restrict__ U,
-                 const cplx<T> *__restrict__ tw, int TW) {
+                 const cplx<T> *__restrict__ tw, int TW, long long fbs, long long ubs, int SP) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    F += blockIdx.y * fbs;
+    U += blockIdx.y * ubs;
+    const int q = blockIdx.z;
     const int r1 = 2 * blockIdx.x, r2 = r1 + 1;
     const bool has2 = r2 < nrows;
-    for (int i = threadIdx.x; i < Npf; i += blockDim.x) buf[i] = czero<T>();
+    const int Nb = Npf / SP;
+    const int tstep = TW / Npf;
+    for (int i = threadIdx.x; i < Nb; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
     for (int m = threadIdx.x; m < ncols; m += blockDim.x) {
         const cplx<T> a = F[(long long)r1 * ncols + m];
@@ -289,16 +348,23 @@ __global__ void __launch_bounds__(FFT_TPB)
         if (m == 0) {
             buf[0] = mk<T>(a.x, b.x);
         } else {
-            buf[m] = mk<T>(a.x - b.y, a.y + b.x);
-            buf[Npf - m] = mk<T>(a.x + b.y, b.x - a.y);
+            cplx<T> pp = mk<T>(a.x - b.y, a.y + b.x);  // a + i b at +m
+            cplx<T> pn = mk<T>(a.x + b.y, b.x - a.y);  // conj a + i conj b at -m
+            if (q) {
+                pp = cmul(pp, twk<T>(tw, m, tstep, +1));
+                pn = cmul(pn, twk<T>(tw, -m, tstep, +1));
+            }
+            buf[m] = pp;
+            buf[Nb - m] = pn;
         }
     }
     __syncthreads();
-    fft_smem<T>(buf, Npf, +1, tw, TW);
+    fft_smem<T>(buf, Nb, +1, tw, TW);
     TU *u1 = U + (long long)r1 * Npf;
     TU *u2 = U + (long long)r2 * Npf;
-    for (int p = threadIdx.x; p < Npf; p += blockDim.x) {
-        const cplx<T> z = buf[p];
+    for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
+        const cplx<T> z = buf[j];
+        const int p = SP * j + q;
         u1[p] = to_t<TU>(z.x);
         if (has2) u2[p] = to_t<TU>(z.y);
     }
@@ -307,22 +373,37 @@ __global__ void __launch_bounds__(FFT_TPB)
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_adj_s0(const T *__restrict__ U, int nrows, int Npf, cplx<T> *__restrict__ F, int ncols,
-                 const cplx<T> *__restrict__ tw, int TW) {
+                 const cplx<T> *__restrict__ tw, int TW, int SP, int q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
     const int r1 = 2 * blockIdx.x, r2 = r1 + 1;
     const bool has2 = r2 < nrows;
     const T *u1 = U + (long long)r1 * Npf;
     const T *u2 = U + (long long)r2 * Npf;
-    for (int p = threadIdx.x; p < Npf; p += blockDim.x) buf[p] = mk<T>(u1[p], has2 ? u2[p] : cvt<T>(0.0));
+    const int Nb = Npf / SP;
+    const int tstep = TW / Npf;
+    for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
+        const int p = SP * j + q;
+        buf[j] = mk<T>(u1[p], has2 ? u2[p] : cvt<T>(0.0));
+    }
     __syncthreads();
-    fft_smem<T>(buf, Npf, -1, tw, TW);
+    fft_smem<T>(buf, Nb, -1, tw, TW);
     for (int m = threadIdx.x; m < ncols; m += blockDim.x) {
-        const cplx<T> zm = buf[m];
-        const cplx<T> zn = buf[m == 0 ? 0 : Npf - m];
+        cplx<T> zm = buf[m];
+        cplx<T> zn = buf[m == 0 ? 0 : Nb - m];
+        if (q) {  // odd samples: Z_m gets e^{-i pi m / Np} O_m
+            zm = cmul(zm, twk<T>(tw, m, tstep, -1));
+            zn = cmul(zn, twk<T>(tw, -m, tstep, -1));
+        }
         // U1 = (zm + conj zn)/2 ; U2 = (zm - conj zn)/(2i)
-        F[(long long)r1 * ncols + m] = mk<T>(cvt<T>(0.5) * (zm.x + zn.x), cvt<T>(0.5) * (zm.y - zn.y));
-        if (has2) F[(long long)r2 * ncols + m] = mk<T>(cvt<T>(0.5) * (zm.y + zn.y), cvt<T>(-0.5) * (zm.x - zn.x));
+        cplx<T> f1 = mk<T>(cvt<T>(0.5) * (zm.x + zn.x), cvt<T>(0.5) * (zm.y - zn.y));
+        cplx<T> f2 = mk<T>(cvt<T>(0.5) * (zm.y + zn.y), cvt<T>(-0.5) * (zm.x - zn.x));
+        if (SP == 2 && q == 0) {
+            f1 = cadd(f1, F[(long long)r1 * ncols + m]);
+            if (has2) f2 = cadd(f2, F[(long long)r2 * ncols + m]);
+        }
+        F[(long long)r1 * ncols + m] = f1;
+        if (has2) F[(long long)r2 * ncols + m] = f2;
     }
 }
 
@@ -330,90 +411,133 @@ __global__ void __launch_bounds__(FFT_TPB)
 template <typename T, typename TU>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_fwd_spin(const cplx<T> *__restrict__ F, int L, int Npf, cplx<TU> *__restrict__ U,
-                   const cplx<T> *__restrict__ tw, int TW) {
+                   const cplx<T> *__restrict__ tw, int TW, long long fbs, long long ubs, int SP) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    F += blockIdx.y * fbs;
+    U += blockIdx.y * ubs;
+    const int q = blockIdx.z;
     const int r = blockIdx.x;
     const int ncols = 2 * L + 1;
-    for (int i = threadIdx.x; i < Npf; i += blockDim.x) buf[i] = czero<T>();
+    const int Nb = Npf / SP;
+    const int tstep = TW / Npf;
+    for (int i = threadIdx.x; i < Nb; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
-    for (int c = threadIdx.x; c < ncols; c += blockDim.x) buf[wrapi(c - L, Npf)] = F[(long long)r * ncols + c];
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        cplx<T> v = F[(long long)r * ncols + c];
+        if (q) v = cmul(v, twk<T>(tw, c - L, tstep, +1));
+        buf[wrapi(c - L, Nb)] = v;
+    }
     __syncthreads();
-    fft_smem<T>(buf, Npf, +1, tw, TW);
-    for (int p = threadIdx.x; p < Npf; p += blockDim.x) U[(long long)r * Npf + p] = ccast<TU>(buf[p]);
+    fft_smem<T>(buf, Nb, +1, tw, TW);
+    for (int j = threadIdx.x; j < Nb; j += blockDim.x) U[(long long)r * Npf + SP * j + q] = ccast<TU>(buf[j]);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_adj_spin(const cplx<T> *__restrict__ U, int L, int Npf, cplx<T> *__restrict__ F,
-                   const cplx<T> *__restrict__ tw, int TW) {
+                   const cplx<T> *__restrict__ tw, int TW, int SP, int q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
     const int r = blockIdx.x;
     const int ncols = 2 * L + 1;
-    for (int p = threadIdx.x; p < Npf; p += blockDim.x) buf[p] = U[(long long)r * Npf + p];
+    const int Nb = Npf / SP;
+    const int tstep = TW / Npf;
+    for (int j = threadIdx.x; j < Nb; j += blockDim.x) buf[j] = U[(long long)r * Npf + SP * j + q];
     __syncthreads();
-    fft_smem<T>(buf, Npf, -1, tw, TW);
-    for (int c = threadIdx.x; c < ncols; c += blockDim.x) F[(long long)r * ncols + c] = buf[wrapi(c - L, Npf)];
+    fft_smem<T>(buf, Nb, -1, tw, TW);
+    for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
+        cplx<T> v = buf[wrapi(c - L, Nb)];
+        if (q) v = cmul(v, twk<T>(tw, c - L, tstep, -1));
+        else if (SP == 2) v = cadd(v, F[(long long)r * ncols + c]);
+        F[(long long)r * ncols + c] = v;
+    }
 }
 
 // ------------------------------------------------------------ ring transform (Bluestein)
 // z_p = sum_m h_m e^{i m (phi0 + 2 pi p / N)}, p < N, for one ring per block.
 // spin 0: real output from m in [0, L] (h_{-m} = conj h_m); spin s: complex.
 // T = double (plain path) or dfl (mixed path); tables are given in T.
+// SP = 2 (Mb > 16 x FFT_TPB): the Mb-point circular convolution is done in a
+// buffer of Mb/2 >= N points, one launch per frequency parity q (1, then 0):
+// the chirped input x (length N) gives X_{2k+q} = FFT_{Mb/2}(x_j w^{jq})_k,
+// w = e^{-2 pi i / Mb}, and the convolution at p < N is the sum over q of
+// w^{-pq} IFFT_{Mb/2}(X_{2k+q} B_{2k+q})_p, accumulated in the output.
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_ring_synth(const double2 *__restrict__ Hgl, int nring, int L, int spin,
                  const double *__restrict__ phi0, const long long *__restrict__ ofs, int N, int Mb,
                  const cplx<T> *__restrict__ chirp, const cplx<T> *__restrict__ bker,
                  double *__restrict__ out0, double *__restrict__ out1,
-                 const cplx<T> *__restrict__ tw, int TW) {
+                 const cplx<T> *__restrict__ tw, int TW, long long hbs, long long obs, int SP, int q) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *buf = reinterpret_cast<C *>(smem_raw);
+    Hgl += blockIdx.y * hbs;
+    out0 += blockIdx.y * obs;
+    if (out1) out1 += blockIdx.y * obs;
     const int ring = blockIdx.x;
     const double ph0 = phi0[ring];
-    for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = czero<T>();
-    __syncthreads();
-    if (spin == 0) {
-        for (int m = threadIdx.x; m <= L; m += blockDim.x) {
-            double2 h = Hgl[(long long)m * nring + ring];
-            if (m == 0) {
-                buf[0] = mk<T>(cvt<T>(h.x), cvt<T>(0.0));
-            } else {
+    const int Hb = Mb / SP;
+    const int tstep = TW / Mb;
+    const long long o = ofs[ring];
+    {
+        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = czero<T>();
+        __syncthreads();
+        if (spin == 0) {
+            for (int m = threadIdx.x; m <= L; m += blockDim.x) {
+                double2 h = Hgl[(long long)m * nring + ring];
+                if (m == 0) {
+                    buf[0] = mk<T>(cvt<T>(h.x), cvt<T>(0.0));
+                } else {
+                    if (ph0 != 0.0) {
+                        double sn, cs;
+                        sincos(m * ph0, &sn, &cs);
+                        h = cmul(h, make_double2(cs, sn));
+                    }
+                    const C hc = mk<T>(cvt<T>(h.x), cvt<T>(h.y));
+                    C vp = cmul(hc, chirp[m]);
+                    C vn = cmul(cconj(hc), chirp[N - m]);
+                    if (q) {
+                        vp = cmul(vp, twk<T>(tw, m, tstep, -1));
+                        vn = cmul(vn, twk<T>(tw, N - m, tstep, -1));
+                    }
+                    buf[m] = vp;
+                    buf[N - m] = vn;
+                }
+            }
+        } else {
+            for (int cidx = threadIdx.x; cidx < 2 * L + 1; cidx += blockDim.x) {
+                const int m = cidx - L;
+                double2 h = Hgl[(long long)cidx * nring + ring];
                 if (ph0 != 0.0) {
                     double sn, cs;
                     sincos(m * ph0, &sn, &cs);
                     h = cmul(h, make_double2(cs, sn));
                 }
-                const C hc = mk<T>(cvt<T>(h.x), cvt<T>(h.y));
-                buf[m] = cmul(hc, chirp[m]);
-                buf[N - m] = cmul(cconj(hc), chirp[N - m]);
+                const int qi = wrapi(m, N);
+                C v = cmul(mk<T>(cvt<T>(h.x), cvt<T>(h.y)), chirp[qi]);
+                if (q) v = cmul(v, twk<T>(tw, qi, tstep, -1));
+                buf[qi] = v;
             }
         }
-    } else {
-        for (int cidx = threadIdx.x; cidx < 2 * L + 1; cidx += blockDim.x) {
-            const int m = cidx - L;
-            double2 h = Hgl[(long long)cidx * nring + ring];
-            if (ph0 != 0.0) {
-                double sn, cs;
-                sincos(m * ph0, &sn, &cs);
-                h = cmul(h, make_double2(cs, sn));
+        __syncthreads();
+        fft_smem<T>(buf, Hb, -1, tw, TW);
+        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
+        __syncthreads();
+        fft_smem<T>(buf, Hb, +1, tw, TW);
+        for (int p = threadIdx.x; p < N; p += blockDim.x) {
+            C y = buf[p];
+            if (q) y = cmul(y, twk<T>(tw, p, tstep, +1));
+            const C z = cmul(y, chirp[p]);
+            double z0 = to_d(z.x), z1 = to_d(z.y);
+            if (SP == 2 && q == 0) {
+                z0 += out0[o + p];
+                if (spin != 0) z1 += out1[o + p];
             }
-            const int q = wrapi(m, N);
-            buf[q] = cmul(mk<T>(cvt<T>(h.x), cvt<T>(h.y)), chirp[q]);
+            out0[o + p] = z0;
+            if (spin != 0) out1[o + p] = z1;
         }
-    }
-    __syncthreads();
-    fft_smem<T>(buf, Mb, -1, tw, TW);
-    for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = cmul(buf[i], bker[i]);
-    __syncthreads();
-    fft_smem<T>(buf, Mb, +1, tw, TW);
-    const long long o = ofs[ring];
-    for (int p = threadIdx.x; p < N; p += blockDim.x) {
-        const C z = cmul(buf[p], chirp[p]);
-        out0[o + p] = to_d(z.x);
-        if (spin != 0) out1[o + p] = to_d(z.y);
     }
 }
 
@@ -434,44 +558,50 @@ int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st)
     return CUNUSHT_OK;
 }
 
-// h'_m = e^{-i m phi0} sum_p z'_p e^{-2 pi i m p / N} (adjoint of k_ring_synth)
+// h'_m = e^{-i m phi0} sum_p z'_p e^{-2 pi i m p / N} (adjoint of k_ring_synth);
+// SP = 2 as in k_ring_synth, the two parity launches summed into Hgl
 __global__ void __launch_bounds__(FFT_TPB)
     k_ring_adj(const double *__restrict__ in0, const double *__restrict__ in1, int nring, int L,
                int spin, const double *__restrict__ phi0, const long long *__restrict__ ofs, int N,
                int Mb, const double2 *__restrict__ chirp, const double2 *__restrict__ bker,
-               double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW) {
+               double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW, int SP, int q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *buf = reinterpret_cast<double2 *>(smem_raw);
     const int ring = blockIdx.x;
     const double ph0 = phi0[ring];
     const long long o = ofs[ring];
-    for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = make_double2(0, 0);
-    __syncthreads();
-    // Bluestein on conj(z'): c_p = conj(z'_p)
-    for (int p = threadIdx.x; p < N; p += blockDim.x) {
-        const double2 z = make_double2(in0[o + p], spin ? -in1[o + p] : 0.0);
-        buf[p] = cmul(z, chirp[p]);
-    }
-    __syncthreads();
-    fft_smem<double>(buf, Mb, -1, tw, TW);
-    for (int i = threadIdx.x; i < Mb; i += blockDim.x) buf[i] = cmul(buf[i], bker[i]);
-    __syncthreads();
-    fft_smem<double>(buf, Mb, +1, tw, TW);
-    if (spin == 0) {
-        for (int m = threadIdx.x; m <= L; m += blockDim.x) {
-            const double2 y = cconj(cmul(buf[m], chirp[m]));  // sum_p z' e^{-2 pi i m p/N}
-            double s, c;
-            sincos(m * ph0, &s, &c);
-            Hgl[(long long)m * nring + ring] = cmul(y, make_double2(c, -s));
+    const int Hb = Mb / SP;
+    const int tstep = TW / Mb;
+    {
+        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = make_double2(0, 0);
+        __syncthreads();
+        // Bluestein on conj(z'): c_p = conj(z'_p)
+        for (int p = threadIdx.x; p < N; p += blockDim.x) {
+            const double2 z = make_double2(in0[o + p], spin ? -in1[o + p] : 0.0);
+            double2 v = cmul(z, chirp[p]);
+            if (q) v = cmul(v, twk<double>(tw, p, tstep, -1));
+            buf[p] = v;
         }
-    } else {
-        for (int cidx = threadIdx.x; cidx < 2 * L + 1; cidx += blockDim.x) {
-            const int m = cidx - L;
-            const int q = wrapi(m, N);
-            const double2 y = cconj(cmul(buf[q], chirp[q]));
+        __syncthreads();
+        fft_smem<double>(buf, Hb, -1, tw, TW);
+        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
+        __syncthreads();
+        fft_smem<double>(buf, Hb, +1, tw, TW);
+        const int nc = spin == 0 ? L + 1 : 2 * L + 1;
+        for (int cidx = threadIdx.x; cidx < nc; cidx += blockDim.x) {
+            const int m = spin == 0 ? cidx : cidx - L;
+            const int qi = wrapi(m, N);
+            double2 y = buf[qi];
+            if (q) y = cmul(y, twk<double>(tw, qi, tstep, +1));
+            y = cconj(cmul(y, chirp[qi]));  // sum_p z' e^{-2 pi i m p/N}
             double s, c;
             sincos(m * ph0, &s, &c);
-            Hgl[(long long)cidx * nring + ring] = cmul(y, make_double2(c, -s));
+            double2 h = cmul(y, make_double2(c, -s));
+            if (SP == 2 && q == 0) {
+                const double2 prev = Hgl[(long long)cidx * nring + ring];
+                h = make_double2(h.x + prev.x, h.y + prev.y);
+            }
+            Hgl[(long long)cidx * nring + ring] = h;
         }
     }
 }
@@ -501,148 +631,182 @@ int fft_global_f64(double2 *data, int N, int dir, const double2 *tw, int TW, cud
     return CUNUSHT_OK;
 }
 
-int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cudaStream_t st) {
+int theta_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *H, long long hbs, void *F,
+                    long long fbs, cudaStream_t st) {
     const int L = P->lmax;
     const int ncols = spin ? 2 * L + 1 : L + 1;
     const int mofs = spin ? L : 0;
-    size_t sm = fft_smem_bytes(P->Ntf, P->grid_fp32);
+    size_t sm = fft_smem_bytes(P->Ntf / P->sp_theta, P->grid_fp32);
+    dim3 grid(ncols, nreq, P->sp_theta);
     if (P->grid_fp32) {
         RC_TRY(set_smem(k_theta_fwd<float>, sm));
-        k_theta_fwd<float><<<ncols, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
-                                                       (float2 *)F, ncols, P->n_lo, P->nrows, P->d_tw32, P->TW);
+        k_theta_fwd<float><<<grid, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
+                                                      (float2 *)F, ncols, P->n_lo, P->nrows, P->d_tw32, P->TW, hbs,
+                                                      fbs, P->sp_theta);
     } else if (P->fft_df) {
         RC_TRY(set_smem(k_theta_fwd<dfl>, sm));
-        k_theta_fwd<dfl><<<ncols, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
-                                                     (dcplx *)F, ncols, P->n_lo, P->nrows, (const dcplx *)P->d_twdf,
-                                                     P->TW);
+        k_theta_fwd<dfl><<<grid, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
+                                                    (dcplx *)F, ncols, P->n_lo, P->nrows, (const dcplx *)P->d_twdf,
+                                                    P->TW, hbs, fbs, P->sp_theta);
     } else {
         RC_TRY(set_smem(k_theta_fwd<double>, sm));
-        k_theta_fwd<double><<<ncols, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
-                                                        (double2 *)F, ncols, P->n_lo, P->nrows, P->d_tw64, P->TW);
+        k_theta_fwd<double><<<grid, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
+                                                       (double2 *)F, ncols, P->n_lo, P->nrows, P->d_tw64, P->TW, hbs,
+                                                       fbs, P->sp_theta);
     }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
+}
+
+int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cudaStream_t st) {
+    return theta_fwd_batch(P, 1, spin, H, 0, F, 0, st);
 }
 
 int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cudaStream_t st) {
     const int L = P->lmax;
     const int ncols = spin ? 2 * L + 1 : L + 1;
     const int mofs = spin ? L : 0;
-    size_t sm = fft_smem_bytes(P->Ntf, P->grid_fp32);
-    if (P->grid_fp32) {
-        RC_TRY(set_smem(k_theta_adj<float>, sm));
-        k_theta_adj<float><<<ncols, FFT_TPB, sm, st>>>((const float2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf, spin,
-                                                       mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32, P->TW);
+    const int SP = P->sp_theta;
+    size_t sm = fft_smem_bytes(P->Ntf / SP, P->grid_fp32);
+    // the odd-row spectra of the split transform go through the fine-grid
+    // workspace U, which the phi pass has consumed by now
+    for (int q = SP - 1; q >= 0; --q) {
+        if (P->grid_fp32) {
+            RC_TRY(set_smem(k_theta_adj<float>, sm));
+            k_theta_adj<float><<<ncols, FFT_TPB, sm, st>>>((const float2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
+                                                           spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32,
+                                                           P->TW, SP, q, (float2 *)P->d_U);
+        } else {
+            RC_TRY(set_smem(k_theta_adj<double>, sm));
+            k_theta_adj<double><<<ncols, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt,
+                                                            P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc,
+                                                            P->d_tw64, P->TW, SP, q, (double2 *)P->d_U);
+        }
+        CU_LAUNCH_CHECK();
+    }
+    return CUNUSHT_OK;
+}
+
+int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, void *U, long long ubs,
+                  cudaStream_t st) {
+    const int L = P->lmax;
+    size_t sm = fft_smem_bytes(P->Npf / P->sp_phi, P->grid_fp32);
+    const int SP = P->sp_phi;
+    if (spin == 0) {
+        const int nb = (P->nrows + 1) / 2;
+        if (P->grid_fp32) {
+            RC_TRY(set_smem(k_phi_fwd_s0<float, float>, sm));
+            k_phi_fwd_s0<float, float><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const float2 *)F, L + 1, P->nrows, P->Npf,
+                                                                (float *)U, P->d_tw32, P->TW, fbs, ubs, SP);
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_phi_fwd_s0<dfl, float>, sm));
+            k_phi_fwd_s0<dfl, float><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const dcplx *)F, L + 1, P->nrows, P->Npf,
+                                                              (float *)U, (const dcplx *)P->d_twdf, P->TW, fbs, ubs, SP);
+        } else if (P->fwd_u32) {
+            RC_TRY(set_smem(k_phi_fwd_s0<double, float>, sm));
+            k_phi_fwd_s0<double, float><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
+                                                                 (float *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+        } else {
+            RC_TRY(set_smem(k_phi_fwd_s0<double, double>, sm));
+            k_phi_fwd_s0<double, double><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
+                                                                  (double *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+        }
     } else {
-        RC_TRY(set_smem(k_theta_adj<double>, sm));
-        k_theta_adj<double><<<ncols, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
-                                                        spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw64, P->TW);
+        if (P->grid_fp32) {
+            RC_TRY(set_smem(k_phi_fwd_spin<float, float>, sm));
+            k_phi_fwd_spin<float, float><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const float2 *)F, L, P->Npf,
+                                                                        (float2 *)U, P->d_tw32, P->TW, fbs, ubs, SP);
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_phi_fwd_spin<dfl, float>, sm));
+            k_phi_fwd_spin<dfl, float><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const dcplx *)F, L, P->Npf, (float2 *)U,
+                                                                      (const dcplx *)P->d_twdf, P->TW, fbs, ubs, SP);
+        } else if (P->fwd_u32) {
+            RC_TRY(set_smem(k_phi_fwd_spin<double, float>, sm));
+            k_phi_fwd_spin<double, float><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
+                                                                         (float2 *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+        } else {
+            RC_TRY(set_smem(k_phi_fwd_spin<double, double>, sm));
+            k_phi_fwd_spin<double, double><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
+                                                                          (double2 *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+        }
     }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
 
 int phi_fwd(const cunusht_plan_s *P, int spin, const void *F, void *U, cudaStream_t st) {
-    const int L = P->lmax;
-    size_t sm = fft_smem_bytes(P->Npf, P->grid_fp32);
-    if (spin == 0) {
-        const int nb = (P->nrows + 1) / 2;
-        if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_fwd_s0<float, float>, sm));
-            k_phi_fwd_s0<float, float><<<nb, FFT_TPB, sm, st>>>((const float2 *)F, L + 1, P->nrows, P->Npf,
-                                                                (float *)U, P->d_tw32, P->TW);
-        } else if (P->fft_df) {
-            RC_TRY(set_smem(k_phi_fwd_s0<dfl, float>, sm));
-            k_phi_fwd_s0<dfl, float><<<nb, FFT_TPB, sm, st>>>((const dcplx *)F, L + 1, P->nrows, P->Npf,
-                                                              (float *)U, (const dcplx *)P->d_twdf, P->TW);
-        } else if (P->fwd_u32) {
-            RC_TRY(set_smem(k_phi_fwd_s0<double, float>, sm));
-            k_phi_fwd_s0<double, float><<<nb, FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
-                                                                 (float *)U, P->d_tw64, P->TW);
-        } else {
-            RC_TRY(set_smem(k_phi_fwd_s0<double, double>, sm));
-            k_phi_fwd_s0<double, double><<<nb, FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
-                                                                  (double *)U, P->d_tw64, P->TW);
-        }
-    } else {
-        if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_fwd_spin<float, float>, sm));
-            k_phi_fwd_spin<float, float><<<P->nrows, FFT_TPB, sm, st>>>((const float2 *)F, L, P->Npf,
-                                                                        (float2 *)U, P->d_tw32, P->TW);
-        } else if (P->fft_df) {
-            RC_TRY(set_smem(k_phi_fwd_spin<dfl, float>, sm));
-            k_phi_fwd_spin<dfl, float><<<P->nrows, FFT_TPB, sm, st>>>((const dcplx *)F, L, P->Npf, (float2 *)U,
-                                                                      (const dcplx *)P->d_twdf, P->TW);
-        } else if (P->fwd_u32) {
-            RC_TRY(set_smem(k_phi_fwd_spin<double, float>, sm));
-            k_phi_fwd_spin<double, float><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
-                                                                         (float2 *)U, P->d_tw64, P->TW);
-        } else {
-            RC_TRY(set_smem(k_phi_fwd_spin<double, double>, sm));
-            k_phi_fwd_spin<double, double><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
-                                                                          (double2 *)U, P->d_tw64, P->TW);
-        }
-    }
-    CU_LAUNCH_CHECK();
-    return CUNUSHT_OK;
+    return phi_fwd_batch(P, 1, spin, F, 0, U, 0, st);
 }
 
 int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStream_t st) {
     const int L = P->lmax;
-    size_t sm = fft_smem_bytes(P->Npf, P->grid_fp32);
-    if (spin == 0) {
-        const int nb = (P->nrows + 1) / 2;
-        if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_adj_s0<float>, sm));
-            k_phi_adj_s0<float><<<nb, FFT_TPB, sm, st>>>((const float *)U, P->nrows, P->Npf, (float2 *)F, L + 1,
-                                                         P->d_tw32, P->TW);
+    size_t sm = fft_smem_bytes(P->Npf / P->sp_phi, P->grid_fp32);
+    const int SP = P->sp_phi;
+    for (int q = SP - 1; q >= 0; --q) {
+        if (spin == 0) {
+            const int nb = (P->nrows + 1) / 2;
+            if (P->grid_fp32) {
+                RC_TRY(set_smem(k_phi_adj_s0<float>, sm));
+                k_phi_adj_s0<float><<<nb, FFT_TPB, sm, st>>>((const float *)U, P->nrows, P->Npf, (float2 *)F, L + 1,
+                                                             P->d_tw32, P->TW, SP, q);
+            } else {
+                RC_TRY(set_smem(k_phi_adj_s0<double>, sm));
+                k_phi_adj_s0<double><<<nb, FFT_TPB, sm, st>>>((const double *)U, P->nrows, P->Npf, (double2 *)F, L + 1,
+                                                              P->d_tw64, P->TW, SP, q);
+            }
         } else {
-            RC_TRY(set_smem(k_phi_adj_s0<double>, sm));
-            k_phi_adj_s0<double><<<nb, FFT_TPB, sm, st>>>((const double *)U, P->nrows, P->Npf, (double2 *)F, L + 1,
-                                                          P->d_tw64, P->TW);
+            if (P->grid_fp32) {
+                RC_TRY(set_smem(k_phi_adj_spin<float>, sm));
+                k_phi_adj_spin<float><<<P->nrows, FFT_TPB, sm, st>>>((const float2 *)U, L, P->Npf, (float2 *)F,
+                                                                     P->d_tw32, P->TW, SP, q);
+            } else {
+                RC_TRY(set_smem(k_phi_adj_spin<double>, sm));
+                k_phi_adj_spin<double><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)U, L, P->Npf, (double2 *)F,
+                                                                      P->d_tw64, P->TW, SP, q);
+            }
         }
-    } else {
-        if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_adj_spin<float>, sm));
-            k_phi_adj_spin<float><<<P->nrows, FFT_TPB, sm, st>>>((const float2 *)U, L, P->Npf, (float2 *)F,
-                                                                 P->d_tw32, P->TW);
-        } else {
-            RC_TRY(set_smem(k_phi_adj_spin<double>, sm));
-            k_phi_adj_spin<double><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)U, L, P->Npf, (double2 *)F,
-                                                                  P->d_tw64, P->TW);
-        }
+        CU_LAUNCH_CHECK();
     }
-    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,
+                     double *out1, long long obs, cudaStream_t st) {
+    size_t sm = fft_smem_bytes(P->Mb / P->sp_ring, false);
+    dim3 grid(P->nring, nreq);
+    for (int q = P->sp_ring - 1; q >= 0; --q) {
+        if (P->fft_df && P->d_chirp_df) {
+            RC_TRY(set_smem(k_ring_synth<dfl>, sm));
+            k_ring_synth<dfl><<<grid, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
+                                                         P->nph_uniform, P->Mb, (const dcplx *)P->d_chirp_df,
+                                                         (const dcplx *)P->d_bker_df, out0, out1,
+                                                         (const dcplx *)P->d_twdf, P->TW, hbs, obs, P->sp_ring, q);
+        } else {
+            RC_TRY(set_smem(k_ring_synth<double>, sm));
+            k_ring_synth<double><<<grid, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
+                                                            P->nph_uniform, P->Mb, P->d_chirp, P->d_bker, out0, out1,
+                                                            P->d_tw64, P->TW, hbs, obs, P->sp_ring, q);
+        }
+        CU_LAUNCH_CHECK();
+    }
     return CUNUSHT_OK;
 }
 
 int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *out0, double *out1,
                cudaStream_t st) {
-    size_t sm = fft_smem_bytes(P->Mb, false);
-    if (P->fft_df && P->d_chirp_df) {
-        RC_TRY(set_smem(k_ring_synth<dfl>, sm));
-        k_ring_synth<dfl><<<P->nring, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0,
-                                                         P->d_ring_ofs, P->nph_uniform, P->Mb,
-                                                         (const dcplx *)P->d_chirp_df, (const dcplx *)P->d_bker_df,
-                                                         out0, out1, (const dcplx *)P->d_twdf, P->TW);
-    } else {
-        RC_TRY(set_smem(k_ring_synth<double>, sm));
-        k_ring_synth<double><<<P->nring, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0,
-                                                            P->d_ring_ofs, P->nph_uniform, P->Mb, P->d_chirp,
-                                                            P->d_bker, out0, out1, P->d_tw64, P->TW);
-    }
-    CU_LAUNCH_CHECK();
-    return CUNUSHT_OK;
+    return ring_synth_batch(P, 1, spin, Hgl, 0, out0, out1, 0, st);
 }
 
 int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
                  double2 *Hgl, cudaStream_t st) {
-    size_t sm = fft_smem_bytes(P->Mb, false);
+    size_t sm = fft_smem_bytes(P->Mb / P->sp_ring, false);
     RC_TRY(set_smem(k_ring_adj, sm));
-    k_ring_adj<<<P->nring, FFT_TPB, sm, st>>>(in0, in1, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
-                                              P->nph_uniform, P->Mb, P->d_chirp, P->d_bker, Hgl, P->d_tw64,
-                                              P->TW);
-    CU_LAUNCH_CHECK();
+    for (int q = P->sp_ring - 1; q >= 0; --q) {
+        k_ring_adj<<<P->nring, FFT_TPB, sm, st>>>(in0, in1, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
+                                                  P->nph_uniform, P->Mb, P->d_chirp, P->d_bker, Hgl, P->d_tw64,
+                                                  P->TW, P->sp_ring, q);
+        CU_LAUNCH_CHECK();
+    }
     return CUNUSHT_OK;
 }
 

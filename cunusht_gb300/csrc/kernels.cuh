@@ -12,6 +12,8 @@ int build_coef_tables_df(cunusht_plan_s *P, cudaStream_t st);
 int build_coef_tables_spin(const cunusht_plan_s *P, int spin, double *coef, cudaStream_t st);
 int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C,
               bool use_lfac, bool cc, double2 *H, cudaStream_t st);
+int leg_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
+                    long long astride, bool use_lfac, bool cc, double2 *H, long long hstride, cudaStream_t st);
 int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
                 bool cc, double2 *G, double2 *C, cudaStream_t st);
 
@@ -22,6 +24,12 @@ int phi_fwd(const cunusht_plan_s *P, int spin, const void *F, void *U, cudaStrea
 int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStream_t st);
 int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *out0, double *out1,
                cudaStream_t st);
+int theta_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *H, long long hbs, void *F,
+                    long long fbs, cudaStream_t st);
+int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, void *U, long long ubs,
+                  cudaStream_t st);
+int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,
+                     double *out1, long long obs, cudaStream_t st);
 int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
                  double2 *Hgl, cudaStream_t st);
 int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st);
@@ -31,6 +39,11 @@ size_t fft_smem_bytes(int N, bool f32);
 // nufft.cu
 int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long npts,
                  int layout, const double *gamma, void *out, int out_dtype, cudaStream_t st);
+int nufft_interp_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, long long ubs, const double *loc,
+                       long long lbs, long long npts, int layout, const double *gamma, void *out, long long obs,
+                       int out_dtype, cudaStream_t st);
+int pointing_batch(const cunusht_plan_s *P, int nreq, const double *d, long long dbs, double *ptg, long long pbs,
+                   double *gamma, cudaStream_t st);
 int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts,
                  int layout, const double *gamma, const void *in, int in_dtype,
                  cudaStream_t st);

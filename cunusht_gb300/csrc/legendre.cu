@@ -308,14 +308,17 @@ int build_coef_tables_df(cunusht_plan_s *P, cudaStream_t st) {
     return CUNUSHT_OK;
 }
 
+// NB requests per launch share the recursion: request r reads its alm at
+// alm + r * astride and writes its columns at H + r * hstride.
+template <int NB>
 __global__ void __launch_bounds__(LEG_TPB)
-    k_leg_synth_s0_df(int L, const double2 *__restrict__ alm, const double *__restrict__ lfac,
+    k_leg_synth_s0_df(int L, const double2 *__restrict__ alm, long long astride, const double *__restrict__ lfac,
                       const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
                       int npairs, const double *__restrict__ px, const double *__restrict__ psh,
                       const double *__restrict__ pch, const int *__restrict__ prn,
-                      const int *__restrict__ prs, double2 *__restrict__ H, int ldH) {
+                      const int *__restrict__ prs, double2 *__restrict__ H, long long hstride, int ldH) {
     __shared__ float2 s_al[LEG_CH], s_be[LEG_CH];
-    __shared__ float4 s_a[LEG_CH];
+    __shared__ float4 s_a[NB][LEG_CH];
     const int m = blockIdx.y;
     const int p = blockIdx.x * LEG_TPB + threadIdx.x;
     const bool act = p < npairs;
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(LEG_TPB)
     dfl cur, prev;
     int e;
     rec_start_df(lg0[m], m, 0, sh, ch, cur, prev, e);
-    kahan Er, Ei, Or, Oi;
+    kahan Er[NB], Ei[NB], Or[NB], Oi[NB];
     const float2 *al = coef, *be = coef + 2 * nalm;
     const long long b = almidx(L, m, m) - m;
     for (int lb = m; lb <= L; lb += LEG_CH) {
@@ -339,22 +342,29 @@ __global__ void __launch_bounds__(LEG_TPB)
             const long long ix = b + lb + i;
             s_al[i] = al[ix];
             s_be[i] = be[ix];
-            const double2 a = alm[ix];
             const double f = lfac ? lfac[lb + i] : 1.0;
-            const dfl re = df_from(a.x * f), im = df_from(a.y * f);
-            s_a[i] = make_float4(re.h, re.l, im.h, im.l);
+#pragma unroll
+            for (int r = 0; r < NB; ++r) {
+                const double2 a = alm[r * astride + ix];
+                const dfl re = df_from(a.x * f), im = df_from(a.y * f);
+                s_a[r][i] = make_float4(re.h, re.l, im.h, im.l);
+            }
         }
         __syncthreads();
         for (int i = 0; i < cnt; ++i) {
             if (e == 0) {
-                const float4 a = s_a[i];
-                const float pr = df_prod(a.x, a.y, cur), pi = df_prod(a.z, a.w, cur);
-                if ((lb + i + m) & 1) {
-                    Or.add(pr);
-                    Oi.add(pi);
-                } else {
-                    Er.add(pr);
-                    Ei.add(pi);
+                const bool odd = (lb + i + m) & 1;
+#pragma unroll
+                for (int r = 0; r < NB; ++r) {
+                    const float4 a = s_a[r][i];
+                    const float pr = df_prod(a.x, a.y, cur), pi = df_prod(a.z, a.w, cur);
+                    if (odd) {
+                        Or[r].add(pr);
+                        Oi[r].add(pi);
+                    } else {
+                        Er[r].add(pr);
+                        Ei[r].add(pi);
+                    }
                 }
             }
             const float2 a2 = s_al[i], b2 = s_be[i];
@@ -367,21 +377,26 @@ __global__ void __launch_bounds__(LEG_TPB)
     }
     if (act) {
         const int n = prn[p], s = prs[p];
-        const double er = Er.value(), ei = Ei.value(), orr = Or.value(), oi = Oi.value();
-        H[(long long)m * ldH + n] = make_double2(er + orr, ei + oi);
-        if (s != n) H[(long long)m * ldH + s] = make_double2(er - orr, ei - oi);
+#pragma unroll
+        for (int r = 0; r < NB; ++r) {
+            double2 *Hr = H + r * hstride;
+            const double er = Er[r].value(), ei = Ei[r].value(), orr = Or[r].value(), oi = Oi[r].value();
+            Hr[(long long)m * ldH + n] = make_double2(er + orr, ei + oi);
+            if (s != n) Hr[(long long)m * ldH + s] = make_double2(er - orr, ei - oi);
+        }
     }
 }
 
+template <int NB>
 __global__ void __launch_bounds__(LEG_TPB)
     k_leg_synth_spin_df(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
-                        const double *__restrict__ lfac, const float2 *__restrict__ coef, long long nalm,
-                        const double *__restrict__ lg0, int npairs, const double *__restrict__ px,
+                        long long astride, const double *__restrict__ lfac, const float2 *__restrict__ coef,
+                        long long nalm, const double *__restrict__ lg0, int npairs, const double *__restrict__ px,
                         const double *__restrict__ psh, const double *__restrict__ pch,
                         const int *__restrict__ prn, const int *__restrict__ prs, double2 *__restrict__ H,
-                        int ldH) {
+                        long long hstride, int ldH) {
     __shared__ float2 s_al[LEG_CH], s_ga[LEG_CH], s_be[LEG_CH];
-    __shared__ float4 s_A[LEG_CH], s_B[LEG_CH];
+    __shared__ float4 s_A[NB][LEG_CH], s_B[NB][LEG_CH];
     const int m = blockIdx.y;
     const int l0 = max(m, spin);
     const int p = blockIdx.x * LEG_TPB + threadIdx.x;
@@ -397,7 +412,7 @@ __global__ void __launch_bounds__(LEG_TPB)
     int eN, eS;
     rec_start_df(lg0[m], m, spin, sh, ch, cN, pN, eN);
     rec_start_df(lg0[m], m, spin, ch, sh, cS, pS, eS);
-    kahan hpn_r, hpn_i, hps_r, hps_i, hmn_r, hmn_i, hms_r, hms_i;
+    kahan hpn_r[NB], hpn_i[NB], hps_r[NB], hps_i[NB], hmn_r[NB], hmn_i[NB], hms_r[NB], hms_i[NB];
     const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
     const long long b = almidx(L, m, m) - m;
     for (int lb = l0; lb <= L; lb += LEG_CH) {
@@ -410,28 +425,34 @@ __global__ void __launch_bounds__(LEG_TPB)
             s_ga[i] = ga[ix];
             s_be[i] = be[ix];
             const double f = lfac ? lfac[l] : 1.0;
-            const double2 g = G[ix];
-            const double2 c = C ? C[ix] : make_double2(0.0, 0.0);
-            const dfl ar = df_from(f * (g.x - c.y)), ai = df_from(f * (g.y + c.x));
             const double par = ((l + m) & 1) ? -f : f;
-            const dfl br = df_from(par * (g.x + c.y)), bi = df_from(par * (c.x - g.y));
-            s_A[i] = make_float4(ar.h, ar.l, ai.h, ai.l);
-            s_B[i] = make_float4(br.h, br.l, bi.h, bi.l);
+#pragma unroll
+            for (int r = 0; r < NB; ++r) {
+                const double2 g = G[r * astride + ix];
+                const double2 c = C ? C[r * astride + ix] : make_double2(0.0, 0.0);
+                const dfl ar = df_from(f * (g.x - c.y)), ai = df_from(f * (g.y + c.x));
+                const dfl br = df_from(par * (g.x + c.y)), bi = df_from(par * (c.x - g.y));
+                s_A[r][i] = make_float4(ar.h, ar.l, ai.h, ai.l);
+                s_B[r][i] = make_float4(br.h, br.l, bi.h, bi.l);
+            }
         }
         __syncthreads();
         for (int i = 0; i < cnt; ++i) {
-            const float4 A = s_A[i], B = s_B[i];
-            if (eN == 0) {
-                hpn_r.add(df_prod(A.x, A.y, cN));
-                hpn_i.add(df_prod(A.z, A.w, cN));
-                hms_r.add(df_prod(B.x, B.y, cN));
-                hms_i.add(df_prod(B.z, B.w, cN));
-            }
-            if (eS == 0) {
-                hps_r.add(df_prod(A.x, A.y, cS));
-                hps_i.add(df_prod(A.z, A.w, cS));
-                hmn_r.add(df_prod(B.x, B.y, cS));
-                hmn_i.add(df_prod(B.z, B.w, cS));
+#pragma unroll
+            for (int r = 0; r < NB; ++r) {
+                const float4 A = s_A[r][i], B = s_B[r][i];
+                if (eN == 0) {
+                    hpn_r[r].add(df_prod(A.x, A.y, cN));
+                    hpn_i[r].add(df_prod(A.z, A.w, cN));
+                    hms_r[r].add(df_prod(B.x, B.y, cN));
+                    hms_i[r].add(df_prod(B.z, B.w, cN));
+                }
+                if (eS == 0) {
+                    hps_r[r].add(df_prod(A.x, A.y, cS));
+                    hps_i[r].add(df_prod(A.z, A.w, cS));
+                    hmn_r[r].add(df_prod(B.x, B.y, cS));
+                    hmn_i[r].add(df_prod(B.z, B.w, cS));
+                }
             }
             const float2 a2 = s_al[i], g2 = s_ga[i], b2 = s_be[i];
             const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
@@ -450,11 +471,16 @@ __global__ void __launch_bounds__(LEG_TPB)
     if (act) {
         const int n = prn[p], s = prs[p];
         const double sgs = (spin & 1) ? -1.0 : 1.0;
-        H[(long long)(L + m) * ldH + n] = make_double2(-hpn_r.value(), -hpn_i.value());
-        if (s != n) H[(long long)(L + m) * ldH + s] = make_double2(-hps_r.value(), -hps_i.value());
-        if (m > 0) {
-            H[(long long)(L - m) * ldH + n] = make_double2(-sgs * hmn_r.value(), -sgs * hmn_i.value());
-            if (s != n) H[(long long)(L - m) * ldH + s] = make_double2(-sgs * hms_r.value(), -sgs * hms_i.value());
+#pragma unroll
+        for (int r = 0; r < NB; ++r) {
+            double2 *Hr = H + r * hstride;
+            Hr[(long long)(L + m) * ldH + n] = make_double2(-hpn_r[r].value(), -hpn_i[r].value());
+            if (s != n) Hr[(long long)(L + m) * ldH + s] = make_double2(-hps_r[r].value(), -hps_i[r].value());
+            if (m > 0) {
+                Hr[(long long)(L - m) * ldH + n] = make_double2(-sgs * hmn_r[r].value(), -sgs * hmn_i[r].value());
+                if (s != n)
+                    Hr[(long long)(L - m) * ldH + s] = make_double2(-sgs * hms_r[r].value(), -sgs * hms_i[r].value());
+            }
         }
     }
 }
@@ -679,33 +705,67 @@ static RingPairs pairs_of(const cunusht_plan_s *P, bool cc) {
     return {P->gl_npairs, P->d_gl_x, P->d_gl_sh, P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->nring};
 }
 
-int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C,
-              bool use_lfac, bool cc, double2 *H, cudaStream_t st) {
+template <int NB>
+static void launch_synth_df(const cunusht_plan_s *P, const RingPairs &R, dim3 grid, int spin, const double2 *G,
+                            const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
+                            cudaStream_t st) {
+    const int L = P->lmax;
+    if (spin == 0)
+        k_leg_synth_s0_df<NB><<<grid, LEG_TPB, 0, st>>>(L, G, astride, lf, P->d_coef_df[0], P->nalm, P->d_lg0[0],
+                                                        R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H, hstride, R.ld);
+    else
+        k_leg_synth_spin_df<NB><<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm,
+                                                          P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H,
+                                                          hstride, R.ld);
+}
+
+// nreq requests (alm at G + r * astride, columns at H + r * hstride); the
+// mixed-precision kernels process up to four requests per launch with one
+// shared recursion, the FP64 kernels one request per launch.
+int leg_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
+                    long long astride, bool use_lfac, bool cc, double2 *H, long long hstride, cudaStream_t st) {
     const RingPairs R = pairs_of(P, cc);
     const int L = P->lmax;
     dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
     const double *lf = use_lfac ? P->d_lfac : nullptr;
     if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
-        if (spin == 0)
-            k_leg_synth_s0_df<<<grid, LEG_TPB, 0, st>>>(L, G, lf, P->d_coef_df[0], P->nalm, P->d_lg0[0], R.npairs,
-                                                        R.x, R.sh, R.ch, R.rn, R.rs, H, R.ld);
-        else
-            k_leg_synth_spin_df<<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, lf, P->d_coef_df[spin], P->nalm,
-                                                          P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
-                                                          H, R.ld);
-        CU_LAUNCH_CHECK();
+        for (int r0 = 0; r0 < nreq;) {
+            const int left = nreq - r0;
+            const double2 *Gr = G + r0 * astride, *Cr = C ? C + r0 * astride : nullptr;
+            double2 *Hr = H + r0 * hstride;
+            if (left >= 4) {
+                launch_synth_df<4>(P, R, grid, spin, Gr, Cr, astride, lf, Hr, hstride, st);
+                r0 += 4;
+            } else if (left >= 2) {
+                launch_synth_df<2>(P, R, grid, spin, Gr, Cr, astride, lf, Hr, hstride, st);
+                r0 += 2;
+            } else {
+                launch_synth_df<1>(P, R, grid, spin, Gr, Cr, astride, lf, Hr, hstride, st);
+                r0 += 1;
+            }
+            CU_LAUNCH_CHECK();
+        }
         return CUNUSHT_OK;
     }
-    if (spin == 0) {
-        k_leg_synth_s0<<<grid, LEG_TPB, 0, st>>>(L, G, lf, P->d_coef[0], P->nalm, P->d_lg0[0],
-                                                 R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H, R.ld);
-    } else {
-        k_leg_synth_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, lf, P->d_coef[spin], P->nalm,
-                                                   P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch,
-                                                   R.rn, R.rs, H, R.ld);
+    for (int r = 0; r < nreq; ++r) {
+        const double2 *Gr = G + r * astride, *Cr = C ? C + r * astride : nullptr;
+        double2 *Hr = H + r * hstride;
+        if (spin == 0) {
+            k_leg_synth_s0<<<grid, LEG_TPB, 0, st>>>(L, Gr, lf, P->d_coef[0], P->nalm, P->d_lg0[0], R.npairs, R.x,
+                                                     R.sh, R.ch, R.rn, R.rs, Hr, R.ld);
+        } else {
+            k_leg_synth_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, Gr, Cr, lf, P->d_coef[spin], P->nalm,
+                                                       P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, Hr,
+                                                       R.ld);
+        }
+        CU_LAUNCH_CHECK();
     }
-    CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
+}
+
+int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C,
+              bool use_lfac, bool cc, double2 *H, cudaStream_t st) {
+    return leg_synth_batch(P, 1, spin, G, C, 0, use_lfac, cc, H, 0, st);
 }
 
 int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,

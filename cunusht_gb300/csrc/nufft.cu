@@ -82,9 +82,14 @@ template <typename T, bool CPLX>
 __global__ void __launch_bounds__(NU_TPB)
     k_interp(const T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
              const double *__restrict__ loc, long long npts, int layout,
-             const double *__restrict__ gamma, int spin, void *__restrict__ out, int out_f32) {
+             const double *__restrict__ gamma, int spin, void *__restrict__ out, int out_f32, long long ubs,
+             long long lbs, long long obs) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= npts) return;
+    U += blockIdx.y * ubs;  // request of a batch (strides in elements)
+    loc += blockIdx.y * lbs;
+    if (gamma) gamma += blockIdx.y * npts;
+    out = out_f32 ? (void *)((float *)out + blockIdx.y * obs) : (void *)((double *)out + blockIdx.y * obs);
     double th, ph;
     load_point(loc, j, npts, layout, th, ph);
     const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
@@ -204,9 +209,13 @@ template <bool CPLX>
 __global__ void __launch_bounds__(NU_TPB)
     k_interp_mixed(const float *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                    const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
-                   int spin, void *__restrict__ out, int out_f32) {
+                   int spin, void *__restrict__ out, int out_f32, long long ubs, long long lbs, long long obs) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= npts) return;
+    U += blockIdx.y * ubs;  // request of a batch (strides in elements)
+    loc += blockIdx.y * lbs;
+    if (gamma) gamma += blockIdx.y * npts;
+    out = out_f32 ? (void *)((float *)out + blockIdx.y * obs) : (void *)((double *)out + blockIdx.y * obs);
     double th, ph;
     load_point(loc, j, npts, layout, th, ph);
     const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
@@ -285,44 +294,47 @@ __global__ void __launch_bounds__(NU_TPB)
     }
 }
 
-int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
-                 const double *gamma, void *out, int out_dtype, cudaStream_t st) {
-    if (npts == 0) return CUNUSHT_OK;
-    const int nb = (int)((npts + NU_TPB - 1) / NU_TPB);
+int nufft_interp_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, long long ubs, const double *loc,
+                       long long lbs, long long npts, int layout, const double *gamma, void *out, long long obs,
+                       int out_dtype, cudaStream_t st) {
+    if (npts == 0 || nreq == 0) return CUNUSHT_OK;
+    dim3 grid((unsigned)((npts + NU_TPB - 1) / NU_TPB), nreq);
     const int f32o = out_dtype == CUNUSHT_F32;
     if (P->fwd_u32) {
         if (spin == 0)
-            k_interp_mixed<false><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                         P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
-                                                         f32o);
+            k_interp_mixed<false><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                           (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
+                                                           ubs, lbs, obs);
         else
-            k_interp_mixed<true><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                        P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
-                                                        f32o);
-        CU_LAUNCH_CHECK();
-        return CUNUSHT_OK;
-    }
-    if (P->grid_fp32) {
+            k_interp_mixed<true><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                          (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
+                                                          ubs, lbs, obs);
+    } else if (P->grid_fp32) {
         if (spin == 0)
-            k_interp<float, false><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                          P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
-                                                          f32o);
+            k_interp<float, false><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                            (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
+                                                            ubs, lbs, obs);
         else
-            k_interp<float, true><<<nb, NU_TPB, 0, st>>>((const float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                         P->w, (float)P->beta, loc, npts, layout, gamma, spin, out,
-                                                         f32o);
+            k_interp<float, true><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                           (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
+                                                           ubs, lbs, obs);
     } else {
         if (spin == 0)
-            k_interp<double, false><<<nb, NU_TPB, 0, st>>>((const double *)P->d_U, P->nrows, P->Npf, P->Ntf,
-                                                           P->n_lo, P->w, P->beta, loc, npts, layout, gamma, spin,
-                                                           out, f32o);
+            k_interp<double, false><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                             P->w, P->beta, loc, npts, layout, gamma, spin, out, f32o,
+                                                             ubs, lbs, obs);
         else
-            k_interp<double, true><<<nb, NU_TPB, 0, st>>>((const double *)P->d_U, P->nrows, P->Npf, P->Ntf,
-                                                          P->n_lo, P->w, P->beta, loc, npts, layout, gamma, spin,
-                                                          out, f32o);
+            k_interp<double, true><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                            P->w, P->beta, loc, npts, layout, gamma, spin, out, f32o,
+                                                            ubs, lbs, obs);
     }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
+}
+
+int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
+                 const double *gamma, void *out, int out_dtype, cudaStream_t st) {
+    return nufft_interp_batch(P, 1, spin, P->d_U, 0, loc, 0, npts, layout, gamma, out, 0, out_dtype, st);
 }
 
 int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
@@ -360,9 +372,15 @@ __global__ void __launch_bounds__(256)
     k_pointing(int nring, const double *__restrict__ rth, const double *__restrict__ rph0,
                const long long *__restrict__ rnph, const long long *__restrict__ rofs, long long npix,
                const double *__restrict__ dth, const double *__restrict__ dph,
-               double *__restrict__ oth, double *__restrict__ oph, double *__restrict__ ogam) {
+               double *__restrict__ oth, double *__restrict__ oph, double *__restrict__ ogam, long long dbs,
+               long long pbs) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= npix) return;
+    dth += blockIdx.y * dbs;  // request of a batch
+    dph += blockIdx.y * dbs;
+    oth += blockIdx.y * pbs;
+    oph += blockIdx.y * pbs;
+    if (ogam) ogam += blockIdx.y * npix;
     int lo = 0, hi = nring - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -438,9 +456,14 @@ __global__ void __launch_bounds__(256)
                      const float4 *__restrict__ rsc, const double *__restrict__ rph0,
                      const long long *__restrict__ rnph, const long long *__restrict__ rofs, long long npix,
                      const double *__restrict__ dth, const double *__restrict__ dph, double *__restrict__ oth,
-                     double *__restrict__ oph, double *__restrict__ ogam) {
+                     double *__restrict__ oph, double *__restrict__ ogam, long long dbs, long long pbs) {
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= npix) return;
+    dth += blockIdx.y * dbs;  // request of a batch
+    dph += blockIdx.y * dbs;
+    oth += blockIdx.y * pbs;
+    oph += blockIdx.y * pbs;
+    if (ogam) ogam += blockIdx.y * npix;
     int ring;
     if (nph_uniform > 0) {
         ring = (int)(j / nph_uniform);
@@ -627,14 +650,28 @@ int lens_vjp_launch(const cunusht_plan_s *P, const double *ptg, const double *gr
     return CUNUSHT_OK;
 }
 
+int pointing_batch(const cunusht_plan_s *P, int nreq, const double *d, long long dbs, double *ptg, long long pbs,
+                   double *gamma, cudaStream_t st) {
+    if (P->npix == 0 || nreq == 0) return CUNUSHT_OK;
+    dim3 grid((unsigned)((P->npix + 255) / 256), nreq);
+    if (P->prec == CUNUSHT_PREC_MIXED)
+        k_pointing_mixed<<<grid, 256, 0, st>>>(P->nring, P->nph_uniform, P->d_ring_theta, P->d_ring_sc, P->d_ring_phi0,
+                                               P->d_ring_nph, P->d_ring_ofs, P->npix, d, d + P->npix, ptg,
+                                               ptg + P->npix, gamma, dbs, pbs);
+    else
+        k_pointing<<<grid, 256, 0, st>>>(P->nring, P->d_ring_theta, P->d_ring_phi0, P->d_ring_nph, P->d_ring_ofs,
+                                         P->npix, d, d + P->npix, ptg, ptg + P->npix, gamma, dbs, pbs);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
 int pointing_mixed_launch(int nring, int nph_uniform, const double *rth, const float4 *rsc, const double *rph0,
-                          const long long *rnph,
-                          const long long *rofs, long long npix, const double *dth, const double *dph,
-                          double *out_th, double *out_ph, double *out_gamma, cudaStream_t st) {
+                          const long long *rnph, const long long *rofs, long long npix, const double *dth,
+                          const double *dph, double *out_th, double *out_ph, double *out_gamma, cudaStream_t st) {
     if (npix == 0) return CUNUSHT_OK;
     const int nb = (int)((npix + 255) / 256);
-    k_pointing_mixed<<<nb, 256, 0, st>>>(nring, nph_uniform, rth, rsc, rph0, rnph, rofs, npix, dth, dph, out_th, out_ph,
-                                         out_gamma);
+    k_pointing_mixed<<<nb, 256, 0, st>>>(nring, nph_uniform, rth, rsc, rph0, rnph, rofs, npix, dth, dph, out_th,
+                                         out_ph, out_gamma, 0, 0);
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
@@ -644,7 +681,7 @@ int pointing_launch(int nring, const double *rth, const double *rph0, const long
                     double *out_th, double *out_ph, double *out_gamma, cudaStream_t st) {
     if (npix == 0) return CUNUSHT_OK;
     const int nb = (int)((npix + 255) / 256);
-    k_pointing<<<nb, 256, 0, st>>>(nring, rth, rph0, rnph, rofs, npix, dth, dph, out_th, out_ph, out_gamma);
+    k_pointing<<<nb, 256, 0, st>>>(nring, rth, rph0, rnph, rofs, npix, dth, dph, out_th, out_ph, out_gamma, 0, 0);
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }

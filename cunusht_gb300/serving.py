@@ -1,0 +1,234 @@
+"""Continuous-batching lensing server.
+
+Requests -- lensing (gclm -> lensed map, gclm2lenmap) or delensing (lensed
+map -> gclm, lenmap2gclm) of any lmax, spin and accuracy -- are queued per
+bucket (lmax, spin, epsilon).  A bucket owns ``slots_per_bucket`` device
+slots; each slot is a plan with its batch workspace, static input/output
+buffers and its own CUDA stream, and runs at most one launch at a time.  Every
+call of :meth:`LensingServer.step` retires the launches whose completion
+events have fired and fills every idle slot with the requests waiting in its
+bucket's queue, so requests that arrive while others are on the GPU are
+admitted as soon as a slot frees up, and launches of different slots and
+buckets overlap on the device.
+
+A launch is one CUDA-graph replay: lensing requests of a bucket go up to
+``max_batch`` per launch through cunusht_lensing_batch (one shared Legendre
+recursion per four requests on the mixed path); a delensing request runs
+dlm2pointing + nusht2d1.  The graph of each (slot, direction, batch size) is
+captured on first use; the request's inputs are copied into the slot's
+static buffers before the replay and its result copied out after.
+
+Admission: a bucket's slots are created when the bucket first has work and
+only if the device memory they take (measured) stays within the HBM budget;
+otherwise idle buckets are released and the bucket waits.
+
+The reference has no serving layer: its transformers process one call at a
+time with device-wide synchronisation (cunusht/helper_GPU.py:27-51).
+"""
+from __future__ import annotations
+
+import collections
+import dataclasses
+import itertools
+import time
+from typing import Optional
+
+import torch
+
+from .transformer import GPU_cufinufft_transformer
+
+
+@dataclasses.dataclass
+class Request:
+    kind: str                       # "g2l" (gclm2lenmap) or "l2g" (lenmap2gclm)
+    lmax: int
+    spin: int
+    epsilon: float
+    data: torch.Tensor              # gclm (ncomp, nalm) / (nalm,) for g2l; lenmap (2, npix) / (npix,) for l2g
+    dlm_scaled: torch.Tensor        # (nalm,) complex128 on the device
+    arrival: float = 0.0            # server clock, seconds
+    rid: int = 0
+    result: Optional[torch.Tensor] = None
+    t_launch: Optional[float] = None
+    t_done: Optional[float] = None
+
+
+class _Slot:
+    """Plan + batch workspace + static buffers + stream; one launch in flight."""
+
+    def __init__(self, lmax, spin, eps, max_batch, nphi, precision, graphs):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        self.stream = torch.cuda.Stream()
+        self.spin = spin
+        self.max_batch = max_batch
+        self.use_graphs = graphs
+        with torch.cuda.stream(self.stream):
+            gi = {"lmax": lmax} if nphi is None else {"lmax": lmax, "nphi": nphi}
+            self.T = GPU_cufinufft_transformer(("gl", gi), nuFFTtype=2, epsilon=eps, precision=precision,
+                                               max_spin=max(spin, 1))
+            self.T.reserve_batch(max_batch)
+            nalm, npix = self.T.nalm, self.T.npix()
+            self.ncomp = 2 if spin else 1
+            f64, c128 = torch.float64, torch.complex128
+            self.gin = torch.zeros((max_batch, self.ncomp, nalm), dtype=c128, device="cuda")
+            self.din = torch.zeros((max_batch, nalm), dtype=c128, device="cuda")
+            self.out = torch.zeros((max_batch, 2, npix) if spin else (max_batch, npix), dtype=f64, device="cuda")
+            self.lin = torch.zeros((2, npix) if spin else (npix,), dtype=f64, device="cuda")
+            self.aout = torch.zeros((self.ncomp, nalm), dtype=c128, device="cuda")
+            self.ptg = torch.zeros((2, npix), dtype=f64, device="cuda")
+            self.gam = torch.zeros((npix,), dtype=f64, device="cuda")
+        torch.cuda.synchronize()
+        self.bytes = max(0, free0 - torch.cuda.mem_get_info()[0])
+        self.graphs: dict[tuple, torch.cuda.CUDAGraph] = {}
+        self.busy: list[Request] = []
+        self.event: Optional[torch.cuda.Event] = None
+
+    def _work(self, kind, n):
+        if kind == "g2l":
+            self.T.lensing_batch(self.gin[:n], self.din[:n], self.spin, out=self.out[:n])
+        else:
+            self.T.delensing_solve(self.lin, self.din[0], self.aout, self.ptg, self.gam, self.spin)
+
+    def run(self, kind, n):
+        """Launch the work of n staged requests on the slot's stream (the
+        caller holds torch.cuda.stream(self.stream))."""
+        if not self.use_graphs:
+            self._work(kind, n)
+            return
+        g = self.graphs.get((kind, n))
+        if g is None:
+            self._work(kind, n)             # eager run first: kernel attributes, lazy module loading
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+                self._work(kind, n)
+            self.graphs[(kind, n)] = g
+        g.replay()
+
+
+class LensingServer:
+    def __init__(self, max_batch: int = 4, hbm_budget_bytes: float = 150e9, precision: str = "mixed",
+                 slots_per_bucket: int = 2, graphs: bool = True, nphi_of=lambda lmax: None):
+        self.max_batch = max_batch
+        self.budget = hbm_budget_bytes
+        self.precision = precision
+        self.slots_per_bucket = slots_per_bucket
+        self.graphs = graphs
+        self.nphi_of = nphi_of
+        self.buckets: dict[tuple, list[_Slot]] = {}
+        self.queues: dict[tuple, collections.deque] = collections.defaultdict(collections.deque)
+        self.t0 = time.perf_counter()
+        self.ids = itertools.count()
+        self.completed: list[Request] = []
+        self.launches = 0
+        self.rejected_admissions = 0
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    # ------------------------------------------------------------------ admission
+    def used_bytes(self) -> int:
+        return sum(sl.bytes for slots in self.buckets.values() for sl in slots)
+
+    def _admit(self, key) -> bool:
+        if key in self.buckets:
+            return True
+        lmax, spin, eps = key
+        slots = []
+        for _ in range(self.slots_per_bucket):
+            sl = _Slot(lmax, spin, eps, self.max_batch, self.nphi_of(lmax), self.precision, self.graphs)
+            slots.append(sl)
+            if self.used_bytes() + sum(s.bytes for s in slots) > self.budget:
+                slots.pop()
+                del sl
+                break
+        if not slots:
+            self.rejected_admissions += 1
+            self._evict_idle(keep=key)
+            torch.cuda.empty_cache()
+            return False
+        self.buckets[key] = slots
+        return True
+
+    def _evict_idle(self, keep):
+        for k in list(self.buckets):
+            if k != keep and not self.queues[k] and all(not sl.busy for sl in self.buckets[k]):
+                del self.buckets[k]
+
+    # ------------------------------------------------------------------ API
+    def submit(self, kind, lmax, spin, epsilon, data, dlm_scaled, arrival=None) -> Request:
+        if kind not in ("g2l", "l2g"):
+            raise ValueError(f"kind must be 'g2l' or 'l2g', got {kind!r}")
+        r = Request(kind, lmax, spin, epsilon, data, dlm_scaled, self.now() if arrival is None else arrival,
+                    next(self.ids))
+        self.queues[(lmax, spin, epsilon)].append(r)
+        return r
+
+    def _retire(self):
+        for slots in self.buckets.values():
+            for sl in slots:
+                if sl.busy and sl.event.query():
+                    t = self.now()
+                    for r in sl.busy:
+                        r.t_done = t
+                        self.completed.append(r)
+                    sl.busy = []
+                    sl.event = None
+
+    def busy(self) -> bool:
+        return any(sl.busy for slots in self.buckets.values() for sl in slots)
+
+    def step(self) -> bool:
+        """Retire finished launches, launch queued work on idle slots; True
+        while requests are queued or in flight."""
+        self._retire()
+        pending = False
+        for key, q in list(self.queues.items()):
+            if not q:
+                continue
+            pending = True
+            if not self._admit(key):
+                continue
+            for sl in self.buckets[key]:
+                if q and not sl.busy:
+                    self._launch(sl, q)
+        return pending or self.busy()
+
+    def _launch(self, sl: _Slot, q: collections.deque):
+        producer = torch.cuda.current_stream()
+        with torch.cuda.stream(sl.stream):
+            sl.stream.wait_stream(producer)     # request tensors were made on the caller's stream
+            if q[0].kind == "l2g":
+                batch = [q.popleft()]
+                r = batch[0]
+                sl.lin.copy_(r.data.reshape(sl.lin.shape), non_blocking=True)
+                sl.din[0].copy_(r.dlm_scaled.reshape(-1), non_blocking=True)
+                sl.run("l2g", 1)
+                r.result = sl.aout[0].clone() if sl.spin == 0 else sl.aout.clone()
+            else:
+                batch = []
+                while q and q[0].kind == "g2l" and len(batch) < sl.max_batch:
+                    batch.append(q.popleft())
+                for i, r in enumerate(batch):
+                    sl.gin[i].copy_(r.data.reshape(sl.ncomp, -1), non_blocking=True)
+                    sl.din[i].copy_(r.dlm_scaled.reshape(-1), non_blocking=True)
+                sl.run("g2l", len(batch))
+                for i, r in enumerate(batch):
+                    r.result = sl.out[i].clone()
+            ev = torch.cuda.Event()
+            ev.record(sl.stream)
+        t = self.now()
+        for r in batch:
+            r.t_launch = t
+            r.data = None                       # inputs are staged; drop the caller's reference
+        sl.busy = batch
+        sl.event = ev
+        self.launches += 1
+
+    def run_until_idle(self, poll_s: float = 0.0):
+        while self.step():
+            if poll_s:
+                time.sleep(poll_s)
+
+    def latencies_ms(self):
+        return [1e3 * (r.t_done - r.arrival) for r in self.completed]

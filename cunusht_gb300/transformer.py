@@ -292,6 +292,36 @@ class GPU_cufinufft_transformer:
         _lib.check(self._lib.cunusht_plan_stage_times(self._plan, ms, cnt, _lib.NSTAGE))
         return {n: (ms[i], cnt[i]) for i, n in enumerate(_lib.STAGES) if cnt[i]}
 
+    def reserve_batch(self, max_batch: int):
+        """Allocate the per-request workspace for lensing_batch (once)."""
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        _lib.check(self._lib.cunusht_plan_reserve_batch(self._plan, int(max_batch)))
+        self.batch_cap = max(getattr(self, "batch_cap", 0), int(max_batch))
+
+    def lensing_batch(self, gclm: torch.Tensor, dlm_scaled: torch.Tensor, spin: int, out: torch.Tensor | None = None,
+                      ptg: torch.Tensor | None = None, gamma: torch.Tensor | None = None,
+                      dclm_scaled: torch.Tensor | None = None) -> torch.Tensor:
+        """nreq lensing solves in one batched pass (served form).
+        gclm (nreq, ncomp, nalm) complex128, dlm_scaled (nreq, nalm) complex128
+        -> (nreq, 2, npix) Q/U (spin 2) or (nreq, npix) (spin 0)."""
+        g = to_device(gclm, "gclm", torch.complex128)
+        if g.dim() == 2:
+            g = g[:, None, :]
+        nreq, ncomp = g.shape[0], g.shape[1]
+        d = to_device(dlm_scaled, "dlm_scaled", torch.complex128).reshape(nreq, self.nalm)
+        c = to_device(dclm_scaled, "dclm_scaled", torch.complex128).reshape(nreq, self.nalm) if dclm_scaled is not None else None
+        if getattr(self, "batch_cap", 0) < nreq:
+            self.reserve_batch(nreq)
+        npix = self.npix()
+        if out is None:
+            out = torch.empty((nreq, 2, npix) if spin else (nreq, npix), dtype=torch.float64, device="cuda")
+        _lib.check(self._lib.cunusht_lensing_batch(
+            self._plan, nreq, spin, ncomp, g.data_ptr(), d.data_ptr(), c.data_ptr() if c is not None else None,
+            ptg.data_ptr() if ptg is not None else None, gamma.data_ptr() if gamma is not None else None,
+            out.data_ptr(), _lib.F32 if out.dtype == torch.float32 else _lib.F64, _stream()))
+        return out
+
     def lensing_solve(self, gclm: torch.Tensor, dlm_scaled: torch.Tensor, out: torch.Tensor, ptg: torch.Tensor,
                       gamma: torch.Tensor, spin: int, dclm_scaled: torch.Tensor | None = None):
         """One uncached lensing solve on device tensors (dlm2pointing + nusht2d2
@@ -308,6 +338,24 @@ class GPU_cufinufft_transformer:
                                               ptg.shape[1], 1, gamma.data_ptr() if spin else None,
                                               out.data_ptr(), odt, s))
         return out
+
+    def delensing_solve(self, lenmap: torch.Tensor, dlm_scaled: torch.Tensor, alm_out: torch.Tensor,
+                        ptg: torch.Tensor, gamma: torch.Tensor, spin: int,
+                        dclm_scaled: torch.Tensor | None = None):
+        """One uncached adjoint lensing solve on device tensors (dlm2pointing +
+        nusht2d1 with the inverse rotation), no host synchronisation.
+        lenmap (npix,) or (2, npix) float64 -> alm_out (ncomp, nalm)."""
+        s = _stream()
+        _lib.check(self._lib.cunusht_dlm2pointing(self._plan, dlm_scaled.data_ptr(),
+                                                  dclm_scaled.data_ptr() if dclm_scaled is not None else None,
+                                                  _lib.F64, ptg.data_ptr(), gamma.data_ptr(), s))
+        ncomp = 1 if (spin == 0 or alm_out.dim() == 1) else alm_out.shape[0]
+        mdt = _lib.F32 if lenmap.dtype == torch.float32 else _lib.F64
+        adt = _lib.F32 if alm_out.dtype == torch.complex64 else _lib.F64
+        _lib.check(self._lib.cunusht_nusht2d1(self._plan, spin, ncomp, lenmap.data_ptr(), mdt, ptg.data_ptr(),
+                                              ptg.shape[1], 1, gamma.data_ptr() if spin else None,
+                                              alm_out.data_ptr(), adt, s))
+        return alm_out
 
     # -------------------------------------------------------------- lensing
     def _spin_of(self, gclm, spin):

@@ -91,6 +91,17 @@ int cunusht_plan_destroy(cunusht_plan_t *plan);
 int cunusht_plan_set_profiling(cunusht_plan_t *plan, int enable);
 int cunusht_plan_stage_times(cunusht_plan_t *plan, double *ms, int64_t *count, int nstage);
 
+/*
+ * Transforms longer than 8192 points (theta / phi passes above lmax 2047,
+ * Bluestein ring transforms above 4096 pixels per ring) run as two
+ * half-length transforms split by output parity.  force = 1 selects that
+ * split form for every transform of the plan, so that it can be checked
+ * against the direct form at small sizes; force = 0 restores the automatic
+ * choice.  No reference counterpart (the reference delegates its FFTs to
+ * cuFFT / cuFINUFFT).
+ */
+int cunusht_plan_force_split(cunusht_plan_t *plan, int force);
+
 /* Plan sizes: info[0]=npix, [1]=torus theta length, [2]=torus phi length,
  * [3]=fine grid theta length, [4]=fine grid phi length, [5]=kernel width,
  * [6]=fine rows stored, [7]=workspace bytes, [8]=precision in use,
@@ -120,6 +131,23 @@ int cunusht_nusht2d2(cunusht_plan_t *plan, int spin, int ncomp, const void *alm,
 int cunusht_nusht2d1(cunusht_plan_t *plan, int spin, int ncomp, const void *map, int map_dtype,
                      const double *loc, int64_t npts, int loc_layout, const double *gamma,
                      void *alm_out, int alm_dtype, void *stream);
+
+/*
+ * Served form: nreq lensing solves (dlm2pointing + nusht2d2 with the
+ * exp(i spin gamma) rotation, i.e. GPU_cufinufft_transformer.gclm2lenmap,
+ * GPU_nufft_transformer.py:487-578) of one lmax / spin / accuracy in one
+ * pass of batched launches.  The mixed-precision Legendre kernels share one
+ * recursion between up to four requests.  Arrays are contiguous per request:
+ * gclm (nreq, ncomp, nalm) complex128, dlm_scaled / dclm_scaled (nreq, nalm)
+ * complex128 (dclm may be NULL), out (nreq, spin ? 2 : 1, npix); ptg
+ * (nreq, 2, npix) and gamma (nreq, npix) receive the pointing when not NULL.
+ * cunusht_plan_reserve_batch allocates the per-request workspace once
+ * (nreq <= max_batch); the batched call itself allocates nothing.
+ */
+int cunusht_plan_reserve_batch(cunusht_plan_t *plan, int max_batch);
+int cunusht_lensing_batch(cunusht_plan_t *plan, int nreq, int spin, int ncomp, const void *gclm,
+                          const void *dlm_scaled, const void *dclm_scaled, double *ptg, double *gamma,
+                          void *out, int out_dtype, void *stream);
 
 /*
  * dlm2pointing: deflected angles of every pixel of the plan geometry.
