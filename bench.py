@@ -58,6 +58,13 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the cpu_baseline sample")
     p.add_argument("--batch", type=int, default=4, help="requests per launch of the served form")
     p.add_argument("--fp64-steps", type=int, default=3, help="timed solves of the plain FP64 single-request form")
+    p.add_argument("--serve", action="store_true",
+                   help="served mixed workload instead: Poisson arrivals of mixed lmax / spin / direction / eps")
+    p.add_argument("--serve-requests", type=int, default=2000)
+    p.add_argument("--serve-rate", type=float, default=200.0, help="mean arrival rate, requests/s")
+    p.add_argument("--serve-budget-gb", type=float, default=150.0)
+    p.add_argument("--serve-fp64-sample", type=int, default=60,
+                   help="requests of the same mix run as serial plain FP64 calls for the comparison")
     return p.parse_args()
 
 
@@ -451,5 +458,189 @@ def main():
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------- served mixed workload
+SERVE_LMAX = (511, 1023, 2047, 4095)
+SERVE_P = (0.4, 0.3, 0.2, 0.1)
+
+
+def serve_policy(lmax):
+    """(requests per launch, slots) per bucket: sized so that all 16 buckets
+    (4 lmax x 2 spins x 2 accuracies) fit a 150 GB budget together."""
+    return {511: (8, 2), 1023: (8, 2), 2047: (4, 2), 4095: (1, 1)}.get(lmax, (2, 1))
+
+
+class DeviceInputs:
+    """Seeded per-request payloads generated on the device (the same spectra
+    as the single-request workload: C_l = 1e3/(l+10)^2, E ~ CN(0, 0.1 C_l),
+    B = 0; phi ~ CN(0, 4e-7 (l+20)^-4) at 2.5' rms deflection; delensing
+    inputs are white-noise maps)."""
+
+    def __init__(self, torch):
+        self.torch = torch
+        self.cache = {}
+
+    def tables(self, lmax):
+        t = self.cache.get(lmax)
+        if t is None:
+            torch = self.torch
+            ls = np.concatenate([np.arange(m, lmax + 1) for m in range(lmax + 1)]).astype(np.float64)
+            m0 = np.zeros(ls.size, dtype=bool)
+            m0[:lmax + 1] = True
+            cl = 1e3 / (ls + 10.0) ** 2
+            cpp = 4e-7 * (ls + 20.0) ** -4
+            lfac2 = ls * (ls + 1.0)
+            w = np.where(m0, 1.0, 2.0)
+            t = {k: torch.as_tensor(v, device="cuda") for k, v in
+                 dict(scl=np.sqrt(cl), scpp=np.sqrt(cpp), lfac2=lfac2, w=w, m0=m0).items()}
+            self.cache[lmax] = t
+        return t
+
+    def _calm(self, gen, n, m0):
+        torch = self.torch
+        z = torch.randn((2, n), dtype=torch.float64, device="cuda", generator=gen)
+        a = torch.complex(z[0], z[1]) * (0.5 ** 0.5)
+        return torch.where(m0, torch.complex(z[0], torch.zeros_like(z[0])), a)
+
+    def make(self, kind, lmax, spin, seed, npix):
+        torch = self.torch
+
+        def payload():
+            t = self.tables(lmax)
+            n = t["scl"].numel()
+            gen = torch.Generator(device="cuda")
+            gen.manual_seed(int(seed))
+            plm = self._calm(gen, n, t["m0"]) * t["scpp"]
+            rms2 = torch.sum(t["w"] * t["lfac2"] * (plm.real ** 2 + plm.imag ** 2)) / (4 * np.pi)
+            plm = plm * ((2.5 / 60.0 * np.pi / 180.0) / torch.sqrt(rms2))
+            if kind == "g2l":
+                g = self._calm(gen, n, t["m0"]) * t["scl"]
+                data = torch.stack([g * (0.1 ** 0.5), torch.zeros_like(g)]) if spin else g[None]
+            else:
+                data = torch.randn((2, npix) if spin else (npix,), dtype=torch.float64, device="cuda",
+                                   generator=gen)
+            return data, plm
+
+        return payload
+
+
+def serve_main(args):
+    import torch
+    from cunusht_gb300 import build as _b
+    _b.build()
+    import cunusht_gb300 as cu
+    from cunusht_gb300.serving import LensingServer
+
+    rng = np.random.default_rng(2024)
+    n = args.serve_requests
+    lmaxs = rng.choice(SERVE_LMAX, size=n, p=SERVE_P)
+    spins = rng.choice((0, 2), size=n)
+    kinds = rng.choice(("g2l", "l2g"), size=n)
+    epss = rng.choice((1e-5, 1e-7), size=n)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=n))
+    npix_of = {L: cu.get_geom(("gl", {"lmax": int(L)})).npix() for L in SERVE_LMAX}
+    inputs = DeviceInputs(torch)
+
+    srv = LensingServer(precision="mixed", hbm_budget_bytes=args.serve_budget_gb * 1e9, policy=serve_policy)
+    keys = sorted({(int(L), int(s), float(e)) for L, s, e in zip(lmaxs, spins, epss)})
+    t0 = time.perf_counter()
+    admitted = srv.prewarm(keys)
+    setup_s = time.perf_counter() - t0
+    for L in SERVE_LMAX:
+        inputs.tables(int(L))
+    # warm-up: one request per bucket and direction (graph capture, module loading)
+    for k in admitted:
+        for kind in ("g2l", "l2g"):
+            srv.submit(kind, k[0], k[1], k[2], inputs.make(kind, k[0], k[1], 10 ** 6, npix_of[k[0]]), None)
+    srv.run_until_idle()
+    torch.cuda.synchronize()
+    srv.completed.clear()
+    launches0 = srv.launches
+
+    # timed run: Poisson arrivals on the server clock
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    srv.t0 = time.perf_counter()
+    nxt = 0
+    seen = 0
+    while True:
+        now = srv.now()
+        while nxt < n and arrivals[nxt] <= now:
+            L, sp, kd, ep = int(lmaxs[nxt]), int(spins[nxt]), str(kinds[nxt]), float(epss[nxt])
+            srv.submit(kd, L, sp, ep, inputs.make(kd, L, sp, nxt, npix_of[L]), None, arrival=float(arrivals[nxt]))
+            nxt += 1
+        pending = srv.step()
+        for r in srv.completed[seen:]:
+            r.result = None                     # results are consumed (dropped) as they complete
+        seen = len(srv.completed)
+        if nxt >= n and not pending:
+            break
+        if nxt < n and not srv.busy():
+            time.sleep(max(0.0, min(1e-3, arrivals[nxt] - srv.now())))
+    torch.cuda.synchronize()
+    wall = srv.now()
+    clocks = clk.stop()
+    nlaunch = srv.launches - launches0
+    lat = np.array(srv.latencies_ms())
+    done = len(srv.completed)
+    by = {}
+    for r in srv.completed:
+        by.setdefault(r.lmax, []).append(1e3 * (r.t_done - r.arrival))
+
+    # serial plain FP64 calls on a sample of the same mix
+    fp64 = None
+    if args.serve_fp64_sample > 0:
+        del srv
+        torch.cuda.empty_cache()
+        ts = {}
+        m = args.serve_fp64_sample
+        tot = 0.0
+        for i in range(m):
+            L, sp, kd, ep = int(lmaxs[i]), int(spins[i]), str(kinds[i]), float(epss[i])
+            key = (L, sp, ep)
+            if key not in ts:
+                for k in list(ts):
+                    del ts[k]
+                torch.cuda.empty_cache()
+                ts[key] = cu.get_transformer("GPU")(("gl", {"lmax": L}), nuFFTtype=2, epsilon=ep, precision="fp64",
+                                                    max_spin=max(sp, 1))
+            T = ts[key]
+            data, plm = inputs.make(kd, L, sp, i, npix_of[L])()
+            npix = npix_of[L]
+            ptg = torch.empty((2, npix), dtype=torch.float64, device="cuda")
+            gam = torch.empty((npix,), dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            if kd == "g2l":
+                out = torch.empty((2, npix) if sp else (npix,), dtype=torch.float64, device="cuda")
+                T.lensing_solve(data if sp else data[0], plm, out, ptg, gam, sp)
+            else:
+                a = torch.empty((2 if sp else 1, T.nalm), dtype=torch.complex128, device="cuda")
+                T.delensing_solve(data, plm, a, ptg, gam, sp)
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1) * 1e-3
+        fp64 = {"value": m / tot, "unit": "requests/s", "sample": f"first {m} requests of the same stream, "
+                "one plain FP64 call each, back to back (device time, plans built outside the timing)"}
+
+    line = {"metric": "served mixed workload: requests/s and p50/p99 latency", "value": done / wall,
+            "unit": "requests/s", "n_gpus": 1, "requests": done, "higher_is_better": True,
+            "offered_rate": args.serve_rate, "wall_s": wall,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "p50_p99_ms_by_lmax": {int(L): [float(np.percentile(v, 50)), float(np.percentile(v, 99))]
+                                   for L, v in sorted(by.items())},
+            "launches": nlaunch, "requests_per_launch": done / max(1, nlaunch),
+            "fp64_serial": fp64, "buckets_admitted": len(admitted), "buckets": len(keys),
+            "plan_setup_s": setup_s, "hbm_budget_gb": args.serve_budget_gb,
+            "config": {"workload": f"{n} Poisson requests at {args.serve_rate}/s, lmax {list(SERVE_LMAX)} "
+                                   f"p={list(SERVE_P)}, spin {{0,2}}, gclm2lenmap / lenmap2gclm, eps {{1e-5,1e-7}}",
+                       "policy": {str(L): serve_policy(L) for L in SERVE_LMAX}, "precision": "mixed"},
+            "data": "synthetic, seeded per request on the device", "clocks": clocks}
+    print(json.dumps(line))
+
+
 if __name__ == "__main__":
-    main()
+    if "--serve" in sys.argv:
+        serve_main(parse())
+    else:
+        main()

@@ -692,6 +692,250 @@ __global__ void __launch_bounds__(LEG_TPB)
     }
 }
 
+// ---------------------------------------------------------------- mixed precision adjoint
+// The adjoint recursion runs in double-float as in the synthesis kernels; each
+// product lambda * h' is formed as a double-float (h' split into FP32 hi/lo)
+// and the sums over rings -- across the lanes of a warp, then across warps --
+// are double-float additions, converted to FP64 once per (l, m) and block for
+// the atomic accumulation.  No FP64 arithmetic in the inner loop.
+
+__device__ __forceinline__ dfl shfl_xor_df(dfl v, int mask) {
+    return dfl{__shfl_xor_sync(0xffffffffu, v.h, mask), __shfl_xor_sync(0xffffffffu, v.l, mask)};
+}
+
+// warp_reduce_scatter16 in double-float: same lane -> index mapping (rs16_index)
+__device__ __forceinline__ void warp_reduce_scatter16_df(dfl v[16]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const bool up = lane & 16;
+        const dfl send = up ? v[i] : v[i + 8];
+        const dfl keep = up ? v[i + 8] : v[i];
+        v[i] = df_add(keep, shfl_xor_df(send, 16));
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const bool up = lane & 8;
+        const dfl send = up ? v[i] : v[i + 4];
+        const dfl keep = up ? v[i + 4] : v[i];
+        v[i] = df_add(keep, shfl_xor_df(send, 8));
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const bool up = lane & 4;
+        const dfl send = up ? v[i] : v[i + 2];
+        const dfl keep = up ? v[i + 2] : v[i];
+        v[i] = df_add(keep, shfl_xor_df(send, 4));
+    }
+    {
+        const bool up = lane & 2;
+        const dfl send = up ? v[0] : v[1];
+        const dfl keep = up ? v[1] : v[0];
+        v[0] = df_add(keep, shfl_xor_df(send, 2));
+    }
+    v[0] = df_add(v[0], shfl_xor_df(v[0], 1));
+}
+
+// lam * (hh + hl) as a normalised double-float (the lam.l * hl term dropped)
+__device__ __forceinline__ dfl df_prod_split(dfl lam, float hh, float hl) {
+    const float p = lam.h * hh;
+    float e = fmaf(lam.h, hh, -p);
+    e = fmaf(lam.h, hl, e);
+    e = fmaf(lam.l, hh, e);
+    return df_fast(p, e);
+}
+
+struct split2 {
+    float xh, xl, yh, yl;
+};
+
+__device__ __forceinline__ split2 split_c(double2 v) {
+    split2 r;
+    r.xh = (float)v.x;
+    r.xl = (float)(v.x - (double)r.xh);
+    r.yh = (float)v.y;
+    r.yl = (float)(v.y - (double)r.yh);
+    return r;
+}
+
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_adj_s0_df(int L, const double2 *__restrict__ H, int ldH, const double *__restrict__ lfac,
+                    const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
+                    int npairs, const double *__restrict__ px, const double *__restrict__ psh,
+                    const double *__restrict__ pch, const int *__restrict__ prn,
+                    const int *__restrict__ prs, double *__restrict__ alm /* interleaved */) {
+    constexpr int NW = LEG_TPB / 32;
+    __shared__ dfl red[NW][16];
+    const int m = blockIdx.y;
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    double2 Ep = make_double2(0, 0), Op = Ep;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+        const int n = prn[p], s = prs[p];
+        const double2 hn = H[(long long)m * ldH + n];
+        if (s != n) {
+            const double2 hs = H[(long long)m * ldH + s];
+            Ep = make_double2(hn.x + hs.x, hn.y + hs.y);
+            Op = make_double2(hn.x - hs.x, hn.y - hs.y);
+        } else {
+            Ep = hn;
+            Op = hn;
+        }
+    }
+    const split2 E = split_c(Ep), O = split_c(Op);
+    const dfl xd = df_from(x);
+    dfl cur, prev;
+    int e;
+    rec_start_df(lg0[m], m, 0, sh, ch, cur, prev, e);
+    if (!act) {
+        cur.h = cur.l = 0.f;
+        e = 0;
+    }
+    const float2 *al = coef, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const dfl zero{0.f, 0.f};
+    for (int lb = m; lb <= L; lb += 8) {
+        dfl v[16];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int l = lb + i;
+            const dfl lam = (e == 0 && l <= L) ? cur : zero;
+            const split2 &src = ((l + m) & 1) ? O : E;
+            v[2 * i] = df_prod_split(lam, src.xh, src.xl);
+            v[2 * i + 1] = df_prod_split(lam, src.yh, src.yl);
+            if (l < L) {
+                const float2 a2 = __ldg(al + b + l), b2 = __ldg(be + b + l);
+                const dfl t = df_mul(dfl{a2.x, a2.y}, xd);
+                const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                prev = cur;
+                cur = nxt;
+                REC_RESCALE_DF(cur, prev, e);
+            }
+        }
+        warp_reduce_scatter16_df(v);
+        if (!(lane & 1)) red[wid][rs16_index(lane)] = v[0];
+        __syncthreads();
+        if (threadIdx.x < 16) {
+            dfl t = red[0][threadIdx.x];
+#pragma unroll
+            for (int w = 1; w < NW; ++w) t = df_add(t, red[w][threadIdx.x]);
+            const int l = lb + (threadIdx.x >> 1);
+            if (l <= L) {
+                const double f = lfac ? lfac[l] : 1.0;
+                atomicAdd(alm + 2 * (b + l) + (threadIdx.x & 1), df_to(t) * f);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(LEG_TPB)
+    k_leg_adj_spin_df(int L, int spin, int ncomp, const double2 *__restrict__ H, int ldH,
+                      const double *__restrict__ lfac, const float2 *__restrict__ coef,
+                      long long nalm, const double *__restrict__ lg0, int npairs,
+                      const double *__restrict__ px, const double *__restrict__ psh,
+                      const double *__restrict__ pch, const int *__restrict__ prn,
+                      const int *__restrict__ prs, double *__restrict__ Gout,
+                      double *__restrict__ Cout) {
+    constexpr int NW = LEG_TPB / 32;
+    __shared__ dfl red[NW][16];
+    __shared__ double tot[16];
+    const int m = blockIdx.y;
+    const int l0 = max(m, spin);
+    const int p = blockIdx.x * LEG_TPB + threadIdx.x;
+    const bool act = p < npairs;
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    double2 hpn = make_double2(0, 0), hps = hpn, hmn = hpn, hms = hpn;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+        const int n = prn[p], s = prs[p];
+        hpn = H[(long long)(L + m) * ldH + n];
+        hmn = H[(long long)(L - m) * ldH + n];
+        if (s != n) {
+            hps = H[(long long)(L + m) * ldH + s];
+            hms = H[(long long)(L - m) * ldH + s];
+        }
+    }
+    const split2 PN = split_c(hpn), PS = split_c(hps), MN = split_c(hmn), MS = split_c(hms);
+    const dfl xN = df_from(x), xS = df_from(-x);
+    dfl cN, pN, cS, pS;
+    int eN, eS;
+    rec_start_df(lg0[m], m, spin, sh, ch, cN, pN, eN);
+    rec_start_df(lg0[m], m, spin, ch, sh, cS, pS, eS);
+    if (!act) {
+        cN.h = cN.l = cS.h = cS.l = 0.f;
+        eN = eS = 0;
+    }
+    const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const double sgs = (spin & 1) ? -1.0 : 1.0;
+    const dfl zero{0.f, 0.f};
+    for (int lb = l0; lb <= L; lb += 4) {
+        dfl v[16];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int l = lb + i;
+            const dfl lN = (eN == 0 && l <= L) ? cN : zero;
+            const dfl lS = (eS == 0 && l <= L) ? cS : zero;
+            // P = lN hpn + lS hps ; Q = par (lS conj(hmn) + lN conj(hms))
+            v[4 * i + 0] = df_add(df_prod_split(lN, PN.xh, PN.xl), df_prod_split(lS, PS.xh, PS.xl));
+            v[4 * i + 1] = df_add(df_prod_split(lN, PN.yh, PN.yl), df_prod_split(lS, PS.yh, PS.yl));
+            const dfl qr = df_add(df_prod_split(lS, MN.xh, MN.xl), df_prod_split(lN, MS.xh, MS.xl));
+            const dfl qi = df_add(df_prod_split(lS, MN.yh, MN.yl), df_prod_split(lN, MS.yh, MS.yl));
+            const bool odd = (l + m) & 1;
+            v[4 * i + 2] = odd ? df_neg(qr) : qr;
+            v[4 * i + 3] = odd ? qi : df_neg(qi);
+            if (l < L) {
+                const float2 a2 = __ldg(al + b + l), g2 = __ldg(ga + b + l), b2 = __ldg(be + b + l);
+                const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
+                const dfl tN = df_add(df_mul(ad, xN), gd);
+                const dfl tS = df_add(df_mul(ad, xS), gd);
+                const dfl nN = df_mul_sub(tN, cN, bd, pN);
+                const dfl nS = df_mul_sub(tS, cS, bd, pS);
+                pN = cN;
+                cN = nN;
+                pS = cS;
+                cS = nS;
+                REC_RESCALE_DF(cN, pN, eN);
+                REC_RESCALE_DF(cS, pS, eS);
+            }
+        }
+        warp_reduce_scatter16_df(v);
+        if (!(lane & 1)) red[wid][rs16_index(lane)] = v[0];
+        __syncthreads();
+        if (threadIdx.x < 16) {
+            dfl t = red[0][threadIdx.x];
+#pragma unroll
+            for (int w = 1; w < NW; ++w) t = df_add(t, red[w][threadIdx.x]);
+            tot[threadIdx.x] = df_to(t);
+        }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            const int l = lb + threadIdx.x;
+            if (l <= L) {
+                const double f = lfac ? lfac[l] : 1.0;
+                const double Pr = tot[4 * threadIdx.x], Pi = tot[4 * threadIdx.x + 1];
+                const double Qr = sgs * tot[4 * threadIdx.x + 2], Qi = sgs * tot[4 * threadIdx.x + 3];
+                atomicAdd(Gout + 2 * (b + l), -0.5 * f * (Pr + Qr));
+                atomicAdd(Gout + 2 * (b + l) + 1, -0.5 * f * (Pi + Qi));
+                if (ncomp > 1) {
+                    atomicAdd(Cout + 2 * (b + l), -0.5 * f * (Pi - Qi));
+                    atomicAdd(Cout + 2 * (b + l) + 1, 0.5 * f * (Pr - Qr));
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------- host launchers
 struct RingPairs {
     int npairs;
@@ -776,7 +1020,15 @@ int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, 
     if (spin > 0 && ncomp > 1) CU_TRY(cudaMemsetAsync(C, 0, sizeof(double2) * P->nalm, st));
     dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
     const double *lf = use_lfac ? P->d_lfac : nullptr;
-    if (spin == 0) {
+    if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
+        if (spin == 0)
+            k_leg_adj_s0_df<<<grid, LEG_TPB, 0, st>>>(L, H, R.ld, lf, P->d_coef_df[0], P->nalm, P->d_lg0[0],
+                                                      R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, (double *)G);
+        else
+            k_leg_adj_spin_df<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, H, R.ld, lf, P->d_coef_df[spin], P->nalm,
+                                                        P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
+                                                        (double *)G, (double *)C);
+    } else if (spin == 0) {
         k_leg_adj_s0<<<grid, LEG_TPB, 0, st>>>(L, H, R.ld, lf, P->d_coef[0], P->nalm, P->d_lg0[0],
                                                R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
                                                (double *)G);

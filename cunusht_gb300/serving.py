@@ -35,6 +35,7 @@ from typing import Optional
 
 import torch
 
+from ._lib import CunushtError
 from .transformer import GPU_cufinufft_transformer
 
 
@@ -44,8 +45,10 @@ class Request:
     lmax: int
     spin: int
     epsilon: float
-    data: torch.Tensor              # gclm (ncomp, nalm) / (nalm,) for g2l; lenmap (2, npix) / (npix,) for l2g
-    dlm_scaled: torch.Tensor        # (nalm,) complex128 on the device
+    data: object                    # gclm (ncomp, nalm) / (nalm,) for g2l; lenmap (2, npix) / (npix,) for l2g;
+                                    # or a callable returning (data, dlm_scaled), run on the slot's stream when
+                                    # the request is admitted (payload materialised only once it has a slot)
+    dlm_scaled: Optional[torch.Tensor]  # (nalm,) complex128 on the device (None with a callable payload)
     arrival: float = 0.0            # server clock, seconds
     rid: int = 0
     result: Optional[torch.Tensor] = None
@@ -108,11 +111,13 @@ class _Slot:
 
 class LensingServer:
     def __init__(self, max_batch: int = 4, hbm_budget_bytes: float = 150e9, precision: str = "mixed",
-                 slots_per_bucket: int = 2, graphs: bool = True, nphi_of=lambda lmax: None):
+                 slots_per_bucket: int = 2, graphs: bool = True, nphi_of=lambda lmax: None, policy=None):
+        """policy(lmax) -> (max_batch, slots) overrides max_batch / slots_per_bucket per size."""
         self.max_batch = max_batch
         self.budget = hbm_budget_bytes
         self.precision = precision
         self.slots_per_bucket = slots_per_bucket
+        self.policy = policy or (lambda lmax: (max_batch, slots_per_bucket))
         self.graphs = graphs
         self.nphi_of = nphi_of
         self.buckets: dict[tuple, list[_Slot]] = {}
@@ -122,6 +127,7 @@ class LensingServer:
         self.completed: list[Request] = []
         self.launches = 0
         self.rejected_admissions = 0
+        self._blocked: dict[tuple, int] = {}
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -133,20 +139,29 @@ class LensingServer:
     def _admit(self, key) -> bool:
         if key in self.buckets:
             return True
+        used = self.used_bytes()
+        if key in self._blocked and used >= self._blocked[key]:
+            return False                        # nothing was released since the last refusal
         lmax, spin, eps = key
+        nb, nslots = self.policy(lmax)
         slots = []
-        for _ in range(self.slots_per_bucket):
-            sl = _Slot(lmax, spin, eps, self.max_batch, self.nphi_of(lmax), self.precision, self.graphs)
+        for _ in range(nslots):
+            try:
+                sl = _Slot(lmax, spin, eps, nb, self.nphi_of(lmax), self.precision, self.graphs)
+            except (CunushtError, torch.cuda.OutOfMemoryError):
+                break
             slots.append(sl)
-            if self.used_bytes() + sum(s.bytes for s in slots) > self.budget:
+            if used + sum(s.bytes for s in slots) > self.budget:
                 slots.pop()
                 del sl
                 break
         if not slots:
             self.rejected_admissions += 1
+            self._blocked[key] = used
             self._evict_idle(keep=key)
             torch.cuda.empty_cache()
             return False
+        self._blocked.pop(key, None)
         self.buckets[key] = slots
         return True
 
@@ -154,6 +169,11 @@ class LensingServer:
         for k in list(self.buckets):
             if k != keep and not self.queues[k] and all(not sl.busy for sl in self.buckets[k]):
                 del self.buckets[k]
+
+    def prewarm(self, keys) -> list:
+        """Create the slots of these buckets ahead of traffic (within the
+        budget); returns the keys admitted."""
+        return [k for k in keys if self._admit(tuple(k))]
 
     # ------------------------------------------------------------------ API
     def submit(self, kind, lmax, spin, epsilon, data, dlm_scaled, arrival=None) -> Request:
@@ -201,8 +221,9 @@ class LensingServer:
             if q[0].kind == "l2g":
                 batch = [q.popleft()]
                 r = batch[0]
-                sl.lin.copy_(r.data.reshape(sl.lin.shape), non_blocking=True)
-                sl.din[0].copy_(r.dlm_scaled.reshape(-1), non_blocking=True)
+                data, dlm = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
+                sl.lin.copy_(data.reshape(sl.lin.shape), non_blocking=True)
+                sl.din[0].copy_(dlm.reshape(-1), non_blocking=True)
                 sl.run("l2g", 1)
                 r.result = sl.aout[0].clone() if sl.spin == 0 else sl.aout.clone()
             else:
@@ -210,8 +231,9 @@ class LensingServer:
                 while q and q[0].kind == "g2l" and len(batch) < sl.max_batch:
                     batch.append(q.popleft())
                 for i, r in enumerate(batch):
-                    sl.gin[i].copy_(r.data.reshape(sl.ncomp, -1), non_blocking=True)
-                    sl.din[i].copy_(r.dlm_scaled.reshape(-1), non_blocking=True)
+                    data, dlm = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
+                    sl.gin[i].copy_(data.reshape(sl.ncomp, -1), non_blocking=True)
+                    sl.din[i].copy_(dlm.reshape(-1), non_blocking=True)
                 sl.run("g2l", len(batch))
                 for i, r in enumerate(batch):
                     r.result = sl.out[i].clone()
@@ -220,7 +242,8 @@ class LensingServer:
         t = self.now()
         for r in batch:
             r.t_launch = t
-            r.data = None                       # inputs are staged; drop the caller's reference
+            r.data = None                       # inputs are staged; drop the caller's references
+            r.dlm_scaled = None
         sl.busy = batch
         sl.event = ev
         self.launches += 1
