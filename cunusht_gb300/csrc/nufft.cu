@@ -147,49 +147,278 @@ __global__ void __launch_bounds__(NU_TPB)
     }
 }
 
-// ------------------------------------------------------------ spread (type 1)
+// FP32 kernel value from the cancellation-free exponent
+// beta (sqrt(1 - z^2) - 1) = -beta z^2 / (1 + sqrt(1 - z^2))
+__device__ __forceinline__ float es_kernel_acc(float z, float beta) {
+    const float q = 1.f - z * z;
+    if (q <= 0.f) return 0.f;
+    const float r = sqrtf(q);
+    return expf(-beta * (z * z) / (1.f + r));
+}
+
+// ------------------------------------------------------------ warp-strip spreading (type 1)
+// Each warp spreads 32 consecutive points (for lensing: neighbouring pixels of
+// one ring, whose w x w footprints overlap) into a private shared-memory strip
+// covering their joint footprint.  All lanes step through the taps (a, b) in
+// lockstep, so two lanes touch the same strip cell only when their points
+// share the first-tap cell; such lanes are serialised by rank
+// (__match_any_sync), and the strip needs no atomics.  The strip is then added
+// to U with global atomics, one per touched cell instead of one per tap.
+// Warps whose footprint does not fit the strip (a ring boundary, scattered
+// points) add their taps to U directly.
+constexpr int SPW_WARPS = 4;  // warps per block
+
 template <typename T, bool CPLX>
-__global__ void __launch_bounds__(NU_TPB)
-    k_spread(T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
-             const double *__restrict__ loc, long long npts, int layout,
-             const double *__restrict__ gamma, int spin, const void *__restrict__ in, int in_f32) {
-    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= npts) return;
-    double th, ph;
-    load_point(loc, j, npts, layout, th, ph);
-    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+__global__ void __launch_bounds__(SPW_WARPS * 32)
+    k_spread_warp(T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
+                  const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
+                  int spin, const void *__restrict__ in, int in_f32, int SR, int SC) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NC = CPLX ? 2 : 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    T *strip = reinterpret_cast<T *>(smem_raw) + (size_t)wid * SR * SC * NC;
+    const long long j = ((long long)blockIdx.x * SPW_WARPS + wid) * 32 + lane;
+    const bool act = j < npts;
+    const unsigned amask = __ballot_sync(0xffffffffu, act);
+    if (amask == 0) return;
+    PointCoords pc{0, 0, 0.0, 0.0};
+    double vr = 0.0, vi = 0.0;
+    if (act) {
+        double th, ph;
+        load_point(loc, j, npts, layout, th, ph);
+        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+        if (in_f32) {
+            vr = ((const float *)in)[j];
+            if (CPLX) vi = ((const float *)in)[npts + j];
+        } else {
+            vr = ((const double *)in)[j];
+            if (CPLX) vi = ((const double *)in)[npts + j];
+        }
+        if (CPLX && gamma) {
+            double s, c;
+            sincos(spin * gamma[j], &s, &c);  // multiply by e^{-i spin gamma}
+            const double t2 = vr * c + vi * s;
+            vi = vi * c - vr * s;
+            vr = t2;
+        }
+    }
     T kt[MAXW], kp[MAXW];
     weights<T>(pc, w, beta, kt, kp);
-    double vr, vi = 0.0;
-    if (in_f32) {
-        vr = ((const float *)in)[j];
-        if (CPLX) vi = ((const float *)in)[npts + j];
-    } else {
-        vr = ((const double *)in)[j];
-        if (CPLX) vi = ((const double *)in)[npts + j];
-    }
-    if (CPLX && gamma) {
-        double s, c;
-        sincos(spin * gamma[j], &s, &c);  // multiply by e^{-i spin gamma}
-        const double tr = vr * c + vi * s;
-        vi = vi * c - vr * s;
-        vr = tr;
-    }
-    for (int a = 0; a < w; ++a) {
-        const long long rowoff = (long long)(pc.r0 + a) * Npf;
-        const T fr = kt[a] * (T)vr, fi = kt[a] * (T)vi;
-        for (int b = 0; b < w; ++b) {
-            int c = pc.p0 + b;
-            c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
-            if constexpr (CPLX) {
-                T *cell = U + 2 * (rowoff + c);
+    // joint footprint of the warp's points
+    const int big = 1 << 30;
+    const int rmin = __reduce_min_sync(0xffffffffu, act ? pc.r0 : big);
+    const int rmax = __reduce_max_sync(0xffffffffu, act ? pc.r0 : -big);
+    const int pmin = __reduce_min_sync(0xffffffffu, act ? pc.p0 : big);
+    const int pmax = __reduce_max_sync(0xffffffffu, act ? pc.p0 : -big);
+    const int nr = rmax - rmin + w, ncl = pmax - pmin + w;
+    if (nr > SR || ncl > SC) {
+        // footprint too wide for the strip: direct global atomics
+        if (!act) return;
+        for (int a = 0; a < w; ++a) {
+            const long long rowoff = (long long)(pc.r0 + a) * Npf;
+            const T fr = kt[a] * (T)vr, fi = kt[a] * (T)vi;
+            for (int b = 0; b < w; ++b) {
+                int c = pc.p0 + b;
+                c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+                T *cell = U + (rowoff + c) * NC;
                 atomicAdd(cell, kp[b] * fr);
-                atomicAdd(cell + 1, kp[b] * fi);
-            } else {
-                atomicAdd(U + rowoff + c, kp[b] * fr);
+                if constexpr (CPLX) atomicAdd(cell + 1, kp[b] * fi);
+            }
+        }
+        return;
+    }
+    for (int i = lane; i < nr * ncl * NC; i += 32) strip[i] = (T)0;
+    __syncwarp();
+    // lanes with the same first-tap cell go in separate rounds
+    const int key = act ? (pc.r0 - rmin) * SC + (pc.p0 - pmin) : -1 - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int myrank = __popc(peers & ((1u << lane) - 1u));
+    const int nround = __reduce_max_sync(0xffffffffu, act ? myrank : 0) + 1;
+    const int base = (pc.r0 - rmin) * ncl + (pc.p0 - pmin);
+    for (int rd = 0; rd < nround; ++rd) {
+        const bool go = act && myrank == rd;
+        for (int a = 0; a < w; ++a) {
+            const T fr = kt[a] * (T)vr, fi = kt[a] * (T)vi;
+            T *row = strip + (size_t)(base + a * ncl) * NC;
+            for (int b = 0; b < w; ++b) {
+                if (go) {
+                    row[b * NC] += kp[b] * fr;
+                    if constexpr (CPLX) row[b * NC + 1] += kp[b] * fi;
+                }
+                // footprints of neighbouring points overlap: order every
+                // step's read-modify-write before the next step's
+                __syncwarp();
             }
         }
     }
+    __syncwarp();
+    for (int i = lane; i < nr * ncl; i += 32) {
+        const int lr = i / ncl, lc = i - lr * ncl;
+        int c = pmin + lc;
+        c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+        T *cell = U + ((long long)(rmin + lr) * Npf + c) * NC;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            const T v = strip[i * NC + q];
+            if (v != (T)0) atomicAdd(cell + q, v);
+        }
+    }
+}
+
+template <typename T, bool CPLX>
+static int launch_spread_warp(const cunusht_plan_s *P, T *U, const double *loc, long long npts, int layout,
+                              const double *gamma, int spin, const void *in, int f32i, cudaStream_t st) {
+    // strip: the footprint of 32 neighbouring ring pixels at about 2 fine
+    // cells per pixel, plus row jitter from the deflection
+    const int SR = P->w + 4, SC = 80 + P->w;
+    const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(T);
+    if (sm > 48 * 1024)
+        CU_TRY(cudaFuncSetAttribute(k_spread_warp<T, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const long long nwarps = (npts + 31) / 32;
+    const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
+    k_spread_warp<T, CPLX><<<nb, SPW_WARPS * 32, sm, st>>>(U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w, (T)P->beta,
+                                                          loc, npts, layout, gamma, spin, in, f32i, SR, SC);
+    return CUNUSHT_OK;
+}
+
+// Mixed-precision variant for an FP64 grid (eps <= 1e-6 on the mixed path):
+// kernel weights in FP32 from the FP64 tap offset split into hi + lo floats
+// (as k_interp_mixed), FP32 products, Kahan-compensated FP32 strip sums, FP64
+// global accumulation.  The FP64 variant is bound by its FP64 exponentials and
+// products (GB300 runs FP64 at 1/60 of the FP32 rate).
+template <bool CPLX>
+__global__ void __launch_bounds__(SPW_WARPS * 32)
+    k_spread_warp_mixed(double *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
+                        const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
+                        int spin, const void *__restrict__ in, int in_f32, int SR, int SC) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NC = CPLX ? 2 : 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float2 *strip = reinterpret_cast<float2 *>(smem_raw) + (size_t)wid * SR * SC * NC;  // (sum, compensation)
+    const long long j = ((long long)blockIdx.x * SPW_WARPS + wid) * 32 + lane;
+    const bool act = j < npts;
+    const unsigned amask = __ballot_sync(0xffffffffu, act);
+    if (amask == 0) return;
+    PointCoords pc{0, 0, 0.0, 0.0};
+    double vr = 0.0, vi = 0.0;
+    if (act) {
+        double th, ph;
+        load_point(loc, j, npts, layout, th, ph);
+        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+        if (in_f32) {
+            vr = ((const float *)in)[j];
+            if (CPLX) vi = ((const float *)in)[npts + j];
+        } else {
+            vr = ((const double *)in)[j];
+            if (CPLX) vi = ((const double *)in)[npts + j];
+        }
+        if (CPLX && gamma) {
+            // multiply by e^{-i spin gamma}; 1 - cos from 2 sin^2(x/2) keeps
+            // the error relative to the angle
+            const float x = (float)(spin * gamma[j]);
+            const float sh = sinf(0.5f * x);
+            const double d = 2.0 * (double)sh * (double)sh;
+            const double sn = (double)sinf(x);
+            const double t2 = vr - vr * d + vi * sn;
+            vi = vi - vi * d - vr * sn;
+            vr = t2;
+        }
+    }
+    float kt[MAXW], kp[MAXW];
+    {
+        const float sc = 2.f / (float)w;
+        const float fth = (float)pc.ft, ftl = (float)(pc.ft - (double)fth);
+        const float fph = (float)pc.fp, fpl = (float)(pc.fp - (double)fph);
+#pragma unroll
+        for (int a = 0; a < MAXW; ++a) {
+            if (a < w) {
+                kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
+                kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
+            }
+        }
+    }
+    const int big = 1 << 30;
+    const int rmin = __reduce_min_sync(0xffffffffu, act ? pc.r0 : big);
+    const int rmax = __reduce_max_sync(0xffffffffu, act ? pc.r0 : -big);
+    const int pmin = __reduce_min_sync(0xffffffffu, act ? pc.p0 : big);
+    const int pmax = __reduce_max_sync(0xffffffffu, act ? pc.p0 : -big);
+    const int nr = rmax - rmin + w, ncl = pmax - pmin + w;
+    if (nr > SR || ncl > SC) {
+        if (!act) return;
+        for (int a = 0; a < w; ++a) {
+            const long long rowoff = (long long)(pc.r0 + a) * Npf;
+            for (int b = 0; b < w; ++b) {
+                int c = pc.p0 + b;
+                c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+                const double kw = (double)kt[a] * (double)kp[b];
+                double *cell = U + (rowoff + c) * NC;
+                atomicAdd(cell, kw * vr);
+                if constexpr (CPLX) atomicAdd(cell + 1, kw * vi);
+            }
+        }
+        return;
+    }
+    for (int i = lane; i < nr * ncl * NC; i += 32) strip[i] = make_float2(0.f, 0.f);
+    __syncwarp();
+    const int key = act ? (pc.r0 - rmin) * SC + (pc.p0 - pmin) : -1 - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int myrank = __popc(peers & ((1u << lane) - 1u));
+    const int nround = __reduce_max_sync(0xffffffffu, act ? myrank : 0) + 1;
+    const int base = (pc.r0 - rmin) * ncl + (pc.p0 - pmin);
+    for (int rd = 0; rd < nround; ++rd) {
+        const bool go = act && myrank == rd;
+        for (int a = 0; a < w; ++a) {
+            // row factor kt[a] * value in FP64, split into hi + lo floats:
+            // each tap product then carries one FP32 rounding
+            const double fr = (double)kt[a] * vr, fi = (double)kt[a] * vi;
+            const float frh = (float)fr, frl = (float)(fr - (double)frh);
+            const float fih = (float)fi, fil = (float)(fi - (double)fih);
+            float2 *row = strip + (size_t)(base + a * ncl) * NC;
+            for (int b = 0; b < w; ++b) {
+                if (go) {
+                    // Kahan: sum = x, comp = c; value = x - c
+                    float2 t = row[b * NC];
+                    float y = fmaf(kp[b], frh, kp[b] * frl) - t.y;
+                    float s2 = t.x + y;
+                    row[b * NC] = make_float2(s2, (s2 - t.x) - y);
+                    if constexpr (CPLX) {
+                        t = row[b * NC + 1];
+                        y = fmaf(kp[b], fih, kp[b] * fil) - t.y;
+                        s2 = t.x + y;
+                        row[b * NC + 1] = make_float2(s2, (s2 - t.x) - y);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    __syncwarp();
+    for (int i = lane; i < nr * ncl; i += 32) {
+        const int lr = i / ncl, lc = i - lr * ncl;
+        int c = pmin + lc;
+        c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+        double *cell = U + ((long long)(rmin + lr) * Npf + c) * NC;
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+            const float2 v = strip[i * NC + q];
+            if (v.x != 0.f) atomicAdd(cell + q, (double)v.x - (double)v.y);
+        }
+    }
+}
+
+template <bool CPLX>
+static int launch_spread_warp_mixed(const cunusht_plan_s *P, const double *loc, long long npts, int layout,
+                                    const double *gamma, int spin, const void *in, int f32i, cudaStream_t st) {
+    const int SR = P->w + 4, SC = 80 + P->w;
+    const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(float2);
+    if (sm > 48 * 1024)
+        CU_TRY(cudaFuncSetAttribute(k_spread_warp_mixed<CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const long long nwarps = (npts + 31) / 32;
+    const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
+    k_spread_warp_mixed<CPLX><<<nb, SPW_WARPS * 32, sm, st>>>((double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                             P->w, (float)P->beta, loc, npts, layout, gamma, spin,
+                                                             in, f32i, SR, SC);
+    return CUNUSHT_OK;
 }
 
 // ------------------------------------------------------------ interp, mixed precision
@@ -198,12 +427,6 @@ __global__ void __launch_bounds__(NU_TPB)
 // Kahan-compensated FP32 sums, and the exp(i s gamma) rotation applied in FP64
 // from d = 1 - cos(x) = 2 sin^2(x/2) and sin(x) evaluated in FP32 (errors
 // relative to the small angle, not to 1).
-__device__ __forceinline__ float es_kernel_acc(float z, float beta) {
-    const float q = 1.f - z * z;
-    if (q <= 0.f) return 0.f;
-    const float r = sqrtf(q);
-    return expf(-beta * (z * z) / (1.f + r));
-}
 
 template <bool CPLX>
 __global__ void __launch_bounds__(NU_TPB)
@@ -342,22 +565,16 @@ int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long
     const size_t cell = (P->grid_fp32 ? 4 : 8) * (spin ? 2 : 1);
     CU_TRY(cudaMemsetAsync(P->d_U, 0, cell * (size_t)P->nrows * P->Npf, st));
     if (npts == 0) return CUNUSHT_OK;
-    const int nb = (int)((npts + NU_TPB - 1) / NU_TPB);
     const int f32i = in_dtype == CUNUSHT_F32;
     if (P->grid_fp32) {
-        if (spin == 0)
-            k_spread<float, false><<<nb, NU_TPB, 0, st>>>((float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                          (float)P->beta, loc, npts, layout, gamma, spin, in, f32i);
-        else
-            k_spread<float, true><<<nb, NU_TPB, 0, st>>>((float *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                         (float)P->beta, loc, npts, layout, gamma, spin, in, f32i);
+        if (spin == 0) RC_TRY((launch_spread_warp<float, false>(P, (float *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
+        else RC_TRY((launch_spread_warp<float, true>(P, (float *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
+    } else if (P->prec == CUNUSHT_PREC_MIXED) {
+        if (spin == 0) RC_TRY((launch_spread_warp_mixed<false>(P, loc, npts, layout, gamma, spin, in, f32i, st)));
+        else RC_TRY((launch_spread_warp_mixed<true>(P, loc, npts, layout, gamma, spin, in, f32i, st)));
     } else {
-        if (spin == 0)
-            k_spread<double, false><<<nb, NU_TPB, 0, st>>>((double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                           P->w, P->beta, loc, npts, layout, gamma, spin, in, f32i);
-        else
-            k_spread<double, true><<<nb, NU_TPB, 0, st>>>((double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                          P->w, P->beta, loc, npts, layout, gamma, spin, in, f32i);
+        if (spin == 0) RC_TRY((launch_spread_warp<double, false>(P, (double *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
+        else RC_TRY((launch_spread_warp<double, true>(P, (double *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
     }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
