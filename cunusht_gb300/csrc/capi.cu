@@ -118,7 +118,7 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
-                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
+                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
                     P->d_glmapb, P->d_ptgb, P->d_gamb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -321,6 +321,8 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         std::vector<double> lf(lmax + 1);
         for (int l = 0; l <= lmax; ++l) lf[l] = std::sqrt((double)l * (l + 1.0));
         RC_TRY(upload(P, &P->d_lfac, lf));
+        for (int l = 0; l <= lmax; ++l) lf[l] = l >= 1 ? std::sqrt((l - 1.0) * (l + 2.0)) : 0.0;
+        RC_TRY(upload(P, &P->d_lfac_g, lf));
     }
     // Bluestein data for ring transforms
     {
@@ -707,6 +709,61 @@ int cunusht_dlm2pointing(cunusht_plan_t *P, const void *dlm, const void *dclm, i
                                    P->npix, P->d_glmap, P->d_glmap + P->npix, ptg, ptg + P->npix, gamma, st));
     }
     return CUNUSHT_OK;
+}
+
+int cunusht_dlm2A(cunusht_plan_t *P, const void *dlm, const void *dclm, int alm_dtype, double *A, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(dlm && A, "NULL array argument");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2 *G = (const double2 *)dlm, *C = (const double2 *)dclm;
+    if (alm_dtype != CUNUSHT_F64) {
+        RC_TRY(convert_alm(dlm, alm_dtype, P->nalm, P->d_alm, st));
+        G = P->d_alm;
+        if (dclm) {
+            RC_TRY(convert_alm(dclm, alm_dtype, P->nalm, P->d_alm + P->nalm, st));
+            C = P->d_alm + P->nalm;
+        }
+    }
+    const long long npix = P->npix;
+    double *d1 = P->d_vjp, *d2 = P->d_vjp + npix, *g1 = P->d_vjp + 2 * npix, *g2 = P->d_vjp + 3 * npix;
+    double *kp = P->d_glmap, *wp = dclm ? P->d_glmap + npix : nullptr;
+    // deflection (spin 1 of dlm, dclm)
+    RC_TRY(leg_synth_batch_fl(P, 1, 1, G, C, 0, nullptr, false, P->d_Hgl, 0, st));
+    RC_TRY(ring_synth(P, 1, P->d_Hgl, d1, d2, st));
+    // convergence: spin 0 of sqrt(l(l+1)) dlm (x 1/2 in the determinant kernel)
+    RC_TRY(leg_synth_batch_fl(P, 1, 0, G, nullptr, 0, P->d_lfac, false, P->d_Hgl, 0, st));
+    RC_TRY(ring_synth(P, 0, P->d_Hgl, kp, nullptr, st));
+    // shear: spin 2 of sqrt((l-1)(l+2)) (dlm, dclm) (x -1/2)
+    RC_TRY(leg_synth_batch_fl(P, 1, 2, G, C, 0, P->d_lfac_g, false, P->d_Hgl, 0, st));
+    RC_TRY(ring_synth(P, 2, P->d_Hgl, g1, g2, st));
+    if (dclm) {  // rotation: spin 0 of sqrt(l(l+1)) dclm (x 1/2)
+        RC_TRY(leg_synth_batch_fl(P, 1, 0, C, nullptr, 0, P->d_lfac, false, P->d_Hgl, 0, st));
+        RC_TRY(ring_synth(P, 0, P->d_Hgl, wp, nullptr, st));
+    }
+    return magnification_det(npix, kp, g1, g2, d1, d2, wp, A, st);
+}
+
+int cunusht_synth_points(cunusht_plan_t *P, int spin, int ncomp, const void *alm, int alm_dtype, const double *loc,
+                         int64_t npts, int loc_layout, const double *gamma, double *out, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(spin >= 0 && spin <= 2, "spin must be 0, 1 or 2, got %d", spin);
+    if (spin == 0) ARG_CHECK(ncomp == 1, "spin 0 takes ncomp = 1, got %d", ncomp);
+    else ARG_CHECK(ncomp == 1 || ncomp == 2, "spin %d takes ncomp 1 or 2, got %d", spin, ncomp);
+    ARG_CHECK(alm && out && (loc || npts == 0), "NULL array argument");
+    ARG_CHECK(npts >= 0 && npts < (int64_t)1 << 31, "npts must be in [0, 2^31)");
+    ARG_CHECK(loc_layout == 0 || loc_layout == 1, "loc_layout must be 0 or 1");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const double2 *G = (const double2 *)alm;
+    if (alm_dtype != CUNUSHT_F64) {
+        RC_TRY(convert_alm(alm, alm_dtype, ncomp * P->nalm, P->d_alm, st));
+        G = P->d_alm;
+    }
+    const double2 *C = (spin > 0 && ncomp > 1) ? G + P->nalm : nullptr;
+    return synth_points(P, spin, G, C, npts, loc, loc_layout, spin ? gamma : nullptr, out, st);
 }
 
 int cunusht_lensing_vjp_dlm(cunusht_plan_t *P, int spin, const void *gclm, int alm_dtype, const void *dlm_scaled,

@@ -196,6 +196,7 @@ struct cunusht_plan_s {
     double *d_glmap = nullptr; // spin-1 maps on pointing grid       [2][npix]
     double2 *d_alm = nullptr;  // alm staging (dtype conversion)     [2][nalm]
     double *d_vjp = nullptr;   // lensing VJP scratch: pointing + deflection gradient [4][npix]
+    double *d_lfac_g = nullptr; // sqrt((l - 1)(l + 2)): deflection -> shear (spin-raising) factor [lmax + 1]
     // batched-solve workspace (cunusht_plan_reserve_batch), per request:
     int batch_cap = 0;
     double2 *d_Hb = nullptr;    // [cap][ncols][ncc]

@@ -14,6 +14,10 @@ int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2
               bool use_lfac, bool cc, double2 *H, cudaStream_t st);
 int leg_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
                     long long astride, bool use_lfac, bool cc, double2 *H, long long hstride, cudaStream_t st);
+int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
+                       long long astride, const double *fl, bool cc, double2 *H, long long hstride, cudaStream_t st);
+int synth_points(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C, long long npts,
+                 const double *loc, int layout, const double *gamma, double *out, cudaStream_t st);
 int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
                 bool cc, double2 *G, double2 *C, cudaStream_t st);
 
@@ -42,6 +46,8 @@ int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long
 int nufft_interp_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, long long ubs, const double *loc,
                        long long lbs, long long npts, int layout, const double *gamma, void *out, long long obs,
                        int out_dtype, cudaStream_t st);
+int magnification_det(long long npix, const double *k, const double *g1, const double *g2, const double *d1,
+                      const double *d2, const double *w, double *A, cudaStream_t st);
 int pointing_batch(const cunusht_plan_s *P, int nreq, const double *d, long long dbs, double *ptg, long long pbs,
                    double *gamma, cudaStream_t st);
 int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts,

@@ -936,6 +936,128 @@ __global__ void __launch_bounds__(LEG_TPB)
     }
 }
 
+// ---------------------------------------------------------------- exact synthesis at points
+// Direct FP64 spin-s synthesis at arbitrary (theta, phi): one block per
+// point, threads over m, the recursion in l run at theta (and at pi - theta
+// for the negative-m functions, spin > 0), block reduction of the phased
+// sums.  O(lmax^2) per point: the on-device spot check of the remapping
+// (the reference's gclm2lenpixs, CPU_nufft_transformer.py:531-558, which
+// synthesises on one 2-pixel ring per point).  Conventions as the transforms:
+// spin 0 real, spin s Q + iU = -sum (G + iC) sY_lm, optional exp(i s gamma).
+constexpr int SP_PTS_TPB = 128;
+
+__global__ void __launch_bounds__(SP_PTS_TPB)
+    k_synth_points(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
+                   const double *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
+                   const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
+                   double *__restrict__ out) {
+    __shared__ double2 red[SP_PTS_TPB];
+    const long long j = blockIdx.x;
+    double th, ph;
+    if (layout == 0) {
+        th = loc[2 * j];
+        ph = loc[2 * j + 1];
+    } else {
+        th = loc[j];
+        ph = loc[npts + j];
+    }
+    double st, ct, sh, ch;
+    sincos(th, &st, &ct);
+    sincos(0.5 * th, &sh, &ch);
+    const double *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+    double zr = 0.0, zi = 0.0;
+    for (int m = threadIdx.x; m <= L; m += blockDim.x) {
+        const int l0 = max(m, spin);
+        const long long b = almidx(L, m, m) - m;
+        double cN, pN, cS = 0.0, pS = 0.0;
+        int eN, eS = 0;
+        rec_start(lg0[m], m, spin, sh, ch, cN, pN, eN);
+        if (spin) rec_start(lg0[m], m, spin, ch, sh, cS, pS, eS);
+        double2 hp = make_double2(0, 0), hm = hp;
+        for (int l = l0; l <= L; ++l) {
+            const double2 g = G[b + l];
+            if (spin == 0) {
+                if (eN == 0) {
+                    hp.x = fma(g.x, cN, hp.x);
+                    hp.y = fma(g.y, cN, hp.y);
+                }
+            } else {
+                const double2 c = C ? C[b + l] : make_double2(0.0, 0.0);
+                if (eN == 0) {  // (G + iC) lambda(theta)
+                    hp.x = fma(g.x - c.y, cN, hp.x);
+                    hp.y = fma(g.y + c.x, cN, hp.y);
+                }
+                if (eS == 0) {  // (conj G + i conj C) (-1)^{l+m} lambda(pi - theta)
+                    const double par = ((l + m) & 1) ? -cS : cS;
+                    hm.x = fma(g.x + c.y, par, hm.x);
+                    hm.y = fma(c.x - g.y, par, hm.y);
+                }
+            }
+            if (l < L) {
+                const double a_ = al[b + l], g_ = ga[b + l], b_ = be[b + l];
+                const double nN = fma(fma(a_, ct, g_), cN, -b_ * pN);
+                pN = cN;
+                cN = nN;
+                REC_RESCALE(cN, pN, eN);
+                if (spin) {
+                    const double nS = fma(fma(a_, -ct, g_), cS, -b_ * pS);
+                    pS = cS;
+                    cS = nS;
+                    REC_RESCALE(cS, pS, eS);
+                }
+            }
+        }
+        double sn, cs;
+        sincos((double)m * ph, &sn, &cs);
+        if (spin == 0) {
+            zr += (m == 0) ? hp.x : 2.0 * (hp.x * cs - hp.y * sn);
+        } else {
+            // -hp e^{i m phi} - (-1)^s hm e^{-i m phi} (m > 0)
+            zr -= hp.x * cs - hp.y * sn;
+            zi -= hp.x * sn + hp.y * cs;
+            if (m > 0) {
+                const double sg = (spin & 1) ? -1.0 : 1.0;
+                zr -= sg * (hm.x * cs + hm.y * sn);
+                zi -= sg * (hm.y * cs - hm.x * sn);
+            }
+        }
+    }
+    red[threadIdx.x] = make_double2(zr, zi);
+    __syncthreads();
+    for (int o = SP_PTS_TPB / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            red[threadIdx.x].x += red[threadIdx.x + o].x;
+            red[threadIdx.x].y += red[threadIdx.x + o].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double vr = red[0].x, vi = red[0].y;
+        if (spin == 0) {
+            out[j] = vr;
+        } else {
+            if (gamma) {
+                double s, c;
+                sincos(spin * gamma[j], &s, &c);
+                const double t = vr * c - vi * s;
+                vi = vr * s + vi * c;
+                vr = t;
+            }
+            out[j] = vr;
+            out[npts + j] = vi;
+        }
+    }
+}
+
+int synth_points(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C, long long npts,
+                 const double *loc, int layout, const double *gamma, double *out, cudaStream_t st) {
+    if (npts == 0) return CUNUSHT_OK;
+    k_synth_points<<<(unsigned)npts, SP_PTS_TPB, 0, st>>>(P->lmax, spin, G, C, P->d_coef[spin], P->nalm,
+                                                         P->d_lg0[spin], loc, npts, layout, gamma, out);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
 // ---------------------------------------------------------------- host launchers
 struct RingPairs {
     int npairs;
@@ -968,10 +1090,15 @@ static void launch_synth_df(const cunusht_plan_s *P, const RingPairs &R, dim3 gr
 // shared recursion, the FP64 kernels one request per launch.
 int leg_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
                     long long astride, bool use_lfac, bool cc, double2 *H, long long hstride, cudaStream_t st) {
+    return leg_synth_batch_fl(P, nreq, spin, G, C, astride, use_lfac ? P->d_lfac : nullptr, cc, H, hstride, st);
+}
+
+// as leg_synth_batch with the alm multiplied by an arbitrary per-l factor fl (NULL: 1)
+int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
+                       long long astride, const double *lf, bool cc, double2 *H, long long hstride, cudaStream_t st) {
     const RingPairs R = pairs_of(P, cc);
     const int L = P->lmax;
     dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
-    const double *lf = use_lfac ? P->d_lfac : nullptr;
     if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
         for (int r0 = 0; r0 < nreq;) {
             const int left = nreq - r0;

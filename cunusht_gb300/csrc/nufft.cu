@@ -903,6 +903,48 @@ int pointing_launch(int nring, const double *rth, const double *rph0, const long
     return CUNUSHT_OK;
 }
 
+// ------------------------------------------------------------ magnification matrix
+// Determinant of the magnification matrix from the convergence kappa, shear
+// (g1, g2), rotation w and deflection (d1, d2) maps (helper_GPU.py:145-161):
+//   A = f0 ((1 - k)^2 - g1^2 - g2^2 + w^2)
+//     + f1 (1 - k - ((d1^2 - d2^2) g1 + 2 d1 d2 g2) / d^2),
+// f0 = sin d / d, f1 = cos d - f0.  Inputs are the unscaled syntheses:
+// k = kp / 2, (g1, g2) = -(g1p, g2p) / 2, w = wp / 2 (wp may be NULL).  For
+// small d the series of f0 and f1 replace the cancelling differences; at
+// d = 0 the f1 term is 0 (the reference divides 0 by 0 there).
+__global__ void k_magnification(long long npix, const double *__restrict__ kp, const double *__restrict__ g1p,
+                                const double *__restrict__ g2p, const double *__restrict__ d1,
+                                const double *__restrict__ d2, const double *__restrict__ wp,
+                                double *__restrict__ A) {
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= npix) return;
+    const double k = 0.5 * kp[j], g1 = -0.5 * g1p[j], g2 = -0.5 * g2p[j], w = wp ? 0.5 * wp[j] : 0.0;
+    const double a = d1[j], b = d2[j];
+    const double dd = a * a + b * b;
+    double f0, f1;
+    if (dd > 1e-4) {
+        const double d = sqrt(dd);
+        double sn, cs;
+        sincos(d, &sn, &cs);
+        f0 = sn / d;
+        f1 = cs - f0;
+    } else {
+        f0 = 1.0 - dd / 6.0 * (1.0 - dd / 20.0 * (1.0 - dd / 42.0 * (1.0 - dd / 72.0)));
+        f1 = -dd / 3.0 * (1.0 - dd / 10.0 * (1.0 - dd / 28.0 * (1.0 - dd / 54.0)));
+    }
+    double r = f0 * ((1.0 - k) * (1.0 - k) - g1 * g1 - g2 * g2 + w * w);
+    if (dd > 0.0) r += f1 * (1.0 - k - ((a * a - b * b) * g1 + 2.0 * a * b * g2) / dd);
+    A[j] = r;
+}
+
+int magnification_det(long long npix, const double *k, const double *g1, const double *g2, const double *d1,
+                      const double *d2, const double *w, double *A, cudaStream_t st) {
+    if (npix == 0) return CUNUSHT_OK;
+    k_magnification<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(npix, k, g1, g2, d1, d2, w, A);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
 // ------------------------------------------------------------ doubling
 template <typename T>
 __global__ void k_doubling(const T *__restrict__ in, long long nt, long long np, int layout, T sg,

@@ -447,6 +447,49 @@ class GPU_cufinufft_transformer:
             return self.ret
         return res
 
+    def dlm2A(self, dlm, dclm=None) -> torch.Tensor:
+        """Determinant of the magnification matrix on the pointing geometry
+        from the gradient deflection alm dlm = sqrt(l(l+1)) phi_lm (and the
+        curl dclm), helper_GPU.py:113-161; (npix,) float64."""
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        d, _, ddt = self._alm_in(dlm, "dlm", 0)
+        c = to_device(dclm, "dclm", d.dtype).reshape(-1) if dclm is not None else None
+        A = torch.empty((self.npix(),), dtype=torch.float64, device="cuda")
+        _lib.check(self._lib.cunusht_dlm2A(self._plan, d.data_ptr(), c.data_ptr() if c is not None else None, ddt,
+                                           A.data_ptr(), _stream()))
+        return A
+
+    def gclm2lenpixs(self, gclm, mmax, spin, pixs, polrot=True, ptg=None):
+        """The remapped field at the pixels ``pixs`` by exact direct summation
+        at their deflected positions (CPU_nufft_transformer.py:531-558):
+        spin 0 -> (npixs,), spin s -> (Q, U).  Uses ``ptg`` or the pointing of
+        the last lensing call on this transformer."""
+        assert spin >= 0, spin
+        if mmax is not None:
+            self._check_lm(self.lmax, mmax)
+        if ptg is None:
+            assert self.ptg is not None, "no pointing yet: call dlm2pointing / gclm2lenmap first or pass ptg"
+            ptg = self.ptg
+        ptg = to_device(ptg, "ptg", torch.float64)
+        if ptg.shape[0] != 2:
+            ptg = ptg.t().contiguous()
+        pix = torch.as_tensor(np.asarray(pixs), device="cuda", dtype=torch.long).reshape(-1)
+        loc = ptg[:, pix].contiguous()                          # (2, n) planar
+        a, ncomp, adt = self._alm_in(gclm, "gclm", spin)
+        n = pix.numel()
+        out = torch.empty((2, n) if spin else (n,), dtype=torch.float64, device="cuda")
+        g = None
+        if spin and polrot:
+            assert self.gamma is not None, "no rotation angle yet: call dlm2pointing / gclm2lenmap first"
+            g = self.gamma[pix].contiguous()
+        _lib.check(self._lib.cunusht_synth_points(self._plan, spin, ncomp, a.data_ptr(), adt, loc.data_ptr(), n, 1,
+                                                  g.data_ptr() if g is not None else None, out.data_ptr(),
+                                                  _stream()))
+        if spin:
+            return out[0], out[1]
+        return out
+
     @staticmethod
     def hashdict():
         """Compatibility with delensalot (GPU_nufft_transformer.py:676-680)."""

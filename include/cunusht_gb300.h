@@ -163,6 +163,28 @@ int cunusht_dlm2pointing(cunusht_plan_t *plan, const void *dlm_scaled, const voi
                          int alm_dtype, double *ptg, double *gamma, void *stream);
 
 /*
+ * Determinant of the magnification matrix of a deflection field on the plan's
+ * pointing geometry (helper_GPU.py:113-161 dlm2A): A (npix, float64) from the
+ * gradient deflection alm dlm = sqrt(l(l+1)) phi_lm (NOT dlm_scaled) and the
+ * optional curl dclm (may be NULL), via spin-0 convergence, spin-2 shear,
+ * spin-1 deflection (and spin-0 rotation) syntheses.  Used to weight lensed
+ * maps for inverse lensing (GPU_nufft_transformer.py:586).
+ */
+int cunusht_dlm2A(cunusht_plan_t *plan, const void *dlm, const void *dclm, int alm_dtype, double *A,
+                  void *stream);
+
+/*
+ * Exact spin-s synthesis at arbitrary points by direct FP64 summation,
+ * O(lmax^2) per point (one block per point): the remapped field at selected
+ * pixels, gclm2lenpixs (CPU_nufft_transformer.py:531-558), as an on-device
+ * spot check of nusht2d2.  alm (ncomp, nalm); loc as cunusht_nusht2d2; out
+ * (npts) spin 0 or (2, npts) Q, U with the optional exp(i spin gamma) rotation.
+ */
+int cunusht_synth_points(cunusht_plan_t *plan, int spin, int ncomp, const void *alm, int alm_dtype,
+                         const double *loc, int64_t npts, int loc_layout, const double *gamma, double *out,
+                         void *stream);
+
+/*
  * Vector-Jacobian product of the spin-0 lensing map with respect to the
  * scaled lensing potential: for lenmap = gclm2lenmap(gclm, dlm_scaled) and a
  * map gradient g = dL/dlenmap (npix float64), returns grad_dlm (complex128,
