@@ -34,6 +34,7 @@ SIGNATURES = {
     "cunusht_plan_set_profiling": (_i, [_vp, _i]),
     "cunusht_plan_force_split": (_i, [_vp, _i]),
     "cunusht_dlm2A": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
+    "cunusht_delensing_batch": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cunusht_synth_points": (_i, [_vp, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp]),
     "cunusht_plan_stage_times": (_i, [_vp, _vp, _vp, _i]),
     "cunusht_plan_reserve_batch": (_i, [_vp, _i]),

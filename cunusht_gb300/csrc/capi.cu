@@ -540,7 +540,7 @@ int cunusht_plan_stage_times(cunusht_plan_t *P, double *ms, int64_t *count, int 
 }
 
 static size_t f_elem(const cunusht_plan_s *P) { return P->grid_fp32 ? sizeof(float2) : 16; }
-static size_t u_scalar(const cunusht_plan_s *P) { return (P->grid_fp32 || P->fwd_u32) ? sizeof(float) : sizeof(double); }
+static size_t adj_scalar(const cunusht_plan_s *P) { return P->grid_fp32 ? sizeof(float) : sizeof(double); }
 
 int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     clear_error();
@@ -562,7 +562,9 @@ int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     char *f = nullptr, *u = nullptr;
     RC_TRY(dalloc(P, &P->d_Hb, B * ncols * P->ncc));
     RC_TRY(dalloc(P, &f, B * f_elem(P) * ncols * P->nrows));
-    RC_TRY(dalloc(P, &u, B * u_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf));
+    // sized for the adjoint (FP64 grid unless eps > 1e-6); the forward's FP32
+    // grid uses the first half of each request's slot
+    RC_TRY(dalloc(P, &u, B * adj_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf));
     P->d_Fb = f;
     P->d_Ub = u;
     RC_TRY(dalloc(P, &P->d_Hglb, B * (2 * (size_t)L + 1) * P->nring));
@@ -626,6 +628,64 @@ int cunusht_lensing_batch(cunusht_plan_t *P, int nreq, int spin, int ncomp, cons
         StageScope sc(P, CUNUSHT_STAGE_INTERP, st);
         RC_TRY(nufft_interp_batch(P, nreq, spin, P->d_Ub, (spin ? 2 : 1) * us, ptg_b, 2 * npix, npix, 1, gam_b, out,
                                   (spin ? 2 : 1) * npix, out_dtype, st));
+    }
+    return CUNUSHT_OK;
+}
+
+int cunusht_delensing_batch(cunusht_plan_t *P, int nreq, int spin, int ncomp, const void *lenmap, int map_dtype,
+                            const void *dlm_scaled, const void *dclm_scaled, double *ptg, double *gamma,
+                            void *alm_out, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    RC_TRY(check_spin(P, spin, ncomp));
+    ARG_CHECK(nreq >= 1, "nreq must be >= 1");
+    ARG_CHECK(nreq <= P->batch_cap, "nreq %d exceeds the reserved batch capacity %d (cunusht_plan_reserve_batch)",
+              nreq, P->batch_cap);
+    ARG_CHECK(lenmap && dlm_scaled && alm_out, "NULL array argument");
+    ARG_CHECK(map_dtype == CUNUSHT_F64 || map_dtype == CUNUSHT_F32, "bad map dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int L = P->lmax;
+    const long long npix = P->npix, nalm = P->nalm;
+    const long long ncols = spin ? 2LL * L + 1 : (long long)L + 1;
+    const long long hgl_s = (2LL * L + 1) * P->nring;
+    double *ptg_b = ptg ? ptg : P->d_ptgb;
+    double *gam_b = gamma ? gamma : (spin ? P->d_gamb : nullptr);
+    // pointing of every request (shared recursion on the mixed path)
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_LEG, st);
+        RC_TRY(leg_synth_batch(P, nreq, 1, (const double2 *)dlm_scaled, (const double2 *)dclm_scaled, nalm, true,
+                               false, P->d_Hglb, hgl_s, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_RING, st);
+        RC_TRY(ring_synth_batch(P, nreq, 1, P->d_Hglb, hgl_s, P->d_glmapb, P->d_glmapb + npix, 2 * npix, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PTG_ROT, st);
+        RC_TRY(pointing_batch(P, nreq, P->d_glmapb, 2 * npix, ptg_b, 2 * npix, gam_b, st));
+    }
+    // adjoint nuFFT and adjoint SHT at the deflected points
+    const long long us = (spin ? 2LL : 1LL) * P->nrows * P->Npf;  // grid scalars per request
+    const long long fs = (long long)P->nrows * ncols;
+    {
+        StageScope sc(P, CUNUSHT_STAGE_SPREAD, st);
+        RC_TRY(nufft_spread_batch(P, nreq, spin, P->d_Ub, us, ptg_b, 2 * npix, npix, 1, gam_b, lenmap,
+                                  (spin ? 2 : 1) * npix, map_dtype, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_PHI_ADJ, st);
+        RC_TRY(phi_adj_batch(P, nreq, spin, P->d_Ub, us, P->d_Fb, fs, st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_THETA_ADJ, st);
+        RC_TRY(theta_adj_batch(P, nreq, spin, P->d_Fb, fs, P->d_Hb, ncols * P->ncc, P->d_Ub,
+                               us * (long long)adj_scalar(P), st));
+    }
+    {
+        StageScope sc(P, CUNUSHT_STAGE_LEG_ADJ, st);
+        double2 *G = (double2 *)alm_out;
+        RC_TRY(leg_adjoint_batch(P, nreq, spin, ncomp, P->d_Hb, ncols * P->ncc, false, true, G, G + nalm,
+                                 ncomp * nalm, st));
     }
     return CUNUSHT_OK;
 }

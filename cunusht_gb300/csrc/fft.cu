@@ -275,9 +275,13 @@ __global__ void __launch_bounds__(FFT_TPB)
     k_theta_adj(const cplx<T> *__restrict__ F, int ncols, int n_lo, int nrows, int Nt, int Ntf,
                 int spin, int mofs, int L, const double *__restrict__ Dth,
                 const double *__restrict__ Dph, double2 *__restrict__ H, int ldH,
-                const cplx<T> *__restrict__ tw, int TW, int SP, int q, cplx<T> *__restrict__ S) {
+                const cplx<T> *__restrict__ tw, int TW, int SP, int q, cplx<T> *__restrict__ S, long long fbs,
+                long long hbs, long long sbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    F += blockIdx.y * fbs;  // request of a batch
+    H += blockIdx.y * hbs;
+    S += blockIdx.y * sbs;
     const int c = blockIdx.x;
     const int m = c - mofs;
     const T sgn = cvt<T>(((abs(m) + spin) & 1) ? -1.0 : 1.0);
@@ -373,9 +377,11 @@ __global__ void __launch_bounds__(FFT_TPB)
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_adj_s0(const T *__restrict__ U, int nrows, int Npf, cplx<T> *__restrict__ F, int ncols,
-                 const cplx<T> *__restrict__ tw, int TW, int SP, int q) {
+                 const cplx<T> *__restrict__ tw, int TW, int SP, int q, long long ubs, long long fbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    U += blockIdx.y * ubs;
+    F += blockIdx.y * fbs;
     const int r1 = 2 * blockIdx.x, r2 = r1 + 1;
     const bool has2 = r2 < nrows;
     const T *u1 = U + (long long)r1 * Npf;
@@ -436,9 +442,11 @@ __global__ void __launch_bounds__(FFT_TPB)
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_adj_spin(const cplx<T> *__restrict__ U, int L, int Npf, cplx<T> *__restrict__ F,
-                   const cplx<T> *__restrict__ tw, int TW, int SP, int q) {
+                   const cplx<T> *__restrict__ tw, int TW, int SP, int q, long long ubs, long long fbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    U += blockIdx.y * ubs;
+    F += blockIdx.y * fbs;
     const int r = blockIdx.x;
     const int ncols = 2 * L + 1;
     const int Nb = Npf / SP;
@@ -662,29 +670,38 @@ int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cuda
     return theta_fwd_batch(P, 1, spin, H, 0, F, 0, st);
 }
 
-int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cudaStream_t st) {
+// nreq requests: F + r fbs, H + r hbs (elements); the split transform's
+// scratch is the request's fine-grid workspace U + r ubs (consumed by the phi
+// pass adjoint before this pass runs)
+int theta_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, double2 *H,
+                    long long hbs, void *U, long long ubs_bytes, cudaStream_t st) {
     const int L = P->lmax;
     const int ncols = spin ? 2 * L + 1 : L + 1;
     const int mofs = spin ? L : 0;
     const int SP = P->sp_theta;
     size_t sm = fft_smem_bytes(P->Ntf / SP, P->grid_fp32);
-    // the odd-row spectra of the split transform go through the fine-grid
-    // workspace U, which the phi pass has consumed by now
+    dim3 grid(ncols, nreq);
     for (int q = SP - 1; q >= 0; --q) {
         if (P->grid_fp32) {
             RC_TRY(set_smem(k_theta_adj<float>, sm));
-            k_theta_adj<float><<<ncols, FFT_TPB, sm, st>>>((const float2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
-                                                           spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32,
-                                                           P->TW, SP, q, (float2 *)P->d_U);
+            k_theta_adj<float><<<grid, FFT_TPB, sm, st>>>((const float2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
+                                                          spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32,
+                                                          P->TW, SP, q, (float2 *)U, fbs, hbs,
+                                                          ubs_bytes / (long long)sizeof(float2));
         } else {
             RC_TRY(set_smem(k_theta_adj<double>, sm));
-            k_theta_adj<double><<<ncols, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt,
-                                                            P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc,
-                                                            P->d_tw64, P->TW, SP, q, (double2 *)P->d_U);
+            k_theta_adj<double><<<grid, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt,
+                                                           P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc,
+                                                           P->d_tw64, P->TW, SP, q, (double2 *)U, fbs, hbs,
+                                                           ubs_bytes / (long long)sizeof(double2));
         }
         CU_LAUNCH_CHECK();
     }
     return CUNUSHT_OK;
+}
+
+int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cudaStream_t st) {
+    return theta_adj_batch(P, 1, spin, F, 0, H, 0, P->d_U, 0, st);
 }
 
 int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, void *U, long long ubs,
@@ -738,36 +755,43 @@ int phi_fwd(const cunusht_plan_s *P, int spin, const void *F, void *U, cudaStrea
     return phi_fwd_batch(P, 1, spin, F, 0, U, 0, st);
 }
 
-int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStream_t st) {
+// nreq requests: U + r ubs (scalars), F + r fbs (complex elements)
+int phi_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, long long ubs, void *F, long long fbs,
+                  cudaStream_t st) {
     const int L = P->lmax;
     size_t sm = fft_smem_bytes(P->Npf / P->sp_phi, P->grid_fp32);
     const int SP = P->sp_phi;
     for (int q = SP - 1; q >= 0; --q) {
         if (spin == 0) {
-            const int nb = (P->nrows + 1) / 2;
+            const dim3 grid((P->nrows + 1) / 2, nreq);
             if (P->grid_fp32) {
                 RC_TRY(set_smem(k_phi_adj_s0<float>, sm));
-                k_phi_adj_s0<float><<<nb, FFT_TPB, sm, st>>>((const float *)U, P->nrows, P->Npf, (float2 *)F, L + 1,
-                                                             P->d_tw32, P->TW, SP, q);
+                k_phi_adj_s0<float><<<grid, FFT_TPB, sm, st>>>((const float *)U, P->nrows, P->Npf, (float2 *)F, L + 1,
+                                                               P->d_tw32, P->TW, SP, q, ubs, fbs);
             } else {
                 RC_TRY(set_smem(k_phi_adj_s0<double>, sm));
-                k_phi_adj_s0<double><<<nb, FFT_TPB, sm, st>>>((const double *)U, P->nrows, P->Npf, (double2 *)F, L + 1,
-                                                              P->d_tw64, P->TW, SP, q);
+                k_phi_adj_s0<double><<<grid, FFT_TPB, sm, st>>>((const double *)U, P->nrows, P->Npf, (double2 *)F,
+                                                                L + 1, P->d_tw64, P->TW, SP, q, ubs, fbs);
             }
         } else {
+            const dim3 grid(P->nrows, nreq);
             if (P->grid_fp32) {
                 RC_TRY(set_smem(k_phi_adj_spin<float>, sm));
-                k_phi_adj_spin<float><<<P->nrows, FFT_TPB, sm, st>>>((const float2 *)U, L, P->Npf, (float2 *)F,
-                                                                     P->d_tw32, P->TW, SP, q);
+                k_phi_adj_spin<float><<<grid, FFT_TPB, sm, st>>>((const float2 *)U, L, P->Npf, (float2 *)F,
+                                                                 P->d_tw32, P->TW, SP, q, ubs / 2, fbs);
             } else {
                 RC_TRY(set_smem(k_phi_adj_spin<double>, sm));
-                k_phi_adj_spin<double><<<P->nrows, FFT_TPB, sm, st>>>((const double2 *)U, L, P->Npf, (double2 *)F,
-                                                                      P->d_tw64, P->TW, SP, q);
+                k_phi_adj_spin<double><<<grid, FFT_TPB, sm, st>>>((const double2 *)U, L, P->Npf, (double2 *)F,
+                                                                  P->d_tw64, P->TW, SP, q, ubs / 2, fbs);
             }
         }
         CU_LAUNCH_CHECK();
     }
     return CUNUSHT_OK;
+}
+
+int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStream_t st) {
+    return phi_adj_batch(P, 1, spin, U, 0, F, 0, st);
 }
 
 int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,

@@ -20,12 +20,18 @@ int synth_points(const cunusht_plan_s *P, int spin, const double2 *G, const doub
                  const double *loc, int layout, const double *gamma, double *out, cudaStream_t st);
 int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
                 bool cc, double2 *G, double2 *C, cudaStream_t st);
+int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                      bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st);
 
 // fft.cu
 int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cudaStream_t st);
 int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cudaStream_t st);
 int phi_fwd(const cunusht_plan_s *P, int spin, const void *F, void *U, cudaStream_t st);
 int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStream_t st);
+int phi_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, long long ubs, void *F, long long fbs,
+                  cudaStream_t st);
+int theta_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, double2 *H,
+                    long long hbs, void *U, long long ubs_bytes, cudaStream_t st);
 int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *out0, double *out1,
                cudaStream_t st);
 int theta_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *H, long long hbs, void *F,
@@ -50,6 +56,9 @@ int magnification_det(long long npix, const double *k, const double *g1, const d
                       const double *d2, const double *w, double *A, cudaStream_t st);
 int pointing_batch(const cunusht_plan_s *P, int nreq, const double *d, long long dbs, double *ptg, long long pbs,
                    double *gamma, cudaStream_t st);
+int nufft_spread_batch(const cunusht_plan_s *P, int nreq, int spin, void *U, long long ubs, const double *loc,
+                       long long lbs, long long npts, int layout, const double *gamma, const void *in, long long ibs,
+                       int in_dtype, cudaStream_t st);
 int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts,
                  int layout, const double *gamma, const void *in, int in_dtype,
                  cudaStream_t st);

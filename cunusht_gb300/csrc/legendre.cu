@@ -758,35 +758,46 @@ __device__ __forceinline__ split2 split_c(double2 v) {
     return r;
 }
 
+// NB requests share the recursion: request r reads its columns at
+// H + r * hstride and accumulates into its alm at alm + 2 r astride.
+template <int NB>
 __global__ void __launch_bounds__(LEG_TPB)
-    k_leg_adj_s0_df(int L, const double2 *__restrict__ H, int ldH, const double *__restrict__ lfac,
-                    const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
-                    int npairs, const double *__restrict__ px, const double *__restrict__ psh,
-                    const double *__restrict__ pch, const int *__restrict__ prn,
-                    const int *__restrict__ prs, double *__restrict__ alm /* interleaved */) {
+    k_leg_adj_s0_df(int L, const double2 *__restrict__ H, long long hstride, int ldH,
+                    const double *__restrict__ lfac, const float2 *__restrict__ coef, long long nalm,
+                    const double *__restrict__ lg0, int npairs, const double *__restrict__ px,
+                    const double *__restrict__ psh, const double *__restrict__ pch, const int *__restrict__ prn,
+                    const int *__restrict__ prs, double *__restrict__ alm /* interleaved */, long long astride) {
     constexpr int NW = LEG_TPB / 32;
-    __shared__ dfl red[NW][16];
+    __shared__ dfl red[NB][NW][16];
     const int m = blockIdx.y;
     const int p = blockIdx.x * LEG_TPB + threadIdx.x;
     const bool act = p < npairs;
     double x = 0.0, sh = 0.0, ch = 1.0;
-    double2 Ep = make_double2(0, 0), Op = Ep;
+    split2 E[NB], O[NB];
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+        double2 Ep = make_double2(0, 0), Op = Ep;
+        if (act) {
+            const double2 *Hr = H + r * hstride;
+            const int n = prn[p], s = prs[p];
+            const double2 hn = Hr[(long long)m * ldH + n];
+            if (s != n) {
+                const double2 hs = Hr[(long long)m * ldH + s];
+                Ep = make_double2(hn.x + hs.x, hn.y + hs.y);
+                Op = make_double2(hn.x - hs.x, hn.y - hs.y);
+            } else {
+                Ep = hn;
+                Op = hn;
+            }
+        }
+        E[r] = split_c(Ep);
+        O[r] = split_c(Op);
+    }
     if (act) {
         x = px[p];
         sh = psh[p];
         ch = pch[p];
-        const int n = prn[p], s = prs[p];
-        const double2 hn = H[(long long)m * ldH + n];
-        if (s != n) {
-            const double2 hs = H[(long long)m * ldH + s];
-            Ep = make_double2(hn.x + hs.x, hn.y + hs.y);
-            Op = make_double2(hn.x - hs.x, hn.y - hs.y);
-        } else {
-            Ep = hn;
-            Op = hn;
-        }
     }
-    const split2 E = split_c(Ep), O = split_c(Op);
     const dfl xd = df_from(x);
     dfl cur, prev;
     int e;
@@ -800,14 +811,11 @@ __global__ void __launch_bounds__(LEG_TPB)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const dfl zero{0.f, 0.f};
     for (int lb = m; lb <= L; lb += 8) {
-        dfl v[16];
+        dfl lam[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int l = lb + i;
-            const dfl lam = (e == 0 && l <= L) ? cur : zero;
-            const split2 &src = ((l + m) & 1) ? O : E;
-            v[2 * i] = df_prod_split(lam, src.xh, src.xl);
-            v[2 * i + 1] = df_prod_split(lam, src.yh, src.yl);
+            lam[i] = (e == 0 && l <= L) ? cur : zero;
             if (l < L) {
                 const float2 a2 = __ldg(al + b + l), b2 = __ldg(be + b + l);
                 const dfl t = df_mul(dfl{a2.x, a2.y}, xd);
@@ -817,53 +825,75 @@ __global__ void __launch_bounds__(LEG_TPB)
                 REC_RESCALE_DF(cur, prev, e);
             }
         }
-        warp_reduce_scatter16_df(v);
-        if (!(lane & 1)) red[wid][rs16_index(lane)] = v[0];
-        __syncthreads();
-        if (threadIdx.x < 16) {
-            dfl t = red[0][threadIdx.x];
 #pragma unroll
-            for (int w = 1; w < NW; ++w) t = df_add(t, red[w][threadIdx.x]);
-            const int l = lb + (threadIdx.x >> 1);
+        for (int r = 0; r < NB; ++r) {
+            dfl v[16];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const split2 &src = ((lb + i + m) & 1) ? O[r] : E[r];
+                v[2 * i] = df_prod_split(lam[i], src.xh, src.xl);
+                v[2 * i + 1] = df_prod_split(lam[i], src.yh, src.yl);
+            }
+            warp_reduce_scatter16_df(v);
+            if (!(lane & 1)) red[r][wid][rs16_index(lane)] = v[0];
+        }
+        __syncthreads();
+        if (threadIdx.x < 16 * NB) {
+            const int r = threadIdx.x >> 4, q = threadIdx.x & 15;
+            dfl t = red[r][0][q];
+#pragma unroll
+            for (int w2 = 1; w2 < NW; ++w2) t = df_add(t, red[r][w2][q]);
+            const int l = lb + (q >> 1);
             if (l <= L) {
                 const double f = lfac ? lfac[l] : 1.0;
-                atomicAdd(alm + 2 * (b + l) + (threadIdx.x & 1), df_to(t) * f);
+                atomicAdd(alm + 2 * (r * astride + b + l) + (q & 1), df_to(t) * f);
             }
         }
         __syncthreads();
     }
 }
 
+template <int NB>
 __global__ void __launch_bounds__(LEG_TPB)
-    k_leg_adj_spin_df(int L, int spin, int ncomp, const double2 *__restrict__ H, int ldH,
+    k_leg_adj_spin_df(int L, int spin, int ncomp, const double2 *__restrict__ H, long long hstride, int ldH,
                       const double *__restrict__ lfac, const float2 *__restrict__ coef,
                       long long nalm, const double *__restrict__ lg0, int npairs,
                       const double *__restrict__ px, const double *__restrict__ psh,
                       const double *__restrict__ pch, const int *__restrict__ prn,
                       const int *__restrict__ prs, double *__restrict__ Gout,
-                      double *__restrict__ Cout) {
+                      double *__restrict__ Cout, long long astride) {
     constexpr int NW = LEG_TPB / 32;
-    __shared__ dfl red[NW][16];
-    __shared__ double tot[16];
+    __shared__ dfl red[NB][NW][16];
+    __shared__ double tot[NB][16];
     const int m = blockIdx.y;
     const int l0 = max(m, spin);
     const int p = blockIdx.x * LEG_TPB + threadIdx.x;
     const bool act = p < npairs;
     double x = 0.0, sh = 0.0, ch = 1.0;
-    double2 hpn = make_double2(0, 0), hps = hpn, hmn = hpn, hms = hpn;
+    split2 PN[NB], PS[NB], MN[NB], MS[NB];
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+        double2 hpn = make_double2(0, 0), hps = hpn, hmn = hpn, hms = hpn;
+        if (act) {
+            const double2 *Hr = H + r * hstride;
+            const int n = prn[p], s = prs[p];
+            hpn = Hr[(long long)(L + m) * ldH + n];
+            hmn = Hr[(long long)(L - m) * ldH + n];
+            if (s != n) {
+                hps = Hr[(long long)(L + m) * ldH + s];
+                hms = Hr[(long long)(L - m) * ldH + s];
+            }
+        }
+        PN[r] = split_c(hpn);
+        PS[r] = split_c(hps);
+        MN[r] = split_c(hmn);
+        MS[r] = split_c(hms);
+    }
     if (act) {
         x = px[p];
         sh = psh[p];
         ch = pch[p];
-        const int n = prn[p], s = prs[p];
-        hpn = H[(long long)(L + m) * ldH + n];
-        hmn = H[(long long)(L - m) * ldH + n];
-        if (s != n) {
-            hps = H[(long long)(L + m) * ldH + s];
-            hms = H[(long long)(L - m) * ldH + s];
-        }
     }
-    const split2 PN = split_c(hpn), PS = split_c(hps), MN = split_c(hmn), MS = split_c(hms);
     const dfl xN = df_from(x), xS = df_from(-x);
     dfl cN, pN, cS, pS;
     int eN, eS;
@@ -879,20 +909,12 @@ __global__ void __launch_bounds__(LEG_TPB)
     const double sgs = (spin & 1) ? -1.0 : 1.0;
     const dfl zero{0.f, 0.f};
     for (int lb = l0; lb <= L; lb += 4) {
-        dfl v[16];
+        dfl lN[4], lS[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             const int l = lb + i;
-            const dfl lN = (eN == 0 && l <= L) ? cN : zero;
-            const dfl lS = (eS == 0 && l <= L) ? cS : zero;
-            // P = lN hpn + lS hps ; Q = par (lS conj(hmn) + lN conj(hms))
-            v[4 * i + 0] = df_add(df_prod_split(lN, PN.xh, PN.xl), df_prod_split(lS, PS.xh, PS.xl));
-            v[4 * i + 1] = df_add(df_prod_split(lN, PN.yh, PN.yl), df_prod_split(lS, PS.yh, PS.yl));
-            const dfl qr = df_add(df_prod_split(lS, MN.xh, MN.xl), df_prod_split(lN, MS.xh, MS.xl));
-            const dfl qi = df_add(df_prod_split(lS, MN.yh, MN.yl), df_prod_split(lN, MS.yh, MS.yl));
-            const bool odd = (l + m) & 1;
-            v[4 * i + 2] = odd ? df_neg(qr) : qr;
-            v[4 * i + 3] = odd ? qi : df_neg(qi);
+            lN[i] = (eN == 0 && l <= L) ? cN : zero;
+            lS[i] = (eS == 0 && l <= L) ? cS : zero;
             if (l < L) {
                 const float2 a2 = __ldg(al + b + l), g2 = __ldg(ga + b + l), b2 = __ldg(be + b + l);
                 const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
@@ -908,27 +930,45 @@ __global__ void __launch_bounds__(LEG_TPB)
                 REC_RESCALE_DF(cS, pS, eS);
             }
         }
-        warp_reduce_scatter16_df(v);
-        if (!(lane & 1)) red[wid][rs16_index(lane)] = v[0];
-        __syncthreads();
-        if (threadIdx.x < 16) {
-            dfl t = red[0][threadIdx.x];
 #pragma unroll
-            for (int w = 1; w < NW; ++w) t = df_add(t, red[w][threadIdx.x]);
-            tot[threadIdx.x] = df_to(t);
+        for (int r = 0; r < NB; ++r) {
+            dfl v[16];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                // P = lN hpn + lS hps ; Q = par (lS conj(hmn) + lN conj(hms))
+                v[4 * i + 0] = df_add(df_prod_split(lN[i], PN[r].xh, PN[r].xl), df_prod_split(lS[i], PS[r].xh, PS[r].xl));
+                v[4 * i + 1] = df_add(df_prod_split(lN[i], PN[r].yh, PN[r].yl), df_prod_split(lS[i], PS[r].yh, PS[r].yl));
+                const dfl qr = df_add(df_prod_split(lS[i], MN[r].xh, MN[r].xl), df_prod_split(lN[i], MS[r].xh, MS[r].xl));
+                const dfl qi = df_add(df_prod_split(lS[i], MN[r].yh, MN[r].yl), df_prod_split(lN[i], MS[r].yh, MS[r].yl));
+                const bool odd = (lb + i + m) & 1;
+                v[4 * i + 2] = odd ? df_neg(qr) : qr;
+                v[4 * i + 3] = odd ? qi : df_neg(qi);
+            }
+            warp_reduce_scatter16_df(v);
+            if (!(lane & 1)) red[r][wid][rs16_index(lane)] = v[0];
         }
         __syncthreads();
-        if (threadIdx.x < 4) {
-            const int l = lb + threadIdx.x;
+        if (threadIdx.x < 16 * NB) {
+            const int r = threadIdx.x >> 4, q = threadIdx.x & 15;
+            dfl t = red[r][0][q];
+#pragma unroll
+            for (int w2 = 1; w2 < NW; ++w2) t = df_add(t, red[r][w2][q]);
+            tot[r][q] = df_to(t);
+        }
+        __syncthreads();
+        if (threadIdx.x < 4 * NB) {
+            const int r = threadIdx.x >> 2, i = threadIdx.x & 3;
+            const int l = lb + i;
             if (l <= L) {
                 const double f = lfac ? lfac[l] : 1.0;
-                const double Pr = tot[4 * threadIdx.x], Pi = tot[4 * threadIdx.x + 1];
-                const double Qr = sgs * tot[4 * threadIdx.x + 2], Qi = sgs * tot[4 * threadIdx.x + 3];
-                atomicAdd(Gout + 2 * (b + l), -0.5 * f * (Pr + Qr));
-                atomicAdd(Gout + 2 * (b + l) + 1, -0.5 * f * (Pi + Qi));
+                const double Pr = tot[r][4 * i], Pi = tot[r][4 * i + 1];
+                const double Qr = sgs * tot[r][4 * i + 2], Qi = sgs * tot[r][4 * i + 3];
+                double *Gr = Gout + 2 * r * astride, *Cr = Cout ? Cout + 2 * r * astride : nullptr;
+                atomicAdd(Gr + 2 * (b + l), -0.5 * f * (Pr + Qr));
+                atomicAdd(Gr + 2 * (b + l) + 1, -0.5 * f * (Pi + Qi));
                 if (ncomp > 1) {
-                    atomicAdd(Cout + 2 * (b + l), -0.5 * f * (Pi - Qi));
-                    atomicAdd(Cout + 2 * (b + l) + 1, 0.5 * f * (Pr - Qr));
+                    atomicAdd(Cr + 2 * (b + l), -0.5 * f * (Pi - Qi));
+                    atomicAdd(Cr + 2 * (b + l) + 1, 0.5 * f * (Pr - Qr));
                 }
             }
         }
@@ -1139,33 +1179,72 @@ int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2
     return leg_synth_batch(P, 1, spin, G, C, 0, use_lfac, cc, H, 0, st);
 }
 
-int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
-                bool cc, double2 *G, double2 *C, cudaStream_t st) {
+template <int NB>
+static void launch_adj_df(const cunusht_plan_s *P, const RingPairs &R, dim3 grid, int spin, int ncomp,
+                          const double2 *H, long long hstride, const double *lf, double2 *G, double2 *C,
+                          long long astride, cudaStream_t st) {
+    const int L = P->lmax;
+    if (spin == 0)
+        k_leg_adj_s0_df<NB><<<grid, LEG_TPB, 0, st>>>(L, H, hstride, R.ld, lf, P->d_coef_df[0], P->nalm,
+                                                      P->d_lg0[0], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
+                                                      (double *)G, astride);
+    else
+        k_leg_adj_spin_df<NB><<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, H, hstride, R.ld, lf, P->d_coef_df[spin],
+                                                        P->nalm, P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn,
+                                                        R.rs, (double *)G, (double *)C, astride);
+}
+
+// nreq requests: columns at H + r * hstride, alm written at G + r * astride
+// (and C + r * astride); the mixed-precision kernels share one recursion
+// between up to four requests, the FP64 kernels run one request per launch.
+int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                      bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st) {
     const RingPairs R = pairs_of(P, cc);
     const int L = P->lmax;
-    CU_TRY(cudaMemsetAsync(G, 0, sizeof(double2) * P->nalm, st));
-    if (spin > 0 && ncomp > 1) CU_TRY(cudaMemsetAsync(C, 0, sizeof(double2) * P->nalm, st));
+    for (int r = 0; r < nreq; ++r) {
+        CU_TRY(cudaMemsetAsync(G + r * astride, 0, sizeof(double2) * P->nalm, st));
+        if (spin > 0 && ncomp > 1) CU_TRY(cudaMemsetAsync(C + r * astride, 0, sizeof(double2) * P->nalm, st));
+    }
     dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
     const double *lf = use_lfac ? P->d_lfac : nullptr;
     if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
-        if (spin == 0)
-            k_leg_adj_s0_df<<<grid, LEG_TPB, 0, st>>>(L, H, R.ld, lf, P->d_coef_df[0], P->nalm, P->d_lg0[0],
-                                                      R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, (double *)G);
-        else
-            k_leg_adj_spin_df<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, H, R.ld, lf, P->d_coef_df[spin], P->nalm,
-                                                        P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
-                                                        (double *)G, (double *)C);
-    } else if (spin == 0) {
-        k_leg_adj_s0<<<grid, LEG_TPB, 0, st>>>(L, H, R.ld, lf, P->d_coef[0], P->nalm, P->d_lg0[0],
-                                               R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
-                                               (double *)G);
-    } else {
-        k_leg_adj_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, H, R.ld, lf, P->d_coef[spin],
-                                                 P->nalm, P->d_lg0[spin], R.npairs, R.x, R.sh,
-                                                 R.ch, R.rn, R.rs, (double *)G, (double *)C);
+        for (int r0 = 0; r0 < nreq;) {
+            const int left = nreq - r0;
+            const double2 *Hr = H + r0 * hstride;
+            double2 *Gr = G + r0 * astride, *Cr = (spin > 0 && ncomp > 1) ? C + r0 * astride : nullptr;
+            if (left >= 4) {
+                launch_adj_df<4>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+                r0 += 4;
+            } else if (left >= 2) {
+                launch_adj_df<2>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+                r0 += 2;
+            } else {
+                launch_adj_df<1>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+                r0 += 1;
+            }
+            CU_LAUNCH_CHECK();
+        }
+        return CUNUSHT_OK;
     }
-    CU_LAUNCH_CHECK();
+    for (int r = 0; r < nreq; ++r) {
+        const double2 *Hr = H + r * hstride;
+        double2 *Gr = G + r * astride, *Cr = (spin > 0 && ncomp > 1) ? C + r * astride : nullptr;
+        if (spin == 0) {
+            k_leg_adj_s0<<<grid, LEG_TPB, 0, st>>>(L, Hr, R.ld, lf, P->d_coef[0], P->nalm, P->d_lg0[0], R.npairs,
+                                                   R.x, R.sh, R.ch, R.rn, R.rs, (double *)Gr);
+        } else {
+            k_leg_adj_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, Hr, R.ld, lf, P->d_coef[spin], P->nalm,
+                                                     P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
+                                                     (double *)Gr, (double *)Cr);
+        }
+        CU_LAUNCH_CHECK();
+    }
     return CUNUSHT_OK;
+}
+
+int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
+                bool cc, double2 *G, double2 *C, cudaStream_t st) {
+    return leg_adjoint_batch(P, 1, spin, ncomp, H, 0, use_lfac, cc, G, C, 0, st);
 }
 
 }  // namespace cunusht

@@ -172,11 +172,16 @@ template <typename T, bool CPLX>
 __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp(T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
                   const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
-                  int spin, const void *__restrict__ in, int in_f32, int SR, int SC) {
+                  int spin, const void *__restrict__ in, int in_f32, int SR, int SC, long long ubs, long long lbs,
+                  long long ibs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NC = CPLX ? 2 : 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     T *strip = reinterpret_cast<T *>(smem_raw) + (size_t)wid * SR * SC * NC;
+    U += blockIdx.y * ubs;  // request of a batch
+    loc += blockIdx.y * lbs;
+    if (gamma) gamma += blockIdx.y * npts;
+    in = in_f32 ? (const void *)((const float *)in + blockIdx.y * ibs) : (const void *)((const double *)in + blockIdx.y * ibs);
     const long long j = ((long long)blockIdx.x * SPW_WARPS + wid) * 32 + lane;
     const bool act = j < npts;
     const unsigned amask = __ballot_sync(0xffffffffu, act);
@@ -266,8 +271,9 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
 }
 
 template <typename T, bool CPLX>
-static int launch_spread_warp(const cunusht_plan_s *P, T *U, const double *loc, long long npts, int layout,
-                              const double *gamma, int spin, const void *in, int f32i, cudaStream_t st) {
+static int launch_spread_warp(const cunusht_plan_s *P, int nreq, T *U, long long ubs, const double *loc, long long lbs,
+                              long long npts, int layout, const double *gamma, int spin, const void *in,
+                              long long ibs, int f32i, cudaStream_t st) {
     // strip: the footprint of 32 neighbouring ring pixels at about 2 fine
     // cells per pixel, plus row jitter from the deflection
     const int SR = P->w + 4, SC = 80 + P->w;
@@ -276,8 +282,9 @@ static int launch_spread_warp(const cunusht_plan_s *P, T *U, const double *loc, 
         CU_TRY(cudaFuncSetAttribute(k_spread_warp<T, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const long long nwarps = (npts + 31) / 32;
     const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
-    k_spread_warp<T, CPLX><<<nb, SPW_WARPS * 32, sm, st>>>(U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w, (T)P->beta,
-                                                          loc, npts, layout, gamma, spin, in, f32i, SR, SC);
+    k_spread_warp<T, CPLX><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
+                                                                      (T)P->beta, loc, npts, layout, gamma, spin, in,
+                                                                      f32i, SR, SC, ubs, lbs, ibs);
     return CUNUSHT_OK;
 }
 
@@ -290,11 +297,16 @@ template <bool CPLX>
 __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp_mixed(double *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                         const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
-                        int spin, const void *__restrict__ in, int in_f32, int SR, int SC) {
+                        int spin, const void *__restrict__ in, int in_f32, int SR, int SC, long long ubs,
+                        long long lbs, long long ibs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NC = CPLX ? 2 : 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float2 *strip = reinterpret_cast<float2 *>(smem_raw) + (size_t)wid * SR * SC * NC;  // (sum, compensation)
+    U += blockIdx.y * ubs;  // request of a batch
+    loc += blockIdx.y * lbs;
+    if (gamma) gamma += blockIdx.y * npts;
+    in = in_f32 ? (const void *)((const float *)in + blockIdx.y * ibs) : (const void *)((const double *)in + blockIdx.y * ibs);
     const long long j = ((long long)blockIdx.x * SPW_WARPS + wid) * 32 + lane;
     const bool act = j < npts;
     const unsigned amask = __ballot_sync(0xffffffffu, act);
@@ -407,17 +419,19 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
 }
 
 template <bool CPLX>
-static int launch_spread_warp_mixed(const cunusht_plan_s *P, const double *loc, long long npts, int layout,
-                                    const double *gamma, int spin, const void *in, int f32i, cudaStream_t st) {
+static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U, long long ubs, const double *loc,
+                                    long long lbs, long long npts, int layout, const double *gamma, int spin,
+                                    const void *in, long long ibs, int f32i, cudaStream_t st) {
     const int SR = P->w + 4, SC = 80 + P->w;
     const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(float2);
     if (sm > 48 * 1024)
         CU_TRY(cudaFuncSetAttribute(k_spread_warp_mixed<CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const long long nwarps = (npts + 31) / 32;
     const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
-    k_spread_warp_mixed<CPLX><<<nb, SPW_WARPS * 32, sm, st>>>((double *)P->d_U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                             P->w, (float)P->beta, loc, npts, layout, gamma, spin,
-                                                             in, f32i, SR, SC);
+    k_spread_warp_mixed<CPLX><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                                         P->w, (float)P->beta, loc, npts, layout,
+                                                                         gamma, spin, in, f32i, SR, SC, ubs, lbs,
+                                                                         ibs);
     return CUNUSHT_OK;
 }
 
@@ -560,24 +574,34 @@ int nufft_interp(const cunusht_plan_s *P, int spin, const double *loc, long long
     return nufft_interp_batch(P, 1, spin, P->d_U, 0, loc, 0, npts, layout, gamma, out, 0, out_dtype, st);
 }
 
-int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
-                 const double *gamma, const void *in, int in_dtype, cudaStream_t st) {
-    const size_t cell = (P->grid_fp32 ? 4 : 8) * (spin ? 2 : 1);
-    CU_TRY(cudaMemsetAsync(P->d_U, 0, cell * (size_t)P->nrows * P->Npf, st));
+// nreq requests: grid U + r ubs (scalars of the grid type, zeroed here),
+// points loc + r lbs, values in + r ibs (elements), gamma + r npts
+int nufft_spread_batch(const cunusht_plan_s *P, int nreq, int spin, void *U, long long ubs, const double *loc,
+                       long long lbs, long long npts, int layout, const double *gamma, const void *in, long long ibs,
+                       int in_dtype, cudaStream_t st) {
+    const size_t scal = P->grid_fp32 ? 4 : 8;
+    const size_t cell = scal * (spin ? 2 : 1);
+    for (int r = 0; r < nreq; ++r)
+        CU_TRY(cudaMemsetAsync((char *)U + r * ubs * scal, 0, cell * (size_t)P->nrows * P->Npf, st));
     if (npts == 0) return CUNUSHT_OK;
     const int f32i = in_dtype == CUNUSHT_F32;
     if (P->grid_fp32) {
-        if (spin == 0) RC_TRY((launch_spread_warp<float, false>(P, (float *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
-        else RC_TRY((launch_spread_warp<float, true>(P, (float *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
+        if (spin == 0) RC_TRY((launch_spread_warp<float, false>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+        else RC_TRY((launch_spread_warp<float, true>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
     } else if (P->prec == CUNUSHT_PREC_MIXED) {
-        if (spin == 0) RC_TRY((launch_spread_warp_mixed<false>(P, loc, npts, layout, gamma, spin, in, f32i, st)));
-        else RC_TRY((launch_spread_warp_mixed<true>(P, loc, npts, layout, gamma, spin, in, f32i, st)));
+        if (spin == 0) RC_TRY((launch_spread_warp_mixed<false>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+        else RC_TRY((launch_spread_warp_mixed<true>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
     } else {
-        if (spin == 0) RC_TRY((launch_spread_warp<double, false>(P, (double *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
-        else RC_TRY((launch_spread_warp<double, true>(P, (double *)P->d_U, loc, npts, layout, gamma, spin, in, f32i, st)));
+        if (spin == 0) RC_TRY((launch_spread_warp<double, false>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+        else RC_TRY((launch_spread_warp<double, true>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
     }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
+}
+
+int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,
+                 const double *gamma, const void *in, int in_dtype, cudaStream_t st) {
+    return nufft_spread_batch(P, 1, spin, P->d_U, 0, loc, 0, npts, layout, gamma, in, 0, in_dtype, st);
 }
 
 // ------------------------------------------------------------ pointing

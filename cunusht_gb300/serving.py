@@ -12,9 +12,9 @@ admitted as soon as a slot frees up, and launches of different slots and
 buckets overlap on the device.
 
 A launch is one CUDA-graph replay: lensing requests of a bucket go up to
-``max_batch`` per launch through cunusht_lensing_batch (one shared Legendre
-recursion per four requests on the mixed path); a delensing request runs
-dlm2pointing + nusht2d1.  The graph of each (slot, direction, batch size) is
+``max_batch`` per launch through cunusht_lensing_batch, delensing requests
+through cunusht_delensing_batch (one shared Legendre recursion per four
+requests on the mixed path, forward and adjoint).  The graph of each (slot, direction, batch size) is
 captured on first use; the request's inputs are copied into the slot's
 static buffers before the replay and its result copied out after.
 
@@ -77,10 +77,8 @@ class _Slot:
             self.gin = torch.zeros((max_batch, self.ncomp, nalm), dtype=c128, device="cuda")
             self.din = torch.zeros((max_batch, nalm), dtype=c128, device="cuda")
             self.out = torch.zeros((max_batch, 2, npix) if spin else (max_batch, npix), dtype=f64, device="cuda")
-            self.lin = torch.zeros((2, npix) if spin else (npix,), dtype=f64, device="cuda")
-            self.aout = torch.zeros((self.ncomp, nalm), dtype=c128, device="cuda")
-            self.ptg = torch.zeros((2, npix), dtype=f64, device="cuda")
-            self.gam = torch.zeros((npix,), dtype=f64, device="cuda")
+            self.lin = torch.zeros((max_batch, 2, npix) if spin else (max_batch, npix), dtype=f64, device="cuda")
+            self.aout = torch.zeros((max_batch, self.ncomp, nalm), dtype=c128, device="cuda")
         torch.cuda.synchronize()
         self.bytes = max(0, free0 - torch.cuda.mem_get_info()[0])
         self.graphs: dict[tuple, torch.cuda.CUDAGraph] = {}
@@ -91,7 +89,7 @@ class _Slot:
         if kind == "g2l":
             self.T.lensing_batch(self.gin[:n], self.din[:n], self.spin, out=self.out[:n])
         else:
-            self.T.delensing_solve(self.lin, self.din[0], self.aout, self.ptg, self.gam, self.spin)
+            self.T.delensing_batch(self.lin[:n], self.din[:n], self.spin, ncomp=self.ncomp, out=self.aout[:n])
 
     def run(self, kind, n):
         """Launch the work of n staged requests on the slot's stream (the
@@ -219,13 +217,16 @@ class LensingServer:
         with torch.cuda.stream(sl.stream):
             sl.stream.wait_stream(producer)     # request tensors were made on the caller's stream
             if q[0].kind == "l2g":
-                batch = [q.popleft()]
-                r = batch[0]
-                data, dlm = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
-                sl.lin.copy_(data.reshape(sl.lin.shape), non_blocking=True)
-                sl.din[0].copy_(dlm.reshape(-1), non_blocking=True)
-                sl.run("l2g", 1)
-                r.result = sl.aout[0].clone() if sl.spin == 0 else sl.aout.clone()
+                batch = []
+                while q and q[0].kind == "l2g" and len(batch) < sl.max_batch:
+                    batch.append(q.popleft())
+                for i, r in enumerate(batch):
+                    data, dlm = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
+                    sl.lin[i].copy_(data.reshape(sl.lin.shape[1:]), non_blocking=True)
+                    sl.din[i].copy_(dlm.reshape(-1), non_blocking=True)
+                sl.run("l2g", len(batch))
+                for i, r in enumerate(batch):
+                    r.result = sl.aout[i, 0].clone() if sl.spin == 0 else sl.aout[i].clone()
             else:
                 batch = []
                 while q and q[0].kind == "g2l" and len(batch) < sl.max_batch:

@@ -322,6 +322,29 @@ class GPU_cufinufft_transformer:
             out.data_ptr(), _lib.F32 if out.dtype == torch.float32 else _lib.F64, _stream()))
         return out
 
+    def delensing_batch(self, lenmap: torch.Tensor, dlm_scaled: torch.Tensor, spin: int, ncomp: int | None = None,
+                        out: torch.Tensor | None = None, ptg: torch.Tensor | None = None,
+                        gamma: torch.Tensor | None = None, dclm_scaled: torch.Tensor | None = None) -> torch.Tensor:
+        """nreq delensing solves (lenmap2gclm) in one batched pass (served form).
+        lenmap (nreq, 2, npix) (spin s) or (nreq, npix) (spin 0) float64,
+        dlm_scaled (nreq, nalm) complex128 -> (nreq, ncomp, nalm) complex128."""
+        m = to_device(lenmap, "lenmap")
+        if m.dtype not in (torch.float32, torch.float64):
+            m = m.to(torch.float64)
+        nreq = m.shape[0]
+        ncomp = (2 if spin else 1) if ncomp is None else ncomp
+        d = to_device(dlm_scaled, "dlm_scaled", torch.complex128).reshape(nreq, self.nalm)
+        c = to_device(dclm_scaled, "dclm_scaled", torch.complex128).reshape(nreq, self.nalm) if dclm_scaled is not None else None
+        if getattr(self, "batch_cap", 0) < nreq:
+            self.reserve_batch(nreq)
+        if out is None:
+            out = torch.empty((nreq, ncomp, self.nalm), dtype=torch.complex128, device="cuda")
+        _lib.check(self._lib.cunusht_delensing_batch(
+            self._plan, nreq, spin, ncomp, m.data_ptr(), _lib.F32 if m.dtype == torch.float32 else _lib.F64,
+            d.data_ptr(), c.data_ptr() if c is not None else None, ptg.data_ptr() if ptg is not None else None,
+            gamma.data_ptr() if gamma is not None else None, out.data_ptr(), _stream()))
+        return out
+
     def lensing_solve(self, gclm: torch.Tensor, dlm_scaled: torch.Tensor, out: torch.Tensor, ptg: torch.Tensor,
                       gamma: torch.Tensor, spin: int, dclm_scaled: torch.Tensor | None = None):
         """One uncached lensing solve on device tensors (dlm2pointing + nusht2d2

@@ -150,6 +150,22 @@ int cunusht_lensing_batch(cunusht_plan_t *plan, int nreq, int spin, int ncomp, c
                           void *out, int out_dtype, void *stream);
 
 /*
+ * Served form of the adjoint: nreq delensing solves (dlm2pointing + nusht2d1
+ * with the exp(-i spin gamma) rotation, i.e. GPU_cufinufft_transformer.
+ * lenmap2gclm, GPU_nufft_transformer.py:581-673) of one lmax / spin /
+ * accuracy in one batched pass; the mixed-precision Legendre kernels share one
+ * recursion between up to four requests.  lenmap (nreq, spin ? 2 : 1, npix)
+ * float64 / float32; dlm_scaled / dclm_scaled (nreq, nalm) complex128 (dclm
+ * may be NULL); alm_out (nreq, ncomp, nalm) complex128; ptg (nreq, 2, npix)
+ * and gamma (nreq, npix) receive the pointing when not NULL.  Needs
+ * cunusht_plan_reserve_batch(plan, >= nreq).  No reference counterpart as a
+ * batch.
+ */
+int cunusht_delensing_batch(cunusht_plan_t *plan, int nreq, int spin, int ncomp, const void *lenmap, int map_dtype,
+                            const void *dlm_scaled, const void *dclm_scaled, double *ptg, double *gamma,
+                            void *alm_out, void *stream);
+
+/*
  * dlm2pointing: deflected angles of every pixel of the plan geometry.
  * Replaces GPU_cufinufft_transformer.dlm2pointing / deflection.dlm2pointing
  * (GPU_nufft_transformer.py:64-104, :344-351: SHTns synth_grad on the GL

@@ -58,6 +58,41 @@ def test_batch_equals_single_requests(built_lib, precision, eps, spin):
         assert diff <= 1e-12 * rms, (r, diff, rms)
 
 
+@pytest.mark.parametrize("precision,eps", [("fp64", 1e-10), ("mixed", 1e-7), ("mixed", 1e-5)])
+@pytest.mark.parametrize("spin", [0, 2])
+def test_delensing_batch_equals_single_requests(built_lib, precision, eps, spin):
+    import cunusht_gb300 as cu
+    lmax = 127
+    T = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=eps, precision=precision, max_spin=2)
+    nreq = 5  # chunks of 4 + 1 requests sharing one recursion on the mixed path
+    _, d = _inputs(lmax, spin, nreq, 60)
+    npix = T.npix()
+    rng = np.random.default_rng(8)
+    maps = torch.as_tensor(rng.standard_normal((nreq, 2, npix) if spin else (nreq, npix)), device="cuda")
+    ncomp = 2 if spin else 1
+    T.reserve_batch(nreq)
+    outb = T.delensing_batch(maps, d, spin, ncomp=ncomp)
+    for r in range(nreq):
+        ptg = torch.empty((2, npix), dtype=torch.float64, device="cuda")
+        gam = torch.empty(npix, dtype=torch.float64, device="cuda")
+        a = torch.empty((ncomp, T.nalm), dtype=torch.complex128, device="cuda")
+        T.delensing_solve(maps[r], d[r], a, ptg, gam, spin)
+        rel = float(torch.linalg.norm(outb[r] - a) / torch.linalg.norm(a))
+        # the spread accumulates with floating-point atomics in an order that
+        # varies between launches: FP64 grid ~1e-16, FP32 grid (eps > 1e-6) ~1e-7
+        assert rel < (1e-10 if eps < 1e-6 else 1e-6), (r, rel)
+    # and the batch is the adjoint of the lensing batch: <y, A x> = <A^H y, x>
+    g, _ = _inputs(lmax, spin, nreq, 90)
+    if not spin:
+        g = g[:, :1]
+    Ax = T.lensing_batch(g, d, spin)
+    for r in range(nreq):
+        lhs = float(torch.sum(maps[r] * Ax[r]))
+        rhs = sum(orc.alm_dot(outb[r, c].cpu().numpy(), g[r, c].cpu().numpy(), lmax) for c in range(ncomp))
+        tol = 1e-9 if precision == "fp64" else (5e-7 if eps < 1e-6 else 1e-5)
+        assert abs(lhs - rhs) <= tol * abs(lhs), (r, lhs, rhs)
+
+
 def test_batch_spread_over_launches_and_reference_accuracy(built_lib):
     """batches of 1..5 agree with the direct-sum oracle at sampled pixels."""
     import cunusht_gb300 as cu
