@@ -60,6 +60,10 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU work of the cpu_baseline leg")
     p.add_argument("--batch", type=int, default=4, help="requests per launch of the served form")
     p.add_argument("--fp64-steps", type=int, default=3, help="timed solves of the plain FP64 single-request form")
+    p.add_argument("--op", default=None, choices=["doubling", "adjoint_doubling"],
+                   help="time one standalone kernel of the C ABI instead (HBM roofline)")
+    p.add_argument("--direction", default="g2l", choices=["g2l", "l2g"],
+                   help="g2l: lensing (headline); l2g: delensing (lenmap2gclm) served form")
     p.add_argument("--serve", action="store_true",
                    help="served mixed workload instead: Poisson arrivals of mixed lmax / spin / direction / eps")
     p.add_argument("--serve-requests", type=int, default=2000)
@@ -666,8 +670,129 @@ def serve_main(args):
     print(json.dumps(line))
 
 
+# ----------------------------------------------------------------------------- standalone kernels
+def op_main(args):
+    """HBM roofline of the standalone doubling / adjoint doubling kernels of the
+    C ABI (doubling.cu:137-220, :53-92) at the lmax 4095 CC-grid size, FP64,
+    ring-major: inputs and outputs larger than L2, CUDA events."""
+    import torch
+    from cunusht_gb300 import build as _b
+    _b.build()
+    from cunusht_gb300 import _lib
+    lib = _lib.load()
+    nt, npx = 4100, 8192
+    dt = 2 * nt - 2
+    src = torch.randn((nt if args.op == "doubling" else dt) * npx, dtype=torch.float64, device="cuda")
+    dst = torch.empty((dt if args.op == "doubling" else nt) * npx, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    if args.op == "doubling":
+        call = lambda: _lib.check(lib.cunusht_doubling(src.data_ptr(), nt, npx, 0, 2, _lib.F64, dst.data_ptr(), st))
+        nbytes = 8 * (nt * npx + dt * npx)          # every input read once (the mirror is an L2 hit) + output
+    else:
+        call = lambda: _lib.check(lib.cunusht_adjoint_doubling(src.data_ptr(), nt, npx, 2, _lib.F64,
+                                                               dst.data_ptr(), st))
+        nbytes = 8 * (dt * npx + nt * npx)
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    for k in range(args.steps):
+        ev[2 * k].record()
+        call()
+        ev[2 * k + 1].record()
+    torch.cuda.synchronize()
+    ms = float(np.median([ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    print(json.dumps({"metric": f"{args.op} GB/s", "value": gbs, "unit": "GB/s", "ms_per_launch": ms,
+                      "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                      "config": {"workload": f"{args.op} FP64 ring-major, {nt} x {npx} CC rings -> {dt} torus rings, "
+                                             f"spin 2", "algorithmic_bytes": nbytes,
+                                 "l2": "input and output larger than L2"},
+                      "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                   "frac": gbs / peak,
+                                   "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}}))
+
+
+def delensing_main(args):
+    """Delensing (lenmap2gclm) served form at the headline configuration:
+    B requests per cunusht_delensing_batch launch against the plain FP64
+    single-request delensing on the same GPU, accuracy of the served output
+    against the FP64 result."""
+    import torch
+    from cunusht_gb300 import build as _b
+    _b.build()
+    import cunusht_gb300 as cu
+    lmax, spin, eps, B = args.lmax, args.spin, args.eps, args.batch
+    nphi = args.nphi or 2 * lmax + 1
+    geo = ("gl", {"lmax": lmax, "nphi": nphi})
+    T = cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=eps, precision=args.precision, max_spin=max(spin, 1))
+    npix, ncomp = T.npix(), (2 if spin else 1)
+    rng = np.random.default_rng(5)
+    D = torch.stack([torch.as_tensor(synth_inputs(lmax, spin, seed=1 + b)[1], device="cuda") for b in range(B)])
+    M = torch.as_tensor(rng.standard_normal((B, 2, npix) if spin else (B, npix)), device="cuda")
+    out = torch.empty((B, ncomp, T.nalm), dtype=torch.complex128, device="cuda")
+    T.reserve_batch(B)
+
+    def timed(fn, steps, warmup):
+        for i in range(warmup):
+            fn(i)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record()
+        for k in range(steps):
+            fn(k)
+            ev[k + 1].record()
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[-1]) * 1e-3, [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+
+    T.profile(True)
+    T.stage_times()
+    tot, per = timed(lambda k: T.delensing_batch(M, D, spin, ncomp=ncomp, out=out), args.steps, args.warmup)
+    stages = T.stage_times()
+    T.profile(False)
+    ptg = torch.empty((2, npix), dtype=torch.float64, device="cuda")
+    gam = torch.empty((npix,), dtype=torch.float64, device="cuda")
+    a1 = torch.empty((ncomp, T.nalm), dtype=torch.complex128, device="cuda")
+    n1 = max(2, args.steps // 2)
+    t1, _ = timed(lambda k: T.delensing_solve(M[k % B], D[k % B], a1, ptg, gam, spin), n1, 1)
+    fp64 = None
+    acc = None
+    if args.fp64_steps > 0 and args.precision != "fp64":
+        T64 = cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=eps, precision="fp64", max_spin=max(spin, 1))
+        a64 = torch.empty((ncomp, T.nalm), dtype=torch.complex128, device="cuda")
+        t64, _ = timed(lambda k: T64.delensing_solve(M[k % B], D[k % B], a64, ptg, gam, spin), args.fp64_steps, 1)
+        T64.delensing_solve(M[0], D[0], a64, ptg, gam, spin)
+        T.delensing_batch(M, D, spin, ncomp=ncomp, out=out)
+        acc = float(torch.linalg.norm(out[0] - a64) / torch.linalg.norm(a64))
+        fp64 = {"value": args.fp64_steps / t64, "unit": "solves/s", "precision": "fp64", "requests_per_launch": 1}
+        T64._destroy()
+    p50, p99 = np.percentile(per, [50, 99])
+    print(json.dumps({"metric": f"delensing solves/s at lmax={lmax} spin-{spin} eps={eps} (served mixed vs plain FP64)",
+                      "value": B * args.steps / tot, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": tot * 1e3 / args.steps, "higher_is_better": True,
+                      "p50_ms": float(p50), "p99_ms": float(p99),
+                      "config": {"workload": f"served delensing lmax={lmax} GL {lmax + 1}x{nphi} spin-{spin} eps={eps}, "
+                                             f"{B} requests per launch", "precision": args.precision,
+                                 "requests_per_launch": B},
+                      "single_request": {"value": n1 / t1, "unit": "solves/s"}, "fp64_single_request": fp64,
+                      "rel_err_vs_fp64": acc,
+                      "stages_ms_per_request": {k: v[0] / v[1] / B for k, v in stages.items()},
+                      "gpu_launches": int(sum(c for _, c in stages.values()))}))
+
+
 if __name__ == "__main__":
-    if "--serve" in sys.argv:
-        serve_main(parse())
+    _args = parse()
+    if _args.serve:
+        serve_main(_args)
+    elif _args.op:
+        op_main(_args)
+    elif _args.direction == "l2g" and _args.impl == "gb300":
+        delensing_main(_args)
     else:
         main()

@@ -288,6 +288,20 @@ static int launch_spread_warp(const cunusht_plan_s *P, int nreq, T *U, long long
     return CUNUSHT_OK;
 }
 
+// Exact float -> double conversion on the integer pipe (GB300's FP64 pipe
+// runs conversions at the FP64 rate): sign, exponent rebias 127 -> 1023,
+// mantissa shifted into the top of the 52-bit field.  FP32 denormals
+// (|x| < 2^-126) are flushed to zero; infinities / NaN are not expected.
+__device__ __forceinline__ double f2d_exact_int(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex == 0) return 0.0;
+    const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                    ((unsigned long long)(ex + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
 // Mixed-precision variant for an FP64 grid (eps <= 1e-6 on the mixed path):
 // kernel weights in FP32 from the FP64 tap offset split into hi + lo floats
 // (as k_interp_mixed), FP32 products, Kahan-compensated FP32 strip sums, FP64
@@ -355,6 +369,9 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const int pmin = __reduce_min_sync(0xffffffffu, act ? pc.p0 : big);
     const int pmax = __reduce_max_sync(0xffffffffu, act ? pc.p0 : -big);
     const int nr = rmax - rmin + w, ncl = pmax - pmin + w;
+    // the value split once into hi + lo floats (FP64 work per point, not per tap)
+    const float vrh = (float)vr, vrl = (float)(vr - (double)vrh);
+    const float vih = (float)vi, vil = (float)(vi - (double)vih);
     if (nr > SR || ncl > SC) {
         if (!act) return;
         for (int a = 0; a < w; ++a) {
@@ -380,11 +397,10 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     for (int rd = 0; rd < nround; ++rd) {
         const bool go = act && myrank == rd;
         for (int a = 0; a < w; ++a) {
-            // row factor kt[a] * value in FP64, split into hi + lo floats:
-            // each tap product then carries one FP32 rounding
-            const double fr = (double)kt[a] * vr, fi = (double)kt[a] * vi;
-            const float frh = (float)fr, frl = (float)(fr - (double)frh);
-            const float fih = (float)fi, fil = (float)(fi - (double)fih);
+            // row factor kt[a] * value as a double-float (FP32 TwoProduct on
+            // the split value): each tap product then carries one FP32 rounding
+            const float frh = kt[a] * vrh, frl = fmaf(kt[a], vrh, -frh) + kt[a] * vrl;
+            const float fih = kt[a] * vih, fil = fmaf(kt[a], vih, -fih) + kt[a] * vil;
             float2 *row = strip + (size_t)(base + a * ncl) * NC;
             for (int b = 0; b < w; ++b) {
                 if (go) {
@@ -412,8 +428,11 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
         double *cell = U + ((long long)(rmin + lr) * Npf + c) * NC;
 #pragma unroll
         for (int q = 0; q < NC; ++q) {
+            // Kahan value x - c as two exact FP64 atomic adds (the additions
+            // happen in L2, the conversions on the integer pipe)
             const float2 v = strip[i * NC + q];
-            if (v.x != 0.f) atomicAdd(cell + q, (double)v.x - (double)v.y);
+            if (v.x != 0.f) atomicAdd(cell + q, f2d_exact_int(v.x));
+            if (v.y != 0.f) atomicAdd(cell + q, -f2d_exact_int(v.y));
         }
     }
 }
@@ -970,74 +989,134 @@ int magnification_det(long long npix, const double *k, const double *g1, const d
 }
 
 // ------------------------------------------------------------ doubling
-template <typename T>
-__global__ void k_doubling(const T *__restrict__ in, long long nt, long long np, int layout, T sg,
-                           T *__restrict__ out) {
-    const long long dt = 2 * nt - 2;
-    const long long tot = dt * np;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= tot) return;
-    const long long h = np / 2;
-    long long k, i;  // ring k of the torus, longitude i
-    if (layout == 1) {
-        i = idx / dt;
-        k = idx - i * dt;
-    } else {
-        k = idx / np;
-        i = idx - k * np;
-    }
-    T v;
-    if (k < nt) {
-        v = layout == 1 ? in[i * nt + k] : in[k * np + i];
-    } else {
-        const long long km = dt - k;
-        const long long im = i < h ? i + h : i - h;
-        v = sg * (layout == 1 ? in[im * nt + km] : in[km * np + im]);
-    }
-    out[idx] = v;
+// The reference's doubling (doubling.cu:137-220): the CC map (nt rings x np
+// longitudes, theta from 0 to pi) extended to the 2 pi theta torus (2 nt - 2
+// rings): ring k >= nt is ring 2 nt - 2 - k shifted by pi in longitude,
+// times (-1)^spin.  One CTA row per output row (blockIdx.y), threads along the
+// contiguous axis -- no index division -- with 16-byte accesses (2 doubles /
+// 4 floats per thread) when the rows and the pi shift stay 16-byte aligned.
+// layout 0: ring-major in / out [ring][np]; layout 1: theta-contiguous
+// in [np][nt] -> out [np][2 nt - 2].
+// V consecutive elements as one access (16 bytes when V > 1; the caller
+// guarantees the alignment)
+template <typename T, int V> struct vecT;
+template <> struct vecT<double, 1> { using t = double; };
+template <> struct vecT<float, 1> { using t = float; };
+template <> struct vecT<double, 2> { using t = double2; };
+template <> struct vecT<float, 4> { using t = float4; };
+
+template <typename T, int V> __device__ __forceinline__ void ldv(const T *p, T (&v)[V]) {
+    const typename vecT<T, V>::t w = *reinterpret_cast<const typename vecT<T, V>::t *>(p);
+    static_assert(sizeof(w) == V * sizeof(T), "vector size");
+    memcpy(v, &w, sizeof(w));
 }
 
-template <typename T>
-__global__ void k_adjoint_doubling(const T *__restrict__ in, long long nt, long long np, T sg,
-                                   T *__restrict__ out) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nt * np) return;
-    const long long k = idx / np, i = idx - k * np;
-    const long long h = np / 2;
-    T v = in[idx];
-    if (k > 0 && k < nt - 1) {
-        const long long km = 2 * nt - 2 - k;
-        const long long im = i < h ? i + h : i - h;
-        v += sg * in[km * np + im];
-    }
-    out[idx] = v;
+template <typename T, int V> __device__ __forceinline__ void stv(T *p, const T (&v)[V]) {
+    typename vecT<T, V>::t w;
+    memcpy(&w, v, sizeof(w));
+    *reinterpret_cast<typename vecT<T, V>::t *>(p) = w;
 }
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256)
+    k_doubling(const T *__restrict__ in, long long nt, long long np, int layout, T sg, T *__restrict__ out) {
+    const long long dt = 2 * nt - 2;
+    const long long h = np / 2;
+    if (layout == 0) {
+        // one CTA row per input ring j: read once, write torus rings j and
+        // 2 nt - 2 - j (the latter shifted by pi, times sg)
+        for (long long j = blockIdx.y; j < nt; j += gridDim.y) {
+            const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * V;
+            if (c0 >= np) continue;
+            T v[V];
+            ldv<T, V>(in + j * np + c0, v);
+            stv<T, V>(out + j * np + c0, v);
+            if (j > 0 && j < nt - 1) {
+#pragma unroll
+                for (int e = 0; e < V; ++e) v[e] *= sg;
+                const long long cm = c0 < h ? c0 + h : c0 - h;  // a V-group never straddles h (h % V == 0)
+                stv<T, V>(out + (dt - j) * np + cm, v);
+            }
+        }
+    } else {
+        // theta-contiguous: one CTA row per longitude i of the output
+        for (long long i = blockIdx.y; i < np; i += gridDim.y) {
+            const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+            if (k >= dt) continue;
+            const long long im = i < h ? i + h : i - h;
+            out[i * dt + k] = k < nt ? in[i * nt + k] : sg * in[im * nt + (dt - k)];
+        }
+    }
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256)
+    k_adjoint_doubling(const T *__restrict__ in, long long nt, long long np, T sg, T *__restrict__ out) {
+    const long long h = np / 2;
+    for (long long k = blockIdx.y; k < nt; k += gridDim.y) {
+        const long long c0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * V;
+        if (c0 >= np) continue;
+        T v[V];
+        ldv<T, V>(in + k * np + c0, v);
+        if (k > 0 && k < nt - 1) {
+            const long long km = 2 * nt - 2 - k;
+            const long long im = c0 < h ? c0 + h : c0 - h;
+            T u[V];
+            ldv<T, V>(in + km * np + im, u);
+#pragma unroll
+            for (int e = 0; e < V; ++e) v[e] += sg * u[e];
+        }
+        stv<T, V>(out + k * np + c0, v);
+    }
+}
+
+template <typename T, int V>
+static void doubling_go(const void *in, long long nt, long long np, int layout, T sg, void *out, cudaStream_t st) {
+    const long long nrow = layout == 1 ? np : nt, ncol = layout == 1 ? 2 * nt - 2 : np;
+    const dim3 grid((unsigned)((ncol / V + 255) / 256), (unsigned)std::min<long long>(nrow, 65535));
+    k_doubling<T, V><<<grid, 256, 0, st>>>((const T *)in, nt, np, layout, sg, (T *)out);
+}
+
+template <typename T, int V>
+static void adjoint_doubling_go(const void *in, long long nt, long long np, T sg, void *out, cudaStream_t st) {
+    const dim3 grid((unsigned)((np / V + 255) / 256), (unsigned)std::min<long long>(nt, 65535));
+    k_adjoint_doubling<T, V><<<grid, 256, 0, st>>>((const T *)in, nt, np, sg, (T *)out);
+}
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
 
 int doubling_launch(const void *in, long long nt, long long np, int layout, int spin, int dtype, void *out,
                     cudaStream_t st) {
-    const long long tot = (2 * nt - 2) * np;
-    if (tot <= 0) return CUNUSHT_OK;
-    const int nb = (int)((tot + 255) / 256);
-    if (dtype == CUNUSHT_F32)
-        k_doubling<float><<<nb, 256, 0, st>>>((const float *)in, nt, np, layout, (spin & 1) ? -1.f : 1.f, (float *)out);
-    else
-        k_doubling<double><<<nb, 256, 0, st>>>((const double *)in, nt, np, layout, (spin & 1) ? -1.0 : 1.0,
-                                               (double *)out);
+    if ((2 * nt - 2) * np <= 0) return CUNUSHT_OK;
+    const bool f32 = dtype == CUNUSHT_F32;
+    const int V = f32 ? 4 : 2;  // 16 bytes
+    // vector path: ring-major rows of np elements, pi shift h = np / 2, all multiples of V
+    const bool vec = layout == 0 && np % V == 0 && (np / 2) % V == 0 && aligned16(in) && aligned16(out);
+    // (layout 1 runs one element per thread)
+    if (f32) {
+        if (vec) doubling_go<float, 4>(in, nt, np, layout, (spin & 1) ? -1.f : 1.f, out, st);
+        else doubling_go<float, 1>(in, nt, np, layout, (spin & 1) ? -1.f : 1.f, out, st);
+    } else {
+        if (vec) doubling_go<double, 2>(in, nt, np, layout, (spin & 1) ? -1.0 : 1.0, out, st);
+        else doubling_go<double, 1>(in, nt, np, layout, (spin & 1) ? -1.0 : 1.0, out, st);
+    }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
 
 int adjoint_doubling_launch(const void *in, long long nt, long long np, int spin, int dtype, void *out,
                             cudaStream_t st) {
-    const long long tot = nt * np;
-    if (tot <= 0) return CUNUSHT_OK;
-    const int nb = (int)((tot + 255) / 256);
-    if (dtype == CUNUSHT_F32)
-        k_adjoint_doubling<float><<<nb, 256, 0, st>>>((const float *)in, nt, np, (spin & 1) ? -1.f : 1.f,
-                                                      (float *)out);
-    else
-        k_adjoint_doubling<double><<<nb, 256, 0, st>>>((const double *)in, nt, np, (spin & 1) ? -1.0 : 1.0,
-                                                       (double *)out);
+    if (nt * np <= 0) return CUNUSHT_OK;
+    const bool f32 = dtype == CUNUSHT_F32;
+    const int V = f32 ? 4 : 2;
+    const bool vec = np % V == 0 && (np / 2) % V == 0 && aligned16(in) && aligned16(out);
+    if (f32) {
+        if (vec) adjoint_doubling_go<float, 4>(in, nt, np, (spin & 1) ? -1.f : 1.f, out, st);
+        else adjoint_doubling_go<float, 1>(in, nt, np, (spin & 1) ? -1.f : 1.f, out, st);
+    } else {
+        if (vec) adjoint_doubling_go<double, 2>(in, nt, np, (spin & 1) ? -1.0 : 1.0, out, st);
+        else adjoint_doubling_go<double, 1>(in, nt, np, (spin & 1) ? -1.0 : 1.0, out, st);
+    }
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
