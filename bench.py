@@ -256,15 +256,10 @@ def main():
         reference_arm(args)
         return
     import torch
-    import torch.distributed as dist
+    from cunusht_gb300.replicas import Replicas
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    dev = torch.device("cuda", local if world > 1 else 0)
+    R = Replicas(backend="nccl")           # independent replicas, one per GPU
+    world, rank, dev = R.world, R.rank, R.device
 
     from cunusht_gb300 import build as _b
     _b.build()
@@ -277,9 +272,9 @@ def main():
                                   precision=args.precision, max_spin=max(spin, 1))
     npix, nring = T.npix(), lmax + 1
     # B distinct requests (request 0 is the one the CPU baseline samples)
-    reqs = [synth_inputs(lmax, spin, seed=1 + 17 * rank + 1000 * b) for b in range(B)]
+    reqs = [synth_inputs(lmax, spin, seed=R.seed(1) + 1000 * b) for b in range(B)]
     gclm_h, plm_a = reqs[0]
-    _, plm_b = synth_inputs(lmax, spin, seed=2 + 17 * rank)
+    _, plm_b = synth_inputs(lmax, spin, seed=R.seed(2))
     ncomp = gclm_h.shape[0]
     G = torch.as_tensor(gclm_h if spin else gclm_h[0], device=dev)
     D = [torch.as_tensor(plm_a, device=dev), torch.as_tensor(plm_b, device=dev)]
@@ -291,16 +286,7 @@ def main():
     outB = torch.empty((B, 2, npix) if spin else (B, npix), dtype=torch.float64, device=dev)
     T.reserve_batch(B)
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def maxall(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, maxall = R.barrier, R.max
 
     def timed(fn, steps, warmup, profile=False, sample_clocks=False):
         """CUDA-event timing of `steps` calls after `warmup` untimed ones;
@@ -485,8 +471,7 @@ def main():
                 "rel_err_vs_fp64_oracle_sample": acc, "rel_err_vs_fp64_cpu_port_full_map": acc_full,
                 "clocks": clocks}
         print(json.dumps(line))
-    if world > 1:
-        dist.destroy_process_group()
+    R.close()
 
 
 # ----------------------------------------------------------------------------- served mixed workload

@@ -1,8 +1,10 @@
-"""Differentiable lensing (config 3 pattern at reduced lmax): gradients of
-L = ||gclm2lenmap(gclm, dlm) - d||^2 from the hand-written adjoint / Jacobian
-kernels against central finite differences along random directions
-(step 1e-6 relative), and the gclm gradient against the adjoint operator
-(dot-product test, test/test_adjointOperator.py:246-277 pattern)."""
+"""Differentiable lensing at the differentiable-lensing configuration
+(spin 0, lmax 1023, float64): gradients of L = ||gclm2lenmap(gclm, dlm) - d||^2,
+d = a lensed seeded realisation plus white noise of 10 uK.arcmin, from the
+hand-written adjoint (gclm) and pointing-Jacobian VJP (dlm) kernels, against
+central finite differences (step 1e-6 relative) on 64 random directions each,
+and the gclm gradient against the adjoint operator (dot-product test,
+test/test_adjointOperator.py:246-277 pattern)."""
 import numpy as np
 import pytest
 
@@ -10,6 +12,9 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
+
+LMAX = 1023
+NDIR = 64
 
 
 def _direction(lmax, rng):
@@ -23,16 +28,17 @@ def _direction(lmax, rng):
 def setup(built_lib):
     import cunusht_gb300 as cu
     from cunusht_gb300.autograd import gclm2lenmap
-    lmax = 95
+    lmax = LMAX
     T = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=1e-10, precision="fp64", max_spin=0)
     gclm, dls = orc.make_inputs(lmax, 0, seed=5)
     rng = np.random.default_rng(6)
     g = torch.as_tensor(gclm[0], device="cuda")
     d = torch.as_tensor(dls[0], device="cuda")
-    # data: a lensed realisation of another field plus white noise
+    # data: a lensed realisation of another field plus 10 uK.arcmin white noise
     g2, _ = orc.make_inputs(lmax, 0, seed=9)
     data = T.gclm2lenmap(torch.as_tensor(g2[0], device="cuda"), lmax, lmax, dlm_scaled=d, verbose=0)
-    data = data + torch.as_tensor(rng.standard_normal(data.numel()) * 0.1, device="cuda")
+    pix_arcmin = np.sqrt(4 * np.pi / T.npix()) * 180 * 60 / np.pi
+    data = data + torch.as_tensor(rng.standard_normal(data.numel()) * (10.0 / pix_arcmin), device="cuda")
     T.dlm_scaled = None
 
     def loss(gg, dd):
@@ -55,12 +61,14 @@ def test_gclm_gradient_matches_finite_differences(setup):
     L = loss(gg, d)
     L.backward()
     grad = gg.grad.cpu().numpy()
-    for _ in range(4):
+    h = 1e-6 * float(torch.linalg.norm(g))
+    worst = 0.0
+    for _ in range(NDIR):
         v = _direction(lmax, rng)
-        h = 1e-6 * float(torch.linalg.norm(g))
         fd = _fd(loss, g, d, torch.as_tensor(v, device="cuda"), torch.zeros_like(d), h)
         an = float(np.sum((np.conj(grad) * v).real))
-        assert abs(fd - an) <= 1e-6 * abs(an) + 1e-8 * L.item()
+        worst = max(worst, abs(fd - an) / (abs(an) + 1e-8 * L.item()))
+        assert abs(fd - an) <= 1e-6 * abs(an) + 1e-8 * L.item(), (fd, an)
 
 
 def test_dlm_gradient_matches_finite_differences(setup):
@@ -69,9 +77,9 @@ def test_dlm_gradient_matches_finite_differences(setup):
     L = loss(g, dd)
     L.backward()
     grad = dd.grad.cpu().numpy()
-    for _ in range(8):
+    h = 1e-6 * float(torch.linalg.norm(d))
+    for _ in range(NDIR):
         v = _direction(lmax, rng)
-        h = 1e-6 * float(torch.linalg.norm(d))
         fd = _fd(loss, g, d, torch.zeros_like(g), torch.as_tensor(v, device="cuda"), h)
         an = float(np.sum((np.conj(grad) * v).real))
         assert abs(fd - an) <= 1e-5 * abs(an) + 1e-9 * L.item(), (fd, an)
