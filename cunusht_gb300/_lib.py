@@ -34,6 +34,12 @@ SIGNATURES = {
     "cunusht_plan_set_profiling": (_i, [_vp, _i]),
     "cunusht_plan_force_split": (_i, [_vp, _i]),
     "cunusht_dlm2A": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
+    "cunusht_server_create": (_i, [ctypes.POINTER(_vp), _d, _i]),
+    "cunusht_server_set_policy": (_i, [_vp, _i, _i, _i]),
+    "cunusht_server_submit": (_i, [_vp, _i, _i, _i, _d, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_i64)]),
+    "cunusht_server_poll": (_i, [_vp, _vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
+    "cunusht_server_stats": (_i, [_vp, _vp, _i]),
+    "cunusht_server_destroy": (_i, [_vp]),
     "cunusht_delensing_batch": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cunusht_synth_points": (_i, [_vp, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp]),
     "cunusht_plan_stage_times": (_i, [_vp, _vp, _vp, _i]),

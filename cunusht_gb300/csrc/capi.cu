@@ -31,7 +31,7 @@ static int next_pow2(long long n) {
 }
 
 // Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on P_n.
-static void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
     x.resize(n);
     w.resize(n);
     for (int i = 0; i < n; ++i) {

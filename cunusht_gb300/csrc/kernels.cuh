@@ -6,6 +6,9 @@ namespace cunusht {
 
 constexpr int FFT_TPB = 512;
 
+// capi.cu: Gauss-Legendre nodes x (descending cos theta) and weights, Newton iteration
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w);
+
 // legendre.cu
 int build_coef_tables(cunusht_plan_s *P, cudaStream_t st);
 int build_coef_tables_df(cunusht_plan_s *P, cudaStream_t st);

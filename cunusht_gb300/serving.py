@@ -256,3 +256,101 @@ class LensingServer:
 
     def latencies_ms(self):
         return [1e3 * (r.t_done - r.arrival) for r in self.completed]
+
+
+class NativeLensingServer:
+    """The same continuous-batching server run by the library's C++ scheduler
+    (cunusht_server_*): Python only submits device tensors and polls.
+
+    submit() returns a request id; results land in ``out`` (allocated here if
+    not given) once poll() has returned the id."""
+
+    def __init__(self, hbm_budget_bytes: float = 150e9, precision: str = "mixed", policy=None):
+        import ctypes
+        from . import _lib
+        from .transformer import _PREC
+        self._lib = _lib.load()
+        self._c = ctypes
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.cunusht_server_create(ctypes.byref(h), float(hbm_budget_bytes), _PREC[precision]))
+        self._srv = h
+        for lmax, (nb, ns) in (policy or {}).items():
+            _lib.check(self._lib.cunusht_server_set_policy(self._srv, int(lmax), int(nb), int(ns)))
+        self.t0 = time.perf_counter()
+        self.live: dict[int, Request] = {}
+        self.completed: list[Request] = []
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def submit(self, kind, lmax, spin, epsilon, data, dlm_scaled, arrival=None, out=None, nphi=0) -> Request:
+        from . import _lib
+        from .utils import Alm
+        if kind not in ("g2l", "l2g"):
+            raise ValueError(f"kind must be 'g2l' or 'l2g', got {kind!r}")
+        if callable(data):
+            data, dlm_scaled = data()
+        if not nphi:  # the package's default GL geometry (geometry.get_gl_geometry)
+            from .geometry import get_geom
+            nphi = int(get_geom(("gl", {"lmax": lmax})).nph[0])
+        nalm = Alm.getsize(lmax, lmax)
+        ncm = 2 if spin else 1
+        npix = (lmax + 1) * nphi
+        if kind == "g2l":
+            inp = data.reshape(ncm, nalm).to(torch.complex128).contiguous()
+            res = out if out is not None else torch.empty((ncm, npix) if spin else (npix,), dtype=torch.float64,
+                                                          device="cuda")
+        else:
+            inp = data.reshape(ncm, npix).to(torch.float64).contiguous()
+            res = out if out is not None else torch.empty((ncm, nalm) if spin else (nalm,), dtype=torch.complex128,
+                                                          device="cuda")
+        d = dlm_scaled.reshape(-1).to(torch.complex128).contiguous()
+        rid = self._c.c_int64()
+        _lib.check(self._lib.cunusht_server_submit(self._srv, 0 if kind == "g2l" else 1, lmax, spin, float(epsilon),
+                                                   int(nphi), inp.data_ptr(), d.data_ptr(), res.data_ptr(),
+                                                   torch.cuda.current_stream().cuda_stream, self._c.byref(rid)))
+        r = Request(kind, lmax, spin, epsilon, inp, d, self.now() if arrival is None else arrival, rid.value)
+        r.result = res
+        self.live[rid.value] = r
+        return r
+
+    def step(self) -> bool:
+        from . import _lib
+        ids = (self._c.c_int64 * 256)()
+        nd, pend = self._c.c_int(), self._c.c_int()
+        while True:
+            _lib.check(self._lib.cunusht_server_poll(self._srv, ids, 256, self._c.byref(nd), self._c.byref(pend)))
+            t = self.now()
+            for i in range(nd.value):
+                r = self.live.pop(ids[i])
+                r.t_done = t
+                r.data = r.dlm_scaled = None  # inputs may be released now
+                self.completed.append(r)
+            if nd.value < 256:
+                break
+        return pend.value > 0 or bool(self.live)
+
+    def run_until_idle(self, poll_s: float = 0.0):
+        while self.step():
+            if poll_s:
+                time.sleep(poll_s)
+
+    def latencies_ms(self):
+        return [1e3 * (r.t_done - r.arrival) for r in self.completed]
+
+    def stats(self) -> dict:
+        from . import _lib
+        v = (self._c.c_double * 6)()
+        _lib.check(self._lib.cunusht_server_stats(self._srv, v, 6))
+        return dict(zip(["launches", "completed", "bytes", "buckets", "slots", "refusals"], list(v)))
+
+    def close(self):
+        if getattr(self, "_srv", None):
+            self._lib.cunusht_server_destroy(self._srv)
+            self._srv = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

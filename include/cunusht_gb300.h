@@ -179,6 +179,37 @@ int cunusht_dlm2pointing(cunusht_plan_t *plan, const void *dlm_scaled, const voi
                          int alm_dtype, double *ptg, double *gamma, void *stream);
 
 /*
+ * Continuous-batching lensing server (the served form's host scheduler; the
+ * reference has no serving layer).  Requests of any lmax (GL grid, nphi
+ * pixels per ring, 0 = 2 lmax + 1), spin and accuracy are queued per bucket;
+ * each bucket gets slots (plan + batch workspace + stream) when its measured
+ * device memory fits the HBM budget; cunusht_server_poll() retires finished
+ * launches and launches queued requests on idle slots, batching up to the
+ * bucket's requests-per-launch through cunusht_lensing_batch /
+ * cunusht_delensing_batch replayed as CUDA graphs.
+ *   direction 0 (gclm2lenmap): input gclm (spin ? 2 : 1, nalm) complex128,
+ *     output (spin ? 2 : 1, npix) float64;
+ *   direction 1 (lenmap2gclm): input lensed map (spin ? 2 : 1, npix) float64,
+ *     output (spin ? 2 : 1, nalm) complex128;
+ *   dlm_scaled (nalm) complex128.  All device pointers, owned by the caller
+ *   and valid until the request id is returned by cunusht_server_poll; inputs
+ *   are read after the work already queued on producer_stream.
+ * One host thread drives a server.  Default policy: lmax >= 4095: 1 request
+ * per launch, 1 slot; >= 2047: 4, 2; else 8, 2 (cunusht_server_set_policy).
+ * cunusht_server_stats: [launches, completed, bytes in use, buckets, slots,
+ * refused admissions].
+ */
+typedef struct cunusht_server_s cunusht_server_t;
+int cunusht_server_create(cunusht_server_t **server, double hbm_budget_bytes, int precision);
+int cunusht_server_set_policy(cunusht_server_t *server, int lmax, int requests_per_launch, int slots);
+int cunusht_server_submit(cunusht_server_t *server, int direction, int lmax, int spin, double eps, int nphi,
+                          const void *input, const void *dlm_scaled, void *output, void *producer_stream,
+                          int64_t *request_id);
+int cunusht_server_poll(cunusht_server_t *server, int64_t *done_ids, int max_ids, int *ndone, int *pending);
+int cunusht_server_stats(cunusht_server_t *server, double *stats, int n);
+int cunusht_server_destroy(cunusht_server_t *server);
+
+/*
  * Determinant of the magnification matrix of a deflection field on the plan's
  * pointing geometry (helper_GPU.py:113-161 dlm2A): A (npix, float64) from the
  * gradient deflection alm dlm = sqrt(l(l+1)) phi_lm (NOT dlm_scaled) and the

@@ -126,12 +126,14 @@ def test_batch_rejects_over_capacity(built_lib):
         T.lensing_batch(g, d, 0, out=out)
 
 
-def test_server_mixed_stream_matches_isolated_results(built_lib):
+@pytest.mark.parametrize("native", [False, True])
+def test_server_mixed_stream_matches_isolated_results(built_lib, native):
     import cunusht_gb300 as cu
-    from cunusht_gb300.serving import LensingServer
-    srv = LensingServer(max_batch=4, precision="mixed")
+    from cunusht_gb300.serving import LensingServer, NativeLensingServer
+    srv = NativeLensingServer(precision="mixed", policy={63: (4, 2), 127: (4, 2)}) if native else \
+        LensingServer(max_batch=4, precision="mixed")
     rng = np.random.default_rng(11)
-    kinds = []
+    kinds, reqs = [], []
     for i in range(14):
         lmax = [63, 127][i % 2]
         spin = [0, 2][(i // 2) % 2]
@@ -145,25 +147,43 @@ def test_server_mixed_stream_matches_isolated_results(built_lib):
             npix = cu.get_geom(("gl", {"lmax": lmax})).npix()
             data = torch.as_tensor(rng.standard_normal((2, npix) if spin else npix), device="cuda")
         kinds.append((kind, lmax, spin, eps, data, d))
-        srv.submit(kind, lmax, spin, eps, data, d)
+        reqs.append(srv.submit(kind, lmax, spin, eps, data, d))
     srv.run_until_idle()
     torch.cuda.synchronize()
     assert len(srv.completed) == len(kinds)
+    if native:
+        st = srv.stats()
+        assert st["completed"] == len(kinds) and st["launches"] < len(kinds)  # batched
     lat = srv.latencies_ms()
     assert all(x >= 0 for x in lat)
-    by_id = {r.rid: r for r in srv.completed}
     for i, (kind, lmax, spin, eps, data, d) in enumerate(kinds):
+        got = reqs[i].result
+        if native:
+            # alone on the same (native) server vs in the mix; the native
+            # server builds its GL rings in C++ (colatitudes within 1 ulp of
+            # the Python geometry), so the Python plan is only compared at eps
+            alone = NativeLensingServer(precision="mixed", policy={63: (4, 2), 127: (4, 2)})
+            ra = alone.submit(kind, lmax, spin, eps, data, d)
+            alone.run_until_idle()
+            torch.cuda.synchronize()
+            ref_alone = ra.result
+            alone.close()
         T = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=eps, precision="mixed",
                                        max_spin=max(spin, 1))
         if kind == "g2l":
             ref = T.gclm2lenmap(data, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0)
         else:
             ref = T.lenmap2gclm(data, d, None, lmax, lmax, spin=spin, verbose=0)
-        got = by_id[i].result
         scale = float(torch.max(torch.abs(ref)))
         # lensing is deterministic (no atomics): the same bits up to 1e-12;
         # delensing spreads with floating-point atomics whose order varies
         # between runs, so alone and in the mix agree to a tenth of epsilon
         tol = 1e-12 if kind == "g2l" else 0.1 * eps
-        err = float(torch.max(torch.abs(got.reshape(ref.shape) - ref)))
-        assert err <= tol * scale, (i, kind, lmax, spin, eps, err / scale)
+        if native:
+            err = float(torch.max(torch.abs(got.reshape(ref_alone.shape) - ref_alone)))
+            assert err <= tol * scale, (i, kind, lmax, spin, eps, err / scale)
+            err = float(torch.max(torch.abs(got.reshape(ref.shape) - ref)))
+            assert err <= eps * scale, (i, kind, lmax, spin, eps, err / scale)
+        else:
+            err = float(torch.max(torch.abs(got.reshape(ref.shape) - ref)))
+            assert err <= tol * scale, (i, kind, lmax, spin, eps, err / scale)
