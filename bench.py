@@ -69,6 +69,7 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=2000)
     p.add_argument("--serve-rate", type=float, default=200.0, help="mean arrival rate, requests/s")
     p.add_argument("--serve-budget-gb", type=float, default=150.0)
+    p.add_argument("--serve-native", action="store_true", help="drive the library's C++ server (cunusht_server_*)")
     p.add_argument("--serve-fp64-sample", type=int, default=60,
                    help="requests of the same mix run as serial plain FP64 calls for the comparison")
     return p.parse_args()
@@ -544,7 +545,7 @@ def serve_main(args):
     from cunusht_gb300 import build as _b
     _b.build()
     import cunusht_gb300 as cu
-    from cunusht_gb300.serving import LensingServer
+    from cunusht_gb300.serving import LensingServer, NativeLensingServer
 
     rng = np.random.default_rng(2024)
     n = args.serve_requests
@@ -556,10 +557,15 @@ def serve_main(args):
     npix_of = {L: cu.get_geom(("gl", {"lmax": int(L)})).npix() for L in SERVE_LMAX}
     inputs = DeviceInputs(torch)
 
-    srv = LensingServer(precision="mixed", hbm_budget_bytes=args.serve_budget_gb * 1e9, policy=serve_policy)
     keys = sorted({(int(L), int(s), float(e)) for L, s, e in zip(lmaxs, spins, epss)})
     t0 = time.perf_counter()
-    admitted = srv.prewarm(keys)
+    if args.serve_native:
+        srv = NativeLensingServer(precision="mixed", hbm_budget_bytes=args.serve_budget_gb * 1e9,
+                                  policy={L: serve_policy(L) for L in SERVE_LMAX})
+        admitted = keys  # buckets are admitted on first use; the warm-up below creates them
+    else:
+        srv = LensingServer(precision="mixed", hbm_budget_bytes=args.serve_budget_gb * 1e9, policy=serve_policy)
+        admitted = srv.prewarm(keys)
     setup_s = time.perf_counter() - t0
     for L in SERVE_LMAX:
         inputs.tables(int(L))
@@ -570,7 +576,7 @@ def serve_main(args):
     srv.run_until_idle()
     torch.cuda.synchronize()
     srv.completed.clear()
-    launches0 = srv.launches
+    launches0 = srv.stats()["launches"] if args.serve_native else srv.launches
 
     # timed run: Poisson arrivals on the server clock
     clk = ClockSampler(torch.cuda.current_device())
@@ -590,12 +596,14 @@ def serve_main(args):
         seen = len(srv.completed)
         if nxt >= n and not pending:
             break
-        if nxt < n and not srv.busy():
+        if nxt < n and not pending:
             time.sleep(max(0.0, min(1e-3, arrivals[nxt] - srv.now())))
     torch.cuda.synchronize()
     wall = srv.now()
     clocks = clk.stop()
-    nlaunch = srv.launches - launches0
+    nlaunch = (srv.stats()["launches"] if args.serve_native else srv.launches) - launches0
+    if args.serve_native:
+        admitted = [None] * int(srv.stats()["buckets"])
     lat = np.array(srv.latencies_ms())
     done = len(srv.completed)
     by = {}
@@ -648,6 +656,7 @@ def serve_main(args):
             "launches": nlaunch, "requests_per_launch": done / max(1, nlaunch),
             "fp64_serial": fp64, "buckets_admitted": len(admitted), "buckets": len(keys),
             "plan_setup_s": setup_s, "hbm_budget_gb": args.serve_budget_gb,
+            "server": "native (cunusht_server_*)" if args.serve_native else "python (serving.LensingServer)",
             "config": {"workload": f"{n} Poisson requests at {args.serve_rate}/s, lmax {list(SERVE_LMAX)} "
                                    f"p={list(SERVE_P)}, spin {{0,2}}, gclm2lenmap / lenmap2gclm, eps {{1e-5,1e-7}}",
                        "policy": {str(L): serve_policy(L) for L in SERVE_LMAX}, "precision": "mixed"},

@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import collections
 import dataclasses
+import functools
 import itertools
 import time
 from typing import Optional
@@ -258,6 +259,14 @@ class LensingServer:
         return [1e3 * (r.t_done - r.arrival) for r in self.completed]
 
 
+@functools.lru_cache(maxsize=None)
+def _default_nphi(lmax: int) -> int:
+    """Pixels per ring of the package's default GL geometry for lmax (cached:
+    building the geometry computes the Gauss-Legendre nodes)."""
+    from .utils import good_size
+    return good_size(2 * lmax + 1, True)
+
+
 class NativeLensingServer:
     """The same continuous-batching server run by the library's C++ scheduler
     (cunusht_server_*): Python only submits device tensors and polls.
@@ -274,25 +283,47 @@ class NativeLensingServer:
         h = ctypes.c_void_p()
         _lib.check(self._lib.cunusht_server_create(ctypes.byref(h), float(hbm_budget_bytes), _PREC[precision]))
         self._srv = h
-        for lmax, (nb, ns) in (policy or {}).items():
+        self.policy = dict(policy or {})
+        for lmax, (nb, ns) in self.policy.items():
             _lib.check(self._lib.cunusht_server_set_policy(self._srv, int(lmax), int(nb), int(ns)))
         self.t0 = time.perf_counter()
         self.live: dict[int, Request] = {}
         self.completed: list[Request] = []
+        # requests with callable payloads wait here until their bucket has room
+        self.waiting: dict[tuple, collections.deque] = collections.defaultdict(collections.deque)
+        self.inflight: dict[tuple, int] = collections.defaultdict(int)
+
+    def _cap(self, lmax: int) -> int:
+        """Requests of one bucket handed to the library at a time: two full
+        launches on every slot (the library's default policy otherwise)."""
+        nb, ns = self.policy.get(lmax, (1, 1) if lmax >= 4095 else ((4, 2) if lmax >= 2047 else (8, 2)))
+        return 2 * nb * ns
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
 
     def submit(self, kind, lmax, spin, epsilon, data, dlm_scaled, arrival=None, out=None, nphi=0) -> Request:
-        from . import _lib
-        from .utils import Alm
+        """Queue a request.  A callable payload (returning (data, dlm_scaled))
+        is materialised only when its bucket has room in the library, so a
+        backlog holds no device memory."""
         if kind not in ("g2l", "l2g"):
             raise ValueError(f"kind must be 'g2l' or 'l2g', got {kind!r}")
-        if callable(data):
-            data, dlm_scaled = data()
+        r = Request(kind, lmax, spin, epsilon, data, dlm_scaled, self.now() if arrival is None else arrival, -1)
+        r.out_arg, r.nphi = out, nphi
+        key = (lmax, spin, float(epsilon), nphi)
+        if callable(data) or self.waiting[key] or self.inflight[key] >= self._cap(lmax):
+            self.waiting[key].append(r)
+        else:
+            self._hand_over(key, r)
+        return r
+
+    def _hand_over(self, key, r: Request):
+        from . import _lib
+        from .utils import Alm
+        kind, lmax, spin, epsilon, nphi, out = r.kind, r.lmax, r.spin, r.epsilon, r.nphi, r.out_arg
+        data, dlm_scaled = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
         if not nphi:  # the package's default GL geometry (geometry.get_gl_geometry)
-            from .geometry import get_geom
-            nphi = int(get_geom(("gl", {"lmax": lmax})).nph[0])
+            nphi = _default_nphi(lmax)
         nalm = Alm.getsize(lmax, lmax)
         ncm = 2 if spin else 1
         npix = (lmax + 1) * nphi
@@ -309,10 +340,9 @@ class NativeLensingServer:
         _lib.check(self._lib.cunusht_server_submit(self._srv, 0 if kind == "g2l" else 1, lmax, spin, float(epsilon),
                                                    int(nphi), inp.data_ptr(), d.data_ptr(), res.data_ptr(),
                                                    torch.cuda.current_stream().cuda_stream, self._c.byref(rid)))
-        r = Request(kind, lmax, spin, epsilon, inp, d, self.now() if arrival is None else arrival, rid.value)
-        r.result = res
+        r.data, r.dlm_scaled, r.result, r.rid, r.key = inp, d, res, rid.value, key
         self.live[rid.value] = r
-        return r
+        self.inflight[key] += 1
 
     def step(self) -> bool:
         from . import _lib
@@ -325,10 +355,18 @@ class NativeLensingServer:
                 r = self.live.pop(ids[i])
                 r.t_done = t
                 r.data = r.dlm_scaled = None  # inputs may be released now
+                self.inflight[r.key] -= 1
                 self.completed.append(r)
             if nd.value < 256:
                 break
-        return pend.value > 0 or bool(self.live)
+        handed = False
+        for key, q in self.waiting.items():
+            while q and self.inflight[key] < self._cap(key[0]):
+                self._hand_over(key, q.popleft())
+                handed = True
+        if handed:  # launch what was just handed over
+            _lib.check(self._lib.cunusht_server_poll(self._srv, None, 0, self._c.byref(nd), self._c.byref(pend)))
+        return pend.value > 0 or bool(self.live) or any(self.waiting.values())
 
     def run_until_idle(self, poll_s: float = 0.0):
         while self.step():
