@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <map>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -118,7 +119,8 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn,
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
-                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
+                    P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_ring_cls, P->d_cls_N, P->d_cls_Mb, P->d_cls_SP,
+                    P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
                     P->d_glmapb, P->d_ptgb, P->d_gamb};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -204,15 +206,11 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     P->npix = npix;
     const long long npix_span = P->h_ofs[nring - 1] + P->h_nph[nring - 1];
     ARG_CHECK(npix_span == npix && P->h_ofs[0] == 0, "ring pixels must tile [0, npix) contiguously");
+    // rings may have different pixel counts (HEALPix, thinned grids), fewer than
+    // 2 lmax + 1 included (the ring transforms fold the aliased modes)
     P->nph_uniform = (int)P->h_nph[0];
     for (int i = 1; i < nring; ++i)
         if (P->h_nph[i] != P->h_nph[0]) P->nph_uniform = 0;
-    if (P->nph_uniform == 0) {
-        set_error("rings with different pixel counts are not supported yet");
-        return CUNUSHT_ERR_UNSUPPORTED;
-    }
-    ARG_CHECK(P->nph_uniform >= 2 * lmax + 1, "pixels per ring (%d) must be >= 2 lmax + 1 (%d)",
-              P->nph_uniform, 2 * lmax + 1);
 
     // ring pairs (theta, pi - theta)
     {
@@ -324,30 +322,70 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         for (int l = 0; l <= lmax; ++l) lf[l] = l >= 1 ? std::sqrt((l - 1.0) * (l + 2.0)) : 0.0;
         RC_TRY(upload(P, &P->d_lfac_g, lf));
     }
-    // Bluestein data for ring transforms
+    // Bluestein data for the ring transforms, one set per distinct ring length
+    std::vector<int> cls_N, cls_Mb, cls_SP;
+    std::vector<long long> cls_coff, cls_boff;
     {
-        const int N = P->nph_uniform;
-        P->Mb = next_pow2(2LL * N - 1);
-        P->sp_ring = P->Mb > 16 * FFT_TPB ? 2 : 1;
-        if (P->Mb / P->sp_ring > 16 * FFT_TPB) {
-            set_error("ring length %d needs a Bluestein FFT of %d points; at most 8192 pixels per ring are supported",
-                      N, P->Mb);
-            return CUNUSHT_ERR_UNSUPPORTED;
+        std::map<long long, int> cls_of;
+        std::vector<int> rcls(nring);
+        long long csum = 0, bsum = 0;
+        P->Mb = 0;
+        P->sp_ring = 1;
+        P->ring_buf = 0;
+        for (int i = 0; i < nring; ++i) {
+            const long long N = P->h_nph[i];
+            auto it = cls_of.find(N);
+            if (it == cls_of.end()) {
+                const int Mb = next_pow2(2LL * N - 1);
+                const int SP = Mb > 16 * FFT_TPB ? 2 : 1;
+                if (Mb / SP > 16 * FFT_TPB) {
+                    set_error("ring length %lld needs a Bluestein FFT of %d points; at most 8192 pixels per ring "
+                              "are supported", N, Mb);
+                    return CUNUSHT_ERR_UNSUPPORTED;
+                }
+                it = cls_of.emplace(N, (int)cls_N.size()).first;
+                cls_N.push_back((int)N);
+                cls_Mb.push_back(Mb);
+                cls_SP.push_back(SP);
+                cls_coff.push_back(csum);
+                cls_boff.push_back(bsum);
+                csum += N;
+                bsum += Mb;
+                P->Mb = std::max(P->Mb, Mb);
+                P->sp_ring = std::max(P->sp_ring, SP);
+                P->ring_buf = std::max(P->ring_buf, Mb / SP);
+            }
+            rcls[i] = it->second;
         }
-        std::vector<double2> chirp(N), bk(P->Mb, make_double2(0.0, 0.0));
-        for (int q = 0; q < N; ++q) {
-            const long long qq = ((long long)q * q) % (2LL * N);
-            const double a = PI * (double)qq / N;
-            chirp[q] = make_double2(std::cos(a), std::sin(a));
-        }
-        const double inv = 1.0 / P->Mb;
-        for (int k = 0; k < N; ++k) {
-            const double2 b = make_double2(chirp[k].x * inv, -chirp[k].y * inv);
-            bk[k] = b;
-            if (k > 0) bk[P->Mb - k] = b;
+        P->ncls = (int)cls_N.size();
+        P->nchirp = csum;
+        P->nbker = bsum;
+        std::vector<double2> chirp(csum), bk(bsum, make_double2(0.0, 0.0));
+        for (int c = 0; c < P->ncls; ++c) {
+            const int N = cls_N[c], Mb = cls_Mb[c];
+            double2 *ch = chirp.data() + cls_coff[c], *bkc = bk.data() + cls_boff[c];
+            for (int q = 0; q < N; ++q) {
+                const long long qq = ((long long)q * q) % (2LL * N);
+                const double a = PI * (double)qq / N;
+                ch[q] = make_double2(std::cos(a), std::sin(a));
+            }
+            const double inv = 1.0 / Mb;
+            for (int k = 0; k < N; ++k) {
+                const double2 b = make_double2(ch[k].x * inv, -ch[k].y * inv);
+                bkc[k] = b;
+                if (k > 0) bkc[Mb - k] = b;
+            }
         }
         RC_TRY(upload(P, &P->d_chirp, chirp));
         RC_TRY(upload(P, &P->d_bker, bk));
+        if (P->ncls > 1) {
+            RC_TRY(upload(P, &P->d_ring_cls, rcls));
+            RC_TRY(upload(P, &P->d_cls_N, cls_N));
+            RC_TRY(upload(P, &P->d_cls_Mb, cls_Mb));
+            RC_TRY(upload(P, &P->d_cls_SP, cls_SP));
+            RC_TRY(upload(P, &P->d_cls_coff, cls_coff));
+            RC_TRY(upload(P, &P->d_cls_boff, cls_boff));
+        }
     }
     // twiddles
     {
@@ -362,26 +400,31 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         RC_TRY(upload(P, &P->d_tw64, tw));
         RC_TRY(upload(P, &P->d_tw32, tw32));
     }
-    if (P->sp_ring == 1) {
-        RC_TRY(fft_global_f64(P->d_bker, P->Mb, -1, P->d_tw64, P->TW, 0));
-    } else {
-        // too long for one shared-memory transform: the kernel spectrum on the host
-        std::vector<double2> bk(P->Mb);
-        CU_TRY(cudaMemcpy(bk.data(), P->d_bker, P->Mb * sizeof(double2), cudaMemcpyDeviceToHost));
-        host_fft_forward(bk);
-        CU_TRY(cudaMemcpy(P->d_bker, bk.data(), P->Mb * sizeof(double2), cudaMemcpyHostToDevice));
+    // kernel spectra, per class
+    for (int c = 0; c < P->ncls; ++c) {
+        double2 *b = P->d_bker + cls_boff[c];
+        const int Mb = cls_Mb[c];
+        if (cls_SP[c] == 1) {
+            RC_TRY(fft_global_f64(b, Mb, -1, P->d_tw64, P->TW, 0));
+        } else {
+            // too long for one shared-memory transform: the kernel spectrum on the host
+            std::vector<double2> bk(Mb);
+            CU_TRY(cudaMemcpy(bk.data(), b, Mb * sizeof(double2), cudaMemcpyDeviceToHost));
+            host_fft_forward(bk);
+            CU_TRY(cudaMemcpy(b, bk.data(), Mb * sizeof(double2), cudaMemcpyHostToDevice));
+        }
     }
     if (P->fft_df) {
         char *t = nullptr, *c = nullptr, *b = nullptr;
         RC_TRY(dalloc(P, &t, 16 * (size_t)P->TW));
-        RC_TRY(dalloc(P, &c, 16 * (size_t)P->nph_uniform));
-        RC_TRY(dalloc(P, &b, 16 * (size_t)P->Mb));
+        RC_TRY(dalloc(P, &c, 16 * (size_t)P->nchirp));
+        RC_TRY(dalloc(P, &b, 16 * (size_t)P->nbker));
         P->d_twdf = t;
         P->d_chirp_df = c;
         P->d_bker_df = b;
         RC_TRY(split_c128_to_df(P->d_tw64, P->TW, P->d_twdf, 0));
-        RC_TRY(split_c128_to_df(P->d_chirp, P->nph_uniform, P->d_chirp_df, 0));
-        RC_TRY(split_c128_to_df(P->d_bker, P->Mb, P->d_bker_df, 0));
+        RC_TRY(split_c128_to_df(P->d_chirp, P->nchirp, P->d_chirp_df, 0));
+        RC_TRY(split_c128_to_df(P->d_bker, P->nbker, P->d_bker_df, 0));
     }
     // workspace
     {

@@ -183,9 +183,16 @@ struct cunusht_plan_s {
     void *d_bker_df = nullptr;
 
     // Bluestein data for the ring (phi) transform of the pointing geometry
-    int Mb = 0;
-    double2 *d_chirp = nullptr;  // [nph] e^{i pi q^2 / nph}
-    double2 *d_bker = nullptr;   // [Mb] FFT_Mb(conj chirp, circular) / Mb
+    int Mb = 0;                  // largest Bluestein length over the ring-length classes
+    double2 *d_chirp = nullptr;  // per class [N] e^{i pi q^2 / N}, concatenated
+    double2 *d_bker = nullptr;   // per class [Mb] FFT_Mb(conj chirp, circular) / Mb, concatenated
+    // ring-length classes (rings of equal pixel count share Bluestein tables);
+    // ncls <= 1: one class, described by nph_uniform / Mb / sp_ring
+    int ncls = 0;
+    int ring_buf = 0;  // largest Mb / SP over the classes (shared-memory buffer of the ring transforms)
+    long long nchirp = 0, nbker = 0;
+    int *d_ring_cls = nullptr, *d_cls_N = nullptr, *d_cls_Mb = nullptr, *d_cls_SP = nullptr;
+    long long *d_cls_coff = nullptr, *d_cls_boff = nullptr;
 
     // workspace
     double2 *d_H = nullptr;    // Legendre columns on the CC rings  [ncols][ncc]
@@ -219,3 +226,30 @@ struct cunusht_plan_s {
     double stage_ms[CUNUSHT_NSTAGE] = {0};
     long long stage_cnt[CUNUSHT_NSTAGE] = {0};
 };
+
+// Ring-length class of a ring for the Bluestein ring transforms: per-ring
+// class index and per-class length N, Bluestein length Mb, parity split SP and
+// offsets of the class's chirp / kernel tables (rcls == NULL: every ring has
+// N0, Mb0, SP0 and the tables start at 0).
+struct RingCls {
+    const int *rcls = nullptr, *N = nullptr, *Mb = nullptr, *SP = nullptr;
+    const long long *coff = nullptr, *boff = nullptr;
+    int N0 = 0, Mb0 = 0, SP0 = 1;
+};
+
+inline RingCls ring_cls_of(const cunusht_plan_s *P) {
+    RingCls rc;
+    if (P->ncls > 1) {
+        rc.rcls = P->d_ring_cls;
+        rc.N = P->d_cls_N;
+        rc.Mb = P->d_cls_Mb;
+        rc.SP = P->d_cls_SP;
+        rc.coff = P->d_cls_coff;
+        rc.boff = P->d_cls_boff;
+    } else {
+        rc.N0 = P->nph_uniform;
+        rc.Mb0 = P->Mb;
+        rc.SP0 = P->sp_ring;
+    }
+    return rc;
+}

@@ -466,86 +466,96 @@ __global__ void __launch_bounds__(FFT_TPB)
 // z_p = sum_m h_m e^{i m (phi0 + 2 pi p / N)}, p < N, for one ring per block.
 // spin 0: real output from m in [0, L] (h_{-m} = conj h_m); spin s: complex.
 // T = double (plain path) or dfl (mixed path); tables are given in T.
+// Rings may have different lengths N (HEALPix, thinned grids): each ring uses
+// the tables of its length class (RingCls).  Rings shorter than 2L + 1 alias
+// the modes: bin q of the length-N transform gathers every m = q (mod N).
 // SP = 2 (Mb > 16 x FFT_TPB): the Mb-point circular convolution is done in a
 // buffer of Mb/2 >= N points, one launch per frequency parity q (1, then 0):
 // the chirped input x (length N) gives X_{2k+q} = FFT_{Mb/2}(x_j w^{jq})_k,
 // w = e^{-2 pi i / Mb}, and the convolution at p < N is the sum over q of
-// w^{-pq} IFFT_{Mb/2}(X_{2k+q} B_{2k+q})_p, accumulated in the output.
+// w^{-pq} IFFT_{Mb/2}(X_{2k+q} B_{2k+q})_p, accumulated in the output (rings
+// with SP = 1 do all their work in the q = 0 launch).
+__device__ __forceinline__ void ring_class(const RingCls &rc, int ring, int &N, int &Mb, int &SP, long long &co,
+                                           long long &bo) {
+    if (rc.rcls) {
+        const int c = rc.rcls[ring];
+        N = rc.N[c];
+        Mb = rc.Mb[c];
+        SP = rc.SP[c];
+        co = rc.coff[c];
+        bo = rc.boff[c];
+    } else {
+        N = rc.N0;
+        Mb = rc.Mb0;
+        SP = rc.SP0;
+        co = bo = 0;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(FFT_TPB)
     k_ring_synth(const double2 *__restrict__ Hgl, int nring, int L, int spin,
-                 const double *__restrict__ phi0, const long long *__restrict__ ofs, int N, int Mb,
-                 const cplx<T> *__restrict__ chirp, const cplx<T> *__restrict__ bker,
+                 const double *__restrict__ phi0, const long long *__restrict__ ofs, RingCls rc,
+                 const cplx<T> *__restrict__ chirp_all, const cplx<T> *__restrict__ bker_all,
                  double *__restrict__ out0, double *__restrict__ out1,
-                 const cplx<T> *__restrict__ tw, int TW, long long hbs, long long obs, int SP, int q) {
+                 const cplx<T> *__restrict__ tw, int TW, long long hbs, long long obs, int q) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *buf = reinterpret_cast<C *>(smem_raw);
+    const int ring = blockIdx.x;
+    int N, Mb, SP;
+    long long co, bo;
+    ring_class(rc, ring, N, Mb, SP, co, bo);
+    if (q >= SP) return;  // odd-parity launch: split rings only
     Hgl += blockIdx.y * hbs;
     out0 += blockIdx.y * obs;
     if (out1) out1 += blockIdx.y * obs;
-    const int ring = blockIdx.x;
+    const C *chirp = chirp_all + co, *bker = bker_all + bo;
     const double ph0 = phi0[ring];
     const int Hb = Mb / SP;
     const int tstep = TW / Mb;
     const long long o = ofs[ring];
-    {
-        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = czero<T>();
-        __syncthreads();
-        if (spin == 0) {
-            for (int m = threadIdx.x; m <= L; m += blockDim.x) {
-                double2 h = Hgl[(long long)m * nring + ring];
-                if (m == 0) {
-                    buf[0] = mk<T>(cvt<T>(h.x), cvt<T>(0.0));
-                } else {
-                    if (ph0 != 0.0) {
-                        double sn, cs;
-                        sincos(m * ph0, &sn, &cs);
-                        h = cmul(h, make_double2(cs, sn));
-                    }
-                    const C hc = mk<T>(cvt<T>(h.x), cvt<T>(h.y));
-                    C vp = cmul(hc, chirp[m]);
-                    C vn = cmul(cconj(hc), chirp[N - m]);
-                    if (q) {
-                        vp = cmul(vp, twk<T>(tw, m, tstep, -1));
-                        vn = cmul(vn, twk<T>(tw, N - m, tstep, -1));
-                    }
-                    buf[m] = vp;
-                    buf[N - m] = vn;
-                }
+    for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = czero<T>();
+    __syncthreads();
+    // bin qi gathers h_m e^{i m phi0} over m = qi (mod N), m in [-L, L]
+    for (int qi = threadIdx.x; qi < N; qi += blockDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int m = qi - N * ((qi + L) / N); m <= L; m += N) {
+            double2 h;
+            if (spin == 0) {
+                const double2 hm = Hgl[(long long)(m < 0 ? -m : m) * nring + ring];
+                h = m == 0 ? make_double2(hm.x, 0.0) : (m > 0 ? hm : make_double2(hm.x, -hm.y));
+            } else {
+                h = Hgl[(long long)(m + L) * nring + ring];
             }
-        } else {
-            for (int cidx = threadIdx.x; cidx < 2 * L + 1; cidx += blockDim.x) {
-                const int m = cidx - L;
-                double2 h = Hgl[(long long)cidx * nring + ring];
-                if (ph0 != 0.0) {
-                    double sn, cs;
-                    sincos(m * ph0, &sn, &cs);
-                    h = cmul(h, make_double2(cs, sn));
-                }
-                const int qi = wrapi(m, N);
-                C v = cmul(mk<T>(cvt<T>(h.x), cvt<T>(h.y)), chirp[qi]);
-                if (q) v = cmul(v, twk<T>(tw, qi, tstep, -1));
-                buf[qi] = v;
+            if (ph0 != 0.0 && m != 0) {
+                double sn, cs;
+                sincos(m * ph0, &sn, &cs);
+                h = cmul(h, make_double2(cs, sn));
             }
+            acc.x += h.x;
+            acc.y += h.y;
         }
-        __syncthreads();
-        fft_smem<T>(buf, Hb, -1, tw, TW);
-        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
-        __syncthreads();
-        fft_smem<T>(buf, Hb, +1, tw, TW);
-        for (int p = threadIdx.x; p < N; p += blockDim.x) {
-            C y = buf[p];
-            if (q) y = cmul(y, twk<T>(tw, p, tstep, +1));
-            const C z = cmul(y, chirp[p]);
-            double z0 = to_d(z.x), z1 = to_d(z.y);
-            if (SP == 2 && q == 0) {
-                z0 += out0[o + p];
-                if (spin != 0) z1 += out1[o + p];
-            }
-            out0[o + p] = z0;
-            if (spin != 0) out1[o + p] = z1;
+        C v = cmul(mk<T>(cvt<T>(acc.x), cvt<T>(acc.y)), chirp[qi]);
+        if (q) v = cmul(v, twk<T>(tw, qi, tstep, -1));
+        buf[qi] = v;
+    }
+    __syncthreads();
+    fft_smem<T>(buf, Hb, -1, tw, TW);
+    for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
+    __syncthreads();
+    fft_smem<T>(buf, Hb, +1, tw, TW);
+    for (int p = threadIdx.x; p < N; p += blockDim.x) {
+        C y = buf[p];
+        if (q) y = cmul(y, twk<T>(tw, p, tstep, +1));
+        const C z = cmul(y, chirp[p]);
+        double z0 = to_d(z.x), z1 = to_d(z.y);
+        if (SP == 2 && q == 0) {
+            z0 += out0[o + p];
+            if (spin != 0) z1 += out1[o + p];
         }
+        out0[o + p] = z0;
+        if (spin != 0) out1[o + p] = z1;
     }
 }
 
@@ -566,51 +576,55 @@ int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st)
     return CUNUSHT_OK;
 }
 
-// h'_m = e^{-i m phi0} sum_p z'_p e^{-2 pi i m p / N} (adjoint of k_ring_synth);
-// SP = 2 as in k_ring_synth, the two parity launches summed into Hgl
+// h'_m = e^{-i m phi0} sum_p z'_p e^{-2 pi i m p / N} (adjoint of k_ring_synth;
+// a mode reads its bin m mod N, so rings shorter than 2L + 1 alias as in the
+// synthesis); SP = 2 as in k_ring_synth, the two parity launches summed into Hgl
 __global__ void __launch_bounds__(FFT_TPB)
     k_ring_adj(const double *__restrict__ in0, const double *__restrict__ in1, int nring, int L,
-               int spin, const double *__restrict__ phi0, const long long *__restrict__ ofs, int N,
-               int Mb, const double2 *__restrict__ chirp, const double2 *__restrict__ bker,
-               double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW, int SP, int q) {
+               int spin, const double *__restrict__ phi0, const long long *__restrict__ ofs, RingCls rc,
+               const double2 *__restrict__ chirp_all, const double2 *__restrict__ bker_all,
+               double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW, int q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *buf = reinterpret_cast<double2 *>(smem_raw);
     const int ring = blockIdx.x;
+    int N, Mb, SP;
+    long long co, bo;
+    ring_class(rc, ring, N, Mb, SP, co, bo);
+    if (q >= SP) return;
+    const double2 *chirp = chirp_all + co, *bker = bker_all + bo;
     const double ph0 = phi0[ring];
     const long long o = ofs[ring];
     const int Hb = Mb / SP;
     const int tstep = TW / Mb;
-    {
-        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = make_double2(0, 0);
-        __syncthreads();
-        // Bluestein on conj(z'): c_p = conj(z'_p)
-        for (int p = threadIdx.x; p < N; p += blockDim.x) {
-            const double2 z = make_double2(in0[o + p], spin ? -in1[o + p] : 0.0);
-            double2 v = cmul(z, chirp[p]);
-            if (q) v = cmul(v, twk<double>(tw, p, tstep, -1));
-            buf[p] = v;
+    for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = make_double2(0, 0);
+    __syncthreads();
+    // Bluestein on conj(z'): c_p = conj(z'_p)
+    for (int p = threadIdx.x; p < N; p += blockDim.x) {
+        const double2 z = make_double2(in0[o + p], spin ? -in1[o + p] : 0.0);
+        double2 v = cmul(z, chirp[p]);
+        if (q) v = cmul(v, twk<double>(tw, p, tstep, -1));
+        buf[p] = v;
+    }
+    __syncthreads();
+    fft_smem<double>(buf, Hb, -1, tw, TW);
+    for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
+    __syncthreads();
+    fft_smem<double>(buf, Hb, +1, tw, TW);
+    const int nc = spin == 0 ? L + 1 : 2 * L + 1;
+    for (int cidx = threadIdx.x; cidx < nc; cidx += blockDim.x) {
+        const int m = spin == 0 ? cidx : cidx - L;
+        const int qi = wrapi(m, N);
+        double2 y = buf[qi];
+        if (q) y = cmul(y, twk<double>(tw, qi, tstep, +1));
+        y = cconj(cmul(y, chirp[qi]));  // sum_p z' e^{-2 pi i m p/N}
+        double s, c;
+        sincos(m * ph0, &s, &c);
+        double2 h = cmul(y, make_double2(c, -s));
+        if (SP == 2 && q == 0) {
+            const double2 prev = Hgl[(long long)cidx * nring + ring];
+            h = make_double2(h.x + prev.x, h.y + prev.y);
         }
-        __syncthreads();
-        fft_smem<double>(buf, Hb, -1, tw, TW);
-        for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
-        __syncthreads();
-        fft_smem<double>(buf, Hb, +1, tw, TW);
-        const int nc = spin == 0 ? L + 1 : 2 * L + 1;
-        for (int cidx = threadIdx.x; cidx < nc; cidx += blockDim.x) {
-            const int m = spin == 0 ? cidx : cidx - L;
-            const int qi = wrapi(m, N);
-            double2 y = buf[qi];
-            if (q) y = cmul(y, twk<double>(tw, qi, tstep, +1));
-            y = cconj(cmul(y, chirp[qi]));  // sum_p z' e^{-2 pi i m p/N}
-            double s, c;
-            sincos(m * ph0, &s, &c);
-            double2 h = cmul(y, make_double2(c, -s));
-            if (SP == 2 && q == 0) {
-                const double2 prev = Hgl[(long long)cidx * nring + ring];
-                h = make_double2(h.x + prev.x, h.y + prev.y);
-            }
-            Hgl[(long long)cidx * nring + ring] = h;
-        }
+        Hgl[(long long)cidx * nring + ring] = h;
     }
 }
 
@@ -794,22 +808,27 @@ int phi_adj(const cunusht_plan_s *P, int spin, const void *U, void *F, cudaStrea
     return phi_adj_batch(P, 1, spin, U, 0, F, 0, st);
 }
 
+// shared-memory buffer (complex elements) of the ring transforms: the largest
+// Mb / SP over the ring-length classes
+static int ring_buffer_len(const cunusht_plan_s *P) { return P->ncls > 1 ? P->ring_buf : P->Mb / P->sp_ring; }
+
 int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,
                      double *out1, long long obs, cudaStream_t st) {
-    size_t sm = fft_smem_bytes(P->Mb / P->sp_ring, false);
+    size_t sm = fft_smem_bytes(ring_buffer_len(P), false);
     dim3 grid(P->nring, nreq);
+    const RingCls rc = ring_cls_of(P);
     for (int q = P->sp_ring - 1; q >= 0; --q) {
         if (P->fft_df && P->d_chirp_df) {
             RC_TRY(set_smem(k_ring_synth<dfl>, sm));
             k_ring_synth<dfl><<<grid, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
-                                                         P->nph_uniform, P->Mb, (const dcplx *)P->d_chirp_df,
+                                                         rc, (const dcplx *)P->d_chirp_df,
                                                          (const dcplx *)P->d_bker_df, out0, out1,
-                                                         (const dcplx *)P->d_twdf, P->TW, hbs, obs, P->sp_ring, q);
+                                                         (const dcplx *)P->d_twdf, P->TW, hbs, obs, q);
         } else {
             RC_TRY(set_smem(k_ring_synth<double>, sm));
-            k_ring_synth<double><<<grid, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
-                                                            P->nph_uniform, P->Mb, P->d_chirp, P->d_bker, out0, out1,
-                                                            P->d_tw64, P->TW, hbs, obs, P->sp_ring, q);
+            k_ring_synth<double><<<grid, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0,
+                                                            P->d_ring_ofs, rc, P->d_chirp, P->d_bker, out0, out1,
+                                                            P->d_tw64, P->TW, hbs, obs, q);
         }
         CU_LAUNCH_CHECK();
     }
@@ -823,12 +842,12 @@ int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *ou
 
 int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
                  double2 *Hgl, cudaStream_t st) {
-    size_t sm = fft_smem_bytes(P->Mb / P->sp_ring, false);
+    size_t sm = fft_smem_bytes(ring_buffer_len(P), false);
     RC_TRY(set_smem(k_ring_adj, sm));
+    const RingCls rc = ring_cls_of(P);
     for (int q = P->sp_ring - 1; q >= 0; --q) {
         k_ring_adj<<<P->nring, FFT_TPB, sm, st>>>(in0, in1, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
-                                                  P->nph_uniform, P->Mb, P->d_chirp, P->d_bker, Hgl, P->d_tw64,
-                                                  P->TW, P->sp_ring, q);
+                                                  rc, P->d_chirp, P->d_bker, Hgl, P->d_tw64, P->TW, q);
         CU_LAUNCH_CHECK();
     }
     return CUNUSHT_OK;
