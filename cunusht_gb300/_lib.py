@@ -33,6 +33,7 @@ SIGNATURES = {
     "cunusht_plan_info": (_i, [_vp, _vp, _i]),
     "cunusht_plan_set_profiling": (_i, [_vp, _i]),
     "cunusht_plan_force_split": (_i, [_vp, _i]),
+    "cunusht_plan_set_mmax": (_i, [_vp, _i]),
     "cunusht_dlm2A": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "cunusht_server_create": (_i, [ctypes.POINTER(_vp), _d, _i]),
     "cunusht_server_set_policy": (_i, [_vp, _i, _i, _i]),

@@ -176,6 +176,8 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     P->eps = eps;
     P->max_spin = max_spin;
     P->nalm = (long long)(lmax + 1) * (lmax + 2) / 2;
+    P->nalm_tab = P->nalm;
+    P->mmax = lmax;
     P->prec = precision == CUNUSHT_PREC_AUTO ? (eps > 1e-6 ? CUNUSHT_PREC_MIXED : CUNUSHT_PREC_FP64) : precision;
     P->grid_fp32 = (P->prec != CUNUSHT_PREC_FP64) && eps > 1e-6;
     P->fwd_u32 = (P->prec == CUNUSHT_PREC_MIXED) && !P->grid_fp32;
@@ -305,14 +307,14 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     }
     // recursion tables
     for (int s = 0; s <= 2; ++s) {
-        RC_TRY(dalloc(P, &P->d_coef[s], 3 * (size_t)P->nalm));
+        RC_TRY(dalloc(P, &P->d_coef[s], 3 * (size_t)P->nalm_tab));
         std::vector<double> lg(lmax + 1);
         for (int m = 0; m <= lmax; ++m) lg[m] = lg0_of(m, s);
         RC_TRY(upload(P, &P->d_lg0[s], lg));
     }
     RC_TRY(build_coef_tables(P, 0));
     if (P->prec == CUNUSHT_PREC_MIXED) {
-        for (int s = 0; s <= 2; ++s) RC_TRY(dalloc(P, &P->d_coef_df[s], 3 * (size_t)P->nalm));
+        for (int s = 0; s <= 2; ++s) RC_TRY(dalloc(P, &P->d_coef_df[s], 3 * (size_t)P->nalm_tab));
         RC_TRY(build_coef_tables_df(P, 0));
     }
     {
@@ -541,6 +543,15 @@ int cunusht_plan_info(const cunusht_plan_t *P, int64_t *info, int ninfo) {
     int n = std::min(ninfo, 10);
     for (int i = 0; i < n; ++i) info[i] = v[i];
     return n;
+}
+
+int cunusht_plan_set_mmax(cunusht_plan_t *P, int mmax) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(mmax >= 0 && mmax <= P->lmax, "mmax must be in [0, lmax = %d], got %d", P->lmax, mmax);
+    P->mmax = mmax;
+    P->nalm = (long long)(mmax + 1) * (mmax + 2) / 2 + (long long)(mmax + 1) * (P->lmax - mmax);
+    return CUNUSHT_OK;
 }
 
 int cunusht_plan_force_split(cunusht_plan_t *P, int force) {

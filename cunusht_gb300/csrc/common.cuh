@@ -136,7 +136,9 @@ struct cunusht_plan_s {
     bool fwd_u32 = false;          // forward fine grid stored FP32 (FFTs FP64), mixed-precision interp
     bool fft_df = false;           // forward FFTs (theta, phi, ring) in double-float
     double eps = 1e-7;
-    long long nalm = 0;
+    long long nalm = 0;      // alm count of the arrays the calls take: m <= mmax (healpy m-major layout)
+    long long nalm_tab = 0;  // size of the recursion tables: every (l, m <= lmax), same index as the alm
+    int mmax = 0;            // largest m of the alm arrays (cunusht_plan_set_mmax), <= lmax
 
     // pointing (output) geometry
     int nring = 0;

@@ -93,16 +93,16 @@ __global__ void k_build_coef(int L, int s, double *__restrict__ coef, long long 
 
 int build_coef_tables(cunusht_plan_s *P, cudaStream_t st) {
     for (int s = 0; s <= 2; ++s) {
-        int nb = (int)((P->nalm + 255) / 256);
-        k_build_coef<<<nb, 256, 0, st>>>(P->lmax, s, P->d_coef[s], P->nalm);
+        int nb = (int)((P->nalm_tab + 255) / 256);
+        k_build_coef<<<nb, 256, 0, st>>>(P->lmax, s, P->d_coef[s], P->nalm_tab);
         CU_LAUNCH_CHECK();
     }
     return CUNUSHT_OK;
 }
 
 int build_coef_tables_spin(const cunusht_plan_s *P, int spin, double *coef, cudaStream_t st) {
-    const int nb = (int)((P->nalm + 255) / 256);
-    k_build_coef<<<nb, 256, 0, st>>>(P->lmax, spin, coef, P->nalm);
+    const int nb = (int)((P->nalm_tab + 255) / 256);
+    k_build_coef<<<nb, 256, 0, st>>>(P->lmax, spin, coef, P->nalm_tab);
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
@@ -301,7 +301,7 @@ __global__ void k_split_coef(const double *__restrict__ c, long long n, float2 *
 
 int build_coef_tables_df(cunusht_plan_s *P, cudaStream_t st) {
     for (int s = 0; s <= 2; ++s) {
-        const long long n = 3 * P->nalm;
+        const long long n = 3 * P->nalm_tab;
         k_split_coef<<<(int)((n + 255) / 256), 256, 0, st>>>(P->d_coef[s], n, P->d_coef_df[s]);
         CU_LAUNCH_CHECK();
     }
@@ -987,7 +987,7 @@ __global__ void __launch_bounds__(LEG_TPB)
 constexpr int SP_PTS_TPB = 128;
 
 __global__ void __launch_bounds__(SP_PTS_TPB)
-    k_synth_points(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
+    k_synth_points(int L, int mmax, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
                    const double *__restrict__ coef, long long nalm, const double *__restrict__ lg0,
                    const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
                    double *__restrict__ out) {
@@ -1006,7 +1006,7 @@ __global__ void __launch_bounds__(SP_PTS_TPB)
     sincos(0.5 * th, &sh, &ch);
     const double *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
     double zr = 0.0, zi = 0.0;
-    for (int m = threadIdx.x; m <= L; m += blockDim.x) {
+    for (int m = threadIdx.x; m <= mmax; m += blockDim.x) {
         const int l0 = max(m, spin);
         const long long b = almidx(L, m, m) - m;
         double cN, pN, cS = 0.0, pS = 0.0;
@@ -1092,7 +1092,7 @@ __global__ void __launch_bounds__(SP_PTS_TPB)
 int synth_points(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C, long long npts,
                  const double *loc, int layout, const double *gamma, double *out, cudaStream_t st) {
     if (npts == 0) return CUNUSHT_OK;
-    k_synth_points<<<(unsigned)npts, SP_PTS_TPB, 0, st>>>(P->lmax, spin, G, C, P->d_coef[spin], P->nalm,
+    k_synth_points<<<(unsigned)npts, SP_PTS_TPB, 0, st>>>(P->lmax, P->mmax, spin, G, C, P->d_coef[spin], P->nalm_tab,
                                                          P->d_lg0[spin], loc, npts, layout, gamma, out);
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
@@ -1117,10 +1117,10 @@ static void launch_synth_df(const cunusht_plan_s *P, const RingPairs &R, dim3 gr
                             cudaStream_t st) {
     const int L = P->lmax;
     if (spin == 0)
-        k_leg_synth_s0_df<NB><<<grid, LEG_TPB, 0, st>>>(L, G, astride, lf, P->d_coef_df[0], P->nalm, P->d_lg0[0],
+        k_leg_synth_s0_df<NB><<<grid, LEG_TPB, 0, st>>>(L, G, astride, lf, P->d_coef_df[0], P->nalm_tab, P->d_lg0[0],
                                                         R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H, hstride, R.ld);
     else
-        k_leg_synth_spin_df<NB><<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm,
+        k_leg_synth_spin_df<NB><<<grid, LEG_TPB, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm_tab,
                                                           P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, H,
                                                           hstride, R.ld);
 }
@@ -1138,7 +1138,12 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
                        long long astride, const double *lf, bool cc, double2 *H, long long hstride, cudaStream_t st) {
     const RingPairs R = pairs_of(P, cc);
     const int L = P->lmax;
-    dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
+    if (P->mmax < L) {  // alm up to mmax only: the columns of larger |m| are zero
+        const size_t ncols = spin ? 2 * (size_t)L + 1 : (size_t)L + 1;
+        for (int r = 0; r < nreq; ++r)
+            CU_TRY(cudaMemsetAsync(H + r * hstride, 0, sizeof(double2) * ncols * R.ld, st));
+    }
+    dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, P->mmax + 1);
     if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
         for (int r0 = 0; r0 < nreq;) {
             const int left = nreq - r0;
@@ -1162,10 +1167,10 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
         const double2 *Gr = G + r * astride, *Cr = C ? C + r * astride : nullptr;
         double2 *Hr = H + r * hstride;
         if (spin == 0) {
-            k_leg_synth_s0<<<grid, LEG_TPB, 0, st>>>(L, Gr, lf, P->d_coef[0], P->nalm, P->d_lg0[0], R.npairs, R.x,
+            k_leg_synth_s0<<<grid, LEG_TPB, 0, st>>>(L, Gr, lf, P->d_coef[0], P->nalm_tab, P->d_lg0[0], R.npairs, R.x,
                                                      R.sh, R.ch, R.rn, R.rs, Hr, R.ld);
         } else {
-            k_leg_synth_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, Gr, Cr, lf, P->d_coef[spin], P->nalm,
+            k_leg_synth_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, Gr, Cr, lf, P->d_coef[spin], P->nalm_tab,
                                                        P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, Hr,
                                                        R.ld);
         }
@@ -1185,12 +1190,12 @@ static void launch_adj_df(const cunusht_plan_s *P, const RingPairs &R, dim3 grid
                           long long astride, cudaStream_t st) {
     const int L = P->lmax;
     if (spin == 0)
-        k_leg_adj_s0_df<NB><<<grid, LEG_TPB, 0, st>>>(L, H, hstride, R.ld, lf, P->d_coef_df[0], P->nalm,
+        k_leg_adj_s0_df<NB><<<grid, LEG_TPB, 0, st>>>(L, H, hstride, R.ld, lf, P->d_coef_df[0], P->nalm_tab,
                                                       P->d_lg0[0], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
                                                       (double *)G, astride);
     else
         k_leg_adj_spin_df<NB><<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, H, hstride, R.ld, lf, P->d_coef_df[spin],
-                                                        P->nalm, P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn,
+                                                        P->nalm_tab, P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn,
                                                         R.rs, (double *)G, (double *)C, astride);
 }
 
@@ -1205,7 +1210,7 @@ int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, co
         CU_TRY(cudaMemsetAsync(G + r * astride, 0, sizeof(double2) * P->nalm, st));
         if (spin > 0 && ncomp > 1) CU_TRY(cudaMemsetAsync(C + r * astride, 0, sizeof(double2) * P->nalm, st));
     }
-    dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, L + 1);
+    dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, P->mmax + 1);
     const double *lf = use_lfac ? P->d_lfac : nullptr;
     if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
         for (int r0 = 0; r0 < nreq;) {
@@ -1230,10 +1235,10 @@ int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, co
         const double2 *Hr = H + r * hstride;
         double2 *Gr = G + r * astride, *Cr = (spin > 0 && ncomp > 1) ? C + r * astride : nullptr;
         if (spin == 0) {
-            k_leg_adj_s0<<<grid, LEG_TPB, 0, st>>>(L, Hr, R.ld, lf, P->d_coef[0], P->nalm, P->d_lg0[0], R.npairs,
+            k_leg_adj_s0<<<grid, LEG_TPB, 0, st>>>(L, Hr, R.ld, lf, P->d_coef[0], P->nalm_tab, P->d_lg0[0], R.npairs,
                                                    R.x, R.sh, R.ch, R.rn, R.rs, (double *)Gr);
         } else {
-            k_leg_adj_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, Hr, R.ld, lf, P->d_coef[spin], P->nalm,
+            k_leg_adj_spin<<<grid, LEG_TPB, 0, st>>>(L, spin, ncomp, Hr, R.ld, lf, P->d_coef[spin], P->nalm_tab,
                                                      P->d_lg0[spin], R.npairs, R.x, R.sh, R.ch, R.rn, R.rs,
                                                      (double *)Gr, (double *)Cr);
         }

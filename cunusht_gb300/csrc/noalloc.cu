@@ -96,6 +96,8 @@ extern "C" int cunusht_synthesis_noalloc(int lmax, int spin, int ncomp, const vo
     cunusht_plan_s P;  // host-side view; all device pointers point into the scratch array
     P.lmax = lmax;
     P.nalm = (long long)(lmax + 1) * (lmax + 2) / 2;
+    P.nalm_tab = P.nalm;
+    P.mmax = lmax;
     P.nring = nring;
     P.npix = (long long)nring * nphi;
     P.nph_uniform = nphi;

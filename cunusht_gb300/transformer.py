@@ -73,6 +73,7 @@ class GPU_cufinufft_transformer:
         self.geominfo = geominfo_deflection
         self.geom = get_geom(geominfo_deflection)
         self.lmax = int(geominfo_deflection[1]["lmax"])
+        self.mmax = int(geominfo_deflection[1].get("mmax", self.lmax))
         self.execmode = "normal"
         self.dlm_scaled = None
         self.dclm_scaled = None
@@ -105,6 +106,8 @@ class GPU_cufinufft_transformer:
             ctypes.byref(h), self.lmax, float(epsilon), _PREC[self.precision], self.max_spin, th.size,
             th.ctypes.data, p0.ctypes.data, nph.ctypes.data, ofs.ctypes.data))
         self._plan = h
+        if self.mmax != self.lmax:
+            _lib.check(self._lib.cunusht_plan_set_mmax(h, self.mmax))
         self.epsilon = epsilon
         self.single_prec = epsilon > 1e-6
         info = (ctypes.c_int64 * 10)()
@@ -138,12 +141,22 @@ class GPU_cufinufft_transformer:
         return epsilon
 
     def _check_lm(self, lmax, mmax):
+        """lmax must be the plan's; mmax <= lmax selects the alm layout of the
+        call (healpy m-major truncated at mmax) -- one mmax for every alm of
+        the call, gclm and dlm alike.  The reference's GPU transformer only
+        takes mmax == lmax (GPU_nufft_transformer.py:389-390)."""
         assert lmax == self.lmax, "Expected lmax={}. lmax must be same as during init, but is {}".format(self.lmax, lmax)
-        assert mmax == self.lmax, "Expected mmax={}. mmax must be same as lmax during init, but is {}".format(self.lmax, mmax)
+        mmax = self.lmax if mmax is None else int(mmax)
+        assert 0 <= mmax <= self.lmax, "mmax must be in [0, lmax={}], got {}".format(self.lmax, mmax)
+        if mmax != self.mmax:
+            self.mmax = mmax
+            if self._plan is not None:
+                _lib.check(self._lib.cunusht_plan_set_mmax(self._plan, mmax))
+                self.dlm_scaled = None  # the pointing cache was for another layout
 
     @property
     def nalm(self) -> int:
-        return Alm.getsize(self.lmax, self.lmax)
+        return Alm.getsize(self.lmax, self.mmax)
 
     def npix(self) -> int:
         return self.geom.npix()
@@ -223,7 +236,7 @@ class GPU_cufinufft_transformer:
         """Deflected (theta', phi') of every pixel, (2, npix) float64
         (GPU_nufft_transformer.py:344-351); the rotation angle is kept in
         ``self.gamma``."""
-        assert mmax_dlm == self.lmax, (mmax_dlm, self.lmax)
+        self._check_lm(self.lmax, mmax_dlm)
         if self._plan is None:
             self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
         d, _, ddt = self._alm_in(dlm_scaled, "dlm_scaled", 0)
@@ -403,7 +416,7 @@ class GPU_cufinufft_transformer:
         if not same:
             self.dlm_scaled = d.clone()
             self.dclm_scaled = c.clone() if c is not None else None
-            self.ptg = self.dlm2pointing(d, lmax, verbose, dclm_scaled=c)
+            self.ptg = self.dlm2pointing(d, self.mmax, verbose, dclm_scaled=c)
         return self.ptg, self.gamma
 
     def _timed(self, name, fn):

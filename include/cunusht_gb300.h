@@ -92,6 +92,16 @@ int cunusht_plan_set_profiling(cunusht_plan_t *plan, int enable);
 int cunusht_plan_stage_times(cunusht_plan_t *plan, double *ms, int64_t *count, int nstage);
 
 /*
+ * Largest m of the alm arrays the plan's calls take and return (healpy
+ * m-major layout truncated at mmax, nalm = (mmax+1)(mmax+2)/2 +
+ * (mmax+1)(lmax-mmax)); default lmax.  One value for every alm argument of
+ * the plan (gclm, dlm_scaled, outputs).  The reference's GPU transformer
+ * requires mmax == lmax (GPU_nufft_transformer.py:389-390); its CPU paths and
+ * geometries take mmax <= lmax.
+ */
+int cunusht_plan_set_mmax(cunusht_plan_t *plan, int mmax);
+
+/*
  * Transforms longer than 8192 points (theta / phi passes above lmax 2047,
  * Bluestein ring transforms above 4096 pixels per ring) run as two
  * half-length transforms split by output parity.  force = 1 selects that

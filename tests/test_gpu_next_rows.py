@@ -72,3 +72,46 @@ def test_gclm2lenpixs_is_exact_and_matches_lensed_map(built_lib, spin):
     assert np.max(np.abs(got - ref)) < 1e-12 * scale              # exact direct sum
     sel = lenmap[:, pixs] if spin else lenmap[pixs]
     assert np.max(np.abs(sel - got)) < 1e-9 * scale               # the nuFFT map at eps 1e-10
+
+
+@pytest.mark.parametrize("precision,eps", [("fp64", 1e-10), ("mixed", 1e-7)])
+@pytest.mark.parametrize("spin", [0, 2])
+def test_mmax_below_lmax(built_lib, precision, eps, spin):
+    """alm truncated at mmax < lmax (healpy layout) give the lensed map, its
+    adjoint and the exact point synthesis of the full layout with the m > mmax
+    coefficients zeroed."""
+    import cunusht_gb300 as cu
+    from cunusht_gb300.utils import Alm
+    lmax, mmax = 127, 90
+    T = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=eps, precision=precision, max_spin=2)
+    gclm, dls = orc.make_inputs(lmax, spin, seed=21)
+    n = Alm.getsize(lmax, mmax)
+    g = gclm.copy()
+    g[:, n:] = 0.0
+    d = dls[0].copy()
+    d[n:] = 0.0
+    gf = torch.as_tensor(g if spin else g[0], device="cuda")
+    gt = torch.as_tensor(g[:, :n] if spin else g[0, :n], device="cuda")
+    df, dt = torch.as_tensor(d, device="cuda"), torch.as_tensor(d[:n], device="cuda")
+    ref = T.gclm2lenmap(gf, lmax, lmax, dlm_scaled=df, spin=spin, verbose=0).clone()
+    got = T.gclm2lenmap(gt, lmax, mmax, dlm_scaled=dt, spin=spin, verbose=0)
+    assert T.nalm == n
+    scale = float(torch.max(torch.abs(ref)))
+    assert float(torch.max(torch.abs(got - ref))) <= 1e-12 * scale
+    # adjoint: the truncated output is the head of the full one
+    y = torch.as_tensor(np.random.default_rng(4).standard_normal(tuple(ref.shape)), device="cuda")
+    a_t = T.lenmap2gclm(y, dt, None, lmax, mmax, spin=spin, verbose=0).cpu().numpy()
+    a_f = T.lenmap2gclm(y, df, None, lmax, lmax, spin=spin, verbose=0).cpu().numpy()
+    tol = 1e-12 if precision == "fp64" else 1e-9
+    assert np.max(np.abs(a_t - a_f[..., :n])) <= tol * np.max(np.abs(a_f))
+    # exact point synthesis with mmax
+    pix = np.random.default_rng(5).choice(T.npix(), 16, replace=False)
+    T.gclm2lenmap(gt, lmax, mmax, dlm_scaled=dt, spin=spin, verbose=0)
+    sp = T.gclm2lenpixs(gt, mmax, spin, pix)
+    sp = np.stack([x.cpu().numpy() for x in sp]) if spin else sp.cpu().numpy()
+    ptg = T.ptg.cpu().numpy()
+    ex = oracle.synth_points_c(lmax, spin, g if spin else g[0], ptg[0, pix], ptg[1, pix])
+    if spin:
+        z = (ex[0] + 1j * ex[1]) * np.exp(1j * spin * T.gamma.cpu().numpy()[pix])
+        ex = np.stack([z.real, z.imag])
+    assert np.max(np.abs(sp - ex)) < 1e-12 * np.max(np.abs(ex))
