@@ -39,9 +39,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7 (served mixed vs plain FP64); p99 ms"
-# DRAM bytes (read + write) per launch from one ncu capture at lmax 2047
-# (profiles/leg_synth_spin_df_l2047.md)
-LEG_TRAFFIC = {"leg_synth": 196.3e6, "ptg_leg": 161.1e6}
+# DRAM bytes (read + write) per launch of 4 requests from one ncu capture at
+# lmax 2047 (profiles/launches_served_l2047_spin2_mixed.md)
+LEG_TRAFFIC_B4 = {"leg_synth": 796.0e6, "ptg_leg": 662.8e6}
 
 
 def parse():
@@ -371,14 +371,15 @@ def main():
             # double-float Legendre on the FP32 pipe: 152 SMs x 128 lanes x 2 flop x max SM clock
             mhz = peaks.get("sm_max_mhz", 2070.0)
             peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-            tr = LEG_TRAFFIC.get(dom)
+            tr = LEG_TRAFFIC_B4.get(dom)
             roof = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                    "traffic": tr * B if tr else None, "kernel": dom,
+                    "traffic": tr * B / 4 if tr else None, "kernel": dom,
                     "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; "
                                    "achieved counts algorithmic flops only (8 per l,m,ring,component), "
                                    "the double-float arithmetic issues ~15x more: ncu FMA-pipe "
                                    "utilisation 73 %, issue slots 91 % (profiles/leg_synth_spin_df_l2047.md); "
-                                   "traffic scaled from the single-request capture by the requests per launch"}
+                                   "traffic measured per launch of 4 requests "
+                                   "(profiles/launches_served_l2047_spin2_mixed.md), scaled to the batch size"}
     stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
                        "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
     for s, v in stage_table.items():
