@@ -237,6 +237,7 @@ struct RingCls {
     const int *rcls = nullptr, *N = nullptr, *Mb = nullptr, *SP = nullptr;
     const long long *coff = nullptr, *boff = nullptr;
     int N0 = 0, Mb0 = 0, SP0 = 1;
+    int Hmax = 0;  // largest Mb / SP over the rings (shared buffer and twiddle-table length)
 };
 
 inline RingCls ring_cls_of(const cunusht_plan_s *P) {
@@ -248,10 +249,12 @@ inline RingCls ring_cls_of(const cunusht_plan_s *P) {
         rc.SP = P->d_cls_SP;
         rc.coff = P->d_cls_coff;
         rc.boff = P->d_cls_boff;
+        rc.Hmax = P->ring_buf;
     } else {
         rc.N0 = P->nph_uniform;
         rc.Mb0 = P->Mb;
         rc.SP0 = P->sp_ring;
+        rc.Hmax = P->Mb / P->sp_ring;
     }
     return rc;
 }

@@ -100,9 +100,22 @@ template <typename T, int RAD> __device__ __forceinline__ void dftR(cplx<T> *v, 
 // (NB butterflies of R points, E = NB R, all compile-time), so the butterfly
 // data stays in registers: loads, barrier, twiddle + R-point DFT, stores,
 // barrier.
+// e^{-2 pi i t / M} for 0 <= t < M from the quarter table S[u] = e^{-2 pi i u / M},
+// u <= M/4, held in shared memory: t = q M/4 + u gives (-i)^q S[u]
+template <typename T>
+__device__ __forceinline__ cplx<T> tw_quarter(const cplx<T> *S, int t, int Q) {
+    const int q = t / Q, u = t - q * Q;
+    const cplx<T> w = S[u];
+    T x = (q & 1) ? w.y : w.x;
+    T y = (q & 1) ? w.x : w.y;
+    if (q & 2) x = -x;
+    if (q == 1 || q == 2) y = -y;
+    return mk<T>(x, y);
+}
+
 template <typename T, int R, int NB>
 __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
-                                           const cplx<T> *__restrict__ tw, int twstride, int nthr) {
+                                           const cplx<T> *__restrict__ stw, int M, int nthr) {
     using C = cplx<T>;
     const int nb = N / R;  // == nthr * NB
     const bool act = (int)threadIdx.x < nthr;
@@ -117,7 +130,8 @@ __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
     }
     __syncthreads();
     if (act) {
-        const int tstep = (N / (Ns * R)) * twstride;
+        const int tstep = M / (Ns * R);
+        const int Q = M >> 2;
 #pragma unroll
         for (int c = 0; c < NB; ++c) {
             const int j = threadIdx.x + c * nthr;
@@ -125,7 +139,7 @@ __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
             if (Ns > 1) {
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    C w = tw[r * k * tstep];
+                    C w = tw_quarter<T>(stw, r * k * tstep, Q);
                     if (dir > 0) w.y = -w.y;
                     v[c][r] = cmul(v[c][r], w);
                 }
@@ -145,23 +159,22 @@ __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
 // Whole transform with E elements per thread; radices up to min(E, RMAX) with
 // RMAX = 16 for float and 8 for double / double-float (register budget).
 template <typename T, int E, int LMAX = (std::is_same<T, float>::value ? 4 : 3)>
-__device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
+__device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ stw, int M) {
     constexpr int LE = (E >= 16) ? 4 : (E >= 8) ? 3 : (E >= 4) ? 2 : 1;
     constexpr int LR = LE < LMAX ? LE : LMAX;
     const int nthr = N / E;
-    const int twstride = TW / N;
     int rem = __ffs(N) - 1;
     int Ns = 1;
     while (rem > 0) {
         const int r = rem < LR ? rem : LR;
         if (r == 4) {
-            if constexpr (LR >= 4) fft_pass_e<T, 16, E / 16>(buf, N, Ns, dir, tw, twstride, nthr);
+            if constexpr (LR >= 4) fft_pass_e<T, 16, E / 16>(buf, N, Ns, dir, stw, M, nthr);
         } else if (r == 3) {
-            if constexpr (LR >= 3) fft_pass_e<T, 8, E / 8>(buf, N, Ns, dir, tw, twstride, nthr);
+            if constexpr (LR >= 3) fft_pass_e<T, 8, E / 8>(buf, N, Ns, dir, stw, M, nthr);
         } else if (r == 2) {
-            if constexpr (LR >= 2) fft_pass_e<T, 4, E / 4>(buf, N, Ns, dir, tw, twstride, nthr);
+            if constexpr (LR >= 2) fft_pass_e<T, 4, E / 4>(buf, N, Ns, dir, stw, M, nthr);
         } else {
-            fft_pass_e<T, 2, E / 2>(buf, N, Ns, dir, tw, twstride, nthr);
+            fft_pass_e<T, 2, E / 2>(buf, N, Ns, dir, stw, M, nthr);
         }
         Ns <<= r;
         rem -= r;
@@ -170,27 +183,43 @@ __device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const c
 
 // In-place FFT of length N (power of two, 2 <= N <= 16 blockDim) in shared
 // memory.  dir = -1: X_k = sum_n x_n e^{-2 pi i nk/N}; dir = +1: the
-// unnormalised inverse.  tw[t] = e^{-2 pi i t / TW}, N | TW.  Longer
-// transforms are split by output parity in the callers (sp_* of the plan).
+// unnormalised inverse.  stw: the quarter twiddle table of length M >= N in
+// shared memory (load_twiddles).  Longer transforms are split by output parity
+// in the callers (sp_* of the plan).
 template <typename T>
-__device__ __forceinline__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ tw, int TW) {
+__device__ __forceinline__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ stw, int M) {
     const int B = blockDim.x;
     if (N > 8 * B) {
         // 16 elements per thread: radix <= 8 for float, <= 4 for double and
         // double-float keeps the pass within the 128-register budget of a
         // 512-thread block
-        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 16, 3>(buf, N, dir, tw, TW);
-        else fft_smem_e<T, 16, 2>(buf, N, dir, tw, TW);
+        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 16, 3>(buf, N, dir, stw, M);
+        else fft_smem_e<T, 16, 2>(buf, N, dir, stw, M);
     } else if (N > 4 * B) {
-        fft_smem_e<T, 8, 3>(buf, N, dir, tw, TW);
+        fft_smem_e<T, 8, 3>(buf, N, dir, stw, M);
     } else if (N > 2 * B) {
-        fft_smem_e<T, 4>(buf, N, dir, tw, TW);
+        fft_smem_e<T, 4>(buf, N, dir, stw, M);
     } else {
-        fft_smem_e<T, 2>(buf, N, dir, tw, TW);
+        fft_smem_e<T, 2>(buf, N, dir, stw, M);
     }
 }
 
-size_t fft_smem_bytes(int N, bool f32) { return (size_t)N * (f32 ? sizeof(float2) : sizeof(double2)); }
+// Shared memory of a transform kernel with an N-element buffer: the buffer
+// plus its quarter twiddle table (N/4 + 1 entries).  The twiddles are read in
+// every butterfly; from global memory they were L2-latency loads (the data
+// buffer leaves little L1), the first stall reason of these kernels.
+size_t fft_smem_bytes(int N, bool f32) { return (size_t)(N + N / 4 + 1) * (f32 ? sizeof(float2) : sizeof(double2)); }
+
+// S[u] = e^{-2 pi i u / M} for u <= M/4 from the plan's table tw[t] =
+// e^{-2 pi i t / TW} (M | TW), placed after the M-element data buffer.  The
+// first transform pass reads it only after a block barrier.
+template <typename T>
+__device__ __forceinline__ cplx<T> *load_twiddles(cplx<T> *buf, int M, const cplx<T> *__restrict__ tw, int TW) {
+    cplx<T> *S = buf + M;
+    const int st = TW / M;
+    for (int u = threadIdx.x; u <= M / 4; u += blockDim.x) S[u] = tw[u * st];
+    return S;
+}
 
 template <typename T> __device__ __forceinline__ cplx<T> czero() { return mk<T>(cvt<T>(0.0), cvt<T>(0.0)); }
 
@@ -223,6 +252,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                 const cplx<T> *__restrict__ tw, int TW, long long hbs, long long fbs, int SP) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    const int MTW = Ntf / SP;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     H += blockIdx.y * hbs;  // request of a batch
     F += blockIdx.y * fbs;
     const int q = blockIdx.z;
@@ -239,7 +270,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         buf[k] = mk<T>(cvt<T>(v.x * s), cvt<T>(v.y * s));
     }
     __syncthreads();
-    fft_smem<T>(buf, Nt, -1, tw, TW);
+    fft_smem<T>(buf, Nt, -1, stw, MTW);
     if (SP == 1) {
         for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
             const int src = Nt - 1 - i;  // kappa = -(i+1)
@@ -258,7 +289,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         }
     }
     __syncthreads();
-    fft_smem<T>(buf, Ntf / SP, +1, tw, TW);
+    fft_smem<T>(buf, Ntf / SP, +1, stw, MTW);
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
         const int n = wrapi(r + n_lo, Ntf);
         if (SP == 1) F[(long long)r * ncols + c] = buf[n];
@@ -279,6 +310,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                 long long hbs, long long sbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    const int MTW = Ntf / SP;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     F += blockIdx.y * fbs;  // request of a batch
     H += blockIdx.y * hbs;
     S += blockIdx.y * sbs;
@@ -296,7 +329,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         else if ((n & 1) == q) buf[n >> 1] = F[(long long)r * ncols + c];
     }
     __syncthreads();
-    fft_smem<T>(buf, Nb, -1, tw, TW);
+    fft_smem<T>(buf, Nb, -1, stw, MTW);
     if (SP == 1) {
         for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
             const int dst = Nt - 1 - i;  // kappa = -(i+1)
@@ -316,7 +349,7 @@ __global__ void __launch_bounds__(FFT_TPB)
             buf[i] = cscale(cadd(buf[i], sc[i]), cvt<T>(Dth[i] * dm));  // Dth[half] = 0
     }
     __syncthreads();
-    fft_smem<T>(buf, Nt, +1, tw, TW);
+    fft_smem<T>(buf, Nt, +1, stw, MTW);
     double2 *col = H + (long long)c * ldH;
     for (int k = threadIdx.x; k <= half; k += blockDim.x) {
         cplx<T> v = buf[k];
@@ -337,6 +370,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                  const cplx<T> *__restrict__ tw, int TW, long long fbs, long long ubs, int SP) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    const int MTW = Npf / SP;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     F += blockIdx.y * fbs;
     U += blockIdx.y * ubs;
     const int q = blockIdx.z;
@@ -363,7 +398,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         }
     }
     __syncthreads();
-    fft_smem<T>(buf, Nb, +1, tw, TW);
+    fft_smem<T>(buf, Nb, +1, stw, MTW);
     TU *u1 = U + (long long)r1 * Npf;
     TU *u2 = U + (long long)r2 * Npf;
     for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
@@ -380,6 +415,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                  const cplx<T> *__restrict__ tw, int TW, int SP, int q, long long ubs, long long fbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    const int MTW = Npf / SP;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     U += blockIdx.y * ubs;
     F += blockIdx.y * fbs;
     const int r1 = 2 * blockIdx.x, r2 = r1 + 1;
@@ -393,7 +430,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         buf[j] = mk<T>(u1[p], has2 ? u2[p] : cvt<T>(0.0));
     }
     __syncthreads();
-    fft_smem<T>(buf, Nb, -1, tw, TW);
+    fft_smem<T>(buf, Nb, -1, stw, MTW);
     for (int m = threadIdx.x; m < ncols; m += blockDim.x) {
         cplx<T> zm = buf[m];
         cplx<T> zn = buf[m == 0 ? 0 : Nb - m];
@@ -420,6 +457,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                    const cplx<T> *__restrict__ tw, int TW, long long fbs, long long ubs, int SP) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    const int MTW = Npf / SP;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     F += blockIdx.y * fbs;
     U += blockIdx.y * ubs;
     const int q = blockIdx.z;
@@ -435,7 +474,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         buf[wrapi(c - L, Nb)] = v;
     }
     __syncthreads();
-    fft_smem<T>(buf, Nb, +1, tw, TW);
+    fft_smem<T>(buf, Nb, +1, stw, MTW);
     for (int j = threadIdx.x; j < Nb; j += blockDim.x) U[(long long)r * Npf + SP * j + q] = ccast<TU>(buf[j]);
 }
 
@@ -445,6 +484,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                    const cplx<T> *__restrict__ tw, int TW, int SP, int q, long long ubs, long long fbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
+    const int MTW = Npf / SP;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     U += blockIdx.y * ubs;
     F += blockIdx.y * fbs;
     const int r = blockIdx.x;
@@ -453,7 +494,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     const int tstep = TW / Npf;
     for (int j = threadIdx.x; j < Nb; j += blockDim.x) buf[j] = U[(long long)r * Npf + SP * j + q];
     __syncthreads();
-    fft_smem<T>(buf, Nb, -1, tw, TW);
+    fft_smem<T>(buf, Nb, -1, stw, MTW);
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
         cplx<T> v = buf[wrapi(c - L, Nb)];
         if (q) v = cmul(v, twk<T>(tw, c - L, tstep, -1));
@@ -502,6 +543,8 @@ __global__ void __launch_bounds__(FFT_TPB)
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C *buf = reinterpret_cast<C *>(smem_raw);
+    const int MTW = rc.Hmax;  // length of the quarter twiddle table
+    const cplx<T> *stw = load_twiddles<T>(buf, MTW, tw, TW);
     const int ring = blockIdx.x;
     int N, Mb, SP;
     long long co, bo;
@@ -541,10 +584,10 @@ __global__ void __launch_bounds__(FFT_TPB)
         buf[qi] = v;
     }
     __syncthreads();
-    fft_smem<T>(buf, Hb, -1, tw, TW);
+    fft_smem<T>(buf, Hb, -1, stw, MTW);
     for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
     __syncthreads();
-    fft_smem<T>(buf, Hb, +1, tw, TW);
+    fft_smem<T>(buf, Hb, +1, stw, MTW);
     for (int p = threadIdx.x; p < N; p += blockDim.x) {
         C y = buf[p];
         if (q) y = cmul(y, twk<T>(tw, p, tstep, +1));
@@ -586,6 +629,8 @@ __global__ void __launch_bounds__(FFT_TPB)
                double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW, int q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *buf = reinterpret_cast<double2 *>(smem_raw);
+    const int MTW = rc.Hmax;  // length of the quarter twiddle table
+    const cplx<double> *stw = load_twiddles<double>(buf, MTW, tw, TW);
     const int ring = blockIdx.x;
     int N, Mb, SP;
     long long co, bo;
@@ -606,10 +651,10 @@ __global__ void __launch_bounds__(FFT_TPB)
         buf[p] = v;
     }
     __syncthreads();
-    fft_smem<double>(buf, Hb, -1, tw, TW);
+    fft_smem<double>(buf, Hb, -1, stw, MTW);
     for (int i = threadIdx.x; i < Hb; i += blockDim.x) buf[i] = cmul(buf[i], bker[SP * i + q]);
     __syncthreads();
-    fft_smem<double>(buf, Hb, +1, tw, TW);
+    fft_smem<double>(buf, Hb, +1, stw, MTW);
     const int nc = spin == 0 ? L + 1 : 2 * L + 1;
     for (int cidx = threadIdx.x; cidx < nc; cidx += blockDim.x) {
         const int m = spin == 0 ? cidx : cidx - L;
@@ -633,9 +678,11 @@ __global__ void __launch_bounds__(FFT_TPB)
     k_fft_global(double2 *data, int N, int dir, const double2 *__restrict__ tw, int TW) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *buf = reinterpret_cast<double2 *>(smem_raw);
+    const int MTW = N;  // length of the quarter twiddle table
+    const cplx<double> *stw = load_twiddles<double>(buf, MTW, tw, TW);
     for (int i = threadIdx.x; i < N; i += blockDim.x) buf[i] = data[i];
     __syncthreads();
-    fft_smem<double>(buf, N, dir, tw, TW);
+    fft_smem<double>(buf, N, dir, stw, MTW);
     for (int i = threadIdx.x; i < N; i += blockDim.x) data[i] = buf[i];
 }
 
