@@ -34,6 +34,9 @@ SIGNATURES = {
     "cunusht_plan_set_profiling": (_i, [_vp, _i]),
     "cunusht_plan_force_split": (_i, [_vp, _i]),
     "cunusht_plan_set_mmax": (_i, [_vp, _i]),
+    "cunusht_plan_set_tensor_cores": (_i, [_vp, _i]),
+    "cunusht_plan_device_status": (_i, [_vp, ctypes.POINTER(_i)]),
+    "cunusht_tc_selftest": (_i, [_i, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_i)]),
     "cunusht_dlm2A": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "cunusht_server_create": (_i, [ctypes.POINTER(_vp), _d, _i]),
     "cunusht_server_set_policy": (_i, [_vp, _i, _i, _i]),

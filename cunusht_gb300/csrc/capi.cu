@@ -121,7 +121,7 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_ring_cls, P->d_cls_N, P->d_cls_Mb, P->d_cls_SP,
                     P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
-                    P->d_glmapb, P->d_ptgb, P->d_gamb};
+                    P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : P->evt_pool) {
@@ -317,6 +317,8 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         for (int s = 0; s <= 2; ++s) RC_TRY(dalloc(P, &P->d_coef_df[s], 3 * (size_t)P->nalm_tab));
         RC_TRY(build_coef_tables_df(P, 0));
     }
+    RC_TRY(dalloc(P, &P->d_status, 1));
+    CU_TRY(cudaMemset(P->d_status, 0, sizeof(int)));
     {
         std::vector<double> lf(lmax + 1);
         for (int l = 0; l <= lmax; ++l) lf[l] = std::sqrt((double)l * (l + 1.0));
@@ -562,6 +564,34 @@ int cunusht_plan_force_split(cunusht_plan_t *P, int force) {
     P->sp_phi = (force || P->Npf > emax) ? 2 : 1;
     P->sp_ring = (force || P->Mb > emax) ? 2 : 1;
     return CUNUSHT_OK;
+}
+
+int cunusht_plan_set_tensor_cores(cunusht_plan_t *P, int enable) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    P->use_tc = enable != 0;
+    return CUNUSHT_OK;
+}
+
+int cunusht_plan_device_status(cunusht_plan_t *P, int *status) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(status != nullptr, "status must not be NULL");
+    CU_TRY(cudaDeviceSynchronize());
+    int h = 0;
+    CU_TRY(cudaMemcpy(&h, P->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    CU_TRY(cudaMemset(P->d_status, 0, sizeof(int)));
+    *status = h;
+    return CUNUSHT_OK;
+}
+
+int cunusht_tc_selftest(int n, int reps, int mode, double *maxerr, int *timeout) {
+    clear_error();
+    ARG_CHECK(maxerr != nullptr && timeout != nullptr, "maxerr and timeout must not be NULL");
+    ARG_CHECK(n == 16 || n == 32 || n == 64, "n must be 16, 32 or 64, got %d", n);
+    ARG_CHECK(reps >= 1 && reps <= 16, "reps must be in [1, 16], got %d", reps);
+    ARG_CHECK(mode >= 0 && mode <= 2, "mode must be 0, 1 or 2, got %d", mode);
+    return tc_selftest(n, reps, mode, maxerr, timeout);
 }
 
 int cunusht_plan_set_profiling(cunusht_plan_t *P, int enable) {

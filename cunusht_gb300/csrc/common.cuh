@@ -175,6 +175,8 @@ struct cunusht_plan_s {
     double *d_lg0[3] = {nullptr, nullptr, nullptr};  // per m: log2 start normalisation
     double *d_lfac = nullptr;                        // sqrt(l(l+1)), l = 0..L
     float2 *d_coef_df[3] = {nullptr, nullptr, nullptr};  // the same tables as (hi, lo) FP32 pairs
+    bool use_tc = true;       // mixed precision: spin > 0 Legendre synthesis on the tensor cores
+    int *d_status = nullptr;  // device status word: bit 0 = a bounded wait of a tensor-core kernel ran out
 
     // FFT twiddles e^{-2 pi i t / TW}
     int TW = 0;

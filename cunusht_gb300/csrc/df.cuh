@@ -81,6 +81,21 @@ struct kahan {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// Compensated FP32 sum with the exact error of every addition (Knuth's
+// TwoSum) collected in c: value = s + c, error O(u^2) of the addends (Ogita,
+// Rump and Oishi 2005, Sum2).  Kahan's form above rounds the corrected addend
+// and so keeps a relative error u per addend.
+struct sum2 {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        const float bb = t - s;
+        c += (s - (t - bb)) + (x - bb);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // a * lam with both operands as df, rounded once to FP32
 __device__ __forceinline__ float df_prod(float ah, float al, dfl lam) {
     return fmaf(ah, lam.h, fmaf(al, lam.h, ah * lam.l));
@@ -112,5 +127,42 @@ inline dfl df_from_host(double x) {
     r.l = (float)(x - (double)r.h);
     return r;
 }
+
+// Start of the double-float Wigner-d recursion at l0 = max(m, s):
+// (-1)^m 2^lg0 sh^(m+s) ch^|m-s| as an FP32-range mantissa (cur) times 2^e,
+// e a non-positive multiple of 96; prev = 0.  Values below 2^-40 start with
+// e < 0 and are not accumulated until REC_RESCALE_DF has brought e to 0.
+__device__ __forceinline__ void rec_start_df(double lg0, int m, int s, double sh, double ch, dfl &cur,
+                                             dfl &prev, int &e) {
+    prev.h = prev.l = 0.f;
+    double lg = lg0;
+    bool zero = false;
+    if (m + s > 0) {
+        if (sh <= 0.0) zero = true;
+        else lg += (double)(m + s) * log2(sh);
+    }
+    if (m != s) {
+        if (ch <= 0.0) zero = true;
+        else lg += (double)abs(m - s) * log2(ch);
+    }
+    if (zero) {
+        cur.h = cur.l = 0.f;
+        e = 0;
+        return;
+    }
+    int k = 0;
+    if (lg < -40.0) k = (int)ceil((-40.0 - lg) / 96.0);
+    e = -96 * k;
+    double v = exp2(lg + 96.0 * (double)k);
+    if (m & 1) v = -v;
+    cur = df_from(v);
+}
+
+#define REC_RESCALE_DF(cur, prev, e)                                                     \
+    if ((e) < 0 && fabsf((cur).h) > 0x1p40f) {                                          \
+        (cur) = df_scale((cur), 0x1p-96f);                                               \
+        (prev) = df_scale((prev), 0x1p-96f);                                             \
+        (e) += 96;                                                                       \
+    }
 
 }  // namespace cunusht

@@ -258,39 +258,6 @@ __global__ void __launch_bounds__(LEG_TPB)
 // formed from the hi/lo parts, rounded once to FP32 and added with Kahan
 // compensation.  The start mantissa is kept in FP32 range with an exponent in
 // steps of 96 (values below 2^-56 are not accumulated).
-__device__ __forceinline__ void rec_start_df(double lg0, int m, int s, double sh, double ch, dfl &cur,
-                                             dfl &prev, int &e) {
-    prev.h = prev.l = 0.f;
-    double lg = lg0;
-    bool zero = false;
-    if (m + s > 0) {
-        if (sh <= 0.0) zero = true;
-        else lg += (double)(m + s) * log2(sh);
-    }
-    if (m != s) {
-        if (ch <= 0.0) zero = true;
-        else lg += (double)abs(m - s) * log2(ch);
-    }
-    if (zero) {
-        cur.h = cur.l = 0.f;
-        e = 0;
-        return;
-    }
-    int k = 0;
-    if (lg < -40.0) k = (int)ceil((-40.0 - lg) / 96.0);
-    e = -96 * k;
-    double v = exp2(lg + 96.0 * (double)k);
-    if (m & 1) v = -v;
-    cur = df_from(v);
-}
-
-#define REC_RESCALE_DF(cur, prev, e)                                                     \
-    if ((e) < 0 && fabsf((cur).h) > 0x1p40f) {                                          \
-        (cur) = df_scale((cur), 0x1p-96f);                                               \
-        (prev) = df_scale((prev), 0x1p-96f);                                             \
-        (e) += 96;                                                                       \
-    }
-
 __global__ void k_split_coef(const double *__restrict__ c, long long n, float2 *__restrict__ out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1125,6 +1092,19 @@ static void launch_synth_df(const cunusht_plan_s *P, const RingPairs &R, dim3 gr
                                                           hstride, R.ld);
 }
 
+int leg_synth_spin_df_pairs(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
+                            const double *ch, const int *rn, const int *rs, int ld, int spin, const double2 *G,
+                            const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
+                            cudaStream_t st) {
+    const RingPairs R{npairs, x, sh, ch, rn, rs, ld};
+    const dim3 grid((npairs + LEG_TPB - 1) / LEG_TPB, P->mmax + 1);
+    if (nb == 4) launch_synth_df<4>(P, R, grid, spin, G, C, astride, lf, H, hstride, st);
+    else if (nb == 2) launch_synth_df<2>(P, R, grid, spin, G, C, astride, lf, H, hstride, st);
+    else launch_synth_df<1>(P, R, grid, spin, G, C, astride, lf, H, hstride, st);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
 // nreq requests (alm at G + r * astride, columns at H + r * hstride); the
 // mixed-precision kernels process up to four requests per launch with one
 // shared recursion, the FP64 kernels one request per launch.
@@ -1149,6 +1129,13 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
             const int left = nreq - r0;
             const double2 *Gr = G + r0 * astride, *Cr = C ? C + r0 * astride : nullptr;
             double2 *Hr = H + r0 * hstride;
+            if (spin > 0 && P->use_tc) {
+                const int nb = left >= 4 ? 4 : left >= 2 ? 2 : 1;
+                RC_TRY(leg_synth_spin_tc(P, nb, R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, R.ld, spin, Gr, Cr, astride,
+                                         lf, Hr, hstride, st));
+                r0 += nb;
+                continue;
+            }
             if (left >= 4) {
                 launch_synth_df<4>(P, R, grid, spin, Gr, Cr, astride, lf, Hr, hstride, st);
                 r0 += 4;

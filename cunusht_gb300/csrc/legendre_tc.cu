@@ -1,0 +1,586 @@
+// Legendre synthesis on the tensor cores (tcgen05), mixed-precision path.
+//
+// For one order m the synthesis is a product of two matrices,
+//     h(ring, col) = sum_l lambda_l(theta_ring) a(l, col),
+// rings x l times l x cols, with cols = (A re, A im, B re, B im) per request
+// (the spin-s combinations of the reference's SHTns synthesis,
+// cunusht/sht/GPU_sht_transformer.py:56-62 and :88-97; A = G - iC pairs with
+// +s at theta, B with -s, whose values at pi - theta are the +s functions at
+// theta).  The recursion in l stays on the CUDA cores in double-float
+// (legendre.cu); the contraction goes to the tensor cores exactly:
+//
+//   lambda = 2^El 2^-7 (d0 + d1 2^-8 + d2 2^-16 + d3 2^-24),  |d_i| <= 128
+//   a      = 2^Ea 2^-7 (t0 + t1 2^-8 + t2 2^-16 + t3 2^-24),  |t_j| <= 128
+//
+// with integer digits (exact in bf16), El fixed per l-window from the bound
+// |lambda_l| <= sqrt((2l+1)/(4 pi)) and Ea per window and column from the
+// largest |a|.  Digit products of equal weight g = i + j (g = 0..6, all 16
+// products: the low digits span the whole +-128, so dropping g >= 4 would
+// cost 2^-27 of a typical product) are summed by one bf16 MMA (the K axis
+// holds (digit i, l), the N axis (weight g, column) with
+// B'[(g, col)][(i, l)] = t_{g-i}(l, col)); the products are integers below
+// 2^14 and a 128-l window sums at most 4 x 128 of them per weight, so the
+// FP32 accumulation in tensor memory is exact.  Per window the seven weights
+// of each output are scaled (powers of two, exact) and added to compensated
+// FP32 accumulators that keep the exact error of every addition (sum2).  The
+// only truncation is that of the digit strings, 2^-32 of the bounds: the
+// products are more accurate than the double-float CUDA-core kernels, which
+// round every product to FP32.
+//
+// Block: 512 threads, one per ring of 256 ring pairs (threads 0-255 the rings
+// theta, 256-511 the rings pi - theta) = four 128-row MMA tiles; one order m
+// per block row.  Per chunk of 8 l each thread writes its four digit rows
+// (16 bytes each) into the A tile, a subset of threads the B' digits, and one
+// thread issues 4 tiles x 2 K-steps of M=128, N=7 x 4 NB (rounded up to 16),
+// K=16 MMAs.  Two A/B'
+// buffers alternate; an mbarrier per buffer (tcgen05.commit) tells when the
+// MMAs reading it are done.  Every wait is bounded: on a timeout the block
+// records it in the plan's status word, waits once more (bounded) for its
+// MMAs, frees its tensor memory and returns.
+#include "common.cuh"
+#include "df.cuh"
+#include "kernels.cuh"
+
+namespace cunusht {
+
+// ---------------------------------------------------------------- tcgen05 / mbarrier helpers
+constexpr int MBAR_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, no swizzle, K-major: core matrices of
+// 8 rows x 16 bytes (rows 16 bytes apart); lbo = byte distance between core
+// matrices adjacent in K, sbo = between 8-row groups; descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes made visible to the tensor cores
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// Wait for the completion of the barrier phase with the given parity; false
+// when the iteration limit runs out first.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < MBAR_SPIN_LIMIT; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// one warp, converged
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 16 consecutive 32-bit columns of the calling thread's lane (warp-collective)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------- digit split
+// x = h + l (|h| <= 128, l below half an ulp of h) as d0 + d1/256 + d2/256^2 +
+// d3/256^3 + O(2^-25), integer digits |d_i| <= 128.  Rounding to an integer
+// by adding and subtracting 1.5 x 2^23; every other step is exact.
+__device__ __forceinline__ void digits4(float h, float l, float (&d)[4]) {
+    const float RND = 12582912.f;
+    d[0] = __fsub_rn(__fadd_rn(h, RND), RND);
+    float r = __fadd_rn(__fsub_rn(h, d[0]), l);
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        d[k] = __fsub_rn(__fmaf_rn(r, 256.f, RND), RND);
+        r = __fmaf_rn(r, 256.f, -d[k]);
+    }
+}
+
+// two integer-valued floats (|v| <= 256) as packed bf16 (exact: their low 16 bits are zero)
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // -126 <= e <= 127
+// 2^e, or 0 below the normal range (terms scaled that low are below 2^-102 of the sums)
+__device__ __forceinline__ float pow2f_or0(int e) { return e < -126 ? 0.f : pow2f(e); }
+
+// ---------------------------------------------------------------- self test
+// A 128 x n x 32 product of integer matrices (|entries| <= 128) accumulated
+// reps times (reps <= 16: sums below 2^24) through the same descriptors and
+// tensor-memory path as the Legendre kernel; writes the largest
+// |D - reps A B| to out[0] and 1 to out[1] on a barrier timeout.  mode 0:
+// entries of both signs; 1: entries in [64, 128] (sums near 2^23); 2: one
+// product of 2^14 per output among products of at most 4 (small addends
+// against a large partial sum).
+__device__ __forceinline__ int st_a(int r, int k, int mode) {
+    if (mode == 1) return 64 + ((r * 37 + k * 11 + 5) * 73) % 65;
+    if (mode == 2) return k == 0 ? 128 : (r + k) % 5 - 2;
+    return ((r * 37 + k * 11 + 5) * 73) % 257 - 128;
+}
+__device__ __forceinline__ int st_b(int n, int k, int mode) {
+    if (mode == 1) return 64 + ((n * 53 + k * 29 + 3) * 97) % 65;
+    if (mode == 2) return k == 0 ? 128 : (n + 2 * k) % 5 - 2;
+    return ((n * 53 + k * 29 + 3) * 97) % 257 - 128;
+}
+
+__global__ void __launch_bounds__(128) k_tc_selftest(int nn, int reps, int mode, float *out) {
+    __shared__ __align__(1024) unsigned char sA[128 * 64];
+    __shared__ __align__(1024) unsigned char sB[64 * 64];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_base), 64);
+    if (tid == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        mbar_init_fence();
+    }
+    // row r: four K-cores (8 bf16 each) at (r>>3)*512 + c*128 + (r&7)*16
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        uint32_t q[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+            q[h] = pack_bf16((float)st_a(tid, 8 * c + 2 * h, mode), (float)st_a(tid, 8 * c + 2 * h + 1, mode));
+        *reinterpret_cast<uint4 *>(sA + (tid >> 3) * 512 + c * 128 + (tid & 7) * 16) = make_uint4(q[0], q[1], q[2], q[3]);
+        if (tid < nn) {
+#pragma unroll
+            for (int h = 0; h < 4; ++h)
+                q[h] = pack_bf16((float)st_b(tid, 8 * c + 2 * h, mode), (float)st_b(tid, 8 * c + 2 * h + 1, mode));
+            *reinterpret_cast<uint4 *>(sB + (tid >> 3) * 512 + c * 128 + (tid & 7) * 16) =
+                make_uint4(q[0], q[1], q[2], q[3]);
+        }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tb = tmem_base;
+    if (tid == 0) {
+        const uint32_t id = idesc_bf16_f32(128, nn);
+        for (int rep = 0; rep < reps; ++rep)
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                tc_mma(tb, sdesc(smem_u32(sA) + k * 256, 128, 512), sdesc(smem_u32(sB) + k * 256, 128, 512), id,
+                       (rep > 0 || k > 0) ? 1u : 0u);
+        tc_commit(smem_u32(&bar));
+    }
+    const bool ok = mbar_wait(smem_u32(&bar), 0);
+    const int bad = __syncthreads_or(!ok);
+    tc_fence_after();
+    float err = 0.f;
+    if (!bad) {
+        for (int c0 = 0; c0 < nn; c0 += 16) {
+            float v[16];
+            tmem_ld16(tb + ((uint32_t)(warp * 32) << 16) + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                int ref = 0;
+                for (int k = 0; k < 32; ++k) ref += st_a(tid, k, mode) * st_b(c0 + i, k, mode);
+                err = fmaxf(err, fabsf(v[i] - (float)(reps * ref)));  // |reps ref| < 2^24: exact in FP32
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tb, 64);
+    }
+    atomicMax(reinterpret_cast<int *>(out), __float_as_int(err));  // err >= 0: int order = float order
+    if (bad && tid == 0) out[1] = 1.f;
+}
+
+int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout) {
+    if ((nn != 16 && nn != 32 && nn != 64) || reps < 1 || reps > 16 || mode < 0 || mode > 2) return CUNUSHT_ERR_ARG;
+    float *d = nullptr;
+    CU_TRY(cudaMalloc(&d, 2 * sizeof(float)));
+    CU_TRY(cudaMemset(d, 0, 2 * sizeof(float)));
+    k_tc_selftest<<<1, 128>>>(nn, reps, mode, d);
+    cudaError_t e = cudaGetLastError();
+    float h[2] = {0.f, 0.f};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    CU_TRY(e);
+    *maxerr = h[0];
+    *timeout = h[1] != 0.f;
+    return CUNUSHT_OK;
+}
+
+// ---------------------------------------------------------------- spin-s synthesis
+constexpr int TCL_T = 512;     // threads per block = rings (256 pairs)
+constexpr int TCL_W = 128;     // l window accumulated in tensor memory
+constexpr int TCL_KC = 16;     // l per chunk: K = 4 digits x 16 l = 4 MMA K-steps
+constexpr int TCL_TILE = 128 * 128;       // A tile: 128 rows x 8 K-cores x 16 bytes
+constexpr int TCL_ABUF = 4 * TCL_TILE;    // A buffer: 4 tiles
+constexpr int TCL_SBO = 1024;             // 8-row group stride (8 rows x 8 K-cores x 16 bytes)
+constexpr int TCL_TPS = TCL_W + 8;        // digit-plane row stride in elements (272 bytes: 16-byte aligned, fewer bank conflicts)
+constexpr int TCL_MIN_TAIL = 32;          // fewer leftover ring pairs than this go to the CUDA-core kernel
+
+template <int NB>
+struct TclLayout {
+    static constexpr int NO = 4 * NB;                    // outputs per ring
+    static constexpr int NG = 5;                         // digit-product weights g = 0..4
+    static constexpr int NN = (NG * NO + 15) / 16 * 16;  // MMA N: weights x outputs, padded to 16
+    static constexpr int NCOLS = 4 * NN <= 32 ? 32 : 4 * NN <= 64 ? 64 : 4 * NN <= 128 ? 128 : 4 * NN <= 256 ? 256 : 512;
+    static constexpr int QPT = TCL_W * NO / TCL_T;       // alm items per thread per window
+    static constexpr int BBUF = NN * 128;                // B' buffer: NN rows x 8 K-cores x 16 bytes
+    static constexpr int OFF_B = 2 * TCL_ABUF;
+    static constexpr int OFF_TP = OFF_B + 2 * BBUF;              // bf16 digit planes [4][NO][TPS]
+    static constexpr int OFF_CO = OFF_TP + 4 * NO * TCL_TPS * 2; // float4 (alpha, gamma) [W], float2 beta [W]
+    static constexpr int OFF_SC = OFF_CO + TCL_W * 24;           // float [NG][NO] epilogue scales
+    static constexpr int OFF_RED = OFF_SC + NG * NO * 4;         // float [16 warps][NO] column maxima
+    static constexpr int OFF_BAR = OFF_RED + 16 * NO * 4;        // 2 x u64
+    static constexpr int OFF_TM = OFF_BAR + 16;
+    static constexpr int BYTES = OFF_TM + 16;
+};
+
+// B' digit pairs (g, i) with 0 <= g - i <= 3, g < 5, in order:
+// (0,0) (1,0) (1,1) (2,0) (2,1) (2,2) (3,0) .. (3,3) (4,1) (4,2) (4,3)
+__device__ __forceinline__ void tcl_pair(int pr, int &g, int &di) {
+    if (pr == 0) g = 0, di = 0;
+    else if (pr < 3) g = 1, di = pr - 1;
+    else if (pr < 6) g = 2, di = pr - 3;
+    else if (pr < 10) g = 3, di = pr - 6;
+    else g = 4, di = pr - 9;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(TCL_T, 1)
+    k_leg_synth_spin_tc(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
+                        long long astride, const double *__restrict__ lfac, const float2 *__restrict__ coef,
+                        long long nalm, const double *__restrict__ lg0, int npairs, const double *__restrict__ px,
+                        const double *__restrict__ psh, const double *__restrict__ pch,
+                        const int *__restrict__ prn, const int *__restrict__ prs, double2 *__restrict__ H,
+                        long long hstride, int ldH, int *status) {
+    using LY = TclLayout<NB>;
+    constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG, QPT = LY::QPT;
+    static_assert(4 * NN <= 512, "tensor memory holds 512 columns");
+    static_assert(QPT * TCL_T == TCL_W * NO && TCL_T % NO == 0, "alm items per thread");
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned short *s_tp = reinterpret_cast<unsigned short *>(sm + LY::OFF_TP);
+    float4 *s_ag = reinterpret_cast<float4 *>(sm + LY::OFF_CO);
+    float2 *s_be = reinterpret_cast<float2 *>(sm + LY::OFF_CO + TCL_W * 16);
+    float *s_sc = reinterpret_cast<float *>(sm + LY::OFF_SC);
+    float *s_red = reinterpret_cast<float *>(sm + LY::OFF_RED);
+    uint32_t *s_tm = reinterpret_cast<uint32_t *>(sm + LY::OFF_TM);
+    const uint32_t sbase = smem_u32(sm);
+    const uint32_t bar0 = sbase + LY::OFF_BAR;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int side = tid >> 8;  // 0: ring theta, 1: ring pi - theta
+    const int tile = tid >> 7, row = tid & 127;
+    const int m = blockIdx.y;
+    const int l0 = max(m, spin);
+    const int p = blockIdx.x * (TCL_T / 2) + (tid & 255);
+    const bool act = p < npairs;
+    const int my_o = tid % NO;  // alm column of this thread's window items
+
+    if (warp == 0) tmem_alloc(sbase + LY::OFF_TM, LY::NCOLS);
+    if (tid == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar0 + 8, 1);
+        mbar_init_fence();
+    }
+    // B' positions with g - i outside [0, 3] and the padding rows stay zero for the whole kernel
+    for (int i = tid; i < 2 * LY::BBUF / 16; i += TCL_T)
+        reinterpret_cast<uint4 *>(sm + LY::OFF_B)[i] = make_uint4(0u, 0u, 0u, 0u);
+
+    double x = 0.0, sh = 0.0, ch = 1.0;
+    if (act) {
+        x = px[p];
+        sh = psh[p];
+        ch = pch[p];
+    }
+    const dfl xd = df_from(side ? -x : x);
+    dfl cur, prev;
+    int e;
+    if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
+    else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
+    sum2 acc[NO];
+
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *s_tm;
+    const uint32_t t_lane = tbase + ((uint32_t)((warp & 3) * 32) << 16) + tile * NN;  // this thread's row
+    const uint32_t a_row = (uint32_t)tile * TCL_TILE + (row >> 3) * TCL_SBO + (row & 7) * 16;
+    constexpr uint32_t IDESC = idesc_bf16_f32(128, NN);
+    const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+    const long long b = almidx(L, m, m) - m;
+    int gc = 0;  // chunks issued so far (buffer gc & 1, its use number gc >> 1)
+    int bad = 0;
+
+    for (int wb = l0; wb <= L && !bad; wb += TCL_W) {
+        const int cnt = min(TCL_W, L - wb + 1);
+        // recursion coefficients, zero past the window so that the steps beyond lmax stay finite
+        for (int i = tid; i < TCL_W; i += TCL_T) {
+            float4 ag = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 bb = make_float2(0.f, 0.f);
+            if (i < cnt) {
+                const long long ix = b + wb + i;
+                const float2 a2 = al[ix], g2 = ga[ix];
+                ag = make_float4(a2.x, a2.y, g2.x, g2.y);
+                bb = be[ix];
+            }
+            s_ag[i] = ag;
+            s_be[i] = bb;
+        }
+        // this thread's alm items (l = wb + tid / NO + k TCL_T / NO, column my_o) as double-float
+        dfl v[QPT];
+        float mx = 0.f;
+#pragma unroll
+        for (int k = 0; k < QPT; ++k) {
+            const int i = (tid + k * TCL_T) / NO;
+            v[k] = dfl{0.f, 0.f};
+            if (i < cnt) {
+                const int l = wb + i, r = my_o >> 2, comp = my_o & 3;
+                const long long ix = b + l;
+                const double f = lfac ? lfac[l] : 1.0;
+                const double par = ((l + m) & 1) ? -f : f;
+                const double2 g = G[r * astride + ix];
+                const double2 c = C ? C[r * astride + ix] : make_double2(0.0, 0.0);
+                const double val = comp == 0 ? f * (g.x - c.y)
+                                 : comp == 1 ? f * (g.y + c.x)
+                                 : comp == 2 ? par * (g.x + c.y)
+                                             : par * (c.x - g.y);
+                v[k] = df_from(val);
+            }
+            mx = fmaxf(mx, fabsf(v[k].h));
+        }
+#pragma unroll
+        for (int s = NO; s < 32; s <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, s));
+        if (lane < NO) s_red[warp * NO + lane] = mx;
+        // lambda exponent: 2^El > sqrt((2 lhi + 1) / (4 pi)) >= |lambda_l| for l <= lhi
+        int El;
+        frexp(sqrt((2.0 * (wb + cnt - 1) + 1.0) / (4.0 * PI)), &El);
+        const float lsc = pow2f(7 - El);
+        __syncthreads();
+        if (tid < NO) {
+            float cm = 0.f;
+#pragma unroll
+            for (int w = 0; w < TCL_T / 32; ++w) cm = fmaxf(cm, s_red[w * NO + tid]);
+            // column exponent 2^Ea > max |a|, clamped so that the digit scale stays a
+            // normal power of two (columns below 2^-80 contribute digits 0)
+            int ex = 0;
+            if (cm > 0.f) frexpf(cm, &ex);
+            ex = min(max(ex, -80), 100);
+            s_red[tid] = __int_as_float(ex);  // row 0 of s_red reused for the exponents
+#pragma unroll
+            for (int g = 0; g < NG; ++g) s_sc[g * NO + tid] = pow2f_or0(El + ex - 14 - 8 * g);
+        }
+        __syncthreads();
+        {
+            // digit planes of this thread's items (zero past the window)
+            const float sc = pow2f(7 - __float_as_int(s_red[my_o]));
+#pragma unroll
+            for (int k = 0; k < QPT; ++k) {
+                const int i = (tid + k * TCL_T) / NO;
+                float d[4];
+                digits4(v[k].h * sc, v[k].l * sc, d);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    s_tp[(j * NO + my_o) * TCL_TPS + i] = (unsigned short)(__float_as_uint(d[j]) >> 16);
+            }
+        }
+        __syncthreads();
+
+        const int nch = (cnt + TCL_KC - 1) / TCL_KC;
+        for (int c = 0; c < nch; ++c, ++gc) {
+            const int buf = gc & 1;
+            int to = 0;
+            if (gc >= 2) to = !mbar_wait(bar0 + 8 * buf, ((gc - 2) >> 1) & 1);
+            unsigned char *sA = sm + buf * TCL_ABUF;
+            unsigned char *sB = sm + LY::OFF_B + buf * LY::BBUF;
+            // B' of this chunk: one 16-byte K-core (8 l of one digit) per thread
+            if (tid < 13 * 2 * NO) {
+                const int pr = tid / (2 * NO), rem = tid - pr * 2 * NO;
+                const int lh = rem / NO, o = rem - lh * NO;
+                int g, di;
+                tcl_pair(pr, g, di);
+                const int n = g * NO + o;
+                const uint4 q = *reinterpret_cast<const uint4 *>(s_tp + ((g - di) * NO + o) * TCL_TPS + c * TCL_KC + 8 * lh);
+                *reinterpret_cast<uint4 *>(sB + (n >> 3) * TCL_SBO + (2 * di + lh) * 128 + (n & 7) * 16) = q;
+            }
+            // lambda digits for 16 l in two halves of 8, each stored as four 16-byte K-cores
+#pragma unroll
+            for (int lh = 0; lh < 2; ++lh) {
+                uint32_t pk[4][4];
+#pragma unroll
+                for (int j2 = 0; j2 < 4; ++j2) {
+                    float d0[4], d1[4];
+                    // digits of lambda_l (zero unless accumulated), then one recursion step l -> l + 1
+                    auto step = [&](int i, float(&d)[4]) {
+                        digits4(cur.h * lsc, cur.l * lsc, d);
+                        const bool use = act && e == 0 && i < cnt;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) d[k] = use ? d[k] : 0.f;
+                        const float4 ag = s_ag[i];
+                        const float2 b2 = s_be[i];
+                        const dfl t = df_add(df_mul(dfl{ag.x, ag.y}, xd), dfl{ag.z, ag.w});
+                        const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                        prev = cur;
+                        cur = nxt;
+                        REC_RESCALE_DF(cur, prev, e);
+                    };
+                    const int i0 = c * TCL_KC + 8 * lh + 2 * j2;
+                    step(i0, d0);
+                    step(i0 + 1, d1);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    *reinterpret_cast<uint4 *>(sA + a_row + (2 * k + lh) * 128) =
+                        make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
+            }
+            fence_async_smem();
+            bad = __syncthreads_or(to);
+            if (bad) break;
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t aa = sbase + buf * TCL_ABUF, ba = sbase + LY::OFF_B + buf * LY::BBUF;
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)  // K-step k: digit k of lambda, 16 l
+                        tc_mma(tbase + t * NN, sdesc(aa + t * TCL_TILE + k * 256, 128, TCL_SBO),
+                               sdesc(ba + k * 256, 128, TCL_SBO), IDESC, (c > 0 || k > 0) ? 1u : 0u);
+                tc_commit(bar0 + 8 * buf);
+            }
+        }
+        if (bad) break;
+        // window epilogue: the exact weight sums -> compensated accumulators
+        {
+            const int lb = gc - 1;
+            const int to = !mbar_wait(bar0 + 8 * (lb & 1), (lb >> 1) & 1);
+            bad = __syncthreads_or(to);
+            if (bad) break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int q = 0; q < NN / 16; ++q) {
+            float dv[16];
+            tmem_ld16(t_lane + q * 16, dv);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int n = q * 16 + i, g = n / NO, o = n - g * NO;
+                if (g < NG) acc[o].add(dv[i] * s_sc[n]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();  // the window's tables are read by all threads before the next window stages its own
+    }
+
+    if (bad) {
+        if (tid == 0) {
+            if (status) atomicOr(status, 1);
+            if (gc > 0) mbar_wait(bar0 + 8 * ((gc - 1) & 1), ((gc - 1) >> 1) & 1);
+        }
+    } else if (act) {
+        const int n = prn[p], s = prs[p];
+        const double sgs = (spin & 1) ? -1.0 : 1.0;
+#pragma unroll
+        for (int r = 0; r < NB; ++r) {
+            double2 *Hr = H + r * hstride;
+            const double2 A = make_double2(-acc[4 * r].value(), -acc[4 * r + 1].value());
+            const double2 B = make_double2(-sgs * acc[4 * r + 2].value(), -sgs * acc[4 * r + 3].value());
+            if (side == 0) {
+                Hr[(long long)(L + m) * ldH + n] = A;
+                if (m > 0 && s != n) Hr[(long long)(L - m) * ldH + s] = B;
+            } else {
+                if (s != n) Hr[(long long)(L + m) * ldH + s] = A;
+                if (m > 0) Hr[(long long)(L - m) * ldH + n] = B;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, LY::NCOLS);
+    }
+}
+
+template <int NB>
+static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double *x, const double *sh,
+                              const double *ch, const int *rn, const int *rs, int ld, int spin, const double2 *G,
+                              const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
+                              cudaStream_t st) {
+    using LY = TclLayout<NB>;
+    CU_TRY(cudaFuncSetAttribute(k_leg_synth_spin_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::BYTES));
+    dim3 grid((npairs + TCL_T / 2 - 1) / (TCL_T / 2), P->mmax + 1);
+    k_leg_synth_spin_tc<NB><<<grid, TCL_T, LY::BYTES, st>>>(P->lmax, spin, G, C, astride, lf, P->d_coef_df[spin],
+                                                            P->nalm_tab, P->d_lg0[spin], npairs, x, sh, ch, rn, rs, H,
+                                                            hstride, ld, P->d_status);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+// Ring pairs in full blocks of 256 on the tensor cores; a tail of fewer than
+// TCL_MIN_TAIL pairs after at least one full block (the equator pair of the
+// Clenshaw-Curtis grid, 2^k + 1 rings) goes to the double-float CUDA-core
+// kernel instead of a nearly empty block per order m.
+int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
+                      const double *ch, const int *rn, const int *rs, int ld, int spin, const double2 *G,
+                      const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
+                      cudaStream_t st) {
+    const int per = TCL_T / 2, tail = npairs % per;
+    const int ntc = (npairs > per && tail < TCL_MIN_TAIL) ? npairs - tail : npairs;
+    if (nb == 4) RC_TRY(launch_synth_tc_nb<4>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
+    else if (nb == 2) RC_TRY(launch_synth_tc_nb<2>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
+    else RC_TRY(launch_synth_tc_nb<1>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
+    if (ntc < npairs)
+        RC_TRY(leg_synth_spin_df_pairs(P, nb, npairs - ntc, x + ntc, sh + ntc, ch + ntc, rn + ntc, rs + ntc, ld, spin,
+                                       G, C, astride, lf, H, hstride, st));
+    return CUNUSHT_OK;
+}
+
+}  // namespace cunusht

@@ -112,6 +112,37 @@ int cunusht_plan_set_mmax(cunusht_plan_t *plan, int mmax);
  */
 int cunusht_plan_force_split(cunusht_plan_t *plan, int force);
 
+/*
+ * Mixed precision: the Legendre synthesis of spin > 0 (CC synthesis of spin
+ * 1 / 2 maps, the deflection synthesis of dlm2pointing) runs on the tensor
+ * cores (exact integer-digit bf16 products accumulated in tensor memory,
+ * enable = 1, the default) or on the CUDA cores in double-float (enable = 0).
+ * Both replace the SHTns synthesis of the reference
+ * (cunusht/sht/GPU_sht_transformer.py:56-62, :88-97); the switch exists so
+ * that the two can be checked against each other.
+ */
+int cunusht_plan_set_tensor_cores(cunusht_plan_t *plan, int enable);
+
+/*
+ * Device status word of the plan, read after the plan's work so far has
+ * finished (device-wide synchronisation) and then cleared: 0 = fine; bit 0 =
+ * a bounded wait inside a tensor-core kernel ran out (the kernel gave up,
+ * its outputs are not valid).  No reference counterpart.
+ */
+int cunusht_plan_device_status(cunusht_plan_t *plan, int *status);
+
+/*
+ * Tensor-core self test: a 128 x n x 32 product of integer matrices
+ * (n = 16, 32 or 64, entries |.| <= 128) accumulated reps times (1..16, sums
+ * below 2^24) through the descriptors, tensor-memory accumulation and
+ * read-back path of the tensor-core Legendre kernel, on the current device.
+ * mode 0: entries of both signs; 1: entries in [64, 128]; 2: one large
+ * product per output among small ones.  *maxerr = largest |result - exact|
+ * (0 when the accumulation is exact), *timeout = 1 if the completion wait ran
+ * out.  No reference counterpart.
+ */
+int cunusht_tc_selftest(int n, int reps, int mode, double *maxerr, int *timeout);
+
 /* Plan sizes: info[0]=npix, [1]=torus theta length, [2]=torus phi length,
  * [3]=fine grid theta length, [4]=fine grid phi length, [5]=kernel width,
  * [6]=fine rows stored, [7]=workspace bytes, [8]=precision in use,

@@ -1,0 +1,127 @@
+"""Tensor-core Legendre synthesis (mixed precision, spin > 0).
+
+The self test runs integer products through the same shared-memory
+descriptors and tensor-memory path as the Legendre kernel and must be exact.
+The synthesis on the tensor cores is compared with the FP64 path and with the
+double-float CUDA-core kernels (plan switch cunusht_plan_set_tensor_cores),
+for spin 1 and 2, several lmax (windows of 128 l, partial chunks of 8 l),
+mmax < lmax, and batched (4 / 2 / 1 requests per launch) against single
+requests.  The plan's device status word stays 0 (no bounded wait ran out)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _rel(x, y):
+    x, y = np.asarray(x), np.asarray(y)
+    return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+
+
+def _status(t):
+    from cunusht_gb300 import _lib
+    st = ctypes.c_int(-1)
+    _lib.check(t._lib.cunusht_plan_device_status(t._plan, ctypes.byref(st)))
+    return st.value
+
+
+@pytest.mark.parametrize("n", [16, 32, 64])
+@pytest.mark.parametrize("reps,mode", [(1, 0), (16, 0), (16, 1), (16, 2)])
+def test_tc_selftest_exact(built_lib, n, reps, mode):
+    from cunusht_gb300 import _lib
+    lib = _lib.load()
+    err, to = ctypes.c_double(-1.0), ctypes.c_int(-1)
+    _lib.check(lib.cunusht_tc_selftest(n, reps, mode, ctypes.byref(err), ctypes.byref(to)))
+    print(f"selftest n {n} reps {reps} mode {mode}: max error {err.value}")
+    assert to.value == 0
+    assert err.value == 0.0
+
+
+def _transformers(cu, lmax, mmax=None):
+    geo = ("gl", {"lmax": lmax})
+    mk = lambda prec: cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=1e-7, precision=prec, max_spin=2)
+    tc, cc, f64 = mk("mixed"), mk("mixed"), mk("fp64")
+    from cunusht_gb300 import _lib
+    _lib.check(cc._lib.cunusht_plan_set_tensor_cores(cc._plan, 0))
+    return tc, cc, f64
+
+
+@pytest.mark.parametrize("lmax", [40, 127, 300])
+@pytest.mark.parametrize("spin", [1, 2])
+def test_tc_synthesis_matches_fp64(built_lib, lmax, spin):
+    import cunusht_gb300 as cu
+    tc, cc, f64 = _transformers(cu, lmax)
+    gclm, _ = orc.make_inputs(lmax, 2, seed=40 + lmax + spin)
+    alm = torch.as_tensor(gclm, device="cuda")
+    m_tc = tc.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
+    m_cc = cc.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
+    m_64 = f64.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
+    e_tc, e_cc = _rel(m_tc, m_64), _rel(m_cc, m_64)
+    print(f"lmax {lmax} spin {spin}: tensor cores {e_tc:.2e}, CUDA cores {e_cc:.2e} vs FP64")
+    # digit truncation (2^-32 of the lambda bound) leaves ~4e-9; the CUDA-core
+    # kernels round each product to FP32 (~3e-8)
+    assert e_tc < 1e-8
+    assert e_tc < 0.5 * e_cc
+    assert e_cc < 1e-7
+    assert _status(tc) == 0
+
+
+def test_tc_synthesis_mmax(built_lib):
+    import cunusht_gb300 as cu
+    lmax, mmax = 200, 150
+    tc, _, f64 = _transformers(cu, lmax)
+    gclm, _ = orc.make_inputs(lmax, 2, seed=77)
+    full = np.asarray(gclm)
+    n = orc.nalm(lmax, mmax)
+    alm = torch.as_tensor(np.ascontiguousarray(full[:, :n]), device="cuda")
+    m_tc = tc.synthesis(alm, spin=2, lmax=lmax, mmax=mmax).cpu().numpy()
+    m_64 = f64.synthesis(alm, spin=2, lmax=lmax, mmax=mmax).cpu().numpy()
+    assert _rel(m_tc, m_64) < 1e-8
+    assert _status(tc) == 0
+
+
+@pytest.mark.parametrize("nreq", [1, 3, 4, 6])
+def test_tc_lensing_batch_equals_single(built_lib, nreq):
+    """Batched launches (4, 2, 1 requests sharing the recursion) give each
+    request exactly its single-request result: the digit products are summed
+    exactly and each column's exponent depends on its own data only."""
+    import cunusht_gb300 as cu
+    lmax, spin = 127, 2
+    t = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=1e-7, precision="mixed",
+                                  max_spin=2)
+    G, D = [], []
+    for r in range(nreq):
+        gclm, dls = orc.make_inputs(lmax, spin, seed=500 + r)
+        G.append(gclm)
+        D.append(dls[0])
+    Gt = torch.as_tensor(np.stack(G), device="cuda")
+    Dt = torch.as_tensor(np.stack(D), device="cuda")
+    batch = t.lensing_batch(Gt, Dt, spin=spin).cpu().numpy()
+    for r in range(nreq):
+        single = t.gclm2lenmap(Gt[r], lmax, lmax, dlm_scaled=Dt[r], spin=spin, verbose=0).cpu().numpy()
+        assert _rel(batch[r], single) < 1e-12
+    assert _status(t) == 0
+
+
+@pytest.mark.parametrize("spin", [1, 2])
+def test_tc_lensing_against_cuda_cores(built_lib, spin):
+    """End to end (dlm2pointing + nusht2d2): tensor-core and CUDA-core Legendre
+    stages agree well within epsilon, and both agree with the FP64 plan."""
+    import cunusht_gb300 as cu
+    lmax = 255
+    tc, cc, f64 = _transformers(cu, lmax)
+    gclm, dls = orc.make_inputs(lmax, spin, seed=90 + spin)
+    g = torch.as_tensor(gclm, device="cuda")
+    d = torch.as_tensor(dls[0], device="cuda")
+    r_tc = tc.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0).cpu().numpy()
+    r_cc = cc.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0).cpu().numpy()
+    r_64 = f64.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0).cpu().numpy()
+    assert _rel(r_tc, r_64) < 1e-7
+    assert _rel(r_cc, r_64) < 1e-7
+    assert _rel(r_tc, r_cc) < 1e-7
+    assert _status(tc) == 0
