@@ -121,7 +121,7 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_ring_cls, P->d_cls_N, P->d_cls_Mb, P->d_cls_SP,
                     P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
-                    P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status};
+                    P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[1], P->d_tc_woff[2], P->d_tc_rec};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &e : P->evt_pool) {
@@ -319,6 +319,7 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     }
     RC_TRY(dalloc(P, &P->d_status, 1));
     CU_TRY(cudaMemset(P->d_status, 0, sizeof(int)));
+    if (P->prec == CUNUSHT_PREC_MIXED) RC_TRY(tc_plan_init(P));
     {
         std::vector<double> lf(lmax + 1);
         for (int l = 0; l <= lmax; ++l) lf[l] = std::sqrt((double)l * (l + 1.0));

@@ -177,6 +177,11 @@ struct cunusht_plan_s {
     float2 *d_coef_df[3] = {nullptr, nullptr, nullptr};  // the same tables as (hi, lo) FP32 pairs
     bool use_tc = true;       // mixed precision: spin > 0 Legendre synthesis on the tensor cores
     int *d_status = nullptr;  // device status word: bit 0 = a bounded wait of a tensor-core kernel ran out
+    // tensor-core synthesis: per spin 1, 2 the first window record of each m (m = 0..lmax+1),
+    // and the record buffer (alm digit planes and scales per (m, l-window), written per call)
+    int *d_tc_woff[3] = {nullptr, nullptr, nullptr};
+    unsigned char *d_tc_rec = nullptr;
+    size_t tc_rec_bytes = 0;
 
     // FFT twiddles e^{-2 pi i t / TW}
     int TW = 0;

@@ -41,6 +41,9 @@
 #include "df.cuh"
 #include "kernels.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace cunusht {
 
 // ---------------------------------------------------------------- tcgen05 / mbarrier helpers
@@ -100,6 +103,35 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         if (ok) return true;
     }
     return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// bytes from global to shared memory by the bulk-copy engine, completion counted on bar
+// (both addresses 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// barrier 1 over the first nthr threads of the block (the others never wait on it)
+__device__ __forceinline__ void bar_sync_1(int nthr) { asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory"); }
+// barrier 1 that also returns whether any participating thread passed v != 0
+__device__ __forceinline__ int bar_or_1(int nthr, int v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 q, %1, 0;\n\t"
+        "bar.red.or.pred p, 1, %2, q;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r)
+        : "r"(v), "r"(nthr)
+        : "memory");
+    return (int)r;
 }
 
 // one warp, converged
@@ -269,15 +301,16 @@ struct TclLayout {
     static constexpr int NG = 5;                         // digit-product weights g = 0..4
     static constexpr int NN = (NG * NO + 15) / 16 * 16;  // MMA N: weights x outputs, padded to 16
     static constexpr int NCOLS = 4 * NN <= 32 ? 32 : 4 * NN <= 64 ? 64 : 4 * NN <= 128 ? 128 : 4 * NN <= 256 ? 256 : 512;
-    static constexpr int QPT = TCL_W * NO / TCL_T;       // alm items per thread per window
+    // window record (written by k_tc_records, one per (m, l-window)):
+    static constexpr int RSC = 4 * NO * TCL_TPS * 2;     // bf16 digit planes [4][NO][TPS], then
+    static constexpr int RLS = RSC + NG * NO * 4;        // float epilogue scales [NG][NO], then
+    static constexpr int RSZ = (RLS + 4 + 15) / 16 * 16; // float lambda digit scale; 16-byte records
     static constexpr int BBUF = NN * 128;                // B' buffer: NN rows x 8 K-cores x 16 bytes
     static constexpr int OFF_B = 2 * TCL_ABUF;
-    static constexpr int OFF_TP = OFF_B + 2 * BBUF;              // bf16 digit planes [4][NO][TPS]
-    static constexpr int OFF_CO = OFF_TP + 4 * NO * TCL_TPS * 2; // float4 (alpha, gamma) [W], float2 beta [W]
-    static constexpr int OFF_SC = OFF_CO + TCL_W * 24;           // float [NG][NO] epilogue scales
-    static constexpr int OFF_RED = OFF_SC + NG * NO * 4;         // float [16 warps][NO] column maxima
-    static constexpr int OFF_BAR = OFF_RED + 16 * NO * 4;        // 2 x u64
-    static constexpr int OFF_TM = OFF_BAR + 16;
+    static constexpr int OFF_R = OFF_B + 2 * BBUF;       // two window records (current, next)
+    static constexpr int OFF_CO = OFF_R + 2 * RSZ;       // float4 (alpha, gamma) [W + 1], float2 beta [W + 1]
+    static constexpr int OFF_BAR = (OFF_CO + (TCL_W + 1) * 24 + 7) / 8 * 8;  // full[2], empty[2], record[2]
+    static constexpr int OFF_TM = OFF_BAR + 48;          // tensor-memory base, give-up flag
     static constexpr int BYTES = OFF_TM + 16;
 };
 
@@ -291,259 +324,333 @@ __device__ __forceinline__ void tcl_pair(int pr, int &g, int &di) {
     else g = 4, di = pr - 9;
 }
 
+// Window records: one block of TCL_W threads per (l-window k, order m), thread
+// i for l = wb + i.  The NO alm combinations of the NB requests (A = G - iC
+// pairs with +s, B with -s, times the per-l factor) as double-float, the
+// column exponents Ea (2^Ea > max over the window), their digit planes, the
+// epilogue scales 2^(El + Ea - 14 - 8g) and the lambda digit scale
+// 2^(7 - El).  All FP64 work of the tensor-core synthesis happens here, in
+// parallel over every window, rather than between the ring warps' chunks.
 template <int NB>
-__global__ void __launch_bounds__(TCL_T, 1)
-    k_leg_synth_spin_tc(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C,
-                        long long astride, const double *__restrict__ lfac, const float2 *__restrict__ coef,
-                        long long nalm, const double *__restrict__ lg0, int npairs, const double *__restrict__ px,
-                        const double *__restrict__ psh, const double *__restrict__ pch,
-                        const int *__restrict__ prn, const int *__restrict__ prs, double2 *__restrict__ H,
-                        long long hstride, int ldH, int *status) {
+__global__ void __launch_bounds__(TCL_W)
+    k_tc_records(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C, long long astride,
+                 const double *__restrict__ lfac, const int *__restrict__ woff, unsigned char *__restrict__ rec) {
     using LY = TclLayout<NB>;
-    constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG, QPT = LY::QPT;
+    constexpr int NO = LY::NO, NG = LY::NG;
+    __shared__ float s_mx[TCL_W / 32][NO];
+    __shared__ int s_ea[NO];
+    const int m = blockIdx.y, k = blockIdx.x;
+    if (k >= woff[m + 1] - woff[m]) return;
+    const int wb = max(m, spin) + k * TCL_W, cnt = min(TCL_W, L - wb + 1);
+    unsigned char *R = rec + (size_t)(woff[m] + k) * LY::RSZ;
+    const int i = threadIdx.x, lane = i & 31, warp = i >> 5;
+    dfl v[NO];
+#pragma unroll
+    for (int o = 0; o < NO; ++o) v[o] = dfl{0.f, 0.f};
+    if (i < cnt) {
+        const int l = wb + i;
+        const long long ix = almidx(L, m, m) - m + l;
+        const double f = lfac ? lfac[l] : 1.0;
+        const double par = ((l + m) & 1) ? -f : f;
+#pragma unroll
+        for (int r = 0; r < NB; ++r) {
+            const double2 g = G[r * astride + ix];
+            const double2 c = C ? C[r * astride + ix] : make_double2(0.0, 0.0);
+            v[4 * r + 0] = df_from(f * (g.x - c.y));
+            v[4 * r + 1] = df_from(f * (g.y + c.x));
+            v[4 * r + 2] = df_from(par * (g.x + c.y));
+            v[4 * r + 3] = df_from(par * (c.x - g.y));
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+        float mx = fabsf(v[o].h);
+#pragma unroll
+        for (int sft = 16; sft > 0; sft >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, sft));
+        if (lane == 0) s_mx[warp][o] = mx;
+    }
+    // lambda exponent: 2^El > sqrt((2 lhi + 1) / (4 pi)) >= |lambda_l| for l <= lhi
+    int El;
+    frexp(sqrt((2.0 * (wb + cnt - 1) + 1.0) / (4.0 * PI)), &El);
+    __syncthreads();
+    if (i < NO) {
+        float cm = 0.f;
+#pragma unroll
+        for (int w = 0; w < TCL_W / 32; ++w) cm = fmaxf(cm, s_mx[w][i]);
+        // column exponent 2^Ea > max |a|, clamped so that the digit scale stays a
+        // normal power of two (columns below 2^-80 contribute digits 0)
+        int ex = 0;
+        if (cm > 0.f) frexpf(cm, &ex);
+        ex = min(max(ex, -80), 100);
+        s_ea[i] = ex;
+        float *sc = reinterpret_cast<float *>(R + LY::RSC);
+#pragma unroll
+        for (int g = 0; g < NG; ++g) sc[g * NO + i] = pow2f_or0(El + ex - 14 - 8 * g);
+    }
+    if (i == 0) *reinterpret_cast<float *>(R + LY::RLS) = pow2f(7 - El);
+    __syncthreads();
+    unsigned short *tp = reinterpret_cast<unsigned short *>(R);
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+        const float sc = pow2f(7 - s_ea[o]);
+        float d[4];
+        digits4(v[o].h * sc, v[o].l * sc, d);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) tp[(j * NO + o) * TCL_TPS + i] = (unsigned short)(__float_as_uint(d[j]) >> 16);
+    }
+}
+
+// Roles: warps 0-15 (TCL_T threads) hold one ring each and write the digit
+// tiles; warp 16 issues the MMAs.  Per chunk each ring warp waits until the
+// MMAs that last read the buffer are done (empty barrier, tcgen05.commit),
+// writes its rows, and arrives on the buffer's full barrier (one arrival per
+// warp); the MMA warp waits for all 16 arrivals.  The ring warps thus run up
+// to a chunk apart instead of meeting at a block barrier every chunk.  The
+// window records arrive by bulk copy, the next one prefetched while the
+// current window runs; block-wide steps use barrier 1 over the ring warps only.
+constexpr int TCL_BLOCK = TCL_T + 32;
+
+template <int NB>
+__global__ void __launch_bounds__(TCL_BLOCK, 1)
+    k_leg_synth_spin_tc(int L, int spin, const unsigned char *__restrict__ rec, const int *__restrict__ woff,
+                        const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0, int npairs,
+                        const double *__restrict__ px, const double *__restrict__ psh,
+                        const double *__restrict__ pch, const int *__restrict__ prn, const int *__restrict__ prs,
+                        double2 *__restrict__ H, long long hstride, int ldH, int *status) {
+    using LY = TclLayout<NB>;
+    constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG;
     static_assert(4 * NN <= 512, "tensor memory holds 512 columns");
-    static_assert(QPT * TCL_T == TCL_W * NO && TCL_T % NO == 0, "alm items per thread");
+    static_assert(26 * NO <= TCL_T, "one B' K-core per ring thread");
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned short *s_tp = reinterpret_cast<unsigned short *>(sm + LY::OFF_TP);
     float4 *s_ag = reinterpret_cast<float4 *>(sm + LY::OFF_CO);
-    float2 *s_be = reinterpret_cast<float2 *>(sm + LY::OFF_CO + TCL_W * 16);
-    float *s_sc = reinterpret_cast<float *>(sm + LY::OFF_SC);
-    float *s_red = reinterpret_cast<float *>(sm + LY::OFF_RED);
+    float2 *s_be = reinterpret_cast<float2 *>(sm + LY::OFF_CO + (TCL_W + 1) * 16);
     uint32_t *s_tm = reinterpret_cast<uint32_t *>(sm + LY::OFF_TM);
+    volatile int *s_bad = reinterpret_cast<volatile int *>(sm + LY::OFF_TM + 4);
     const uint32_t sbase = smem_u32(sm);
-    const uint32_t bar0 = sbase + LY::OFF_BAR;
+    const uint32_t full0 = sbase + LY::OFF_BAR, empty0 = full0 + 16, rbar0 = full0 + 32;  // [2] each
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int side = tid >> 8;  // 0: ring theta, 1: ring pi - theta
-    const int tile = tid >> 7, row = tid & 127;
     const int m = blockIdx.y;
     const int l0 = max(m, spin);
-    const int p = blockIdx.x * (TCL_T / 2) + (tid & 255);
-    const bool act = p < npairs;
-    const int my_o = tid % NO;  // alm column of this thread's window items
+    const unsigned char *recm = rec + (size_t)woff[m] * LY::RSZ;  // this order's window records
 
-    if (warp == 0) tmem_alloc(sbase + LY::OFF_TM, LY::NCOLS);
+    if (warp == TCL_T / 32) tmem_alloc(sbase + LY::OFF_TM, LY::NCOLS);
     if (tid == 0) {
-        mbar_init(bar0, 1);
-        mbar_init(bar0 + 8, 1);
+        mbar_init(full0, TCL_T / 32);
+        mbar_init(full0 + 8, TCL_T / 32);
+        mbar_init(empty0, 1);
+        mbar_init(empty0 + 8, 1);
+        mbar_init(rbar0, 1);
+        mbar_init(rbar0 + 8, 1);
+        *s_bad = 0;
         mbar_init_fence();
     }
     // B' positions with g - i outside [0, 3] and the padding rows stay zero for the whole kernel
-    for (int i = tid; i < 2 * LY::BBUF / 16; i += TCL_T)
+    for (int i = tid; i < 2 * LY::BBUF / 16; i += TCL_BLOCK)
         reinterpret_cast<uint4 *>(sm + LY::OFF_B)[i] = make_uint4(0u, 0u, 0u, 0u);
-
-    double x = 0.0, sh = 0.0, ch = 1.0;
-    if (act) {
-        x = px[p];
-        sh = psh[p];
-        ch = pch[p];
-    }
-    const dfl xd = df_from(side ? -x : x);
-    dfl cur, prev;
-    int e;
-    if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
-    else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
-    sum2 acc[NO];
-
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *s_tm;
-    const uint32_t t_lane = tbase + ((uint32_t)((warp & 3) * 32) << 16) + tile * NN;  // this thread's row
-    const uint32_t a_row = (uint32_t)tile * TCL_TILE + (row >> 3) * TCL_SBO + (row & 7) * 16;
-    constexpr uint32_t IDESC = idesc_bf16_f32(128, NN);
-    const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
-    const long long b = almidx(L, m, m) - m;
-    int gc = 0;  // chunks issued so far (buffer gc & 1, its use number gc >> 1)
-    int bad = 0;
+    if (tid == 0 && l0 <= L) bulk_g2s(sbase + LY::OFF_R, recm, LY::RSZ, rbar0);  // record of window 0
 
-    for (int wb = l0; wb <= L && !bad; wb += TCL_W) {
-        const int cnt = min(TCL_W, L - wb + 1);
-        // recursion coefficients, zero past the window so that the steps beyond lmax stay finite
-        for (int i = tid; i < TCL_W; i += TCL_T) {
-            float4 ag = make_float4(0.f, 0.f, 0.f, 0.f);
-            float2 bb = make_float2(0.f, 0.f);
-            if (i < cnt) {
-                const long long ix = b + wb + i;
-                const float2 a2 = al[ix], g2 = ga[ix];
-                ag = make_float4(a2.x, a2.y, g2.x, g2.y);
-                bb = be[ix];
-            }
-            s_ag[i] = ag;
-            s_be[i] = bb;
-        }
-        // this thread's alm items (l = wb + tid / NO + k TCL_T / NO, column my_o) as double-float
-        dfl v[QPT];
-        float mx = 0.f;
-#pragma unroll
-        for (int k = 0; k < QPT; ++k) {
-            const int i = (tid + k * TCL_T) / NO;
-            v[k] = dfl{0.f, 0.f};
-            if (i < cnt) {
-                const int l = wb + i, r = my_o >> 2, comp = my_o & 3;
-                const long long ix = b + l;
-                const double f = lfac ? lfac[l] : 1.0;
-                const double par = ((l + m) & 1) ? -f : f;
-                const double2 g = G[r * astride + ix];
-                const double2 c = C ? C[r * astride + ix] : make_double2(0.0, 0.0);
-                const double val = comp == 0 ? f * (g.x - c.y)
-                                 : comp == 1 ? f * (g.y + c.x)
-                                 : comp == 2 ? par * (g.x + c.y)
-                                             : par * (c.x - g.y);
-                v[k] = df_from(val);
-            }
-            mx = fmaxf(mx, fabsf(v[k].h));
-        }
-#pragma unroll
-        for (int s = NO; s < 32; s <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, s));
-        if (lane < NO) s_red[warp * NO + lane] = mx;
-        // lambda exponent: 2^El > sqrt((2 lhi + 1) / (4 pi)) >= |lambda_l| for l <= lhi
-        int El;
-        frexp(sqrt((2.0 * (wb + cnt - 1) + 1.0) / (4.0 * PI)), &El);
-        const float lsc = pow2f(7 - El);
-        __syncthreads();
-        if (tid < NO) {
-            float cm = 0.f;
-#pragma unroll
-            for (int w = 0; w < TCL_T / 32; ++w) cm = fmaxf(cm, s_red[w * NO + tid]);
-            // column exponent 2^Ea > max |a|, clamped so that the digit scale stays a
-            // normal power of two (columns below 2^-80 contribute digits 0)
-            int ex = 0;
-            if (cm > 0.f) frexpf(cm, &ex);
-            ex = min(max(ex, -80), 100);
-            s_red[tid] = __int_as_float(ex);  // row 0 of s_red reused for the exponents
-#pragma unroll
-            for (int g = 0; g < NG; ++g) s_sc[g * NO + tid] = pow2f_or0(El + ex - 14 - 8 * g);
-        }
-        __syncthreads();
-        {
-            // digit planes of this thread's items (zero past the window)
-            const float sc = pow2f(7 - __float_as_int(s_red[my_o]));
-#pragma unroll
-            for (int k = 0; k < QPT; ++k) {
-                const int i = (tid + k * TCL_T) / NO;
-                float d[4];
-                digits4(v[k].h * sc, v[k].l * sc, d);
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    s_tp[(j * NO + my_o) * TCL_TPS + i] = (unsigned short)(__float_as_uint(d[j]) >> 16);
-            }
-        }
-        __syncthreads();
-
-        const int nch = (cnt + TCL_KC - 1) / TCL_KC;
-        for (int c = 0; c < nch; ++c, ++gc) {
-            const int buf = gc & 1;
-            int to = 0;
-            if (gc >= 2) to = !mbar_wait(bar0 + 8 * buf, ((gc - 2) >> 1) & 1);
-            unsigned char *sA = sm + buf * TCL_ABUF;
-            unsigned char *sB = sm + LY::OFF_B + buf * LY::BBUF;
-            // B' of this chunk: one 16-byte K-core (8 l of one digit) per thread
-            if (tid < 13 * 2 * NO) {
-                const int pr = tid / (2 * NO), rem = tid - pr * 2 * NO;
-                const int lh = rem / NO, o = rem - lh * NO;
-                int g, di;
-                tcl_pair(pr, g, di);
-                const int n = g * NO + o;
-                const uint4 q = *reinterpret_cast<const uint4 *>(s_tp + ((g - di) * NO + o) * TCL_TPS + c * TCL_KC + 8 * lh);
-                *reinterpret_cast<uint4 *>(sB + (n >> 3) * TCL_SBO + (2 * di + lh) * 128 + (n & 7) * 16) = q;
-            }
-            // lambda digits for 16 l in two halves of 8, each stored as four 16-byte K-cores
-#pragma unroll
-            for (int lh = 0; lh < 2; ++lh) {
-                uint32_t pk[4][4];
-#pragma unroll
-                for (int j2 = 0; j2 < 4; ++j2) {
-                    float d0[4], d1[4];
-                    // digits of lambda_l (zero unless accumulated), then one recursion step l -> l + 1
-                    auto step = [&](int i, float(&d)[4]) {
-                        digits4(cur.h * lsc, cur.l * lsc, d);
-                        const bool use = act && e == 0 && i < cnt;
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) d[k] = use ? d[k] : 0.f;
-                        const float4 ag = s_ag[i];
-                        const float2 b2 = s_be[i];
-                        const dfl t = df_add(df_mul(dfl{ag.x, ag.y}, xd), dfl{ag.z, ag.w});
-                        const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
-                        prev = cur;
-                        cur = nxt;
-                        REC_RESCALE_DF(cur, prev, e);
-                    };
-                    const int i0 = c * TCL_KC + 8 * lh + 2 * j2;
-                    step(i0, d0);
-                    step(i0 + 1, d1);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+    if (warp == TCL_T / 32) {
+        // ---------------- MMA warp: the whole warp follows the chunk sequence (its
+        // outcome kept warp-uniform), lane 0 issues
+        constexpr uint32_t IDESC = idesc_bf16_f32(128, NN);
+        int gc = 0;
+        bool ok = true;
+        for (int wb = l0; wb <= L && ok; wb += TCL_W) {
+            const int nch = (min(TCL_W, L - wb + 1) + TCL_KC - 1) / TCL_KC;
+            for (int c = 0; c < nch; ++c, ++gc) {
+                const int buf = gc & 1;
+                const bool got = !*s_bad && mbar_wait(full0 + 8 * buf, (gc >> 1) & 1);
+                if (!__all_sync(0xffffffffu, got)) {
+                    *s_bad = 1;
+                    ok = false;
+                    break;
                 }
+                if (lane == 0) {
+                    tc_fence_after();
+                    const uint32_t aa = sbase + buf * TCL_ABUF, ba = sbase + LY::OFF_B + buf * LY::BBUF;
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    *reinterpret_cast<uint4 *>(sA + a_row + (2 * k + lh) * 128) =
-                        make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
-            }
-            fence_async_smem();
-            bad = __syncthreads_or(to);
-            if (bad) break;
-            if (tid == 0) {
-                tc_fence_after();
-                const uint32_t aa = sbase + buf * TCL_ABUF, ba = sbase + LY::OFF_B + buf * LY::BBUF;
+                    for (int t = 0; t < 4; ++t)
 #pragma unroll
-                for (int t = 0; t < 4; ++t)
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)  // K-step k: digit k of lambda, 16 l
-                        tc_mma(tbase + t * NN, sdesc(aa + t * TCL_TILE + k * 256, 128, TCL_SBO),
-                               sdesc(ba + k * 256, 128, TCL_SBO), IDESC, (c > 0 || k > 0) ? 1u : 0u);
-                tc_commit(bar0 + 8 * buf);
+                        for (int k = 0; k < 4; ++k)  // K-step k: digit k of lambda, 16 l
+                            tc_mma(tbase + t * NN, sdesc(aa + t * TCL_TILE + k * 256, 128, TCL_SBO),
+                                   sdesc(ba + k * 256, 128, TCL_SBO), IDESC, (c > 0 || k > 0) ? 1u : 0u);
+                    tc_commit(empty0 + 8 * buf);
+                }
+                __syncwarp();
             }
         }
-        if (bad) break;
-        // window epilogue: the exact weight sums -> compensated accumulators
-        {
-            const int lb = gc - 1;
-            const int to = !mbar_wait(bar0 + 8 * (lb & 1), (lb >> 1) & 1);
-            bad = __syncthreads_or(to);
-            if (bad) break;
+        if (!ok && gc > 0) mbar_wait(empty0 + 8 * ((gc - 1) & 1), ((gc - 1) >> 1) & 1);
+        __syncwarp();
+    } else {
+        // ---------------- ring warps
+        const int side = tid >> 8;  // 0: ring theta, 1: ring pi - theta
+        const int tile = tid >> 7, row = tid & 127;
+        const int p = blockIdx.x * (TCL_T / 2) + (tid & 255);
+        const bool act = p < npairs;
+        double x = 0.0, sh = 0.0, ch = 1.0;
+        if (act) {
+            x = px[p];
+            sh = psh[p];
+            ch = pch[p];
         }
-        tc_fence_after();
-#pragma unroll
-        for (int q = 0; q < NN / 16; ++q) {
-            float dv[16];
-            tmem_ld16(t_lane + q * 16, dv);
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int n = q * 16 + i, g = n / NO, o = n - g * NO;
-                if (g < NG) acc[o].add(dv[i] * s_sc[n]);
-            }
-        }
-        tc_fence_before();
-        __syncthreads();  // the window's tables are read by all threads before the next window stages its own
-    }
+        const dfl xd = df_from(side ? -x : x);
+        dfl cur, prev;
+        int e;
+        if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
+        else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
+        sum2 acc[NO];
+        const uint32_t t_lane = tbase + ((uint32_t)((warp & 3) * 32) << 16) + tile * NN;  // this thread's row
+        const uint32_t a_row = (uint32_t)tile * TCL_TILE + (row >> 3) * TCL_SBO + (row & 7) * 16;
+        const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
+        const long long b = almidx(L, m, m) - m;
+        int gc = 0, kw = 0;
+        int bad = 0;
 
-    if (bad) {
-        if (tid == 0) {
-            if (status) atomicOr(status, 1);
-            if (gc > 0) mbar_wait(bar0 + 8 * ((gc - 1) & 1), ((gc - 1) >> 1) & 1);
-        }
-    } else if (act) {
-        const int n = prn[p], s = prs[p];
-        const double sgs = (spin & 1) ? -1.0 : 1.0;
+        for (int wb = l0; wb <= L; wb += TCL_W, ++kw) {
+            const int cnt = min(TCL_W, L - wb + 1);
+            // prefetch the next window's record into the other buffer (its readers
+            // finished at the previous window's closing barrier)
+            if (tid == 0 && wb + TCL_W <= L) {
+                fence_async_smem();
+                bulk_g2s(sbase + LY::OFF_R + ((kw + 1) & 1) * LY::RSZ, recm + (size_t)(kw + 1) * LY::RSZ, LY::RSZ,
+                         rbar0 + 8 * ((kw + 1) & 1));
+            }
+            // recursion coefficients, zero past the window so that the steps beyond lmax stay finite
+            for (int i = tid; i < TCL_W + 1; i += TCL_T) {
+                float4 ag = make_float4(0.f, 0.f, 0.f, 0.f);
+                float2 bb = make_float2(0.f, 0.f);
+                if (i < cnt) {
+                    const long long ix = b + wb + i;
+                    const float2 a2 = al[ix], g2 = ga[ix];
+                    ag = make_float4(a2.x, a2.y, g2.x, g2.y);
+                    bb = be[ix];
+                }
+                s_ag[i] = ag;
+                s_be[i] = bb;
+            }
+            bad |= !mbar_wait(rbar0 + 8 * (kw & 1), (kw >> 1) & 1);  // this window's record has landed
+            bar_sync_1(TCL_T);
+            const unsigned char *Rw = sm + LY::OFF_R + (kw & 1) * LY::RSZ;
+            const unsigned short *s_tp = reinterpret_cast<const unsigned short *>(Rw);
+            const float *s_sc = reinterpret_cast<const float *>(Rw + LY::RSC);
+            const float lsc = *reinterpret_cast<const float *>(Rw + LY::RLS);
+
+            const int nch = (cnt + TCL_KC - 1) / TCL_KC;
+            float4 agn = s_ag[0];  // coefficients of the next step, loaded one step ahead
+            float2 ben = s_be[0];
+            for (int c = 0; c < nch; ++c, ++gc) {
+                const int buf = gc & 1;
+                if (gc >= 2) bad |= !mbar_wait(empty0 + 8 * buf, ((gc - 2) >> 1) & 1);
+                unsigned char *sA = sm + buf * TCL_ABUF;
+                unsigned char *sB = sm + LY::OFF_B + buf * LY::BBUF;
+                // B' of this chunk: one 16-byte K-core (8 l of one digit) per thread
+                if (tid < 13 * 2 * NO) {
+                    const int pr = tid / (2 * NO), rem = tid - pr * 2 * NO;
+                    const int lh = rem / NO, o = rem - lh * NO;
+                    int g, di;
+                    tcl_pair(pr, g, di);
+                    const int n = g * NO + o;
+                    const uint4 q =
+                        *reinterpret_cast<const uint4 *>(s_tp + ((g - di) * NO + o) * TCL_TPS + c * TCL_KC + 8 * lh);
+                    *reinterpret_cast<uint4 *>(sB + (n >> 3) * TCL_SBO + (2 * di + lh) * 128 + (n & 7) * 16) = q;
+                }
+                // lambda digits for 16 l in two halves of 8, each stored as four 16-byte K-cores.
+                // The exponent check runs once per half: a step grows the mantissa by at
+                // most (alpha + beta) < 2^8.5 (alpha_m ~ sqrt(2m) <= 181 for lmax <= 16383),
+                // so from below 2^40 eight steps stay below 2^108, inside the FP32
+                // range, and e (hence the digit mask) stays fixed within the half.
 #pragma unroll
-        for (int r = 0; r < NB; ++r) {
-            double2 *Hr = H + r * hstride;
-            const double2 A = make_double2(-acc[4 * r].value(), -acc[4 * r + 1].value());
-            const double2 B = make_double2(-sgs * acc[4 * r + 2].value(), -sgs * acc[4 * r + 3].value());
-            if (side == 0) {
-                Hr[(long long)(L + m) * ldH + n] = A;
-                if (m > 0 && s != n) Hr[(long long)(L - m) * ldH + s] = B;
-            } else {
-                if (s != n) Hr[(long long)(L + m) * ldH + s] = A;
-                if (m > 0) Hr[(long long)(L - m) * ldH + n] = B;
+                for (int lh = 0; lh < 2; ++lh) {
+                    uint32_t pk[4][4];
+                    const float scg = (act && e == 0) ? lsc : 0.f;
+#pragma unroll
+                    for (int j2 = 0; j2 < 4; ++j2) {
+                        float d0[4], d1[4];
+                        // digits of lambda_l (zero unless accumulated), then one recursion step l -> l + 1
+                        auto step = [&](int i, float(&d)[4]) {
+                            const float sc = i < cnt ? scg : 0.f;
+                            digits4(cur.h * sc, cur.l * sc, d);
+                            const float4 ag = agn;
+                            const float2 b2 = ben;
+                            agn = s_ag[i + 1];
+                            ben = s_be[i + 1];
+                            const dfl t = df_add(df_mul(dfl{ag.x, ag.y}, xd), dfl{ag.z, ag.w});
+                            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                            prev = cur;
+                            cur = nxt;
+                        };
+                        const int i0 = c * TCL_KC + 8 * lh + 2 * j2;
+                        step(i0, d0);
+                        step(i0 + 1, d1);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        *reinterpret_cast<uint4 *>(sA + a_row + (2 * k + lh) * 128) =
+                            make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
+                    REC_RESCALE_DF(cur, prev, e);
+                }
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(full0 + 8 * buf);
+            }
+            // window epilogue: the exact weight sums -> compensated accumulators
+            bad |= !mbar_wait(empty0 + 8 * ((gc - 1) & 1), ((gc - 1) >> 1) & 1);
+            bad = __any_sync(0xffffffffu, bad);  // warp-uniform: the loads below are warp-collective
+            tc_fence_after();
+            if (!bad) {
+#pragma unroll
+                for (int q = 0; q < NN / 16; ++q) {
+                    float dv[16];
+                    tmem_ld16(t_lane + q * 16, dv);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int n = q * 16 + i, g = n / NO, o = n - g * NO;
+                        if (g < NG) acc[o].add(dv[i] * s_sc[n]);
+                    }
+                }
+            }
+            tc_fence_before();
+            // all ring warps are done with the window's tables; any wait that ran out ends the block
+            bad = bar_or_1(TCL_T, bad | *s_bad);
+            if (bad) break;
+        }
+
+        if (bad) {
+            *s_bad = 1;
+            if (tid == 0) {
+                if (status) atomicOr(status, 1);
+                // the record copy of the window after the last one entered may still be in flight
+                if (l0 + (kw + 1) * TCL_W <= L) mbar_wait(rbar0 + 8 * ((kw + 1) & 1), ((kw + 1) >> 1) & 1);
+            }
+        } else if (act) {
+            const int n = prn[p], s = prs[p];
+            const double sgs = (spin & 1) ? -1.0 : 1.0;
+#pragma unroll
+            for (int r = 0; r < NB; ++r) {
+                double2 *Hr = H + r * hstride;
+                const double2 A = make_double2(-acc[4 * r].value(), -acc[4 * r + 1].value());
+                const double2 B = make_double2(-sgs * acc[4 * r + 2].value(), -sgs * acc[4 * r + 3].value());
+                if (side == 0) {
+                    Hr[(long long)(L + m) * ldH + n] = A;
+                    if (m > 0 && s != n) Hr[(long long)(L - m) * ldH + s] = B;
+                } else {
+                    if (s != n) Hr[(long long)(L + m) * ldH + s] = A;
+                    if (m > 0) Hr[(long long)(L - m) * ldH + n] = B;
+                }
             }
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) {
+    if (warp == TCL_T / 32) {
         tc_fence_after();
         tmem_dealloc(tbase, LY::NCOLS);
     }
@@ -555,12 +662,36 @@ static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double 
                               const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
                               cudaStream_t st) {
     using LY = TclLayout<NB>;
+    const int L = P->lmax;
+    const dim3 rgrid((L - spin + 1 + TCL_W - 1) / TCL_W, P->mmax + 1);  // m <= spin has the most windows
+    k_tc_records<NB><<<rgrid, TCL_W, 0, st>>>(L, spin, G, C, astride, lf, P->d_tc_woff[spin], P->d_tc_rec);
+    CU_LAUNCH_CHECK();
     CU_TRY(cudaFuncSetAttribute(k_leg_synth_spin_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::BYTES));
     dim3 grid((npairs + TCL_T / 2 - 1) / (TCL_T / 2), P->mmax + 1);
-    k_leg_synth_spin_tc<NB><<<grid, TCL_T, LY::BYTES, st>>>(P->lmax, spin, G, C, astride, lf, P->d_coef_df[spin],
-                                                            P->nalm_tab, P->d_lg0[spin], npairs, x, sh, ch, rn, rs, H,
-                                                            hstride, ld, P->d_status);
+    k_leg_synth_spin_tc<NB><<<grid, TCL_BLOCK, LY::BYTES, st>>>(L, spin, P->d_tc_rec, P->d_tc_woff[spin],
+                                                                P->d_coef_df[spin], P->nalm_tab, P->d_lg0[spin],
+                                                                npairs, x, sh, ch, rn, rs, H, hstride, ld,
+                                                                P->d_status);
     CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+int tc_plan_init(cunusht_plan_s *P) {
+    const int L = P->lmax;
+    size_t nrec = 0;
+    for (int s = 1; s <= 2 && s <= L; ++s) {
+        std::vector<int> wo(L + 2, 0);
+        for (int m = 0; m <= L; ++m) wo[m + 1] = wo[m] + (L - std::max(m, s) + 1 + TCL_W - 1) / TCL_W;
+        CU_TRY(cudaMalloc(&P->d_tc_woff[s], wo.size() * sizeof(int)));
+        CU_TRY(cudaMemcpy(P->d_tc_woff[s], wo.data(), wo.size() * sizeof(int), cudaMemcpyHostToDevice));
+        P->ws_bytes += wo.size() * sizeof(int);
+        nrec = std::max(nrec, (size_t)wo[L + 1]);
+    }
+    P->tc_rec_bytes = nrec * (size_t)TclLayout<4>::RSZ;  // four requests per launch at most
+    if (P->tc_rec_bytes) {
+        CU_TRY(cudaMalloc(&P->d_tc_rec, P->tc_rec_bytes));
+        P->ws_bytes += P->tc_rec_bytes;
+    }
     return CUNUSHT_OK;
 }
 
