@@ -174,6 +174,19 @@ __device__ __forceinline__ void digits4(float h, float l, float (&d)[4]) {
     }
 }
 
+// digits4 of (h + l) sc for a power of two sc: the integer part of h sc by one
+// FMA with the rounding constant, its exact remainder by another
+__device__ __forceinline__ void digits4s(float h, float l, float sc, float (&d)[4]) {
+    const float RND = 12582912.f;
+    d[0] = __fsub_rn(__fmaf_rn(h, sc, RND), RND);
+    float r = __fmaf_rn(l, sc, __fmaf_rn(h, sc, -d[0]));
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        d[k] = __fsub_rn(__fmaf_rn(r, 256.f, RND), RND);
+        r = __fmaf_rn(r, 256.f, -d[k]);
+    }
+}
+
 // two integer-valued floats (|v| <= 256) as packed bf16 (exact: their low 16 bits are zero)
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
@@ -302,14 +315,15 @@ struct TclLayout {
     static constexpr int NN = (NG * NO + 15) / 16 * 16;  // MMA N: weights x outputs, padded to 16
     static constexpr int NCOLS = 4 * NN <= 32 ? 32 : 4 * NN <= 64 ? 64 : 4 * NN <= 128 ? 128 : 4 * NN <= 256 ? 256 : 512;
     // window record (written by k_tc_records, one per (m, l-window)):
-    static constexpr int RSC = 4 * NO * TCL_TPS * 2;     // bf16 digit planes [4][NO][TPS], then
-    static constexpr int RLS = RSC + NG * NO * 4;        // float epilogue scales [NG][NO], then
-    static constexpr int RSZ = (RLS + 4 + 15) / 16 * 16; // float lambda digit scale; 16-byte records
+    static constexpr int RSC = 4 * NO * TCL_TPS * 2;        // bf16 digit planes [4][NO][TPS], then
+    static constexpr int RLS = RSC + NG * NO * 4;           // float epilogue scales [NG][NO], then
+    static constexpr int RCO = (RLS + 4 + 15) / 16 * 16;    // float lambda digit scale, then
+    static constexpr int RBE = RCO + (TCL_W + 1) * 16;      // float4 (alpha, gamma) [W + 1] and
+    static constexpr int RSZ = (RBE + (TCL_W + 1) * 8 + 15) / 16 * 16;  // float2 beta [W + 1] (zero past the window)
     static constexpr int BBUF = NN * 128;                // B' buffer: NN rows x 8 K-cores x 16 bytes
     static constexpr int OFF_B = 2 * TCL_ABUF;
     static constexpr int OFF_R = OFF_B + 2 * BBUF;       // two window records (current, next)
-    static constexpr int OFF_CO = OFF_R + 2 * RSZ;       // float4 (alpha, gamma) [W + 1], float2 beta [W + 1]
-    static constexpr int OFF_BAR = (OFF_CO + (TCL_W + 1) * 24 + 7) / 8 * 8;  // full[2], empty[2], record[2]
+    static constexpr int OFF_BAR = OFF_R + 2 * RSZ;      // full[2], empty[2], record[2]
     static constexpr int OFF_TM = OFF_BAR + 48;          // tensor-memory base, give-up flag
     static constexpr int BYTES = OFF_TM + 16;
 };
@@ -334,7 +348,8 @@ __device__ __forceinline__ void tcl_pair(int pr, int &g, int &di) {
 template <int NB>
 __global__ void __launch_bounds__(TCL_W)
     k_tc_records(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C, long long astride,
-                 const double *__restrict__ lfac, const int *__restrict__ woff, unsigned char *__restrict__ rec) {
+                 const double *__restrict__ lfac, const float2 *__restrict__ coef, long long nalm,
+                 const int *__restrict__ woff, unsigned char *__restrict__ rec) {
     using LY = TclLayout<NB>;
     constexpr int NO = LY::NO, NG = LY::NG;
     __shared__ float s_mx[TCL_W / 32][NO];
@@ -344,6 +359,23 @@ __global__ void __launch_bounds__(TCL_W)
     const int wb = max(m, spin) + k * TCL_W, cnt = min(TCL_W, L - wb + 1);
     unsigned char *R = rec + (size_t)(woff[m] + k) * LY::RSZ;
     const int i = threadIdx.x, lane = i & 31, warp = i >> 5;
+    {
+        // recursion coefficients (double-float) of the window, zero past its end
+        float4 *ag = reinterpret_cast<float4 *>(R + LY::RCO);
+        float2 *bt = reinterpret_cast<float2 *>(R + LY::RBE);
+        const long long b = almidx(L, m, m) - m;
+        for (int j = i; j < TCL_W + 1; j += TCL_W) {
+            float4 a4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 b2 = make_float2(0.f, 0.f);
+            if (j < cnt) {
+                const float2 a2 = coef[b + wb + j], g2 = coef[nalm + b + wb + j];
+                a4 = make_float4(a2.x, a2.y, g2.x, g2.y);
+                b2 = coef[2 * nalm + b + wb + j];
+            }
+            ag[j] = a4;
+            bt[j] = b2;
+        }
+    }
     dfl v[NO];
 #pragma unroll
     for (int o = 0; o < NO; ++o) v[o] = dfl{0.f, 0.f};
@@ -392,9 +424,8 @@ __global__ void __launch_bounds__(TCL_W)
     unsigned short *tp = reinterpret_cast<unsigned short *>(R);
 #pragma unroll
     for (int o = 0; o < NO; ++o) {
-        const float sc = pow2f(7 - s_ea[o]);
         float d[4];
-        digits4(v[o].h * sc, v[o].l * sc, d);
+        digits4s(v[o].h, v[o].l, pow2f(7 - s_ea[o]), d);
 #pragma unroll
         for (int j = 0; j < 4; ++j) tp[(j * NO + o) * TCL_TPS + i] = (unsigned short)(__float_as_uint(d[j]) >> 16);
     }
@@ -413,7 +444,7 @@ constexpr int TCL_BLOCK = TCL_T + 32;
 template <int NB>
 __global__ void __launch_bounds__(TCL_BLOCK, 1)
     k_leg_synth_spin_tc(int L, int spin, const unsigned char *__restrict__ rec, const int *__restrict__ woff,
-                        const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0, int npairs,
+                        const double *__restrict__ lg0, int npairs,
                         const double *__restrict__ px, const double *__restrict__ psh,
                         const double *__restrict__ pch, const int *__restrict__ prn, const int *__restrict__ prs,
                         double2 *__restrict__ H, long long hstride, int ldH, int *status) {
@@ -422,8 +453,6 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
     static_assert(4 * NN <= 512, "tensor memory holds 512 columns");
     static_assert(26 * NO <= TCL_T, "one B' K-core per ring thread");
     extern __shared__ __align__(1024) unsigned char sm[];
-    float4 *s_ag = reinterpret_cast<float4 *>(sm + LY::OFF_CO);
-    float2 *s_be = reinterpret_cast<float2 *>(sm + LY::OFF_CO + (TCL_W + 1) * 16);
     uint32_t *s_tm = reinterpret_cast<uint32_t *>(sm + LY::OFF_TM);
     volatile int *s_bad = reinterpret_cast<volatile int *>(sm + LY::OFF_TM + 4);
     const uint32_t sbase = smem_u32(sm);
@@ -507,8 +536,6 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
         sum2 acc[NO];
         const uint32_t t_lane = tbase + ((uint32_t)((warp & 3) * 32) << 16) + tile * NN;  // this thread's row
         const uint32_t a_row = (uint32_t)tile * TCL_TILE + (row >> 3) * TCL_SBO + (row & 7) * 16;
-        const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
-        const long long b = almidx(L, m, m) - m;
         int gc = 0, kw = 0;
         int bad = 0;
 
@@ -521,25 +548,14 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
                 bulk_g2s(sbase + LY::OFF_R + ((kw + 1) & 1) * LY::RSZ, recm + (size_t)(kw + 1) * LY::RSZ, LY::RSZ,
                          rbar0 + 8 * ((kw + 1) & 1));
             }
-            // recursion coefficients, zero past the window so that the steps beyond lmax stay finite
-            for (int i = tid; i < TCL_W + 1; i += TCL_T) {
-                float4 ag = make_float4(0.f, 0.f, 0.f, 0.f);
-                float2 bb = make_float2(0.f, 0.f);
-                if (i < cnt) {
-                    const long long ix = b + wb + i;
-                    const float2 a2 = al[ix], g2 = ga[ix];
-                    ag = make_float4(a2.x, a2.y, g2.x, g2.y);
-                    bb = be[ix];
-                }
-                s_ag[i] = ag;
-                s_be[i] = bb;
-            }
             bad |= !mbar_wait(rbar0 + 8 * (kw & 1), (kw >> 1) & 1);  // this window's record has landed
-            bar_sync_1(TCL_T);
             const unsigned char *Rw = sm + LY::OFF_R + (kw & 1) * LY::RSZ;
             const unsigned short *s_tp = reinterpret_cast<const unsigned short *>(Rw);
             const float *s_sc = reinterpret_cast<const float *>(Rw + LY::RSC);
             const float lsc = *reinterpret_cast<const float *>(Rw + LY::RLS);
+            // recursion coefficients, zero past the window so that the steps beyond lmax stay finite
+            const float4 *s_ag = reinterpret_cast<const float4 *>(Rw + LY::RCO);
+            const float2 *s_be = reinterpret_cast<const float2 *>(Rw + LY::RBE);
 
             const int nch = (cnt + TCL_KC - 1) / TCL_KC;
             float4 agn = s_ag[0];  // coefficients of the next step, loaded one step ahead
@@ -574,8 +590,7 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
                         float d0[4], d1[4];
                         // digits of lambda_l (zero unless accumulated), then one recursion step l -> l + 1
                         auto step = [&](int i, float(&d)[4]) {
-                            const float sc = i < cnt ? scg : 0.f;
-                            digits4(cur.h * sc, cur.l * sc, d);
+                            digits4s(cur.h, cur.l, i < cnt ? scg : 0.f, d);
                             const float4 ag = agn;
                             const float2 b2 = ben;
                             agn = s_ag[i + 1];
@@ -664,13 +679,13 @@ static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double 
     using LY = TclLayout<NB>;
     const int L = P->lmax;
     const dim3 rgrid((L - spin + 1 + TCL_W - 1) / TCL_W, P->mmax + 1);  // m <= spin has the most windows
-    k_tc_records<NB><<<rgrid, TCL_W, 0, st>>>(L, spin, G, C, astride, lf, P->d_tc_woff[spin], P->d_tc_rec);
+    k_tc_records<NB><<<rgrid, TCL_W, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm_tab,
+                                              P->d_tc_woff[spin], P->d_tc_rec);
     CU_LAUNCH_CHECK();
     CU_TRY(cudaFuncSetAttribute(k_leg_synth_spin_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::BYTES));
     dim3 grid((npairs + TCL_T / 2 - 1) / (TCL_T / 2), P->mmax + 1);
     k_leg_synth_spin_tc<NB><<<grid, TCL_BLOCK, LY::BYTES, st>>>(L, spin, P->d_tc_rec, P->d_tc_woff[spin],
-                                                                P->d_coef_df[spin], P->nalm_tab, P->d_lg0[spin],
-                                                                npairs, x, sh, ch, rn, rs, H, hstride, ld,
+                                                                P->d_lg0[spin], npairs, x, sh, ch, rn, rs, H, hstride, ld,
                                                                 P->d_status);
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
