@@ -101,10 +101,10 @@ template <typename T, int RAD> __device__ __forceinline__ void dftR(cplx<T> *v, 
 // data stays in registers: loads, barrier, twiddle + R-point DFT, stores,
 // barrier.
 // e^{-2 pi i t / M} for 0 <= t < M from the quarter table S[u] = e^{-2 pi i u / M},
-// u <= M/4, held in shared memory: t = q M/4 + u gives (-i)^q S[u]
+// u <= M/4, held in shared memory: t = q M/4 + u gives (-i)^q S[u]; lq = log2(M/4)
 template <typename T>
-__device__ __forceinline__ cplx<T> tw_quarter(const cplx<T> *S, int t, int Q) {
-    const int q = t / Q, u = t - q * Q;
+__device__ __forceinline__ cplx<T> tw_quarter(const cplx<T> *S, int t, int lq) {
+    const int q = t >> lq, u = t & ((1 << lq) - 1);
     const cplx<T> w = S[u];
     T x = (q & 1) ? w.y : w.x;
     T y = (q & 1) ? w.x : w.y;
@@ -131,7 +131,7 @@ __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
     __syncthreads();
     if (act) {
         const int tstep = M / (Ns * R);
-        const int Q = M >> 2;
+        const int lq = __ffs(M) - 3;  // log2(M / 4), M a power of two
 #pragma unroll
         for (int c = 0; c < NB; ++c) {
             const int j = threadIdx.x + c * nthr;
@@ -139,7 +139,7 @@ __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
             if (Ns > 1) {
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    C w = tw_quarter<T>(stw, r * k * tstep, Q);
+                    C w = tw_quarter<T>(stw, r * k * tstep, lq);
                     if (dir > 0) w.y = -w.y;
                     v[c][r] = cmul(v[c][r], w);
                 }
@@ -236,6 +236,8 @@ __device__ __forceinline__ int wrapi(int n, int N) {
     n %= N;
     return n < 0 ? n + N : n;
 }
+// n mod N for N a power of two (also for negative n, two's complement)
+__device__ __forceinline__ int wrap2(int n, int N) { return n & (N - 1); }
 
 // ------------------------------------------------------------ theta pass
 // SP = 2 (long columns): the 2 Nt-point inverse is done as two Nt-point
@@ -291,7 +293,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     __syncthreads();
     fft_smem<T>(buf, Ntf / SP, +1, stw, MTW);
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-        const int n = wrapi(r + n_lo, Ntf);
+        const int n = wrap2(r + n_lo, Ntf);
         if (SP == 1) F[(long long)r * ncols + c] = buf[n];
         else if ((n & 1) == q) F[(long long)r * ncols + c] = buf[n >> 1];
     }
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     for (int i = threadIdx.x; i < Nb; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-        const int n = wrapi(r + n_lo, Ntf);
+        const int n = wrap2(r + n_lo, Ntf);
         if (SP == 1) buf[n] = F[(long long)r * ncols + c];
         else if ((n & 1) == q) buf[n >> 1] = F[(long long)r * ncols + c];
     }
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
         cplx<T> v = F[(long long)r * ncols + c];
         if (q) v = cmul(v, twk<T>(tw, c - L, tstep, +1));
-        buf[wrapi(c - L, Nb)] = v;
+        buf[wrap2(c - L, Nb)] = v;
     }
     __syncthreads();
     fft_smem<T>(buf, Nb, +1, stw, MTW);
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(FFT_TPB)
     __syncthreads();
     fft_smem<T>(buf, Nb, -1, stw, MTW);
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
-        cplx<T> v = buf[wrapi(c - L, Nb)];
+        cplx<T> v = buf[wrap2(c - L, Nb)];
         if (q) v = cmul(v, twk<T>(tw, c - L, tstep, -1));
         else if (SP == 2) v = cadd(v, F[(long long)r * ncols + c]);
         F[(long long)r * ncols + c] = v;
