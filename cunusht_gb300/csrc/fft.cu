@@ -102,10 +102,20 @@ template <typename T, int RAD> __device__ __forceinline__ void dftR(cplx<T> *v, 
 // barrier.
 // e^{-2 pi i t / M} for 0 <= t < M from the quarter table S[u] = e^{-2 pi i u / M},
 // u <= M/4, held in shared memory: t = q M/4 + u gives (-i)^q S[u]; lq = log2(M/4)
+// Position of entry u of the quarter table in shared memory: the low bits
+// (one 128-byte row of 8 double / double-float or 16 float entries) XORed with
+// every higher group of as many bits, so that reads at any power-of-two
+// stride (the twiddles of one pass, k consecutive) fall in distinct banks.
+// Entries stay within their aligned group: the table takes M/4 + 16 slots.
+template <typename T> __device__ __forceinline__ int tw_swz(int u) {
+    if constexpr (sizeof(cplx<T>) == 16) return u ^ (((u >> 3) ^ (u >> 6) ^ (u >> 9) ^ (u >> 12)) & 7);
+    else return u ^ (((u >> 4) ^ (u >> 8) ^ (u >> 12)) & 15);
+}
+
 template <typename T>
 __device__ __forceinline__ cplx<T> tw_quarter(const cplx<T> *S, int t, int lq) {
     const int q = t >> lq, u = t & ((1 << lq) - 1);
-    const cplx<T> w = S[u];
+    const cplx<T> w = S[tw_swz<T>(u)];
     T x = (q & 1) ? w.y : w.x;
     T y = (q & 1) ? w.x : w.y;
     if (q & 2) x = -x;
@@ -205,10 +215,11 @@ __device__ __forceinline__ void fft_smem(cplx<T> *buf, int N, int dir, const cpl
 }
 
 // Shared memory of a transform kernel with an N-element buffer: the buffer
-// plus its quarter twiddle table (N/4 + 1 entries).  The twiddles are read in
-// every butterfly; from global memory they were L2-latency loads (the data
-// buffer leaves little L1), the first stall reason of these kernels.
-size_t fft_smem_bytes(int N, bool f32) { return (size_t)(N + N / 4 + 1) * (f32 ? sizeof(float2) : sizeof(double2)); }
+// plus its quarter twiddle table (N/4 + 1 entries, swizzled over N/4 + 16
+// slots).  The twiddles are read in every butterfly; from global memory they
+// were L2-latency loads (the data buffer leaves little L1), the first stall
+// reason of these kernels.
+size_t fft_smem_bytes(int N, bool f32) { return (size_t)(N + N / 4 + 16) * (f32 ? sizeof(float2) : sizeof(double2)); }
 
 // S[u] = e^{-2 pi i u / M} for u <= M/4 from the plan's table tw[t] =
 // e^{-2 pi i t / TW} (M | TW), placed after the M-element data buffer.  The
@@ -217,7 +228,7 @@ template <typename T>
 __device__ __forceinline__ cplx<T> *load_twiddles(cplx<T> *buf, int M, const cplx<T> *__restrict__ tw, int TW) {
     cplx<T> *S = buf + M;
     const int st = TW / M;
-    for (int u = threadIdx.x; u <= M / 4; u += blockDim.x) S[u] = tw[u * st];
+    for (int u = threadIdx.x; u <= M / 4; u += blockDim.x) S[tw_swz<T>(u)] = tw[u * st];
     return S;
 }
 
