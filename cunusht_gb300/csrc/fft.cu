@@ -100,8 +100,6 @@ template <typename T, int RAD> __device__ __forceinline__ void dftR(cplx<T> *v, 
 // (NB butterflies of R points, E = NB R, all compile-time), so the butterfly
 // data stays in registers: loads, barrier, twiddle + R-point DFT, stores,
 // barrier.
-// e^{-2 pi i t / M} for 0 <= t < M from the quarter table S[u] = e^{-2 pi i u / M},
-// u <= M/4, held in shared memory: t = q M/4 + u gives (-i)^q S[u]; lq = log2(M/4)
 // Position of entry u of the quarter table in shared memory: the low bits
 // (one 128-byte row of 8 double / double-float or 16 float entries) XORed with
 // every higher group of as many bits, so that reads at any power-of-two
@@ -112,6 +110,8 @@ template <typename T> __device__ __forceinline__ int tw_swz(int u) {
     else return u ^ (((u >> 4) ^ (u >> 8) ^ (u >> 12)) & 15);
 }
 
+// e^{-2 pi i t / M} for 0 <= t < M from the quarter table S[u] = e^{-2 pi i u / M},
+// u <= M/4, held in shared memory: t = q M/4 + u gives (-i)^q S[u]; lq = log2(M/4)
 template <typename T>
 __device__ __forceinline__ cplx<T> tw_quarter(const cplx<T> *S, int t, int lq) {
     const int q = t >> lq, u = t & ((1 << lq) - 1);
