@@ -234,6 +234,8 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
             rs.push_back(idx[j]);
         }
         P->gl_npairs = (int)x.size();
+        for (int k = 0; k < P->gl_npairs; ++k)
+            if (sh[k] == 0.0) P->gl_pole = k, P->gl_pole_ring[0] = rn[k], P->gl_pole_ring[1] = rs[k];
         RC_TRY(upload(P, &P->d_gl_x, x));
         RC_TRY(upload(P, &P->d_gl_sh, sh));
         RC_TRY(upload(P, &P->d_gl_ch, ch));
@@ -289,6 +291,8 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
             rs.push_back(P->Nt / 2 - k);
         }
         P->cc_npairs = (int)x.size();
+        for (int k = 0; k < P->cc_npairs; ++k)
+            if (sh[k] == 0.0) P->cc_pole = k, P->cc_pole_ring[0] = rn[k], P->cc_pole_ring[1] = rs[k];
         RC_TRY(upload(P, &P->d_cc_x, x));
         RC_TRY(upload(P, &P->d_cc_sh, sh));
         RC_TRY(upload(P, &P->d_cc_ch, ch));

@@ -165,6 +165,8 @@ struct cunusht_plan_s {
     double beta = 0.0;
     int n_lo = 0, nrows = 0;       // fine rows stored: n in [n_lo, n_lo + nrows)
     int cc_npairs = 0;
+    int cc_pole = -1, gl_pole = -1;  // index of the pair (theta = 0, pi) in each pair set, or -1
+    int cc_pole_ring[2] = {0, 0}, gl_pole_ring[2] = {0, 0};  // its ring indices (theta = 0, theta = pi)
     double *d_cc_x = nullptr, *d_cc_sh = nullptr, *d_cc_ch = nullptr;
     int *d_cc_rn = nullptr, *d_cc_rs = nullptr;
     double *d_Dth = nullptr;  // [Nt] deconvolution * 1/Nt, index kappa mod Nt

@@ -28,7 +28,8 @@ int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, co
 
 // legendre_tc.cu: tensor-core synthesis (spin > 0, mixed precision), nb in {1, 2, 4}
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
-                      const double *ch, const int *rn, const int *rs, int ld, int spin, const double2 *G,
+                      const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
+                      int spin, const double2 *G,
                       const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
                       cudaStream_t st);
 int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout);

@@ -1071,11 +1071,16 @@ struct RingPairs {
     const double *x, *sh, *ch;
     const int *rn, *rs;
     int ld;
+    int pole = -1;  // pair (theta = 0, pi), or -1
+    int pole_rn = 0, pole_rs = 0;  // its ring indices
 };
 
 static RingPairs pairs_of(const cunusht_plan_s *P, bool cc) {
-    if (cc) return {P->cc_npairs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn, P->d_cc_rs, P->ncc};
-    return {P->gl_npairs, P->d_gl_x, P->d_gl_sh, P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->nring};
+    if (cc)
+        return {P->cc_npairs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn, P->d_cc_rs, P->ncc,
+                P->cc_pole, P->cc_pole_ring[0], P->cc_pole_ring[1]};
+    return {P->gl_npairs, P->d_gl_x, P->d_gl_sh, P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->nring,
+            P->gl_pole, P->gl_pole_ring[0], P->gl_pole_ring[1]};
 }
 
 template <int NB>
@@ -1131,8 +1136,8 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
             double2 *Hr = H + r0 * hstride;
             if (spin > 0 && P->use_tc) {
                 const int nb = left >= 4 ? 4 : left >= 2 ? 2 : 1;
-                RC_TRY(leg_synth_spin_tc(P, nb, R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, R.ld, spin, Gr, Cr, astride,
-                                         lf, Hr, hstride, st));
+                RC_TRY(leg_synth_spin_tc(P, nb, R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, R.ld, R.pole, R.pole_rn,
+                                         R.pole_rs, spin, Gr, Cr, astride, lf, Hr, hstride, st));
                 r0 += nb;
                 continue;
             }

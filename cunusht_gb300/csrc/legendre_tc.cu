@@ -710,14 +710,84 @@ int tc_plan_init(cunusht_plan_s *P) {
     return CUNUSHT_OK;
 }
 
+// The pole pair (theta = 0, pi) of a spin s >= 1 synthesis: every function
+// vanishes at theta = 0, and at theta = pi all but m = s, where
+// sLambda_ls(pi) = (-1)^l sqrt((2l + 1) / (4 pi)).  The ring values are then
+// one FP64 sum over l per request and component, and zeros; block r handles
+// request r.  Same outputs and signs as the pair in k_leg_synth_spin_tc.
+constexpr int POLE_TPB = 256;
+__global__ void __launch_bounds__(POLE_TPB)
+    k_pole_pair_spin(int L, int spin, int mmax, const double2 *__restrict__ G, const double2 *__restrict__ C,
+                     long long astride, const double *__restrict__ lfac, int rn, int rs, double2 *__restrict__ H,
+                     long long hstride, int ldH) {
+    __shared__ double s_red[4][POLE_TPB / 32];
+    const int r = blockIdx.x, tid = threadIdx.x;
+    double2 *Hr = H + r * hstride;
+    const double2 z = make_double2(0.0, 0.0);
+    for (int m = tid; m <= mmax; m += POLE_TPB) {
+        Hr[(long long)(L + m) * ldH + rn] = z;
+        if (m != spin) Hr[(long long)(L + m) * ldH + rs] = z;
+        if (m > 0) {
+            Hr[(long long)(L - m) * ldH + rs] = z;
+            if (m != spin) Hr[(long long)(L - m) * ldH + rn] = z;
+        }
+    }
+    if (spin > mmax) return;
+    const double2 *Gr = G + r * astride, *Cr = C ? C + r * astride : nullptr;
+    const long long b = almidx(L, spin, spin) - spin;
+    double a_re = 0.0, a_im = 0.0, b_re = 0.0, b_im = 0.0;
+    for (int l = spin + tid; l <= L; l += POLE_TPB) {
+        const double lam = ((l & 1) ? -1.0 : 1.0) * sqrt((2.0 * l + 1.0) / (4.0 * PI));
+        const double f = lfac ? lfac[l] : 1.0;
+        const double par = ((l + spin) & 1) ? -f : f;
+        const double2 g = Gr[b + l];
+        const double2 c = Cr ? Cr[b + l] : z;
+        a_re += f * (g.x - c.y) * lam;
+        a_im += f * (g.y + c.x) * lam;
+        b_re += par * (g.x + c.y) * lam;
+        b_im += par * (c.x - g.y) * lam;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a_re += __shfl_xor_sync(0xffffffffu, a_re, o);
+        a_im += __shfl_xor_sync(0xffffffffu, a_im, o);
+        b_re += __shfl_xor_sync(0xffffffffu, b_re, o);
+        b_im += __shfl_xor_sync(0xffffffffu, b_im, o);
+    }
+    if ((tid & 31) == 0) {
+        s_red[0][tid >> 5] = a_re;
+        s_red[1][tid >> 5] = a_im;
+        s_red[2][tid >> 5] = b_re;
+        s_red[3][tid >> 5] = b_im;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = 0; k < 4; ++k)
+            for (int w = 0; w < POLE_TPB / 32; ++w) t[k] += s_red[k][w];
+        const double sgs = (spin & 1) ? -1.0 : 1.0;
+        Hr[(long long)(L + spin) * ldH + rs] = make_double2(-t[0], -t[1]);
+        Hr[(long long)(L - spin) * ldH + rn] = make_double2(-sgs * t[2], -sgs * t[3]);
+    }
+}
+
 // Ring pairs in full blocks of 256 on the tensor cores; a tail of fewer than
 // TCL_MIN_TAIL pairs after at least one full block (the equator pair of the
 // Clenshaw-Curtis grid, 2^k + 1 rings) goes to the double-float CUDA-core
 // kernel instead of a nearly empty block per order m.
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
-                      const double *ch, const int *rn, const int *rs, int ld, int spin, const double2 *G,
-                      const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
-                      cudaStream_t st) {
+                      const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
+                      int spin, const double2 *G, const double2 *C, long long astride, const double *lf, double2 *H,
+                      long long hstride, cudaStream_t st) {
+    if (pole == 0 && npairs > 1) {
+        // the pole pair in closed form; the tensor cores take the other pairs
+        // (a Clenshaw-Curtis grid of 2^k + 1 rings then fills whole blocks)
+        k_pole_pair_spin<<<nb, POLE_TPB, 0, st>>>(P->lmax, spin, P->mmax, G, C, astride, lf, pole_rn, pole_rs, H,
+                                                  hstride, ld);
+        CU_LAUNCH_CHECK();
+        ++x, ++sh, ++ch, ++rn, ++rs;
+        --npairs;
+    }
     const int per = TCL_T / 2, tail = npairs % per;
     const int ntc = (npairs > per && tail < TCL_MIN_TAIL) ? npairs - tail : npairs;
     if (nb == 4) RC_TRY(launch_synth_tc_nb<4>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
