@@ -41,7 +41,7 @@ sys.path.insert(0, ROOT)
 METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7 (served mixed vs plain FP64); p99 ms"
 # DRAM bytes (read + write) per launch of 4 requests from one ncu capture at
 # lmax 2047 (profiles/launches_served_l2047_spin2_mixed.md)
-LEG_TRAFFIC_B4 = {"leg_synth": 796.0e6, "ptg_leg": 662.8e6}
+LEG_TRAFFIC_B4 = {"leg_synth": 1493.0e6, "ptg_leg": 1354.0e6}  # records + pole + tensor-core kernels, ncu
 
 
 def parse():
@@ -368,17 +368,19 @@ def main():
                     "traffic": None, "kernel": dom,
                     "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)"}
         else:
-            # double-float Legendre on the FP32 pipe: 152 SMs x 128 lanes x 2 flop x max SM clock
+            # Legendre: double-float recursion on the FP32 pipe (the bound), contraction on the
+            # tensor cores; peak = 152 SMs x 128 lanes x 2 flop x max SM clock
             mhz = peaks.get("sm_max_mhz", 2070.0)
             peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
             tr = LEG_TRAFFIC_B4.get(dom)
             roof = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                     "traffic": tr * B / 4 if tr else None, "kernel": dom,
                     "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; "
-                                   "achieved counts algorithmic flops only (8 per l,m,ring,component), "
-                                   "the double-float arithmetic issues ~15x more: ncu FMA-pipe "
-                                   "utilisation 73 %, issue slots 91 % (profiles/leg_synth_spin_df_l2047.md); "
-                                   "traffic measured per launch of 4 requests "
+                                   "achieved counts algorithmic flops only (8 per l,m,ring,component); the "
+                                   "double-float recursion and digit split bound the kernel on the CUDA cores "
+                                   "(ncu: issue slots 70 %, FMA pipe 55 %) while the contraction runs on the "
+                                   "tensor cores (tensor pipe 10 %) (profiles/leg_synth_tc_l2047.md); "
+                                   "traffic = DRAM bytes of the stage's kernels per launch of 4 requests "
                                    "(profiles/launches_served_l2047_spin2_mixed.md), scaled to the batch size"}
     stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
                        "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
@@ -458,7 +460,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if T.info["precision"] == 1 else
-                         "mixed: double-float (f32 hi/lo) Legendre + FFTs, f32 fine grid, f64 seeds/pointing",
+                         "mixed: double-float (f32 hi/lo) Legendre recursion with exact integer-digit bf16 "
+                         "tensor-core contraction, double-float FFTs, f32 fine grid, f64 seeds/pointing",
                 "data": "synthetic (seeded Gaussian alm / deflection, 2.5 arcmin rms)",
                 "config": {"workload": f"served lensing solves lmax={lmax} GL {lmax + 1}x{nphi} spin-{spin} "
                                        f"eps={eps}, {B} requests per launch",
