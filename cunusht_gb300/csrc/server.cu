@@ -213,12 +213,35 @@ int launch(cunusht_server_s *S, Slot *sl, std::deque<Req> &q) {
     return CUNUSHT_OK;
 }
 
+// Release the buckets other than keep whose queue is empty and whose slots
+// have nothing in flight; true if any was released.
+bool release_idle(cunusht_server_s *S, const Key &keep) {
+    bool released = false;
+    for (auto it = S->buckets.begin(); it != S->buckets.end();) {
+        bool idle = S->queues[it->first].empty();
+        for (auto &s : it->second.slots) idle = idle && s->busy.empty();
+        if (idle && it->first != keep) {
+            it = S->buckets.erase(it);
+            released = true;
+        } else {
+            ++it;
+        }
+    }
+    return released;
+}
+
 int admit(cunusht_server_s *S, const Key &k, bool &ok) {
     ok = S->buckets.count(k) > 0;
     if (ok) return CUNUSHT_OK;
-    const size_t used = S->used();
+    size_t used = S->used();
     auto bl = S->blocked.find(k);
-    if (bl != S->blocked.end() && used >= bl->second) return CUNUSHT_OK;  // nothing released since
+    if (bl != S->blocked.end() && used >= bl->second) {
+        // nothing released since the last refusal: release the buckets that
+        // have gone idle since then (a refusal while they were busy released
+        // nothing), or keep waiting if none has
+        if (!release_idle(S, k)) return CUNUSHT_OK;
+        used = S->used();
+    }
     const auto pol = S->policy_of(std::get<0>(k));
     Bucket b;
     size_t add = 0;
@@ -235,13 +258,7 @@ int admit(cunusht_server_s *S, const Key &k, bool &ok) {
     if (b.slots.empty()) {
         S->refusals += 1;
         S->blocked[k] = used;
-        // release idle buckets with empty queues
-        for (auto it = S->buckets.begin(); it != S->buckets.end();) {
-            bool idle = S->queues[it->first].empty();
-            for (auto &s : it->second.slots) idle = idle && s->busy.empty();
-            if (idle && it->first != k) it = S->buckets.erase(it);
-            else ++it;
-        }
+        release_idle(S, k);
         return CUNUSHT_OK;
     }
     S->blocked.erase(k);

@@ -140,7 +140,12 @@ class LensingServer:
             return True
         used = self.used_bytes()
         if key in self._blocked and used >= self._blocked[key]:
-            return False                        # nothing was released since the last refusal
+            # nothing was released since the last refusal: release the buckets
+            # that have gone idle since then, or keep waiting if none has
+            if not self._evict_idle(keep=key):
+                return False
+            torch.cuda.empty_cache()
+            used = self.used_bytes()
         lmax, spin, eps = key
         nb, nslots = self.policy(lmax)
         slots = []
@@ -164,10 +169,15 @@ class LensingServer:
         self.buckets[key] = slots
         return True
 
-    def _evict_idle(self, keep):
+    def _evict_idle(self, keep) -> bool:
+        """Release the buckets other than keep with an empty queue and no launch
+        in flight; True if any was released."""
+        released = False
         for k in list(self.buckets):
             if k != keep and not self.queues[k] and all(not sl.busy for sl in self.buckets[k]):
                 del self.buckets[k]
+                released = True
+        return released
 
     def prewarm(self, keys) -> list:
         """Create the slots of these buckets ahead of traffic (within the

@@ -187,3 +187,53 @@ def test_server_mixed_stream_matches_isolated_results(built_lib, native):
         else:
             err = float(torch.max(torch.abs(got.reshape(ref.shape) - ref)))
             assert err <= tol * scale, (i, kind, lmax, spin, eps, err / scale)
+
+
+@pytest.mark.parametrize("native", [False, True])
+def test_server_admits_after_refusal_while_busy(built_lib, native):
+    """Two buckets whose requests arrive together under a budget that holds
+    only one: the second is refused while the first is busy, and must still
+    be admitted once the first has gone idle (no further refusal or release
+    event comes)."""
+    import time
+    from cunusht_gb300.serving import LensingServer, NativeLensingServer
+    lmax = 63
+    keys = [(lmax, 0, 1e-7), (lmax, 2, 1e-7)]
+
+    def make(budget):
+        if native:
+            return NativeLensingServer(hbm_budget_bytes=budget, precision="mixed", policy={lmax: (2, 1)})
+        return LensingServer(max_batch=2, slots_per_bucket=1, hbm_budget_bytes=budget, precision="mixed")
+
+    def payload(spin, seed):
+        gc, dl = orc.make_inputs(lmax, spin, seed=seed)
+        return torch.as_tensor(gc if spin else gc[0], device="cuda"), torch.as_tensor(dl[0], device="cuda")
+
+    def used(srv):
+        return srv.stats()["bytes"] if native else srv.used_bytes()
+
+    sizes = []
+    for i, (L, s, e) in enumerate(keys):
+        probe = make(1e13)
+        probe.submit("g2l", L, s, e, *payload(s, 300 + i))
+        probe.run_until_idle()
+        torch.cuda.synchronize()
+        sizes.append(used(probe))
+        if native:
+            probe.close()
+        del probe
+        torch.cuda.empty_cache()
+    budget = max(sizes) + 0.5 * min(sizes)  # one bucket fits, both do not
+    srv = make(budget)
+    for i, (L, s, e) in enumerate(keys):
+        srv.submit("g2l", L, s, e, *payload(s, 400 + i))
+    t0 = time.perf_counter()
+    while srv.step():
+        assert time.perf_counter() - t0 < 120, "a refused bucket was never admitted"
+        time.sleep(1e-3)
+    torch.cuda.synchronize()
+    assert len(srv.completed) == len(keys)
+    refusals = srv.stats()["refusals"] if native else srv.rejected_admissions
+    assert refusals >= 1  # the second bucket was refused while the first ran
+    if native:
+        srv.close()
