@@ -660,6 +660,7 @@ int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     RC_TRY(dalloc(P, &P->d_glmapb, B * 2 * (size_t)P->npix));
     RC_TRY(dalloc(P, &P->d_ptgb, B * 2 * (size_t)P->npix));
     RC_TRY(dalloc(P, &P->d_gamb, B * (size_t)P->npix));
+    if (P->prec == CUNUSHT_PREC_MIXED) RC_TRY(tc_reserve(P, max_batch));
     P->batch_cap = max_batch;
     return CUNUSHT_OK;
 }

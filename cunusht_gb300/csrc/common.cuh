@@ -184,6 +184,8 @@ struct cunusht_plan_s {
     int *d_tc_woff[3] = {nullptr, nullptr, nullptr};
     unsigned char *d_tc_rec = nullptr;
     size_t tc_rec_bytes = 0;
+    size_t tc_nrec = 0;  // window records per call (the larger of spin 1 and 2)
+    int tc_rec_nb = 0;   // requests per launch the record buffer holds (1 at creation, up to 4 by reserve_batch)
 
     // FFT twiddles e^{-2 pi i t / TW}
     int TW = 0;

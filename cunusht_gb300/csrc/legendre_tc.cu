@@ -678,6 +678,11 @@ static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double 
                               cudaStream_t st) {
     using LY = TclLayout<NB>;
     const int L = P->lmax;
+    if (P->tc_rec_nb < NB) {
+        set_error("tensor-core records hold %d requests per launch, %d asked (cunusht_plan_reserve_batch)",
+                  P->tc_rec_nb, NB);
+        return CUNUSHT_ERR_ARG;
+    }
     const dim3 rgrid((L - spin + 1 + TCL_W - 1) / TCL_W, P->mmax + 1);  // m <= spin has the most windows
     k_tc_records<NB><<<rgrid, TCL_W, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm_tab,
                                               P->d_tc_woff[spin], P->d_tc_rec);
@@ -688,6 +693,35 @@ static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double 
                                                                 P->d_lg0[spin], npairs, x, sh, ch, rn, rs, H, hstride, ld,
                                                                 P->d_status);
     CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+static size_t tcl_record_bytes(int nb) {
+    return nb >= 4 ? TclLayout<4>::RSZ : nb >= 2 ? TclLayout<2>::RSZ : TclLayout<1>::RSZ;
+}
+
+// record buffer for launches of up to nb (<= 4) requests; grows only
+int tc_reserve(cunusht_plan_s *P, int nb) {
+    nb = std::min(nb, 4);
+    if (nb <= P->tc_rec_nb || P->tc_nrec == 0) return CUNUSHT_OK;
+    const size_t bytes = P->tc_nrec * tcl_record_bytes(nb);
+    if (P->d_tc_rec) {
+        CU_TRY(cudaDeviceSynchronize());  // the old buffer may still be read by queued work
+        cudaFree(P->d_tc_rec);
+        P->ws_bytes -= P->tc_rec_bytes;
+        P->d_tc_rec = nullptr;
+        P->tc_rec_bytes = 0;
+        P->tc_rec_nb = 0;
+    }
+    const cudaError_t e = cudaMalloc(&P->d_tc_rec, bytes);
+    if (e != cudaSuccess) {
+        P->d_tc_rec = nullptr;
+        set_error("cudaMalloc of %zu bytes (tensor-core window records) failed: %s", bytes, cudaGetErrorString(e));
+        return CUNUSHT_ERR_ALLOC;
+    }
+    P->tc_rec_bytes = bytes;
+    P->ws_bytes += bytes;
+    P->tc_rec_nb = nb;
     return CUNUSHT_OK;
 }
 
@@ -702,12 +736,8 @@ int tc_plan_init(cunusht_plan_s *P) {
         P->ws_bytes += wo.size() * sizeof(int);
         nrec = std::max(nrec, (size_t)wo[L + 1]);
     }
-    P->tc_rec_bytes = nrec * (size_t)TclLayout<4>::RSZ;  // four requests per launch at most
-    if (P->tc_rec_bytes) {
-        CU_TRY(cudaMalloc(&P->d_tc_rec, P->tc_rec_bytes));
-        P->ws_bytes += P->tc_rec_bytes;
-    }
-    return CUNUSHT_OK;
+    P->tc_nrec = nrec;
+    return tc_reserve(P, 1);  // single requests; cunusht_plan_reserve_batch grows it
 }
 
 // The pole pair (theta = 0, pi) of a spin s >= 1 synthesis: every function
