@@ -310,6 +310,77 @@ __global__ void __launch_bounds__(FFT_TPB)
     }
 }
 
+// Theta pass of two columns at once (transforms unsplit, SP = 1): the torus
+// extensions of columns c1 = 2b and c2 = 2b + 1 have opposite symmetry
+// (x_{-k} = s x_k with s = (-1)^(|m| + spin), and consecutive m alternate), so
+// one complex transform of z = x1 + i x2 carries both:
+//     X1_j = (Z_j + s1 Z_{-j}) / 2,   X2_j = (Z_j - s1 Z_{-j}) / (2i).
+// The deconvolved spectra recombine as W = Y1 + i Y2, whose inverse
+// w = y1 + i y2 separates the same way (the outputs keep the symmetry of their
+// columns).  Half the transforms of k_theta_fwd; the separation adds an
+// absolute error of the transform's rounding times the partner column.
+template <typename T>
+__global__ void __launch_bounds__(FFT_TPB)
+    k_theta_fwd2(const double2 *__restrict__ H, int ldH, int Nt, int Ntf, int spin, int mofs, int L,
+                 const double *__restrict__ Dth, const double *__restrict__ Dph, cplx<T> *__restrict__ F, int ncols,
+                 int n_lo, int nrows, const cplx<T> *__restrict__ tw, int TW, long long hbs, long long fbs) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *buf = reinterpret_cast<C *>(smem_raw);
+    const C *stw = load_twiddles<T>(buf, Ntf, tw, TW);
+    H += blockIdx.y * hbs;  // request of a batch
+    F += blockIdx.y * fbs;
+    const int c1 = 2 * blockIdx.x, c2 = c1 + 1;
+    const bool two = c2 < ncols;
+    const int m1 = c1 - mofs;
+    const double s1 = ((abs(m1) + spin) & 1) ? -1.0 : 1.0, s2 = -s1;
+    const double2 *col1 = H + (long long)c1 * ldH, *col2 = H + (long long)c2 * ldH;
+    const int half = Nt / 2;
+    const double dm1 = Dph[m1 + L], dm2 = two ? Dph[m1 + 1 + L] : 0.0;
+    for (int k = threadIdx.x; k < Nt; k += blockDim.x) {
+        const bool lo = k <= half;
+        const int kk = lo ? k : Nt - k;
+        double2 v1 = col1[kk], v2 = two ? col2[kk] : make_double2(0.0, 0.0);
+        if (!lo) {
+            v1 = make_double2(s1 * v1.x, s1 * v1.y);
+            v2 = make_double2(s2 * v2.x, s2 * v2.y);
+        }
+        buf[k] = mk<T>(cvt<T>(v1.x - v2.y), cvt<T>(v1.y + v2.x));  // x1 + i x2
+    }
+    __syncthreads();
+    fft_smem<T>(buf, Nt, -1, stw, Ntf);
+    // separate, deconvolve, recombine; thread j owns the frequencies +-j
+    // (reads j and Nt - j, writes j and Ntf - j: no other thread touches them);
+    // the Nyquist term is dropped (Dth[half] = 0)
+    const T hf = cvt<T>(0.5), ts1 = cvt<T>(s1), ts2 = cvt<T>(s2);
+    for (int j = threadIdx.x; j < half; j += blockDim.x) {
+        const int jn = j ? Nt - j : 0;
+        const C zp = buf[j], zn = cscale(buf[jn], ts1);
+        const C x1 = cscale(cadd(zp, zn), hf);
+        const C d = cscale(csub(zp, zn), hf);
+        const C x2 = mk<T>(d.y, -d.x);  // d / i
+        const C y1 = cscale(x1, cvt<T>(Dth[j] * dm1)), y2 = cscale(x2, cvt<T>(Dth[j] * dm2));
+        buf[j] = mk<T>(y1.x - y2.y, y1.y + y2.x);  // y1 + i y2
+        if (j) {
+            const C y1n = cscale(y1, ts1), y2n = cscale(y2, ts2);  // Y_{-j} = s Y_j (D even)
+            buf[Ntf - j] = mk<T>(y1n.x - y2n.y, y1n.y + y2n.x);
+        }
+    }
+    __syncthreads();
+    for (int i = half + threadIdx.x; i <= Ntf - half; i += blockDim.x) buf[i] = czero<T>();
+    __syncthreads();
+    fft_smem<T>(buf, Ntf, +1, stw, Ntf);
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const int n = wrap2(r + n_lo, Ntf);
+        const C wp = buf[n], wn = cscale(buf[wrap2(-n, Ntf)], ts1);
+        F[(long long)r * ncols + c1] = cscale(cadd(wp, wn), hf);
+        if (two) {
+            const C d = cscale(csub(wp, wn), hf);
+            F[(long long)r * ncols + c2] = mk<T>(d.y, -d.x);
+        }
+    }
+}
+
 // SP = 2: Z_k = E_k + e^{-i pi k / Nt} O_k with E / O the Nt-point transforms
 // of the even / odd fine rows: launched for q = 1 (odd rows, phase applied,
 // written to the scratch S, Nt values per column), then q = 0 (even rows plus
@@ -720,6 +791,27 @@ int theta_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *
     const int mofs = spin ? L : 0;
     size_t sm = fft_smem_bytes(P->Ntf / P->sp_theta, P->grid_fp32);
     dim3 grid(ncols, nreq, P->sp_theta);
+    if (P->sp_theta == 1) {  // two columns per block
+        const dim3 g2((ncols + 1) / 2, nreq);
+        if (P->grid_fp32) {
+            RC_TRY(set_smem(k_theta_fwd2<float>, sm));
+            k_theta_fwd2<float><<<g2, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
+                                                         (float2 *)F, ncols, P->n_lo, P->nrows, P->d_tw32, P->TW, hbs,
+                                                         fbs);
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_theta_fwd2<dfl>, sm));
+            k_theta_fwd2<dfl><<<g2, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
+                                                       (dcplx *)F, ncols, P->n_lo, P->nrows, (const dcplx *)P->d_twdf,
+                                                       P->TW, hbs, fbs);
+        } else {
+            RC_TRY(set_smem(k_theta_fwd2<double>, sm));
+            k_theta_fwd2<double><<<g2, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth,
+                                                          P->d_Dph, (double2 *)F, ncols, P->n_lo, P->nrows,
+                                                          P->d_tw64, P->TW, hbs, fbs);
+        }
+        CU_LAUNCH_CHECK();
+        return CUNUSHT_OK;
+    }
     if (P->grid_fp32) {
         RC_TRY(set_smem(k_theta_fwd<float>, sm));
         k_theta_fwd<float><<<grid, FFT_TPB, sm, st>>>(H, P->ncc, P->Nt, P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph,
