@@ -839,6 +839,83 @@ int theta_fwd(const cunusht_plan_s *P, int spin, const double2 *H, void *F, cuda
 // nreq requests: F + r fbs, H + r hbs (elements); the split transform's
 // scratch is the request's fine-grid workspace U + r ubs (consumed by the phi
 // pass adjoint before this pass runs)
+// Adjoint theta pass of two columns at once (SP = 1).  Every step between the
+// fine-grid column and the fold (transforms, band limit, even deconvolution)
+// commutes with the reflection n -> -n, and the fold keeps only the part of
+// symmetry s = (-1)^(|m| + spin): each input column is first projected onto
+// it, g_s = (g + s g_{-n}) / 2, after which columns c1 = 2b, c2 = 2b + 1 (of
+// opposite s) share the transforms as in k_theta_fwd2.  The fold of the
+// s-symmetric result is 2 y_k inside and y_k at the pole rings k = 0, Nt/2;
+// there an odd column's opposite-symmetry part is dropped, which meets the
+// Legendre adjoint's zero weight at the poles for those columns.
+template <typename T>
+__global__ void __launch_bounds__(FFT_TPB)
+    k_theta_adj2(const cplx<T> *__restrict__ F, int ncols, int n_lo, int nrows, int Nt, int Ntf, int spin, int mofs,
+                 int L, const double *__restrict__ Dth, const double *__restrict__ Dph, double2 *__restrict__ H,
+                 int ldH, const cplx<T> *__restrict__ tw, int TW, long long fbs, long long hbs) {
+    using C = cplx<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *buf = reinterpret_cast<C *>(smem_raw);
+    const C *stw = load_twiddles<T>(buf, Ntf, tw, TW);
+    F += blockIdx.y * fbs;  // request of a batch
+    H += blockIdx.y * hbs;
+    const int c1 = 2 * blockIdx.x, c2 = c1 + 1;
+    const bool two = c2 < ncols;
+    const int m1 = c1 - mofs;
+    const double s1 = ((abs(m1) + spin) & 1) ? -1.0 : 1.0, s2 = -s1;
+    const int half = Nt / 2;
+    const double dm1 = Dph[m1 + L], dm2 = two ? Dph[m1 + 1 + L] : 0.0;
+    const T hf = cvt<T>(0.5), ts1 = cvt<T>(s1), ts2 = cvt<T>(s2);
+    // z_n = g1s_n + i g2s_n for the pair (n, -n); rows outside the stored band are zero
+    auto row = [&](int n, int c) -> C {
+        const int r = wrap2(n - n_lo, Ntf);
+        return r < nrows ? F[(long long)r * ncols + c] : czero<T>();
+    };
+    for (int n = threadIdx.x; n <= Ntf / 2; n += blockDim.x) {
+        const int nn = wrap2(-n, Ntf);
+        const C a1 = row(n, c1), b1 = row(nn, c1);
+        const C a2 = two ? row(n, c2) : czero<T>(), b2 = two ? row(nn, c2) : czero<T>();
+        const C p1 = cscale(cadd(a1, cscale(b1, ts1)), hf), p2 = cscale(cadd(a2, cscale(b2, ts2)), hf);
+        buf[n] = mk<T>(p1.x - p2.y, p1.y + p2.x);
+        if (nn != n) {
+            const C q1 = cscale(p1, ts1), q2 = cscale(p2, ts2);
+            buf[nn] = mk<T>(q1.x - q2.y, q1.y + q2.x);
+        }
+    }
+    __syncthreads();
+    fft_smem<T>(buf, Ntf, -1, stw, Ntf);
+    // separate, deconvolve, recombine into the Nt-point band; thread j owns +-j
+    // (reads j and Ntf - j, writes j and Nt - j); the Nyquist term is zero
+    for (int j = threadIdx.x; j < half; j += blockDim.x) {
+        const int jn = j ? Ntf - j : 0;
+        const C zp = buf[j], zn = cscale(buf[jn], ts1);
+        const C x1 = cscale(cadd(zp, zn), hf);
+        const C d = cscale(csub(zp, zn), hf);
+        const C x2 = mk<T>(d.y, -d.x);
+        const C y1 = cscale(x1, cvt<T>(Dth[j] * dm1)), y2 = cscale(x2, cvt<T>(Dth[j] * dm2));
+        buf[j] = mk<T>(y1.x - y2.y, y1.y + y2.x);
+        if (j) {
+            const C y1n = cscale(y1, ts1), y2n = cscale(y2, ts2);
+            buf[Nt - j] = mk<T>(y1n.x - y2n.y, y1n.y + y2n.x);
+        }
+    }
+    if (threadIdx.x == 0) buf[half] = czero<T>();
+    __syncthreads();
+    fft_smem<T>(buf, Nt, +1, stw, Ntf);
+    double2 *col1 = H + (long long)c1 * ldH, *col2 = H + (long long)c2 * ldH;
+    for (int k = threadIdx.x; k <= half; k += blockDim.x) {
+        const C wp = buf[k], wn = cscale(buf[k ? Nt - k : 0], ts1);
+        const bool pole = k == 0 || k == half;
+        const T f = pole ? hf : cvt<T>(1.0);  // 2 y_k inside, y_k at the poles
+        const C v1 = cscale(cadd(wp, wn), f);
+        col1[k] = make_double2(to_d(v1.x), to_d(v1.y));
+        if (two) {
+            const C d = cscale(csub(wp, wn), f);
+            col2[k] = make_double2(to_d(d.y), to_d(-d.x));
+        }
+    }
+}
+
 int theta_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, double2 *H,
                     long long hbs, void *U, long long ubs_bytes, cudaStream_t st) {
     const int L = P->lmax;
@@ -847,6 +924,22 @@ int theta_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, 
     const int SP = P->sp_theta;
     size_t sm = fft_smem_bytes(P->Ntf / SP, P->grid_fp32);
     dim3 grid(ncols, nreq);
+    if (SP == 1) {  // two columns per block
+        const dim3 g2((ncols + 1) / 2, nreq);
+        if (P->grid_fp32) {
+            RC_TRY(set_smem(k_theta_adj2<float>, sm));
+            k_theta_adj2<float><<<g2, FFT_TPB, sm, st>>>((const float2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
+                                                         spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32,
+                                                         P->TW, fbs, hbs);
+        } else {
+            RC_TRY(set_smem(k_theta_adj2<double>, sm));
+            k_theta_adj2<double><<<g2, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt,
+                                                          P->Ntf, spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc,
+                                                          P->d_tw64, P->TW, fbs, hbs);
+        }
+        CU_LAUNCH_CHECK();
+        return CUNUSHT_OK;
+    }
     for (int q = SP - 1; q >= 0; --q) {
         if (P->grid_fp32) {
             RC_TRY(set_smem(k_theta_adj<float>, sm));
