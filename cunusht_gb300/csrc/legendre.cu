@@ -1176,6 +1176,36 @@ int leg_synth(const cunusht_plan_s *P, int spin, const double2 *G, const double2
     return leg_synth_batch(P, 1, spin, G, C, 0, use_lfac, cc, H, 0, st);
 }
 
+// Adjoint of the pole ring pair (theta = 0, pi) for spin s >= 1: every
+// function vanishes at theta = 0 and at pi all but m = s, with
+// sLambda_ls(pi) = (-1)^l sqrt((2l + 1) / (4 pi)), so the pair adds, for
+// m = s only, the terms k_leg_adj_spin_df forms from its S ring (P = lambda
+// h(+m, pi), Q = par lambda conj(h(-m, 0))), in FP64; block row r = request r.
+__global__ void k_pole_pair_adj_spin(int L, int spin, int ncomp, int mmax, const double2 *__restrict__ H,
+                                     long long hstride, int ldH, const double *__restrict__ lfac, int rn, int rs,
+                                     double *__restrict__ Gout, double *__restrict__ Cout, long long astride) {
+    if (spin > mmax) return;
+    const int r = blockIdx.y;
+    const double2 *Hr = H + r * hstride;
+    const double2 hps = Hr[(long long)(L + spin) * ldH + rs], hmn = Hr[(long long)(L - spin) * ldH + rn];
+    const double sgs = (spin & 1) ? -1.0 : 1.0;
+    const long long b = almidx(L, spin, spin) - spin;
+    double *Gr = Gout + 2 * r * astride, *Cr = Cout ? Cout + 2 * r * astride : nullptr;
+    for (int l = spin + blockIdx.x * blockDim.x + threadIdx.x; l <= L; l += gridDim.x * blockDim.x) {
+        const double lam = ((l & 1) ? -1.0 : 1.0) * sqrt((2.0 * l + 1.0) / (4.0 * PI));
+        const double f = lfac ? lfac[l] : 1.0;
+        const bool odd = (l + spin) & 1;
+        const double Pr = lam * hps.x, Pi = lam * hps.y, qr = lam * hmn.x, qi = lam * hmn.y;
+        const double Qr = sgs * (odd ? -qr : qr), Qi = sgs * (odd ? qi : -qi);
+        atomicAdd(Gr + 2 * (b + l), -0.5 * f * (Pr + Qr));
+        atomicAdd(Gr + 2 * (b + l) + 1, -0.5 * f * (Pi + Qi));
+        if (ncomp > 1) {
+            atomicAdd(Cr + 2 * (b + l), -0.5 * f * (Pi - Qi));
+            atomicAdd(Cr + 2 * (b + l) + 1, 0.5 * f * (Pr - Qr));
+        }
+    }
+}
+
 template <int NB>
 static void launch_adj_df(const cunusht_plan_s *P, const RingPairs &R, dim3 grid, int spin, int ncomp,
                           const double2 *H, long long hstride, const double *lf, double2 *G, double2 *C,
@@ -1205,18 +1235,29 @@ int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, co
     dim3 grid((R.npairs + LEG_TPB - 1) / LEG_TPB, P->mmax + 1);
     const double *lf = use_lfac ? P->d_lfac : nullptr;
     if (P->prec == CUNUSHT_PREC_MIXED && P->d_coef_df[spin]) {
+        RingPairs Rm = R;
+        if (spin > 0 && R.pole == 0 && R.npairs > 1) {
+            // the pole pair in closed form; the other 2^k pairs fill whole blocks
+            k_pole_pair_adj_spin<<<dim3((L - spin + 256) / 256, nreq), 256, 0, st>>>(
+                L, spin, ncomp, P->mmax, H, hstride, R.ld, lf, R.pole_rn, R.pole_rs, (double *)G,
+                (spin > 0 && ncomp > 1) ? (double *)C : nullptr, astride);
+            CU_LAUNCH_CHECK();
+            ++Rm.x, ++Rm.sh, ++Rm.ch, ++Rm.rn, ++Rm.rs;
+            --Rm.npairs;
+            grid.x = (Rm.npairs + LEG_TPB - 1) / LEG_TPB;
+        }
         for (int r0 = 0; r0 < nreq;) {
             const int left = nreq - r0;
             const double2 *Hr = H + r0 * hstride;
             double2 *Gr = G + r0 * astride, *Cr = (spin > 0 && ncomp > 1) ? C + r0 * astride : nullptr;
             if (left >= 4) {
-                launch_adj_df<4>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+                launch_adj_df<4>(P, Rm, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
                 r0 += 4;
             } else if (left >= 2) {
-                launch_adj_df<2>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+                launch_adj_df<2>(P, Rm, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
                 r0 += 2;
             } else {
-                launch_adj_df<1>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+                launch_adj_df<1>(P, Rm, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
                 r0 += 1;
             }
             CU_LAUNCH_CHECK();
