@@ -101,15 +101,27 @@ __device__ __forceinline__ float df_prod(float ah, float al, dfl lam) {
     return fmaf(ah, lam.h, fmaf(al, lam.h, ah * lam.l));
 }
 
-// operators so that templated complex code (FFT butterflies) runs on dfl
+// a + b as an unnormalised (value, error) pair: TwoSum of the leading terms,
+// the error terms added.  The same accuracy as df_add relative to the
+// operands (renormalising adds none) in 8 FP32 operations and 5 dependent
+// steps instead of 11 and 8; products (df_mul) accept such pairs.
+__device__ __forceinline__ dfl df_add_u(dfl a, dfl b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float t = (a.h - (s - bb)) + (b.h - bb);
+    return dfl{s, (a.l + b.l) + t};
+}
+
+// operators so that templated complex code (FFT butterflies) runs on dfl;
+// additions leave unnormalised pairs (df_add_u), products renormalise
 __host__ __device__ __forceinline__ dfl df_neg(dfl a) {
     dfl r;
     r.h = -a.h;
     r.l = -a.l;
     return r;
 }
-__device__ __forceinline__ dfl operator+(dfl a, dfl b) { return df_add(a, b); }
-__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ dfl operator+(dfl a, dfl b) { return df_add_u(a, b); }
+__device__ __forceinline__ dfl operator-(dfl a, dfl b) { return df_add_u(a, df_neg(b)); }
 __device__ __forceinline__ dfl operator-(dfl a) { return df_neg(a); }
 __device__ __forceinline__ dfl operator*(dfl a, dfl b) { return df_mul(a, b); }
 // scale by +-1 (FFT direction) or a power of two: exact

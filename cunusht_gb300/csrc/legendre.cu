@@ -666,22 +666,15 @@ __global__ void __launch_bounds__(LEG_TPB)
 // are double-float additions, converted to FP64 once per (l, m) and block for
 // the atomic accumulation.  No FP64 arithmetic in the inner loop.
 
-// The adjoint sums keep (value, error) pairs unnormalised: the same ~2^-48 of
-// the operands as normalised double-floats (renormalising adds no accuracy),
-// with a product of 4 and an addition of 8 FP32 operations instead of 7 and 11.
+// The adjoint sums keep (value, error) pairs unnormalised (df_add_u): the same
+// ~2^-48 of the operands as normalised double-floats (renormalising adds no
+// accuracy), a product of 4 FP32 operations instead of 7.
 __device__ __forceinline__ dfl prod_pair(dfl lam, float hh, float hl) {
     const float p = lam.h * hh;
     float e = fmaf(lam.h, hh, -p);
     e = fmaf(lam.h, hl, e);
     e = fmaf(lam.l, hh, e);
     return dfl{p, e};
-}
-// TwoSum of the leading terms, the error terms added
-__device__ __forceinline__ dfl pair_add(dfl a, dfl b) {
-    const float s = a.h + b.h;
-    const float bb = s - a.h;
-    const float t = (a.h - (s - bb)) + (b.h - bb);
-    return dfl{s, (a.l + b.l) + t};
 }
 
 __device__ __forceinline__ dfl shfl_xor_df(dfl v, int mask) {
@@ -696,29 +689,29 @@ __device__ __forceinline__ void warp_reduce_scatter16_df(dfl v[16]) {
         const bool up = lane & 16;
         const dfl send = up ? v[i] : v[i + 8];
         const dfl keep = up ? v[i + 8] : v[i];
-        v[i] = pair_add(keep, shfl_xor_df(send, 16));
+        v[i] = df_add_u(keep, shfl_xor_df(send, 16));
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const bool up = lane & 8;
         const dfl send = up ? v[i] : v[i + 4];
         const dfl keep = up ? v[i + 4] : v[i];
-        v[i] = pair_add(keep, shfl_xor_df(send, 8));
+        v[i] = df_add_u(keep, shfl_xor_df(send, 8));
     }
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
         const bool up = lane & 4;
         const dfl send = up ? v[i] : v[i + 2];
         const dfl keep = up ? v[i + 2] : v[i];
-        v[i] = pair_add(keep, shfl_xor_df(send, 4));
+        v[i] = df_add_u(keep, shfl_xor_df(send, 4));
     }
     {
         const bool up = lane & 2;
         const dfl send = up ? v[0] : v[1];
         const dfl keep = up ? v[1] : v[0];
-        v[0] = pair_add(keep, shfl_xor_df(send, 2));
+        v[0] = df_add_u(keep, shfl_xor_df(send, 2));
     }
-    v[0] = pair_add(v[0], shfl_xor_df(v[0], 1));
+    v[0] = df_add_u(v[0], shfl_xor_df(v[0], 1));
 }
 
 // lam * (hh + hl) as a normalised double-float (the lam.l * hl term dropped)
@@ -921,10 +914,10 @@ __global__ void __launch_bounds__(LEG_TPB)
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 // P = lN hpn + lS hps ; Q = par (lS conj(hmn) + lN conj(hms))
-                v[4 * i + 0] = pair_add(prod_pair(lN[i], PN[r].xh, PN[r].xl), prod_pair(lS[i], PS[r].xh, PS[r].xl));
-                v[4 * i + 1] = pair_add(prod_pair(lN[i], PN[r].yh, PN[r].yl), prod_pair(lS[i], PS[r].yh, PS[r].yl));
-                const dfl qr = pair_add(prod_pair(lS[i], MN[r].xh, MN[r].xl), prod_pair(lN[i], MS[r].xh, MS[r].xl));
-                const dfl qi = pair_add(prod_pair(lS[i], MN[r].yh, MN[r].yl), prod_pair(lN[i], MS[r].yh, MS[r].yl));
+                v[4 * i + 0] = df_add_u(prod_pair(lN[i], PN[r].xh, PN[r].xl), prod_pair(lS[i], PS[r].xh, PS[r].xl));
+                v[4 * i + 1] = df_add_u(prod_pair(lN[i], PN[r].yh, PN[r].yl), prod_pair(lS[i], PS[r].yh, PS[r].yl));
+                const dfl qr = df_add_u(prod_pair(lS[i], MN[r].xh, MN[r].xl), prod_pair(lN[i], MS[r].xh, MS[r].xl));
+                const dfl qi = df_add_u(prod_pair(lS[i], MN[r].yh, MN[r].yl), prod_pair(lN[i], MS[r].yh, MS[r].yl));
                 const bool odd = (lb + i + m) & 1;
                 v[4 * i + 2] = odd ? df_neg(qr) : qr;
                 v[4 * i + 3] = odd ? qi : df_neg(qi);
