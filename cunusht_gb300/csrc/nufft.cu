@@ -10,6 +10,8 @@
 // r = n - n_lo), each row Npf longitudes; real (spin 0) or complex (spin s).
 // Points are read in the caller's order; for lensing they are the deflected
 // pixels in ring order, so neighbouring threads touch neighbouring columns.
+#include <type_traits>
+
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.cuh"
@@ -65,20 +67,30 @@ __device__ __forceinline__ void load_point(const double *loc, long long j, long 
     }
 }
 
-template <typename T>
+template <typename T, int W = MAXW>
 __device__ __forceinline__ void weights(const PointCoords &pc, int w, T beta, T *kt, T *kp) {
     const T s = (T)2 / (T)w;
 #pragma unroll
-    for (int a = 0; a < MAXW; ++a) {
-        if (a < w) {
+    for (int a = 0; a < W; ++a) {
+        if (W < MAXW || a < w) {  // exact trip count when the width is a template argument
             kt[a] = es_kernel<T>(((T)pc.ft + (T)a) * s, beta);
             kp[a] = es_kernel<T>(((T)pc.fp + (T)a) * s, beta);
         }
     }
 }
 
+// f(std::integral_constant<int, w>) for a runtime kernel width 2 <= w <= MAXW:
+// kernels whose tap loops take the width as a template argument run exactly
+// w x w taps instead of MAXW-wide predicated loops
+template <int W0 = 2, typename F> static void with_width(int w, F &&f) {
+    if constexpr (W0 <= MAXW) {
+        if (w == W0) f(std::integral_constant<int, W0>{});
+        else with_width<W0 + 1>(w, f);
+    }
+}
+
 // ------------------------------------------------------------ interp (type 2)
-template <typename T, bool CPLX>
+template <typename T, bool CPLX, int W>
 __global__ void __launch_bounds__(NU_TPB)
     k_interp(const T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
              const double *__restrict__ loc, long long npts, int layout,
@@ -92,35 +104,33 @@ __global__ void __launch_bounds__(NU_TPB)
     out = out_f32 ? (void *)((float *)out + blockIdx.y * obs) : (void *)((double *)out + blockIdx.y * obs);
     double th, ph;
     load_point(loc, j, npts, layout, th, ph);
-    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
-    T kt[MAXW], kp[MAXW];
-    weights<T>(pc, w, beta, kt, kp);
-    int cols[MAXW];
+    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, W);
+    T kt[W], kp[W];
+    weights<T, W>(pc, W, beta, kt, kp);
+    int cols[W];
 #pragma unroll
-    for (int b = 0; b < MAXW; ++b) {
+    for (int b = 0; b < W; ++b) {
         int c = pc.p0 + b;
         c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
         cols[b] = c;
     }
     T ar = 0, ai = 0;
-    for (int a = 0; a < w; ++a) {
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
         const long long rowoff = (long long)(pc.r0 + a) * Npf;
         T rr = 0, ri = 0;
         if constexpr (CPLX) {
             const cplx<T> *row = reinterpret_cast<const cplx<T> *>(U) + rowoff;
 #pragma unroll
-            for (int b = 0; b < MAXW; ++b) {
-                if (b < w) {
-                    const cplx<T> v = row[cols[b]];
-                    rr = fma(kp[b], v.x, rr);
-                    ri = fma(kp[b], v.y, ri);
-                }
+            for (int b = 0; b < W; ++b) {
+                const cplx<T> v = row[cols[b]];
+                rr = fma(kp[b], v.x, rr);
+                ri = fma(kp[b], v.y, ri);
             }
         } else {
             const T *row = U + rowoff;
 #pragma unroll
-            for (int b = 0; b < MAXW; ++b)
-                if (b < w) rr = fma(kp[b], row[cols[b]], rr);
+            for (int b = 0; b < W; ++b) rr = fma(kp[b], row[cols[b]], rr);
         }
         ar = fma(kt[a], rr, ar);
         if constexpr (CPLX) ai = fma(kt[a], ri, ai);
@@ -461,7 +471,7 @@ static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U
 // from d = 1 - cos(x) = 2 sin^2(x/2) and sin(x) evaluated in FP32 (errors
 // relative to the small angle, not to 1).
 
-template <bool CPLX>
+template <bool CPLX, int W>
 __global__ void __launch_bounds__(NU_TPB)
     k_interp_mixed(const float *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                    const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
@@ -474,48 +484,44 @@ __global__ void __launch_bounds__(NU_TPB)
     out = out_f32 ? (void *)((float *)out + blockIdx.y * obs) : (void *)((double *)out + blockIdx.y * obs);
     double th, ph;
     load_point(loc, j, npts, layout, th, ph);
-    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
-    float kt[MAXW], kp[MAXW];
+    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, W);
+    float kt[W], kp[W];
     // tap offsets (n0 + a - t) from the FP64 offset split into hi + lo floats:
     // (a + ft_h) is exact in FP32, so each tap argument carries only its own
     // final rounding (a single FP32 rounding of ft would shift every tap of
     // the point by up to 2.4e-7 grid cells, a coherent position error)
-    const float sc = 2.f / (float)w;
+    const float sc = 2.f / (float)W;
     const float fth = (float)pc.ft, ftl = (float)(pc.ft - (double)fth);
     const float fph = (float)pc.fp, fpl = (float)(pc.fp - (double)fph);
 #pragma unroll
-    for (int a = 0; a < MAXW; ++a) {
-        if (a < w) {
-            kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
-            kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
-        }
+    for (int a = 0; a < W; ++a) {
+        kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
+        kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
     }
-    int cols[MAXW];
+    int cols[W];
 #pragma unroll
-    for (int b = 0; b < MAXW; ++b) {
+    for (int b = 0; b < W; ++b) {
         int c = pc.p0 + b;
         c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
         cols[b] = c;
     }
     kahan zr, zi;
-    for (int a = 0; a < w; ++a) {
+#pragma unroll
+    for (int a = 0; a < W; ++a) {
         const long long rowoff = (long long)(pc.r0 + a) * Npf;
         kahan rr, ri;
         if constexpr (CPLX) {
             const float2 *row = reinterpret_cast<const float2 *>(U) + rowoff;
 #pragma unroll
-            for (int b = 0; b < MAXW; ++b) {
-                if (b < w) {
-                    const float2 v = row[cols[b]];
-                    rr.add(kp[b] * v.x);
-                    ri.add(kp[b] * v.y);
-                }
+            for (int b = 0; b < W; ++b) {
+                const float2 v = row[cols[b]];
+                rr.add(kp[b] * v.x);
+                ri.add(kp[b] * v.y);
             }
         } else {
             const float *row = U + rowoff;
 #pragma unroll
-            for (int b = 0; b < MAXW; ++b)
-                if (b < w) rr.add(kp[b] * row[cols[b]]);
+            for (int b = 0; b < W; ++b) rr.add(kp[b] * row[cols[b]]);
         }
         // row sums carry their compensation into the outer sum
         zr.add(kt[a] * rr.s);
@@ -556,34 +562,37 @@ int nufft_interp_batch(const cunusht_plan_s *P, int nreq, int spin, const void *
     if (npts == 0 || nreq == 0) return CUNUSHT_OK;
     dim3 grid((unsigned)((npts + NU_TPB - 1) / NU_TPB), nreq);
     const int f32o = out_dtype == CUNUSHT_F32;
-    if (P->fwd_u32) {
-        if (spin == 0)
-            k_interp_mixed<false><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                           (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
-                                                           ubs, lbs, obs);
-        else
-            k_interp_mixed<true><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                          (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
-                                                          ubs, lbs, obs);
-    } else if (P->grid_fp32) {
-        if (spin == 0)
-            k_interp<float, false><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                            (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
-                                                            ubs, lbs, obs);
-        else
-            k_interp<float, true><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                           (float)P->beta, loc, npts, layout, gamma, spin, out, f32o,
-                                                           ubs, lbs, obs);
-    } else {
-        if (spin == 0)
-            k_interp<double, false><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                             P->w, P->beta, loc, npts, layout, gamma, spin, out, f32o,
-                                                             ubs, lbs, obs);
-        else
-            k_interp<double, true><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                            P->w, P->beta, loc, npts, layout, gamma, spin, out, f32o,
-                                                            ubs, lbs, obs);
-    }
+    with_width(P->w, [&](auto WC) {
+        constexpr int W = decltype(WC)::value;
+        if (P->fwd_u32) {
+            if (spin == 0)
+                k_interp_mixed<false, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                                  W, (float)P->beta, loc, npts, layout, gamma, spin,
+                                                                  out, f32o, ubs, lbs, obs);
+            else
+                k_interp_mixed<true, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
+                                                                 W, (float)P->beta, loc, npts, layout, gamma, spin,
+                                                                 out, f32o, ubs, lbs, obs);
+        } else if (P->grid_fp32) {
+            if (spin == 0)
+                k_interp<float, false, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf,
+                                                                   P->n_lo, W, (float)P->beta, loc, npts, layout,
+                                                                   gamma, spin, out, f32o, ubs, lbs, obs);
+            else
+                k_interp<float, true, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf,
+                                                                  P->n_lo, W, (float)P->beta, loc, npts, layout,
+                                                                  gamma, spin, out, f32o, ubs, lbs, obs);
+        } else {
+            if (spin == 0)
+                k_interp<double, false, W><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf,
+                                                                    P->n_lo, W, P->beta, loc, npts, layout, gamma,
+                                                                    spin, out, f32o, ubs, lbs, obs);
+            else
+                k_interp<double, true, W><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf,
+                                                                   P->n_lo, W, P->beta, loc, npts, layout, gamma,
+                                                                   spin, out, f32o, ubs, lbs, obs);
+        }
+    });
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
