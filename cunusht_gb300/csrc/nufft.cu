@@ -178,7 +178,7 @@ __device__ __forceinline__ float es_kernel_acc(float z, float beta) {
 // points) add their taps to U directly.
 constexpr int SPW_WARPS = 4;  // warps per block
 
-template <typename T, bool CPLX>
+template <typename T, bool CPLX, int W>
 __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp(T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
                   const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     if (act) {
         double th, ph;
         load_point(loc, j, npts, layout, th, ph);
-        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, W);
         if (in_f32) {
             vr = ((const float *)in)[j];
             if (CPLX) vi = ((const float *)in)[npts + j];
@@ -217,22 +217,24 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
             vr = t2;
         }
     }
-    T kt[MAXW], kp[MAXW];
-    weights<T>(pc, w, beta, kt, kp);
+    T kt[W], kp[W];
+    weights<T, W>(pc, W, beta, kt, kp);
     // joint footprint of the warp's points
     const int big = 1 << 30;
     const int rmin = __reduce_min_sync(0xffffffffu, act ? pc.r0 : big);
     const int rmax = __reduce_max_sync(0xffffffffu, act ? pc.r0 : -big);
     const int pmin = __reduce_min_sync(0xffffffffu, act ? pc.p0 : big);
     const int pmax = __reduce_max_sync(0xffffffffu, act ? pc.p0 : -big);
-    const int nr = rmax - rmin + w, ncl = pmax - pmin + w;
+    const int nr = rmax - rmin + W, ncl = pmax - pmin + W;
     if (nr > SR || ncl > SC) {
         // footprint too wide for the strip: direct global atomics
         if (!act) return;
-        for (int a = 0; a < w; ++a) {
+#pragma unroll 1
+        for (int a = 0; a < W; ++a) {
             const long long rowoff = (long long)(pc.r0 + a) * Npf;
             const T fr = kt[a] * (T)vr, fi = kt[a] * (T)vi;
-            for (int b = 0; b < w; ++b) {
+#pragma unroll
+            for (int b = 0; b < W; ++b) {
                 int c = pc.p0 + b;
                 c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
                 T *cell = U + (rowoff + c) * NC;
@@ -252,10 +254,12 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const int base = (pc.r0 - rmin) * ncl + (pc.p0 - pmin);
     for (int rd = 0; rd < nround; ++rd) {
         const bool go = act && myrank == rd;
-        for (int a = 0; a < w; ++a) {
+#pragma unroll 1
+        for (int a = 0; a < W; ++a) {
             const T fr = kt[a] * (T)vr, fi = kt[a] * (T)vi;
             T *row = strip + (size_t)(base + a * ncl) * NC;
-            for (int b = 0; b < w; ++b) {
+#pragma unroll
+            for (int b = 0; b < W; ++b) {
                 if (go) {
                     row[b * NC] += kp[b] * fr;
                     if constexpr (CPLX) row[b * NC + 1] += kp[b] * fi;
@@ -288,13 +292,19 @@ static int launch_spread_warp(const cunusht_plan_s *P, int nreq, T *U, long long
     // cells per pixel, plus row jitter from the deflection
     const int SR = P->w + 4, SC = 80 + P->w;
     const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(T);
-    if (sm > 48 * 1024)
-        CU_TRY(cudaFuncSetAttribute(k_spread_warp<T, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const long long nwarps = (npts + 31) / 32;
     const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
-    k_spread_warp<T, CPLX><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(U, P->nrows, P->Npf, P->Ntf, P->n_lo, P->w,
-                                                                      (T)P->beta, loc, npts, layout, gamma, spin, in,
-                                                                      f32i, SR, SC, ubs, lbs, ibs);
+    cudaError_t e = cudaSuccess;
+    with_width(P->w, [&](auto WC) {
+        constexpr int W = decltype(WC)::value;
+        if (sm > 48 * 1024)
+            e = cudaFuncSetAttribute(k_spread_warp<T, CPLX, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess)
+            k_spread_warp<T, CPLX, W><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(
+                U, P->nrows, P->Npf, P->Ntf, P->n_lo, W, (T)P->beta, loc, npts, layout, gamma, spin, in, f32i, SR, SC,
+                ubs, lbs, ibs);
+    });
+    CU_TRY(e);
     return CUNUSHT_OK;
 }
 
@@ -317,7 +327,7 @@ __device__ __forceinline__ double f2d_exact_int(float f) {
 // (as k_interp_mixed), FP32 products, Kahan-compensated FP32 strip sums, FP64
 // global accumulation.  The FP64 variant is bound by its FP64 exponentials and
 // products (GB300 runs FP64 at 1/60 of the FP32 rate).
-template <bool CPLX>
+template <bool CPLX, int W>
 __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp_mixed(double *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                         const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
@@ -340,7 +350,7 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     if (act) {
         double th, ph;
         load_point(loc, j, npts, layout, th, ph);
-        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, w);
+        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, W);
         if (in_f32) {
             vr = ((const float *)in)[j];
             if (CPLX) vi = ((const float *)in)[npts + j];
@@ -360,17 +370,15 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
             vr = t2;
         }
     }
-    float kt[MAXW], kp[MAXW];
+    float kt[W], kp[W];
     {
-        const float sc = 2.f / (float)w;
+        const float sc = 2.f / (float)W;
         const float fth = (float)pc.ft, ftl = (float)(pc.ft - (double)fth);
         const float fph = (float)pc.fp, fpl = (float)(pc.fp - (double)fph);
 #pragma unroll
-        for (int a = 0; a < MAXW; ++a) {
-            if (a < w) {
-                kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
-                kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
-            }
+        for (int a = 0; a < W; ++a) {
+            kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
+            kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
         }
     }
     const int big = 1 << 30;
@@ -378,15 +386,17 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const int rmax = __reduce_max_sync(0xffffffffu, act ? pc.r0 : -big);
     const int pmin = __reduce_min_sync(0xffffffffu, act ? pc.p0 : big);
     const int pmax = __reduce_max_sync(0xffffffffu, act ? pc.p0 : -big);
-    const int nr = rmax - rmin + w, ncl = pmax - pmin + w;
+    const int nr = rmax - rmin + W, ncl = pmax - pmin + W;
     // the value split once into hi + lo floats (FP64 work per point, not per tap)
     const float vrh = (float)vr, vrl = (float)(vr - (double)vrh);
     const float vih = (float)vi, vil = (float)(vi - (double)vih);
     if (nr > SR || ncl > SC) {
         if (!act) return;
-        for (int a = 0; a < w; ++a) {
+#pragma unroll 1
+        for (int a = 0; a < W; ++a) {
             const long long rowoff = (long long)(pc.r0 + a) * Npf;
-            for (int b = 0; b < w; ++b) {
+#pragma unroll
+            for (int b = 0; b < W; ++b) {
                 int c = pc.p0 + b;
                 c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
                 const double kw = (double)kt[a] * (double)kp[b];
@@ -406,13 +416,15 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const int base = (pc.r0 - rmin) * ncl + (pc.p0 - pmin);
     for (int rd = 0; rd < nround; ++rd) {
         const bool go = act && myrank == rd;
-        for (int a = 0; a < w; ++a) {
+#pragma unroll 1
+        for (int a = 0; a < W; ++a) {
             // row factor kt[a] * value as a double-float (FP32 TwoProduct on
             // the split value): each tap product then carries one FP32 rounding
             const float frh = kt[a] * vrh, frl = fmaf(kt[a], vrh, -frh) + kt[a] * vrl;
             const float fih = kt[a] * vih, fil = fmaf(kt[a], vih, -fih) + kt[a] * vil;
             float2 *row = strip + (size_t)(base + a * ncl) * NC;
-            for (int b = 0; b < w; ++b) {
+#pragma unroll
+            for (int b = 0; b < W; ++b) {
                 if (go) {
                     // Kahan: sum = x, comp = c; value = x - c
                     float2 t = row[b * NC];
@@ -453,14 +465,20 @@ static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U
                                     const void *in, long long ibs, int f32i, cudaStream_t st) {
     const int SR = P->w + 4, SC = 80 + P->w;
     const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(float2);
-    if (sm > 48 * 1024)
-        CU_TRY(cudaFuncSetAttribute(k_spread_warp_mixed<CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const long long nwarps = (npts + 31) / 32;
     const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
-    k_spread_warp_mixed<CPLX><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(U, P->nrows, P->Npf, P->Ntf, P->n_lo,
-                                                                         P->w, (float)P->beta, loc, npts, layout,
-                                                                         gamma, spin, in, f32i, SR, SC, ubs, lbs,
-                                                                         ibs);
+    cudaError_t e = cudaSuccess;
+    with_width(P->w, [&](auto WC) {
+        constexpr int W = decltype(WC)::value;
+        if (sm > 48 * 1024)
+            e = cudaFuncSetAttribute(k_spread_warp_mixed<CPLX, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm);
+        if (e == cudaSuccess)
+            k_spread_warp_mixed<CPLX, W><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(
+                U, P->nrows, P->Npf, P->Ntf, P->n_lo, W, (float)P->beta, loc, npts, layout, gamma, spin, in, f32i, SR,
+                SC, ubs, lbs, ibs);
+    });
+    CU_TRY(e);
     return CUNUSHT_OK;
 }
 
