@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(LEG_TPB)
                 }
             }
             const float2 a2 = s_al[i], b2 = s_be[i];
-            const dfl t = df_mul(dfl{a2.x, a2.y}, xd);
-            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+            const dfl t = df_mul_u(dfl{a2.x, a2.y}, xd);
+            const dfl nxt = df_mul_sub_u(t, cur, dfl{b2.x, b2.y}, prev);
             prev = cur;
             cur = nxt;
             REC_RESCALE_DF(cur, prev, e);
@@ -423,10 +423,10 @@ __global__ void __launch_bounds__(LEG_TPB)
             }
             const float2 a2 = s_al[i], g2 = s_ga[i], b2 = s_be[i];
             const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
-            const dfl tN = df_add(df_mul(ad, xN), gd);
-            const dfl tS = df_add(df_mul(ad, xS), gd);
-            const dfl nN = df_mul_sub(tN, cN, bd, pN);
-            const dfl nS = df_mul_sub(tS, cS, bd, pS);
+            const dfl tN = df_fma_u(ad, xN, gd);
+            const dfl tS = df_fma_u(ad, xS, gd);
+            const dfl nN = df_mul_sub_u(tN, cN, bd, pN);
+            const dfl nS = df_mul_sub_u(tS, cS, bd, pS);
             pN = cN;
             cN = nN;
             pS = cS;
@@ -669,13 +669,7 @@ __global__ void __launch_bounds__(LEG_TPB)
 // The adjoint sums keep (value, error) pairs unnormalised (df_add_u): the same
 // ~2^-48 of the operands as normalised double-floats (renormalising adds no
 // accuracy), a product of 4 FP32 operations instead of 7.
-__device__ __forceinline__ dfl prod_pair(dfl lam, float hh, float hl) {
-    const float p = lam.h * hh;
-    float e = fmaf(lam.h, hh, -p);
-    e = fmaf(lam.h, hl, e);
-    e = fmaf(lam.l, hh, e);
-    return dfl{p, e};
-}
+__device__ __forceinline__ dfl prod_pair(dfl lam, float hh, float hl) { return df_mul_u(lam, dfl{hh, hl}); }
 
 __device__ __forceinline__ dfl shfl_xor_df(dfl v, int mask) {
     return dfl{__shfl_xor_sync(0xffffffffu, v.h, mask), __shfl_xor_sync(0xffffffffu, v.l, mask)};
@@ -716,11 +710,8 @@ __device__ __forceinline__ void warp_reduce_scatter16_df(dfl v[16]) {
 
 // lam * (hh + hl) as a normalised double-float (the lam.l * hl term dropped)
 __device__ __forceinline__ dfl df_prod_split(dfl lam, float hh, float hl) {
-    const float p = lam.h * hh;
-    float e = fmaf(lam.h, hh, -p);
-    e = fmaf(lam.h, hl, e);
-    e = fmaf(lam.l, hh, e);
-    return df_fast(p, e);
+    const dfl p = df_mul_u(lam, dfl{hh, hl});
+    return df_fast(p.h, p.l);
 }
 
 struct split2 {
@@ -796,8 +787,8 @@ __global__ void __launch_bounds__(LEG_TPB)
             lam[i] = (e == 0 && l <= L) ? cur : zero;
             if (l < L) {
                 const float2 a2 = __ldg(al + b + l), b2 = __ldg(be + b + l);
-                const dfl t = df_mul(dfl{a2.x, a2.y}, xd);
-                const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                const dfl t = df_mul_u(dfl{a2.x, a2.y}, xd);
+                const dfl nxt = df_mul_sub_u(t, cur, dfl{b2.x, b2.y}, prev);
                 prev = cur;
                 cur = nxt;
                 REC_RESCALE_DF(cur, prev, e);
@@ -896,10 +887,10 @@ __global__ void __launch_bounds__(LEG_TPB)
             if (l < L) {
                 const float2 a2 = __ldg(al + b + l), g2 = __ldg(ga + b + l), b2 = __ldg(be + b + l);
                 const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
-                const dfl tN = df_add(df_mul(ad, xN), gd);
-                const dfl tS = df_add(df_mul(ad, xS), gd);
-                const dfl nN = df_mul_sub(tN, cN, bd, pN);
-                const dfl nS = df_mul_sub(tS, cS, bd, pS);
+                const dfl tN = df_fma_u(ad, xN, gd);
+                const dfl tS = df_fma_u(ad, xS, gd);
+                const dfl nN = df_mul_sub_u(tN, cN, bd, pN);
+                const dfl nS = df_mul_sub_u(tS, cS, bd, pS);
                 pN = cN;
                 cN = nN;
                 pS = cS;

@@ -14,29 +14,30 @@
 //
 // with integer digits (exact in bf16), El fixed per l-window from the bound
 // |lambda_l| <= sqrt((2l+1)/(4 pi)) and Ea per window and column from the
-// largest |a|.  Digit products of equal weight g = i + j (g = 0..6, all 16
-// products: the low digits span the whole +-128, so dropping g >= 4 would
-// cost 2^-27 of a typical product) are summed by one bf16 MMA (the K axis
-// holds (digit i, l), the N axis (weight g, column) with
-// B'[(g, col)][(i, l)] = t_{g-i}(l, col)); the products are integers below
-// 2^14 and a 128-l window sums at most 4 x 128 of them per weight, so the
-// FP32 accumulation in tensor memory is exact.  Per window the seven weights
-// of each output are scaled (powers of two, exact) and added to compensated
-// FP32 accumulators that keep the exact error of every addition (sum2).  The
-// only truncation is that of the digit strings, 2^-32 of the bounds: the
-// products are more accurate than the double-float CUDA-core kernels, which
-// round every product to FP32.
+// largest |a|.  Digit products of equal weight g = i + j are summed by one
+// bf16 MMA (the K axis holds (digit i, l), the N axis (weight g, column) with
+// B'[(g, col)][(i, l)] = t_{g-i}(l, col)).  Weights g = 0..4 are kept (13 of
+// the 16 digit pairs: the low digits span the whole +-128, so dropping g = 4
+// would cost 2^-27 of a typical product; g >= 5 is below 2^-40).  The
+// products are integers below 2^14 and a 128-l window sums at most 4 x 128 of
+// them per weight, so the FP32 accumulation in tensor memory is exact.  Per
+// window the weights 4..1 of each output are folded by Horner in FP32 and,
+// with weight 0, scaled by powers of two and added to compensated FP32
+// accumulators that keep the exact error of every addition (sum2).  The
+// truncation of the digit strings (2^-32 of the bounds) dominates the error:
+// the products are more accurate than the double-float CUDA-core kernels,
+// which round every product to FP32.
 //
-// Block: 512 threads, one per ring of 256 ring pairs (threads 0-255 the rings
-// theta, 256-511 the rings pi - theta) = four 128-row MMA tiles; one order m
-// per block row.  Per chunk of 8 l each thread writes its four digit rows
-// (16 bytes each) into the A tile, a subset of threads the B' digits, and one
-// thread issues 4 tiles x 2 K-steps of M=128, N=7 x 4 NB (rounded up to 16),
-// K=16 MMAs.  Two A/B'
-// buffers alternate; an mbarrier per buffer (tcgen05.commit) tells when the
-// MMAs reading it are done.  Every wait is bounded: on a timeout the block
-// records it in the plan's status word, waits once more (bounded) for its
-// MMAs, frees its tensor memory and returns.
+// Block: 544 threads.  The threads of warps 0-15 hold one ring each of 256 ring pairs
+// (threads 0-255 the rings theta, 256-511 the rings pi - theta) = four
+// 128-row MMA tiles, one order m per block row; per chunk of 16 l each writes
+// its four digit rows (two 16-byte K-cores per digit) into the A tile, a
+// subset of them the B' digits.  Warp 16 issues 4 tiles x 4 K-steps of M=128,
+// N=5 x 4 NB (rounded up to 16), K=16 MMAs.  Two A/B' buffers alternate; an
+// mbarrier per buffer (tcgen05.commit) tells when the MMAs reading it are
+// done.  Every wait is bounded: on a timeout the block records it in the
+// plan's status word, waits once more (bounded) for its MMAs, frees its
+// tensor memory and returns.
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.cuh"
@@ -159,23 +160,24 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// ---------------------------------------------------------------- digit split
-// x = h + l (|h| <= 128, l below half an ulp of h) as d0 + d1/256 + d2/256^2 +
-// d3/256^3 + O(2^-25), integer digits |d_i| <= 128.  Rounding to an integer
-// by adding and subtracting 1.5 x 2^23; every other step is exact.
-__device__ __forceinline__ void digits4(float h, float l, float (&d)[4]) {
-    const float RND = 12582912.f;
-    d[0] = __fsub_rn(__fadd_rn(h, RND), RND);
-    float r = __fadd_rn(__fsub_rn(h, d[0]), l);
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int k = 1; k < 4; ++k) {
-        d[k] = __fsub_rn(__fmaf_rn(r, 256.f, RND), RND);
-        r = __fmaf_rn(r, 256.f, -d[k]);
-    }
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// digits4 of (h + l) sc for a power of two sc: the integer part of h sc by one
-// FMA with the rounding constant, its exact remainder by another
+// ---------------------------------------------------------------- digit split
+// x = (h + l) sc for a power of two sc (|h sc| <= 128) as d0 + d1/256 +
+// d2/256^2 + d3/256^3 + O(2^-25), integer digits |d_i| <= 128.  The integer
+// part of h sc by one FMA with the rounding constant 1.5 x 2^23, its exact
+// remainder by another; l sc is added to the remainder.  An unnormalised pair
+// (|l| up to 2^-22 |h|, from the recursion steps) leaves the remainder below
+// 0.5 + 2^-15, so the next digit still rounds to at most 128 in magnitude.
 __device__ __forceinline__ void digits4s(float h, float l, float sc, float (&d)[4]) {
     const float RND = 12582912.f;
     d[0] = __fsub_rn(__fmaf_rn(h, sc, RND), RND);
@@ -595,8 +597,8 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
                             const float2 b2 = ben;
                             agn = s_ag[i + 1];
                             ben = s_be[i + 1];
-                            const dfl t = df_add(df_mul(dfl{ag.x, ag.y}, xd), dfl{ag.z, ag.w});
-                            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                            const dfl t = df_fma_u(dfl{ag.x, ag.y}, xd, dfl{ag.z, ag.w});
+                            const dfl nxt = df_mul_sub_u(t, cur, dfl{b2.x, b2.y}, prev);
                             prev = cur;
                             cur = nxt;
                         };
@@ -621,14 +623,33 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
             bad = __any_sync(0xffffffffu, bad);  // warp-uniform: the loads below are warp-collective
             tc_fence_after();
             if (!bad) {
+                // Column n = g NO + o holds the exact sum of weight 2^-8g (an integer
+                // below 2^24).  Weights 4..1 are folded by Horner in FP32: its rounding,
+                // 2^-24 of a value that carries weight 2^-8, is about 2^-32 of the
+                // window's sum, below the digit truncation of lambda and a.  Weight 0
+                // and the fold then enter the compensated accumulator.  Outputs go in
+                // groups of OG (one 8-column load per weight, starting on a multiple of
+                // 8) so that the fold, the loaded sums and the accumulators fit the
+                // register budget.
+                static_assert(NO % 4 == 0, "outputs per ring");
+                constexpr int OG = NO % 8 == 0 ? 8 : 4;
 #pragma unroll
-                for (int q = 0; q < NN / 16; ++q) {
-                    float dv[16];
-                    tmem_ld16(t_lane + q * 16, dv);
+                for (int o0 = 0; o0 < NO; o0 += OG) {
+                    float hr[OG];
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const int n = q * 16 + i, g = n / NO, o = n - g * NO;
-                        if (g < NG) acc[o].add(dv[i] * s_sc[n]);
+                    for (int g = NG - 1; g >= 0; --g) {
+                        const int col = g * NO + o0, sub = col & 7;  // sub + OG <= 8
+                        float dv[8];
+                        tmem_ld8(t_lane + (col - sub), dv);
+#pragma unroll
+                        for (int i = 0; i < OG; ++i) {
+                            if (g == NG - 1) hr[i] = dv[sub + i];
+                            else if (g > 0) hr[i] = fmaf(hr[i], 0x1p-8f, dv[sub + i]);
+                            else {
+                                acc[o0 + i].add(dv[sub + i] * s_sc[o0 + i]);
+                                acc[o0 + i].add(hr[i] * s_sc[NO + o0 + i]);
+                            }
+                        }
                     }
                 }
             }
