@@ -39,9 +39,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7 (served mixed vs plain FP64); p99 ms"
-# DRAM bytes (read + write) per launch of 4 requests from one ncu capture at
-# lmax 2047 (profiles/launches_served_l2047_spin2_mixed.md)
-LEG_TRAFFIC_B4 = {"leg_synth": 1493.0e6, "ptg_leg": 1354.0e6}  # records + pole + tensor-core kernels, ncu
+# DRAM bytes (read + write) of the Legendre stages (records + pole + tensor-core
+# kernels) per launch of 8 requests at lmax 2047: one ncu capture at lmax 1023
+# (a few GB on the device) scaled by 4.0, the ratio of (l, m) pairs
+# (profiles/leg_synth_tc_l2047.md)
+LEG_TRAFFIC = {"batch": 8, "leg_synth": 2644.0e6, "ptg_leg": 2371.0e6}
 
 
 def parse():
@@ -58,7 +60,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU work of the cpu_baseline leg")
-    p.add_argument("--batch", type=int, default=4, help="requests per launch of the served form")
+    p.add_argument("--batch", type=int, default=8, help="requests per launch of the served form")
     p.add_argument("--fp64-steps", type=int, default=3, help="timed solves of the plain FP64 single-request form")
     p.add_argument("--op", default=None, choices=["doubling", "adjoint_doubling"],
                    help="time one standalone kernel of the C ABI instead (HBM roofline)")
@@ -372,16 +374,16 @@ def main():
             # tensor cores; peak = 152 SMs x 128 lanes x 2 flop x max SM clock
             mhz = peaks.get("sm_max_mhz", 2070.0)
             peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-            tr = LEG_TRAFFIC_B4.get(dom)
+            tr = LEG_TRAFFIC.get(dom)
             roof = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                    "traffic": tr * B / 4 if tr else None, "kernel": dom,
+                    "traffic": tr * B / LEG_TRAFFIC["batch"] if tr else None, "kernel": dom,
                     "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; "
                                    "achieved counts algorithmic flops only (8 per l,m,ring,component); the "
                                    "double-float recursion and digit split bound the kernel on the CUDA cores "
-                                   "(ncu: issue slots 70 %, FMA pipe 55 %) while the contraction runs on the "
-                                   "tensor cores (tensor pipe 10 %) (profiles/leg_synth_tc_l2047.md); "
-                                   "traffic = DRAM bytes of the stage's kernels per launch of 4 requests "
-                                   "(profiles/launches_served_l2047_spin2_mixed.md), scaled to the batch size"}
+                                   "while the contraction runs on the tensor cores (ncu issue, pipe and "
+                                   "tensor-pipe figures in profiles/leg_synth_tc_l2047.md); traffic = DRAM "
+                                   "bytes of the stage's kernels per launch of 8 requests at lmax 2047 (an "
+                                   "lmax 1023 capture scaled by the (l, m) pairs), scaled to the batch size"}
     stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
                        "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
     for s, v in stage_table.items():

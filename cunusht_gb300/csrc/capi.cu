@@ -124,6 +124,11 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[1], P->d_tc_woff[2], P->d_tc_rec};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (int g = 0; g < 2; ++g)
+        for (int s = 0; s < 3; ++s) {
+            if (P->d_tc_stv[g][s]) cudaFree(P->d_tc_stv[g][s]);
+            if (P->d_tc_ste[g][s]) cudaFree(P->d_tc_ste[g][s]);
+        }
     for (auto &e : P->evt_pool) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);

@@ -185,7 +185,12 @@ struct cunusht_plan_s {
     unsigned char *d_tc_rec = nullptr;
     size_t tc_rec_bytes = 0;
     size_t tc_nrec = 0;  // window records per call (the larger of spin 1 and 2)
-    int tc_rec_nb = 0;   // requests per launch the record buffer holds (1 at creation, up to 4 by reserve_batch)
+    int tc_rec_nb = 0;   // requests per launch the record buffer holds (1 at creation, up to 8 by reserve_batch)
+    // recursion starts of the tensor-core synthesis per [grid: 0 GL, 1 CC][spin]: for every
+    // (m, side, pair) the start value (hi, lo) and its exponent / 96, built at plan creation
+    // (NULL: the kernel evaluates the start itself)
+    float2 *d_tc_stv[2][3] = {};
+    short *d_tc_ste[2][3] = {};
 
     // FFT twiddles e^{-2 pi i t / TW}
     int TW = 0;

@@ -26,10 +26,11 @@ int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, 
 int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
                       bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st);
 
-// legendre_tc.cu: tensor-core synthesis (spin > 0, mixed precision), nb in {1, 2, 4}
+// legendre_tc.cu: tensor-core synthesis (spin > 0, mixed precision), nb in {1, 2, 4, 8};
+// stv / ste: the plan's recursion-start table of the grid and spin (row stride npairs), or NULL
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
                       const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
-                      int spin, const double2 *G,
+                      const float2 *stv, const short *ste, int spin, const double2 *G,
                       const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
                       cudaStream_t st);
 int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout);

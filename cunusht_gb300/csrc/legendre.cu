@@ -1075,14 +1075,16 @@ struct RingPairs {
     int ld;
     int pole = -1;  // pair (theta = 0, pi), or -1
     int pole_rn = 0, pole_rs = 0;  // its ring indices
+    const float2 *const *stv = nullptr;  // tensor-core recursion starts per spin (or NULL)
+    const short *const *ste = nullptr;
 };
 
 static RingPairs pairs_of(const cunusht_plan_s *P, bool cc) {
     if (cc)
         return {P->cc_npairs, P->d_cc_x, P->d_cc_sh, P->d_cc_ch, P->d_cc_rn, P->d_cc_rs, P->ncc,
-                P->cc_pole, P->cc_pole_ring[0], P->cc_pole_ring[1]};
+                P->cc_pole, P->cc_pole_ring[0], P->cc_pole_ring[1], P->d_tc_stv[1], P->d_tc_ste[1]};
     return {P->gl_npairs, P->d_gl_x, P->d_gl_sh, P->d_gl_ch, P->d_gl_rn, P->d_gl_rs, P->nring,
-            P->gl_pole, P->gl_pole_ring[0], P->gl_pole_ring[1]};
+            P->gl_pole, P->gl_pole_ring[0], P->gl_pole_ring[1], P->d_tc_stv[0], P->d_tc_ste[0]};
 }
 
 template <int NB>
@@ -1113,8 +1115,9 @@ int leg_synth_spin_df_pairs(const cunusht_plan_s *P, int nb, int npairs, const d
 }
 
 // nreq requests (alm at G + r * astride, columns at H + r * hstride); the
-// mixed-precision kernels process up to four requests per launch with one
-// shared recursion, the FP64 kernels one request per launch.
+// mixed-precision kernels process several requests per launch with one shared
+// recursion (tensor cores: up to eight, CUDA cores: up to four), the FP64
+// kernels one request per launch.
 int leg_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *G, const double2 *C,
                     long long astride, bool use_lfac, bool cc, double2 *H, long long hstride, cudaStream_t st) {
     return leg_synth_batch_fl(P, nreq, spin, G, C, astride, use_lfac ? P->d_lfac : nullptr, cc, H, hstride, st);
@@ -1137,9 +1140,12 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
             const double2 *Gr = G + r0 * astride, *Cr = C ? C + r0 * astride : nullptr;
             double2 *Hr = H + r0 * hstride;
             if (spin > 0 && P->use_tc) {
-                const int nb = left >= 4 ? 4 : left >= 2 ? 2 : 1;
+                // as many requests per launch as the window records were reserved for
+                const int cap = left < P->tc_rec_nb ? left : P->tc_rec_nb;
+                const int nb = cap >= 8 ? 8 : cap >= 4 ? 4 : cap >= 2 ? 2 : 1;
                 RC_TRY(leg_synth_spin_tc(P, nb, R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, R.ld, R.pole, R.pole_rn,
-                                         R.pole_rs, spin, Gr, Cr, astride, lf, Hr, hstride, st));
+                                         R.pole_rs, R.stv ? R.stv[spin] : nullptr, R.ste ? R.ste[spin] : nullptr,
+                                         spin, Gr, Cr, astride, lf, Hr, hstride, st));
                 r0 += nb;
                 continue;
             }

@@ -43,6 +43,7 @@
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 namespace cunusht {
@@ -301,21 +302,30 @@ int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout) {
 }
 
 // ---------------------------------------------------------------- spin-s synthesis
-constexpr int TCL_T = 512;     // threads per block = rings (256 pairs)
 constexpr int TCL_W = 128;     // l window accumulated in tensor memory
 constexpr int TCL_KC = 16;     // l per chunk: K = 4 digits x 16 l = 4 MMA K-steps
 constexpr int TCL_TILE = 128 * 128;       // A tile: 128 rows x 8 K-cores x 16 bytes
-constexpr int TCL_ABUF = 4 * TCL_TILE;    // A buffer: 4 tiles
 constexpr int TCL_SBO = 1024;             // 8-row group stride (8 rows x 8 K-cores x 16 bytes)
 constexpr int TCL_TPS = TCL_W + 8;        // digit-plane row stride in elements (272 bytes: 16-byte aligned, fewer bank conflicts)
 constexpr int TCL_MIN_TAIL = 32;          // fewer leftover ring pairs than this go to the CUDA-core kernel
 
+// Launches of NB <= 4 requests run blocks of four 128-ring tiles (256 ring
+// pairs); NB = 8 needs 5 x 32 = 160 tensor-memory columns per tile and runs
+// blocks of two tiles (128 ring pairs) so that they fit the 512 columns.
 template <int NB>
 struct TclLayout {
+    static constexpr int NT = NB >= 8 ? 2 : 4;           // 128-row MMA tiles per block
+    static constexpr int T = 128 * NT;                   // ring threads (one ring each)
+    static constexpr int BLOCK = T + 32;                 // + the MMA warp
+    static constexpr int ABUF = NT * TCL_TILE;           // A buffer: NT tiles
     static constexpr int NO = 4 * NB;                    // outputs per ring
     static constexpr int NG = 5;                         // digit-product weights g = 0..4
     static constexpr int NN = (NG * NO + 15) / 16 * 16;  // MMA N: weights x outputs, padded to 16
-    static constexpr int NCOLS = 4 * NN <= 32 ? 32 : 4 * NN <= 64 ? 64 : 4 * NN <= 128 ? 128 : 4 * NN <= 256 ? 256 : 512;
+    static constexpr int NCOLS = NT * NN <= 32    ? 32
+                                 : NT * NN <= 64  ? 64
+                                 : NT * NN <= 128 ? 128
+                                 : NT * NN <= 256 ? 256
+                                                  : 512;
     // window record (written by k_tc_records, one per (m, l-window)):
     static constexpr int RSC = 4 * NO * TCL_TPS * 2;        // bf16 digit planes [4][NO][TPS], then
     static constexpr int RLS = RSC + NG * NO * 4;           // float epilogue scales [NG][NO], then
@@ -323,7 +333,7 @@ struct TclLayout {
     static constexpr int RBE = RCO + (TCL_W + 1) * 16;      // float4 (alpha, gamma) [W + 1] and
     static constexpr int RSZ = (RBE + (TCL_W + 1) * 8 + 15) / 16 * 16;  // float2 beta [W + 1] (zero past the window)
     static constexpr int BBUF = NN * 128;                // B' buffer: NN rows x 8 K-cores x 16 bytes
-    static constexpr int OFF_B = 2 * TCL_ABUF;
+    static constexpr int OFF_B = 2 * ABUF;
     static constexpr int OFF_R = OFF_B + 2 * BBUF;       // two window records (current, next)
     static constexpr int OFF_BAR = OFF_R + 2 * RSZ;      // full[2], empty[2], record[2]
     static constexpr int OFF_TM = OFF_BAR + 48;          // tensor-memory base, give-up flag
@@ -433,27 +443,27 @@ __global__ void __launch_bounds__(TCL_W)
     }
 }
 
-// Roles: warps 0-15 (TCL_T threads) hold one ring each and write the digit
-// tiles; warp 16 issues the MMAs.  Per chunk each ring warp waits until the
-// MMAs that last read the buffer are done (empty barrier, tcgen05.commit),
-// writes its rows, and arrives on the buffer's full barrier (one arrival per
-// warp); the MMA warp waits for all 16 arrivals.  The ring warps thus run up
-// to a chunk apart instead of meeting at a block barrier every chunk.  The
-// window records arrive by bulk copy, the next one prefetched while the
-// current window runs; block-wide steps use barrier 1 over the ring warps only.
-constexpr int TCL_BLOCK = TCL_T + 32;
-
+// Roles: the ring warps (LY::T threads) hold one ring each and write the
+// digit tiles (lambda into A, the window's alm digits into B'); the last warp
+// issues the MMAs.  Per chunk each ring warp waits until the MMAs that last
+// read the buffer are done (empty barrier, tcgen05.commit), writes its rows,
+// and arrives on the buffer's full barrier (one arrival per warp); the MMA
+// warp waits for all the arrivals.  The ring warps thus run up to a chunk
+// apart instead of meeting at a block barrier every chunk.  The window
+// records arrive by bulk copy, the next one prefetched while the current
+// window runs; block-wide steps use barrier 1 over the ring warps only.
 template <int NB>
-__global__ void __launch_bounds__(TCL_BLOCK, 1)
+__global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
     k_leg_synth_spin_tc(int L, int spin, const unsigned char *__restrict__ rec, const int *__restrict__ woff,
                         const double *__restrict__ lg0, int npairs,
                         const double *__restrict__ px, const double *__restrict__ psh,
                         const double *__restrict__ pch, const int *__restrict__ prn, const int *__restrict__ prs,
+                        const float2 *__restrict__ stv, const short *__restrict__ ste, int st_ld,
                         double2 *__restrict__ H, long long hstride, int ldH, int *status) {
     using LY = TclLayout<NB>;
-    constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG;
-    static_assert(4 * NN <= 512, "tensor memory holds 512 columns");
-    static_assert(26 * NO <= TCL_T, "one B' K-core per ring thread");
+    constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG, T = LY::T, NT = LY::NT;
+    constexpr int NCOPY = 13 * 2 * NO;  // B' K-cores per chunk
+    static_assert(NT * NN <= 512, "tensor memory holds 512 columns");
     extern __shared__ __align__(1024) unsigned char sm[];
     uint32_t *s_tm = reinterpret_cast<uint32_t *>(sm + LY::OFF_TM);
     volatile int *s_bad = reinterpret_cast<volatile int *>(sm + LY::OFF_TM + 4);
@@ -465,10 +475,10 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
     const int l0 = max(m, spin);
     const unsigned char *recm = rec + (size_t)woff[m] * LY::RSZ;  // this order's window records
 
-    if (warp == TCL_T / 32) tmem_alloc(sbase + LY::OFF_TM, LY::NCOLS);
+    if (warp == T / 32) tmem_alloc(sbase + LY::OFF_TM, LY::NCOLS);
     if (tid == 0) {
-        mbar_init(full0, TCL_T / 32);
-        mbar_init(full0 + 8, TCL_T / 32);
+        mbar_init(full0, T / 32);
+        mbar_init(full0 + 8, T / 32);
         mbar_init(empty0, 1);
         mbar_init(empty0 + 8, 1);
         mbar_init(rbar0, 1);
@@ -477,7 +487,7 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
         mbar_init_fence();
     }
     // B' positions with g - i outside [0, 3] and the padding rows stay zero for the whole kernel
-    for (int i = tid; i < 2 * LY::BBUF / 16; i += TCL_BLOCK)
+    for (int i = tid; i < 2 * LY::BBUF / 16; i += LY::BLOCK)
         reinterpret_cast<uint4 *>(sm + LY::OFF_B)[i] = make_uint4(0u, 0u, 0u, 0u);
     fence_async_smem();
     tc_fence_before();
@@ -486,7 +496,7 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
     const uint32_t tbase = *s_tm;
     if (tid == 0 && l0 <= L) bulk_g2s(sbase + LY::OFF_R, recm, LY::RSZ, rbar0);  // record of window 0
 
-    if (warp == TCL_T / 32) {
+    if (warp == T / 32) {
         // ---------------- MMA warp: the whole warp follows the chunk sequence (its
         // outcome kept warp-uniform), lane 0 issues
         constexpr uint32_t IDESC = idesc_bf16_f32(128, NN);
@@ -504,9 +514,9 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
                 }
                 if (lane == 0) {
                     tc_fence_after();
-                    const uint32_t aa = sbase + buf * TCL_ABUF, ba = sbase + LY::OFF_B + buf * LY::BBUF;
+                    const uint32_t aa = sbase + buf * LY::ABUF, ba = sbase + LY::OFF_B + buf * LY::BBUF;
 #pragma unroll
-                    for (int t = 0; t < 4; ++t)
+                    for (int t = 0; t < NT; ++t)
 #pragma unroll
                         for (int k = 0; k < 4; ++k)  // K-step k: digit k of lambda, 16 l
                             tc_mma(tbase + t * NN, sdesc(aa + t * TCL_TILE + k * 256, 128, TCL_SBO),
@@ -520,21 +530,28 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
         __syncwarp();
     } else {
         // ---------------- ring warps
-        const int side = tid >> 8;  // 0: ring theta, 1: ring pi - theta
+        const int side = tid / (T / 2);  // 0: ring theta, 1: ring pi - theta
         const int tile = tid >> 7, row = tid & 127;
-        const int p = blockIdx.x * (TCL_T / 2) + (tid & 255);
+        const int p = blockIdx.x * (T / 2) + (tid & (T / 2 - 1));
         const bool act = p < npairs;
-        double x = 0.0, sh = 0.0, ch = 1.0;
-        if (act) {
-            x = px[p];
-            sh = psh[p];
-            ch = pch[p];
-        }
+        const double x = act ? px[p] : 0.0;
         const dfl xd = df_from(side ? -x : x);
-        dfl cur, prev;
-        int e;
-        if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
-        else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
+        dfl cur{0.f, 0.f}, prev{0.f, 0.f};
+        int e = 0;
+        if (stv) {
+            // the plan's table: the same values as rec_start_df, without its FP64
+            // logarithms and powers (one block per SM would wait for them)
+            if (act) {
+                const size_t ix = ((size_t)m * 2 + side) * st_ld + p;
+                const float2 v = stv[ix];
+                cur = dfl{v.x, v.y};
+                e = 96 * (int)ste[ix];
+            }
+        } else {
+            const double sh = act ? psh[p] : 0.0, ch = act ? pch[p] : 1.0;
+            if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
+            else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
+        }
         sum2 acc[NO];
         const uint32_t t_lane = tbase + ((uint32_t)((warp & 3) * 32) << 16) + tile * NN;  // this thread's row
         const uint32_t a_row = (uint32_t)tile * TCL_TILE + (row >> 3) * TCL_SBO + (row & 7) * 16;
@@ -565,18 +582,24 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
             for (int c = 0; c < nch; ++c, ++gc) {
                 const int buf = gc & 1;
                 if (gc >= 2) bad |= !mbar_wait(empty0 + 8 * buf, ((gc - 2) >> 1) & 1);
-                unsigned char *sA = sm + buf * TCL_ABUF;
+                unsigned char *sA = sm + buf * LY::ABUF;
                 unsigned char *sB = sm + LY::OFF_B + buf * LY::BBUF;
-                // B' of this chunk: one 16-byte K-core (8 l of one digit) per thread
-                if (tid < 13 * 2 * NO) {
-                    const int pr = tid / (2 * NO), rem = tid - pr * 2 * NO;
-                    const int lh = rem / NO, o = rem - lh * NO;
-                    int g, di;
-                    tcl_pair(pr, g, di);
-                    const int n = g * NO + o;
-                    const uint4 q =
-                        *reinterpret_cast<const uint4 *>(s_tp + ((g - di) * NO + o) * TCL_TPS + c * TCL_KC + 8 * lh);
-                    *reinterpret_cast<uint4 *>(sB + (n >> 3) * TCL_SBO + (2 * di + lh) * 128 + (n & 7) * 16) = q;
+                // B' of this chunk: row n = g NO + o, K-core (digit i, 8 l) = t_{g-i} of
+                // output o; one 16-byte copy from the record's digit planes per (pair
+                // (g, i), l half, o), spread over the ring threads
+#pragma unroll
+                for (int q0 = 0; q0 < NCOPY; q0 += T) {
+                    const int q = q0 + tid;
+                    if (q < NCOPY) {
+                        const int pr = q / (2 * NO), rem = q - pr * 2 * NO;
+                        const int lh = rem / NO, o = rem - lh * NO;
+                        int g, di;
+                        tcl_pair(pr, g, di);
+                        const int n = g * NO + o;
+                        const uint4 v = *reinterpret_cast<const uint4 *>(s_tp + ((g - di) * NO + o) * TCL_TPS +
+                                                                         c * TCL_KC + 8 * lh);
+                        *reinterpret_cast<uint4 *>(sB + (n >> 3) * TCL_SBO + (2 * di + lh) * 128 + (n & 7) * 16) = v;
+                    }
                 }
                 // lambda digits for 16 l in two halves of 8, each stored as four 16-byte K-cores.
                 // The exponent check runs once per half: a step grows the mantissa by at
@@ -655,7 +678,7 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
             }
             tc_fence_before();
             // all ring warps are done with the window's tables; any wait that ran out ends the block
-            bad = bar_or_1(TCL_T, bad | *s_bad);
+            bad = bar_or_1(T, bad | *s_bad);
             if (bad) break;
         }
 
@@ -686,7 +709,7 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == TCL_T / 32) {
+    if (warp == T / 32) {
         tc_fence_after();
         tmem_dealloc(tbase, LY::NCOLS);
     }
@@ -694,7 +717,8 @@ __global__ void __launch_bounds__(TCL_BLOCK, 1)
 
 template <int NB>
 static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double *x, const double *sh,
-                              const double *ch, const int *rn, const int *rs, int ld, int spin, const double2 *G,
+                              const double *ch, const int *rn, const int *rs, const float2 *stv, const short *ste,
+                              int st_ld, int ld, int spin, const double2 *G,
                               const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
                               cudaStream_t st) {
     using LY = TclLayout<NB>;
@@ -709,21 +733,24 @@ static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double 
                                               P->d_tc_woff[spin], P->d_tc_rec);
     CU_LAUNCH_CHECK();
     CU_TRY(cudaFuncSetAttribute(k_leg_synth_spin_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::BYTES));
-    dim3 grid((npairs + TCL_T / 2 - 1) / (TCL_T / 2), P->mmax + 1);
-    k_leg_synth_spin_tc<NB><<<grid, TCL_BLOCK, LY::BYTES, st>>>(L, spin, P->d_tc_rec, P->d_tc_woff[spin],
-                                                                P->d_lg0[spin], npairs, x, sh, ch, rn, rs, H, hstride, ld,
-                                                                P->d_status);
+    dim3 grid((npairs + LY::T / 2 - 1) / (LY::T / 2), P->mmax + 1);
+    k_leg_synth_spin_tc<NB><<<grid, LY::BLOCK, LY::BYTES, st>>>(L, spin, P->d_tc_rec, P->d_tc_woff[spin],
+                                                                P->d_lg0[spin], npairs, x, sh, ch, rn, rs, stv, ste,
+                                                                st_ld, H, hstride, ld, P->d_status);
     CU_LAUNCH_CHECK();
     return CUNUSHT_OK;
 }
 
 static size_t tcl_record_bytes(int nb) {
-    return nb >= 4 ? TclLayout<4>::RSZ : nb >= 2 ? TclLayout<2>::RSZ : TclLayout<1>::RSZ;
+    return nb >= 8   ? TclLayout<8>::RSZ
+           : nb >= 4 ? TclLayout<4>::RSZ
+           : nb >= 2 ? TclLayout<2>::RSZ
+                     : TclLayout<1>::RSZ;
 }
 
-// record buffer for launches of up to nb (<= 4) requests; grows only
+// record buffer for launches of up to nb requests (1, 2, 4 or 8); grows only
 int tc_reserve(cunusht_plan_s *P, int nb) {
-    nb = std::min(nb, 4);
+    nb = nb >= 8 ? 8 : nb >= 4 ? 4 : nb >= 2 ? 2 : 1;
     if (nb <= P->tc_rec_nb || P->tc_nrec == 0) return CUNUSHT_OK;
     const size_t bytes = P->tc_nrec * tcl_record_bytes(nb);
     if (P->d_tc_rec) {
@@ -746,8 +773,45 @@ int tc_reserve(cunusht_plan_s *P, int nb) {
     return CUNUSHT_OK;
 }
 
+// Recursion starts of every (m, side, pair) of one grid and spin: the values
+// rec_start_df gives at the start of the synthesis kernels, evaluated once per
+// plan so that the synthesis blocks (one per SM) do not wait for FP64
+// logarithms and powers.  Entry ((m * 2 + side) * npairs + p); e / 96 is
+// clamped to the short range: a start below 2^(-96 * 32767) grows by less than
+// 2^8.5 per step and so never reaches the accumulated range within lmax steps.
+__global__ void k_tc_starts(int L, int spin, const double *__restrict__ lg0, int npairs, const double *__restrict__ sh,
+                            const double *__restrict__ ch, float2 *__restrict__ v, short *__restrict__ e96) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2LL * npairs * (L + 1)) return;
+    const int p = (int)(i % npairs);
+    const long long ms = i / npairs;
+    const int side = (int)(ms & 1), m = (int)(ms >> 1);
+    dfl cur, prev;
+    int e;
+    if (side) rec_start_df(lg0[m], m, spin, ch[p], sh[p], cur, prev, e);
+    else rec_start_df(lg0[m], m, spin, sh[p], ch[p], cur, prev, e);
+    v[i] = make_float2(cur.h, cur.l);
+    e96[i] = (short)max(e / 96, -32767);
+}
+
 int tc_plan_init(cunusht_plan_s *P) {
     const int L = P->lmax;
+    // start tables: GL spin 1 (the pointing's synthesis) and spins up to max_spin on both grids
+    for (int g = 0; g < 2; ++g) {
+        const int np = g ? P->cc_npairs : P->gl_npairs;
+        const double *sh = g ? P->d_cc_sh : P->d_gl_sh, *ch = g ? P->d_cc_ch : P->d_gl_ch;
+        const int smax = g ? P->max_spin : std::max(P->max_spin, 1);
+        for (int s = 1; s <= smax && s <= L && np > 0; ++s) {
+            const size_t n = 2 * (size_t)np * (L + 1);
+            CU_TRY(cudaMalloc(&P->d_tc_stv[g][s], n * sizeof(float2)));
+            CU_TRY(cudaMalloc(&P->d_tc_ste[g][s], n * sizeof(short)));
+            P->ws_bytes += n * (sizeof(float2) + sizeof(short));
+            k_tc_starts<<<(unsigned)((n + 255) / 256), 256>>>(L, s, P->d_lg0[s], np, sh, ch, P->d_tc_stv[g][s],
+                                                             P->d_tc_ste[g][s]);
+            CU_LAUNCH_CHECK();
+        }
+    }
+    CU_TRY(cudaDeviceSynchronize());  // the tables are read from any stream
     size_t nrec = 0;
     for (int s = 1; s <= 2 && s <= L; ++s) {
         std::vector<int> wo(L + 2, 0);
@@ -822,14 +886,14 @@ __global__ void __launch_bounds__(POLE_TPB)
     }
 }
 
-// Ring pairs in full blocks of 256 on the tensor cores; a tail of fewer than
-// TCL_MIN_TAIL pairs after at least one full block (the equator pair of the
-// Clenshaw-Curtis grid, 2^k + 1 rings) goes to the double-float CUDA-core
-// kernel instead of a nearly empty block per order m.
+// Ring pairs in full blocks (256 pairs, 128 for NB = 8) on the tensor cores; a
+// tail of fewer than TCL_MIN_TAIL pairs after at least one full block goes to
+// the double-float CUDA-core kernel instead of a nearly empty block per order m.
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
                       const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
-                      int spin, const double2 *G, const double2 *C, long long astride, const double *lf, double2 *H,
-                      long long hstride, cudaStream_t st) {
+                      const float2 *stv, const short *ste, int spin, const double2 *G, const double2 *C,
+                      long long astride, const double *lf, double2 *H, long long hstride, cudaStream_t st) {
+    const int st_ld = npairs;  // row stride of the start table: all pairs of the grid
     if (pole == 0 && npairs > 1) {
         // the pole pair in closed form; the tensor cores take the other pairs
         // (a Clenshaw-Curtis grid of 2^k + 1 rings then fills whole blocks)
@@ -837,16 +901,25 @@ int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double 
                                                   hstride, ld);
         CU_LAUNCH_CHECK();
         ++x, ++sh, ++ch, ++rn, ++rs;
+        if (stv) ++stv, ++ste;
         --npairs;
     }
-    const int per = TCL_T / 2, tail = npairs % per;
+    const int per = (nb == 8 ? TclLayout<8>::T : TclLayout<4>::T) / 2, tail = npairs % per;
     const int ntc = (npairs > per && tail < TCL_MIN_TAIL) ? npairs - tail : npairs;
-    if (nb == 4) RC_TRY(launch_synth_tc_nb<4>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
-    else if (nb == 2) RC_TRY(launch_synth_tc_nb<2>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
-    else RC_TRY(launch_synth_tc_nb<1>(P, ntc, x, sh, ch, rn, rs, ld, spin, G, C, astride, lf, H, hstride, st));
-    if (ntc < npairs)
-        RC_TRY(leg_synth_spin_df_pairs(P, nb, npairs - ntc, x + ntc, sh + ntc, ch + ntc, rn + ntc, rs + ntc, ld, spin,
-                                       G, C, astride, lf, H, hstride, st));
+    auto launch = [&](auto nbc) {
+        constexpr int NBV = decltype(nbc)::value;
+        return launch_synth_tc_nb<NBV>(P, ntc, x, sh, ch, rn, rs, stv, ste, st_ld, ld, spin, G, C, astride, lf, H,
+                                       hstride, st);
+    };
+    if (nb == 8) RC_TRY(launch(std::integral_constant<int, 8>{}));
+    else if (nb == 4) RC_TRY(launch(std::integral_constant<int, 4>{}));
+    else if (nb == 2) RC_TRY(launch(std::integral_constant<int, 2>{}));
+    else RC_TRY(launch(std::integral_constant<int, 1>{}));
+    // the CUDA-core kernels take at most four requests per launch
+    for (int r0 = 0; ntc < npairs && r0 < nb; r0 += 4)
+        RC_TRY(leg_synth_spin_df_pairs(P, std::min(4, nb - r0), npairs - ntc, x + ntc, sh + ntc, ch + ntc, rn + ntc,
+                                       rs + ntc, ld, spin, G + r0 * astride, C ? C + r0 * astride : nullptr, astride,
+                                       lf, H + r0 * hstride, hstride, st));
     return CUNUSHT_OK;
 }
 

@@ -4,8 +4,8 @@ The self test runs integer products through the same shared-memory
 descriptors and tensor-memory path as the Legendre kernel and must be exact.
 The synthesis on the tensor cores is compared with the FP64 path and with the
 double-float CUDA-core kernels (plan switch cunusht_plan_set_tensor_cores),
-for spin 1 and 2, several lmax (windows of 128 l, partial chunks of 8 l),
-mmax < lmax, and batched (4 / 2 / 1 requests per launch) against single
+for spin 1 and 2, several lmax (windows of 128 l, partial chunks of 16 l),
+mmax < lmax, and batched (8 / 4 / 2 / 1 requests per launch) against single
 requests.  The plan's device status word stays 0 (no bounded wait ran out)."""
 import ctypes
 
@@ -85,11 +85,12 @@ def test_tc_synthesis_mmax(built_lib):
     assert _status(tc) == 0
 
 
-@pytest.mark.parametrize("nreq", [1, 3, 4, 6])
+@pytest.mark.parametrize("nreq", [1, 3, 4, 6, 8, 11])
 def test_tc_lensing_batch_equals_single(built_lib, nreq):
-    """Batched launches (4, 2, 1 requests sharing the recursion) give each
-    request exactly its single-request result: the digit products are summed
-    exactly and each column's exponent depends on its own data only."""
+    """Batched launches (8, 4, 2, 1 requests sharing the recursion; 8 in blocks
+    of two tiles) give each request exactly its single-request result: the
+    digit products are summed exactly and each column's exponent depends on
+    its own data only."""
     import cunusht_gb300 as cu
     lmax, spin = 127, 2
     t = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=1e-7, precision="mixed",
