@@ -95,12 +95,13 @@ __device__ __forceinline__ dfl df_add_u(dfl a, dfl b) {
     return dfl{s, (a.l + b.l) + t};
 }
 
-// Three-term recursion steps on unnormalised pairs.  A pair (h, l) whose l is
-// not below half an ulp of h still stands for h + l; a product of two such
-// pairs drops only the l * l term, which is below 2^-44 of the product even
-// when cancellation left |l| near 2^-22 |h|, and each step builds its pair
-// afresh from products, so the slack does not accumulate.  The digit split
-// (rounding of h, then the remainder plus l) and df_prod take such pairs too.
+// Three-term recursion steps.  The factor t = a x + g of a step is rebuilt
+// from exact inputs every step, so it may stay an unnormalised pair (h, l):
+// a product with it drops only the l * l term.  The step's result must be
+// renormalised: an unnormalised low part propagates through the recursion
+// like the value itself (the high parts then follow an FP32 recursion of
+// their own), grows to about 2^-8 of the value over 2000 steps, and its own
+// FP32 rounding enters the result (4e-6 at lmax 2047 against 1e-11).
 
 // a * x as an unnormalised pair: 4 operations instead of 7
 __device__ __forceinline__ dfl df_mul_u(dfl a, dfl x) {
@@ -114,13 +115,13 @@ __device__ __forceinline__ dfl df_mul_u(dfl a, dfl x) {
 // a * x + g as an unnormalised pair: 12 operations instead of 18 (df_mul, df_add)
 __device__ __forceinline__ dfl df_fma_u(dfl a, dfl x, dfl g) { return df_add_u(df_mul_u(a, x), g); }
 
-// t * x - b * y as an unnormalised pair: 16 operations (19 with a renormalisation)
-__device__ __forceinline__ dfl df_mul_sub_u(dfl t, dfl x, dfl b, dfl y) {
+// t * x - b * y, renormalised (t may be unnormalised)
+__device__ __forceinline__ dfl df_mul_sub(dfl t, dfl x, dfl b, dfl y) {
     const dfl p1 = df_mul_u(t, x), p2 = df_mul_u(b, y);
     const float s = p1.h - p2.h;
     const float bb = s - p1.h;
     const float err = (p1.h - (s - bb)) + (-p2.h - bb);
-    return dfl{s, err + (p1.l - p2.l)};
+    return df_fast(s, err + (p1.l - p2.l));
 }
 
 // operators so that templated complex code (FFT butterflies) runs on dfl;

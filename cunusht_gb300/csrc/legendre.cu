@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(LEG_TPB)
             }
             const float2 a2 = s_al[i], b2 = s_be[i];
             const dfl t = df_mul_u(dfl{a2.x, a2.y}, xd);
-            const dfl nxt = df_mul_sub_u(t, cur, dfl{b2.x, b2.y}, prev);
+            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
             prev = cur;
             cur = nxt;
             REC_RESCALE_DF(cur, prev, e);
@@ -425,8 +425,8 @@ __global__ void __launch_bounds__(LEG_TPB)
             const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
             const dfl tN = df_fma_u(ad, xN, gd);
             const dfl tS = df_fma_u(ad, xS, gd);
-            const dfl nN = df_mul_sub_u(tN, cN, bd, pN);
-            const dfl nS = df_mul_sub_u(tS, cS, bd, pS);
+            const dfl nN = df_mul_sub(tN, cN, bd, pN);
+            const dfl nS = df_mul_sub(tS, cS, bd, pS);
             pN = cN;
             cN = nN;
             pS = cS;
@@ -788,7 +788,7 @@ __global__ void __launch_bounds__(LEG_TPB)
             if (l < L) {
                 const float2 a2 = __ldg(al + b + l), b2 = __ldg(be + b + l);
                 const dfl t = df_mul_u(dfl{a2.x, a2.y}, xd);
-                const dfl nxt = df_mul_sub_u(t, cur, dfl{b2.x, b2.y}, prev);
+                const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
                 prev = cur;
                 cur = nxt;
                 REC_RESCALE_DF(cur, prev, e);
@@ -889,8 +889,8 @@ __global__ void __launch_bounds__(LEG_TPB)
                 const dfl ad{a2.x, a2.y}, gd{g2.x, g2.y}, bd{b2.x, b2.y};
                 const dfl tN = df_fma_u(ad, xN, gd);
                 const dfl tS = df_fma_u(ad, xS, gd);
-                const dfl nN = df_mul_sub_u(tN, cN, bd, pN);
-                const dfl nS = df_mul_sub_u(tS, cS, bd, pS);
+                const dfl nN = df_mul_sub(tN, cN, bd, pN);
+                const dfl nS = df_mul_sub(tS, cS, bd, pS);
                 pN = cN;
                 cN = nN;
                 pS = cS;

@@ -176,9 +176,9 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 // x = (h + l) sc for a power of two sc (|h sc| <= 128) as d0 + d1/256 +
 // d2/256^2 + d3/256^3 + O(2^-25), integer digits |d_i| <= 128.  The integer
 // part of h sc by one FMA with the rounding constant 1.5 x 2^23, its exact
-// remainder by another; l sc is added to the remainder.  An unnormalised pair
-// (|l| up to 2^-22 |h|, from the recursion steps) leaves the remainder below
-// 0.5 + 2^-15, so the next digit still rounds to at most 128 in magnitude.
+// remainder by another; l sc (l below half an ulp of h) is added to the
+// remainder, which stays within 0.5 (plus an ulp), so the next digit rounds to
+// at most 128 in magnitude.
 __device__ __forceinline__ void digits4s(float h, float l, float sc, float (&d)[4]) {
     const float RND = 12582912.f;
     d[0] = __fsub_rn(__fmaf_rn(h, sc, RND), RND);
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
                             agn = s_ag[i + 1];
                             ben = s_be[i + 1];
                             const dfl t = df_fma_u(dfl{ag.x, ag.y}, xd, dfl{ag.z, ag.w});
-                            const dfl nxt = df_mul_sub_u(t, cur, dfl{b2.x, b2.y}, prev);
+                            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
                             prev = cur;
                             cur = nxt;
                         };

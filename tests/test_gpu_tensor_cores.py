@@ -51,9 +51,12 @@ def _transformers(cu, lmax, mmax=None):
     return tc, cc, f64
 
 
-@pytest.mark.parametrize("lmax", [40, 127, 300])
+@pytest.mark.parametrize("lmax", [40, 127, 300, 2047])
 @pytest.mark.parametrize("spin", [1, 2])
 def test_tc_synthesis_matches_fp64(built_lib, lmax, spin):
+    """lmax 2047 runs the recursion over 2048 steps and 16 windows: an error
+    that grows with the number of steps (an unnormalised double-float step
+    gave 4e-6 there and under 1e-8 at lmax 300) shows only at full size."""
     import cunusht_gb300 as cu
     tc, cc, f64 = _transformers(cu, lmax)
     gclm, _ = orc.make_inputs(lmax, 2, seed=40 + lmax + spin)
@@ -126,3 +129,27 @@ def test_tc_lensing_against_cuda_cores(built_lib, spin):
     assert _rel(r_cc, r_64) < 1e-7
     assert _rel(r_tc, r_cc) < 1e-7
     assert _status(tc) == 0
+
+
+def test_tc_lensing_batch8_matches_fp64(built_lib):
+    """Eight requests per launch (blocks of two tiles) over several l-windows
+    (lmax 511: four windows of 128 l) against the FP64 plan, end to end."""
+    import cunusht_gb300 as cu
+    lmax, spin, nreq = 511, 2, 8
+    geo = ("gl", {"lmax": lmax})
+    t = cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=1e-7, precision="mixed", max_spin=2)
+    t64 = cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=1e-7, precision="fp64", max_spin=2)
+    G, D = [], []
+    for r in range(nreq):
+        gclm, dls = orc.make_inputs(lmax, spin, seed=700 + r)
+        G.append(gclm)
+        D.append(dls[0])
+    Gt = torch.as_tensor(np.stack(G), device="cuda")
+    Dt = torch.as_tensor(np.stack(D), device="cuda")
+    batch = t.lensing_batch(Gt, Dt, spin=spin).cpu().numpy()
+    for r in (0, nreq - 1):
+        ref = t64.gclm2lenmap(Gt[r], lmax, lmax, dlm_scaled=Dt[r], spin=spin, verbose=0).cpu().numpy()
+        err = _rel(batch[r], ref)
+        print(f"request {r}: {err:.2e} vs FP64")
+        assert err < 1e-7
+    assert _status(t) == 0
