@@ -178,7 +178,9 @@ int cunusht_nusht2d1(cunusht_plan_t *plan, int spin, int ncomp, const void *map,
  * exp(i spin gamma) rotation, i.e. GPU_cufinufft_transformer.gclm2lenmap,
  * GPU_nufft_transformer.py:487-578) of one lmax / spin / accuracy in one
  * pass of batched launches.  The mixed-precision Legendre kernels share one
- * recursion between up to four requests.  Arrays are contiguous per request:
+ * recursion between the requests of a launch: up to eight on the tensor cores
+ * (as many as cunusht_plan_reserve_batch reserved window records for: 1, 2, 4
+ * or 8), up to four on the CUDA cores.  Arrays are contiguous per request:
  * gclm (nreq, ncomp, nalm) complex128, dlm_scaled / dclm_scaled (nreq, nalm)
  * complex128 (dclm may be NULL), out (nreq, spin ? 2 : 1, npix); ptg
  * (nreq, 2, npix) and gamma (nreq, npix) receive the pointing when not NULL.
