@@ -28,16 +28,19 @@
 // the products are more accurate than the double-float CUDA-core kernels,
 // which round every product to FP32.
 //
-// Block: 544 threads.  The threads of warps 0-15 hold one ring each of 256 ring pairs
-// (threads 0-255 the rings theta, 256-511 the rings pi - theta) = four
-// 128-row MMA tiles, one order m per block row; per chunk of 16 l each writes
-// its four digit rows (two 16-byte K-cores per digit) into the A tile, a
-// subset of them the B' digits.  Warp 16 issues 4 tiles x 4 K-steps of M=128,
-// N=5 x 4 NB (rounded up to 16), K=16 MMAs.  Two A/B' buffers alternate; an
-// mbarrier per buffer (tcgen05.commit) tells when the MMAs reading it are
-// done.  Every wait is bounded: on a timeout the block records it in the
-// plan's status word, waits once more (bounded) for its MMAs, frees its
-// tensor memory and returns.
+// Block: one order m and 256 ring pairs as four 128-row MMA tiles (544
+// threads) for launches of up to 4 requests, 128 ring pairs as two tiles (288
+// threads) for 8 requests, whose 160 tensor-memory columns per tile fit 512
+// only twice.  Each ring thread holds one ring (the first half of them the
+// rings theta, the second half pi - theta); per chunk of 16 l it writes its
+// four digit rows (two 16-byte K-cores per digit) into the A tile, and the
+// ring threads together write the B' digits.  The last warp issues tiles x 4
+// K-steps of M=128, N=5 x 4 NB (rounded up to 16), K=16 MMAs.  Two A/B'
+// buffers alternate; an mbarrier per buffer (tcgen05.commit) tells when the
+// MMAs reading it are done.  Every wait is bounded: on a timeout the block
+// records it in the plan's status word, waits once more (bounded) for its
+// MMAs, frees its tensor memory and returns.  Recursion starts come from the
+// plan's table (k_tc_starts) when it has one.
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.cuh"
