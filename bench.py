@@ -125,6 +125,43 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- workload
+def _launch_chunks(nreq: int, parts) -> int:
+    """Launches a batch of nreq requests takes when the library splits it
+    greedily into launches of the given sizes (largest first, capped by the
+    largest size not above nreq, as the reservation of nreq does)."""
+    cap = max([q for q in parts if q <= max(nreq, 1)] or [1])
+    n = 0
+    left = nreq
+    while left > 0:
+        c = min(left, cap)
+        left -= max(q for q in parts if q <= c)
+        n += 1
+    return n
+
+
+def kernels_per_stage(stage: str, precision: str, eps: float, spin: int, nreq: int) -> int:
+    """Kernels one execution of a library stage launches in a batched pass of
+    nreq requests (launch lists in profiles/launches_served_l2047_spin2_mixed.md).
+    Mixed-precision Legendre synthesis on the tensor cores: window records and
+    the synthesis kernel per launch of up to 8 requests, plus the pole pair
+    of the Clenshaw-Curtis grid.  Spin-0 synthesis and the adjoint on the
+    CUDA cores: one kernel per launch of up to 4 (adjoint spin > 0: plus the
+    pole pair).  FP64 Legendre stages: one kernel per request.  Every other
+    stage: one kernel for all requests."""
+    mixed = precision == "mixed" or (precision == "auto" and eps > 1e-6)
+    if stage not in ("leg_synth", "ptg_leg", "leg_adj"):
+        return 1
+    if not mixed:
+        return nreq
+    if stage == "ptg_leg":  # spin-1 synthesis on the GL rings (no pole pair)
+        return 2 * _launch_chunks(nreq, (8, 4, 2, 1))
+    if stage == "leg_synth":
+        if spin > 0:
+            return 2 * _launch_chunks(nreq, (8, 4, 2, 1)) + 1
+        return _launch_chunks(nreq, (4, 2, 1))
+    return _launch_chunks(nreq, (4, 2, 1)) + (1 if spin > 0 else 0)
+
+
 def synth_inputs(lmax: int, spin: int, seed: int):
     """Seeded synthetic fields of the benchmark configuration (restated from the
     configuration text, independent of the oracle): gclm E ~ CN(0, 0.1 C_l),
@@ -325,7 +362,7 @@ def main():
     total_s, step_ms, stages, clocks = timed(lambda k: T.lensing_batch(GB, DB, spin, out=outB), args.steps,
                                              args.warmup, profile=True, sample_clocks=True)
     value = world * B * args.steps / total_s
-    launches = int(sum(c for _, c in stages.values()))
+    launches = int(sum(c * kernels_per_stage(name, args.precision, eps, spin, B) for name, (_, c) in stages.items()))
 
     # ---------------- single-request forms on the same GPU
     single_s, single_ms, _, _ = timed(lambda k: T.lensing_solve(G, D[k % 2], out, ptg, gam, spin),
@@ -824,7 +861,8 @@ def delensing_main(args):
                       "single_request": {"value": n1 / t1, "unit": "solves/s"}, "fp64_single_request": fp64,
                       "rel_err_vs_fp64": acc,
                       "stages_ms_per_request": {k: v[0] / v[1] / B for k, v in stages.items()},
-                      "gpu_launches": int(sum(c for _, c in stages.values()))}))
+                      "gpu_launches": int(sum(c * kernels_per_stage(name, args.precision, eps, spin, B)
+                                              for name, (_, c) in stages.items()))}))
 
 
 if __name__ == "__main__":

@@ -119,3 +119,25 @@ def test_factory_surface():
         cu.get_transformer("GPU", "nope")
     with pytest.raises(NotImplementedError):
         cu.set_transformer(None)
+
+
+def test_bench_kernel_count_matches_launch_list():
+    """bench.py's gpu_launches: kernels per stage execution.  The headline
+    served launch of 8 requests (mixed, spin 2) launches 10 kernels: window
+    records and tensor-core synthesis for the pointing and for the
+    Clenshaw-Curtis grid, its pole pair, ring transform, pointing, theta pass,
+    phi pass and interpolation (the ncu launch list of that workload)."""
+    import bench
+    stages = {s: (0.0, 10) for s in ("leg_synth", "ptg_leg", "theta_fwd", "phi_fwd", "interp", "ptg_ring",
+                                      "ptg_rot")}
+    n = sum(c * bench.kernels_per_stage(s, "mixed", 1e-7, 2, 8) for s, (_, c) in stages.items())
+    assert n == 100
+    # launches split greedily as the library does: 11 -> 8 + 2 + 1, 6 -> 4 + 2
+    assert bench.kernels_per_stage("leg_synth", "mixed", 1e-7, 2, 11) == 2 * 3 + 1
+    assert bench.kernels_per_stage("ptg_leg", "mixed", 1e-7, 2, 6) == 2 * 2
+    assert bench.kernels_per_stage("leg_synth", "mixed", 1e-7, 0, 8) == 2
+    assert bench.kernels_per_stage("leg_adj", "mixed", 1e-7, 2, 8) == 3
+    # FP64 Legendre: one launch per request ("auto" at eps <= 1e-6 is FP64)
+    assert bench.kernels_per_stage("leg_synth", "fp64", 1e-7, 2, 8) == 8
+    assert bench.kernels_per_stage("ptg_leg", "auto", 1e-7, 2, 4) == 4
+    assert bench.kernels_per_stage("interp", "mixed", 1e-7, 2, 8) == 1
