@@ -13,10 +13,11 @@ buckets overlap on the device.
 
 A launch is one CUDA-graph replay: lensing requests of a bucket go up to
 ``max_batch`` per launch through cunusht_lensing_batch, delensing requests
-through cunusht_delensing_batch (one shared Legendre recursion per four
-requests on the mixed path, forward and adjoint).  The graph of each (slot, direction, batch size) is
-captured on first use; the request's inputs are copied into the slot's
-static buffers before the replay and its result copied out after.
+through cunusht_delensing_batch (on the mixed path one shared Legendre
+recursion per launch of up to eight requests forward, on the tensor cores,
+and up to four in the adjoint).  The graph of each (slot, direction, batch
+size) is captured on first use; the request's inputs are copied into the
+slot's static buffers before the replay and its result copied out after.
 
 Admission: a bucket's slots are created when the bucket first has work and
 only if the device memory they take (measured) stays within the HBM budget;
