@@ -467,6 +467,10 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
     constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG, T = LY::T, NT = LY::NT;
     constexpr int NCOPY = 13 * 2 * NO;  // B' K-cores per chunk
     static_assert(NT * NN <= 512, "tensor memory holds 512 columns");
+    static_assert(LY::BYTES <= 227 * 1024, "dynamic shared memory of one block");
+    static_assert(LY::OFF_R % 16 == 0 && LY::RSZ % 16 == 0, "bulk copies start and end on 16 bytes");
+    static_assert(LY::OFF_B % 1024 == 0 && LY::BBUF % 1024 == 0, "MMA operand tiles on 8-row groups");
+    static_assert(LY::OFF_BAR % 8 == 0, "mbarriers are 8-byte words");
     extern __shared__ __align__(1024) unsigned char sm[];
     uint32_t *s_tm = reinterpret_cast<uint32_t *>(sm + LY::OFF_TM);
     volatile int *s_bad = reinterpret_cast<volatile int *>(sm + LY::OFF_TM + 4);
