@@ -125,18 +125,77 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- workload
-def _launch_chunks(nreq: int, parts) -> int:
-    """Launches a batch of nreq requests takes when the library splits it
-    greedily into launches of the given sizes (largest first, capped by the
-    largest size not above nreq, as the reservation of nreq does)."""
+def _launch_sizes(nreq: int, parts) -> list:
+    """Requests per launch when the library splits a batch of nreq greedily
+    into launches of the given sizes (largest first, capped by the largest
+    size not above nreq, as the reservation of nreq does)."""
     cap = max([q for q in parts if q <= max(nreq, 1)] or [1])
-    n = 0
+    sizes = []
     left = nreq
     while left > 0:
-        c = min(left, cap)
-        left -= max(q for q in parts if q <= c)
-        n += 1
-    return n
+        sizes.append(max(q for q in parts if q <= min(left, cap)))
+        left -= sizes[-1]
+    return sizes
+
+
+def _launch_chunks(nreq: int, parts) -> int:
+    return len(_launch_sizes(nreq, parts))
+
+
+def tc_mma_flops(lmax: int, spin: int, nb: int, npairs: int) -> float:
+    """Tensor-core flops one k_leg_synth_spin_tc launch of nb requests issues
+    over npairs ring pairs: per block (128 pairs for nb = 8, 256 otherwise),
+    order m and chunk of 16 l, tiles x 4 MMAs of 128 x N x 16 with
+    N = 5 x 4 nb rounded up to 16 (digit products of weights 0..4, zero
+    padding included)."""
+    nt = 2 if nb >= 8 else 4
+    nn = (5 * 4 * nb + 15) // 16 * 16
+    blocks = -(-npairs // (64 * nt))
+    chunks = 0
+    for m in range(lmax + 1):
+        n = lmax - max(m, spin) + 1
+        chunks += 8 * (n // 128) + -(-(n % 128) // 16)
+    return float(blocks * chunks * nt * 4 * 2 * 128 * nn * 16)
+
+
+def tc_pairs(stage: str, info: dict, nring: int, nb: int) -> int:
+    """Ring pairs the tensor-core kernel of a Legendre stage covers: the
+    Clenshaw-Curtis grid (Nt/2 + 1 rings) without its pole pair, or the GL
+    rings; a tail of fewer than 32 pairs after whole blocks goes to the
+    CUDA-core kernel."""
+    npairs = info["ntheta_torus"] // 4 if stage == "leg_synth" else (nring + 1) // 2
+    per = 128 if nb >= 8 else 256
+    tail = npairs % per
+    return npairs - tail if npairs > per and tail < 32 else npairs
+
+
+def legendre_roofline(stage, alg_tflops, avg_s, info, lmax, spin, nring, nreq, peaks, traffic):
+    """Roofline of a mixed-precision Legendre stage on the tensor cores:
+    achieved = the MMA flops its tensor-core launches issue / the stage time,
+    against the measured bf16 peak; beside it the FP32 view (algorithmic
+    flops against the CUDA-core rate), the bound that actually limits it."""
+    s = spin if stage == "leg_synth" else 1
+    mma = sum(tc_mma_flops(lmax, s, nb, tc_pairs(stage, info, nring, nb)) for nb in _launch_sizes(nreq, (8, 4, 2, 1)))
+    ach = mma / avg_s / 1e12
+    peak = peaks.get("bf16_tflops", 1900.0)
+    fp32_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    return {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+            "traffic": traffic, "kernel": stage,
+            "peak_source": ("measured bf16 burst (MEASURED_PEAKS.json)" if "bf16_tflops" in peaks
+                            else "fallback 1.9 PFLOP/s bf16"),
+            "achieved_counts": "bf16 MMA flops the tensor-core launches issue (integer digit products of "
+                               "weights 0..4 incl. zero padding) / stage time incl. the window-record and "
+                               "pole-pair kernels",
+            "fp32_view": {"achieved": alg_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                          "frac": alg_tflops / fp32_peak,
+                          "note": "the bound: the double-float recursion and digit split issue on the FP32 "
+                                  "CUDA cores (algorithmic flops, 8 per l,m,ring,component, against 152 SMs x "
+                                  "128 lanes x 2 flop at the max SM clock); ncu issue, pipe and tensor-pipe "
+                                  "figures in profiles/leg_synth_tc_l2047.md"},
+            "traffic_source": "DRAM bytes of the stage's kernels per launch of 8 requests at lmax 2047 (an "
+                              "lmax 1023 capture scaled by the (l, m) pairs), scaled to the batch size"}
+
+
 
 
 def kernels_per_stage(stage: str, precision: str, eps: float, spin: int, nreq: int) -> int:
@@ -406,21 +465,18 @@ def main():
             roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                     "traffic": None, "kernel": dom,
                     "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak in MEASURED_PEAKS.json)"}
+        elif dom == "ptg_leg" or spin > 0:
+            tr = LEG_TRAFFIC.get(dom)
+            roof = legendre_roofline(dom, ach, avg_s, info, lmax, spin, nring, B, peaks,
+                                     tr * B / LEG_TRAFFIC["batch"] if tr else None)
         else:
-            # Legendre: double-float recursion on the FP32 pipe (the bound), contraction on the
-            # tensor cores; peak = 152 SMs x 128 lanes x 2 flop x max SM clock
+            # spin-0 synthesis: double-float CUDA-core kernels, FP32 pipe
             mhz = peaks.get("sm_max_mhz", 2070.0)
             peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-            tr = LEG_TRAFFIC.get(dom)
             roof = {"bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                    "traffic": tr * B / LEG_TRAFFIC["batch"] if tr else None, "kernel": dom,
-                    "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; "
-                                   "achieved counts algorithmic flops only (8 per l,m,ring,component); the "
-                                   "double-float recursion and digit split bound the kernel on the CUDA cores "
-                                   "while the contraction runs on the tensor cores (ncu issue, pipe and "
-                                   "tensor-pipe figures in profiles/leg_synth_tc_l2047.md); traffic = DRAM "
-                                   "bytes of the stage's kernels per launch of 8 requests at lmax 2047 (an "
-                                   "lmax 1023 capture scaled by the (l, m) pairs), scaled to the batch size"}
+                    "traffic": None, "kernel": dom,
+                    "peak_source": "nominal FP32 CUDA-core rate at the measured max SM clock; achieved counts "
+                                   "algorithmic flops only"}
     stage_table = {s: {"ms_per_launch": v[0] / v[1], "launches": v[1],
                        "share": v[0] / sum(x[0] for x in stages.values())} for s, v in stages.items()}
     for s, v in stage_table.items():

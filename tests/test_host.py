@@ -1,6 +1,7 @@
 """Host-side checks that need no GPU: the C-ABI library loads and exports every
 symbol include/cunusht_gb300.h declares, and the Python host logic (geometry,
 alm utilities, argument parsing, factory) matches the reference semantics."""
+import json
 import os
 import re
 import shutil
@@ -141,3 +142,37 @@ def test_bench_kernel_count_matches_launch_list():
     assert bench.kernels_per_stage("leg_synth", "fp64", 1e-7, 2, 8) == 8
     assert bench.kernels_per_stage("ptg_leg", "auto", 1e-7, 2, 4) == 4
     assert bench.kernels_per_stage("interp", "mixed", 1e-7, 2, 8) == 1
+
+
+def test_bench_tensor_roofline_counts_issued_mma_flops():
+    """bench.py's Legendre roofline: the MMA flops of the tensor-core launches
+    (per block, order m and 16-l chunk: tiles x 4 MMAs of 128 x N x 16),
+    checked against a walk over the kernel's windows and chunks, and the
+    roofline of the headline launch of 8 against the measured bf16 peak."""
+    import bench
+
+    def walk(lmax, spin, nb, npairs):
+        nt = 2 if nb >= 8 else 4
+        nn = (20 * nb + 15) // 16 * 16
+        blocks = -(-npairs // (64 * nt))
+        total = 0
+        for m in range(lmax + 1):
+            wb = max(m, spin)
+            while wb <= lmax:                         # windows of 128 l
+                cnt = min(128, lmax - wb + 1)
+                total += blocks * (-(-cnt // 16)) * nt * 4 * 2 * 128 * nn * 16
+                wb += 128
+        return total
+
+    for lmax, spin, nb, npairs in ((300, 2, 8, 150), (300, 1, 4, 151), (1023, 2, 1, 512), (2047, 2, 8, 1024)):
+        assert bench.tc_mma_flops(lmax, spin, nb, npairs) == walk(lmax, spin, nb, npairs)
+    info = {"ntheta_torus": 4096}
+    assert bench.tc_pairs("leg_synth", info, 2048, 8) == 1024      # 1025 pairs less the pole pair
+    assert bench.tc_pairs("ptg_leg", info, 2048, 8) == 1024
+    roof = bench.legendre_roofline("leg_synth", 41.2, 13.35e-3, info, 2047, 2, 2048, 8,
+                                   {"bf16_tflops": 1901.2, "sm_max_mhz": 2070.0}, 2686e6)
+    assert roof["bound"] == "tensor" and roof["unit"] == "TFLOP/s" and roof["peak"] == 1901.2
+    assert 380 < roof["achieved"] < 440 and abs(roof["frac"] - roof["achieved"] / 1901.2) < 1e-12
+    assert abs(roof["fp32_view"]["frac"] - 41.2 / (152 * 128 * 2 * 2070e6 / 1e12)) < 1e-12
+    assert roof["traffic"] == 2686e6
+    json.dumps(roof)
