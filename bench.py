@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark: lensing solves/s at lmax 2047, spin 2, epsilon 1e-7, served form.
 
-A step is one launch of the served form: B lensing requests (default 4), each
+A step is one launch of the served form: B lensing requests (default 8), each
 with its own gclm and deflection, through cunusht_lensing_batch --
 dlm2pointing (spin-1 synthesis of the deflection on the GL 2048 x 4095 grid +
 pointing rotation) followed by the spin-2 nusht2d2 of the E-mode alm at the
@@ -42,7 +42,6 @@ METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7 (served mixed vs plain F
 # DRAM bytes (read + write) of the Legendre stages (records + pole + tensor-core
 # kernels) per launch of 8 requests at lmax 2047: one ncu capture at lmax 1023
 # (a few GB on the device) scaled by 4.0, the ratio of (l, m) pairs
-# (profiles/leg_synth_tc_l2047.md)
 LEG_TRAFFIC = {"batch": 8, "leg_synth": 2686.0e6, "ptg_leg": 2414.0e6}
 
 
@@ -170,37 +169,41 @@ def tc_pairs(stage: str, info: dict, nring: int, nb: int) -> int:
 
 
 def legendre_roofline(stage, alg_tflops, avg_s, info, lmax, spin, nring, nreq, peaks, traffic):
-    """Roofline of a mixed-precision Legendre stage on the tensor cores:
-    achieved = the MMA flops its tensor-core launches issue / the stage time,
-    against the measured bf16 peak; beside it the FP32 view (algorithmic
-    flops against the CUDA-core rate), the bound that actually limits it."""
+    """Roofline of a mixed-precision Legendre stage against the tensor
+    roofline: achieved = ALGORITHMIC flops (8 per l, m, ring, component for
+    spin > 0, 4 for spin 0) / the stage time, against the measured bf16 burst
+    peak.  Two named views sit beside it and never replace it: the bf16 MMA
+    flops the tensor-core launches actually issue (integer digit products of
+    weights 0..4, zero padding included) and the algorithmic flops against
+    the FP32 CUDA-core rate, where the double-float recursion issues."""
     s = spin if stage == "leg_synth" else 1
     mma = sum(tc_mma_flops(lmax, s, nb, tc_pairs(stage, info, nring, nb)) for nb in _launch_sizes(nreq, (8, 4, 2, 1)))
-    ach = mma / avg_s / 1e12
+    issued = mma / avg_s / 1e12
     peak = peaks.get("bf16_tflops", 1900.0)
     fp32_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
-    return {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+    return {"bound": "tensor", "achieved": alg_tflops, "peak": peak, "unit": "TFLOP/s", "frac": alg_tflops / peak,
             "traffic": traffic, "kernel": stage,
             "peak_source": ("measured bf16 burst (MEASURED_PEAKS.json)" if "bf16_tflops" in peaks
                             else "fallback 1.9 PFLOP/s bf16"),
-            "achieved_counts": "bf16 MMA flops the tensor-core launches issue (integer digit products of "
-                               "weights 0..4 incl. zero padding) / stage time incl. the window-record and "
-                               "pole-pair kernels",
+            "achieved_counts": "algorithmic flops of the stage (8 per l, m, ring, component; per launch of "
+                               "the batch) / stage time incl. the window-record and pole-pair kernels",
+            "issued_mma_view": {"achieved": issued, "peak": peak, "unit": "TFLOP/s", "frac": issued / peak,
+                                "mma_flops_per_launch": mma,
+                                "note": "bf16 MMA flops the tensor-core launches issue: integer digit "
+                                        "products of weights 0..4 incl. zero padding, about 10x the "
+                                        "algorithmic flops"},
             "fp32_view": {"achieved": alg_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                           "frac": alg_tflops / fp32_peak,
-                          "note": "the bound: the double-float recursion and digit split issue on the FP32 "
-                                  "CUDA cores (algorithmic flops, 8 per l,m,ring,component, against 152 SMs x "
-                                  "128 lanes x 2 flop at the max SM clock); ncu issue, pipe and tensor-pipe "
-                                  "figures in profiles/leg_synth_tc_l2047.md"},
+                          "note": "algorithmic flops against the FP32 CUDA-core rate (152 SMs x 128 lanes x "
+                                  "2 flop at the max SM clock, computed, not measured): the double-float "
+                                  "recursion and digit split issue there"},
             "traffic_source": "DRAM bytes of the stage's kernels per launch of 8 requests at lmax 2047 (an "
                               "lmax 1023 capture scaled by the (l, m) pairs), scaled to the batch size"}
 
 
-
-
 def kernels_per_stage(stage: str, precision: str, eps: float, spin: int, nreq: int) -> int:
     """Kernels one execution of a library stage launches in a batched pass of
-    nreq requests (launch lists in profiles/launches_served_l2047_spin2_mixed.md).
+    nreq requests (as the ncu launch list of a served launch shows).
     Mixed-precision Legendre synthesis on the tensor cores: window records and
     the synthesis kernel per launch of up to 8 requests, plus the pole pair
     of the Clenshaw-Curtis grid.  Spin-0 synthesis and the adjoint on the

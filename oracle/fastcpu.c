@@ -1,6 +1,6 @@
 /*
- * FP64 CPU restatement of the reference's lensing algorithm -- TEST AND
- * BASELINE INFRASTRUCTURE ONLY (never linked into the product).
+ * FP64 CPU restatement of the reference's lensing algorithm -- TEST AND CPU
+ * TIMING-BASELINE INFRASTRUCTURE ONLY (never linked into the product).
  *
  * The reference's CPU backend (cunusht/deflection/CPU_nufft_transformer.py,
  * ducc0 synthesis_general as called at :645-652, get_deflected_angles at

@@ -145,10 +145,11 @@ def test_bench_kernel_count_matches_launch_list():
 
 
 def test_bench_tensor_roofline_counts_issued_mma_flops():
-    """bench.py's Legendre roofline: the MMA flops of the tensor-core launches
-    (per block, order m and 16-l chunk: tiles x 4 MMAs of 128 x N x 16),
-    checked against a walk over the kernel's windows and chunks, and the
-    roofline of the headline launch of 8 against the measured bf16 peak."""
+    """bench.py's Legendre roofline: achieved = ALGORITHMIC flops / stage
+    time against the measured bf16 peak; the MMA flops the tensor-core
+    launches issue (per block, order m and 16-l chunk: tiles x 4 MMAs of
+    128 x N x 16, checked against a walk over the kernel's windows and
+    chunks) only as the named issued-MMA view beside it."""
     import bench
 
     def walk(lmax, spin, nb, npairs):
@@ -172,7 +173,32 @@ def test_bench_tensor_roofline_counts_issued_mma_flops():
     roof = bench.legendre_roofline("leg_synth", 41.2, 13.35e-3, info, 2047, 2, 2048, 8,
                                    {"bf16_tflops": 1901.2, "sm_max_mhz": 2070.0}, 2686e6)
     assert roof["bound"] == "tensor" and roof["unit"] == "TFLOP/s" and roof["peak"] == 1901.2
-    assert 380 < roof["achieved"] < 440 and abs(roof["frac"] - roof["achieved"] / 1901.2) < 1e-12
+    assert roof["achieved"] == 41.2 and abs(roof["frac"] - 41.2 / 1901.2) < 1e-12
+    iss = roof["issued_mma_view"]
+    assert 380 < iss["achieved"] < 440 and abs(iss["frac"] - iss["achieved"] / 1901.2) < 1e-12
     assert abs(roof["fp32_view"]["frac"] - 41.2 / (152 * 128 * 2 * 2070e6 / 1e12)) < 1e-12
     assert roof["traffic"] == 2686e6
     json.dumps(roof)
+
+
+def test_sht_mode_positional_signatures():
+    """The SHT-only transformer takes the reference's positional arguments
+    (GPU_SHTns_transformer, cunusht/sht/GPU_sht_transformer.py:47-127), so
+    reference call sites bind the same parameters."""
+    import inspect
+    from cunusht_gb300.transformer import GPU_SHT_transformer
+    ref = {
+        "synthesis": ["gclm", "lmax", "mmax", "mode", "nthreads"],
+        "synthesis_cupy": ["gclm", "out", "lmax", "mmax", "mode", "nthreads"],
+        "adjoint_synthesis_cupy": ["synthmap", "gclm", "lmax", "mmax", "mode", "nthreads", "iw"],
+        "synthesis_der1": ["gclm", "out", "nthreads"],
+        "synthesis_der1_cupy": ["gclm", "out_theta", "out_phi", "nthreads"],
+        "analysis": ["map", "lmax", "mmax", "nthreads", "alm", "mode"],
+        "adjoint_synthesis": ["map"],
+        "map2alm": ["m"],
+        "alm2map": ["gclm"],
+    }
+    for name, params in ref.items():
+        got = [p for p in inspect.signature(getattr(GPU_SHT_transformer, name)).parameters if p != "self"]
+        assert got[:len(params)] == params, (name, got)
+
