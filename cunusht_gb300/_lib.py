@@ -55,6 +55,7 @@ SIGNATURES = {
     "cunusht_synthesis": (_i, [_vp, _i, _i, _vp, _i, _vp, _vp]),
     "cunusht_lensing_vjp_dlm": (_i, [_vp, _i, _vp, _i, _vp, _i, _vp, _vp, _vp]),
     "cunusht_adjoint_synthesis": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp]),
+    "cunusht_analysis": (_i, [_vp, _i, _i, _vp, _vp, _vp, _i, _vp]),
     "cunusht_pointing": (_i, [_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cunusht_doubling": (_i, [_vp, _i64, _i64, _i, _i, _i, _vp, _vp]),
     "cunusht_adjoint_doubling": (_i, [_vp, _i64, _i64, _i, _i, _vp, _vp]),

@@ -600,7 +600,7 @@ int cunusht_tc_selftest(int n, int reps, int mode, double *maxerr, int *timeout)
     ARG_CHECK(maxerr != nullptr && timeout != nullptr, "maxerr and timeout must not be NULL");
     ARG_CHECK(n == 16 || n == 32 || n == 64, "n must be 16, 32 or 64, got %d", n);
     ARG_CHECK(reps >= 1 && reps <= 16, "reps must be in [1, 16], got %d", reps);
-    ARG_CHECK(mode >= 0 && mode <= 2, "mode must be 0, 1 or 2, got %d", mode);
+    ARG_CHECK(mode >= 0 && mode <= 3, "mode must be 0, 1, 2 or 3, got %d", mode);
     return tc_selftest(n, reps, mode, maxerr, timeout);
 }
 
@@ -992,6 +992,23 @@ int cunusht_adjoint_synthesis(cunusht_plan_t *P, int spin, int ncomp, const doub
     ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
     cudaStream_t st = (cudaStream_t)stream;
     RC_TRY(ring_adjoint(P, spin, map, spin ? map + P->npix : nullptr, P->d_Hgl, st));
+    double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
+    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st));
+    if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
+    return CUNUSHT_OK;
+}
+
+int cunusht_analysis(cunusht_plan_t *P, int spin, int ncomp, const double *map, const double *ring_weight,
+                     void *alm_out, int alm_dtype, void *stream) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(spin >= 0 && spin <= 2, "spin must be 0, 1 or 2");
+    if (spin == 0) ARG_CHECK(ncomp == 1, "spin 0 takes ncomp = 1");
+    else ARG_CHECK(ncomp == 1 || ncomp == 2, "spin > 0 takes ncomp 1 or 2");
+    ARG_CHECK(alm_out && map && ring_weight, "NULL array argument");
+    ARG_CHECK(alm_dtype == CUNUSHT_F64 || alm_dtype == CUNUSHT_F32, "bad alm dtype");
+    cudaStream_t st = (cudaStream_t)stream;
+    RC_TRY(ring_adjoint(P, spin, map, spin ? map + P->npix : nullptr, P->d_Hgl, st, ring_weight));
     double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
     RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st));
     if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));

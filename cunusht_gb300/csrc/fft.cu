@@ -705,12 +705,15 @@ int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st)
 
 // h'_m = e^{-i m phi0} sum_p z'_p e^{-2 pi i m p / N} (adjoint of k_ring_synth;
 // a mode reads its bin m mod N, so rings shorter than 2L + 1 alias as in the
-// synthesis); SP = 2 as in k_ring_synth, the two parity launches summed into Hgl
+// synthesis); SP = 2 as in k_ring_synth, the two parity launches summed into Hgl.
+// wring (may be NULL): per-ring quadrature weight multiplied into h' (the
+// weighted adjoint = analysis, SHTns analys)
 __global__ void __launch_bounds__(FFT_TPB)
     k_ring_adj(const double *__restrict__ in0, const double *__restrict__ in1, int nring, int L,
                int spin, const double *__restrict__ phi0, const long long *__restrict__ ofs, RingCls rc,
                const double2 *__restrict__ chirp_all, const double2 *__restrict__ bker_all,
-               double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW, int q) {
+               double2 *__restrict__ Hgl, const double2 *__restrict__ tw, int TW, int q,
+               const double *__restrict__ wring) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double2 *buf = reinterpret_cast<double2 *>(smem_raw);
     const int MTW = rc.Hmax;  // length of the quarter twiddle table
@@ -749,6 +752,10 @@ __global__ void __launch_bounds__(FFT_TPB)
         double s, c;
         sincos(m * ph0, &s, &c);
         double2 h = cmul(y, make_double2(c, -s));
+        if (wring) {
+            const double w = wring[ring];
+            h = make_double2(h.x * w, h.y * w);
+        }
         if (SP == 2 && q == 0) {
             const double2 prev = Hgl[(long long)cidx * nring + ring];
             h = make_double2(h.x + prev.x, h.y + prev.y);
@@ -1086,13 +1093,13 @@ int ring_synth(const cunusht_plan_s *P, int spin, const double2 *Hgl, double *ou
 }
 
 int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
-                 double2 *Hgl, cudaStream_t st) {
+                 double2 *Hgl, cudaStream_t st, const double *wring) {
     size_t sm = fft_smem_bytes(ring_buffer_len(P), false);
     RC_TRY(set_smem(k_ring_adj, sm));
     const RingCls rc = ring_cls_of(P);
     for (int q = P->sp_ring - 1; q >= 0; --q) {
         k_ring_adj<<<P->nring, FFT_TPB, sm, st>>>(in0, in1, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
-                                                  rc, P->d_chirp, P->d_bker, Hgl, P->d_tw64, P->TW, q);
+                                                  rc, P->d_chirp, P->d_bker, Hgl, P->d_tw64, P->TW, q, wring);
         CU_LAUNCH_CHECK();
     }
     return CUNUSHT_OK;

@@ -60,7 +60,7 @@ int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, lo
 int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,
                      double *out1, long long obs, cudaStream_t st);
 int ring_adjoint(const cunusht_plan_s *P, int spin, const double *in0, const double *in1,
-                 double2 *Hgl, cudaStream_t st);
+                 double2 *Hgl, cudaStream_t st, const double *wring = nullptr);
 int split_c128_to_df(const double2 *in, long long n, void *out, cudaStream_t st);
 int fft_global_f64(double2 *data, int N, int dir, const double2 *tw, int TW, cudaStream_t st);
 size_t fft_smem_bytes(int N, bool f32);

@@ -25,8 +25,10 @@ def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
-def to_device(x, name: str, dtype: torch.dtype | None = None, warn: bool = True) -> torch.Tensor:
-    """Device tensor view of x (torch / cupy / numpy), contiguous, of dtype."""
+def to_device(x, name: str, dtype: torch.dtype | None = None, warn: bool = True,
+              contiguous: bool = True) -> torch.Tensor:
+    """Device tensor view of x (torch / cupy / numpy) of dtype, contiguous
+    unless ``contiguous`` is False (the caller then handles strides)."""
     if isinstance(x, torch.Tensor) and x.is_cuda:
         t = x
     elif hasattr(x, "__cuda_array_interface__"):
@@ -38,7 +40,7 @@ def to_device(x, name: str, dtype: torch.dtype | None = None, warn: bool = True)
         t = torch.as_tensor(np.asarray(x), device="cuda")
     if dtype is not None and t.dtype != dtype:
         t = t.to(dtype)
-    return t.contiguous()
+    return t.contiguous() if contiguous else t
 
 
 def _loc_args(loc: torch.Tensor, npts_hint: int | None = None):
@@ -192,7 +194,7 @@ class GPU_cufinufft_transformer:
         self._ensure_plan(epsilon)
         a, ncomp, adt = self._alm_in(alm, "alm", spin)
         assert loc is not None, "loc must be provided"
-        loc_t, npts, layout = _loc_args(to_device(loc, "loc", torch.float64))
+        loc_t, npts, layout = _loc_args(to_device(loc, "loc", torch.float64, contiguous=False))
         out = torch.empty((npts,) if spin == 0 else (2, npts), dtype=out_dtype, device="cuda")
         odt = _lib.F32 if out_dtype == torch.float32 else _lib.F64
         g = None
@@ -215,7 +217,7 @@ class GPU_cufinufft_transformer:
         if m.dtype not in (torch.float32, torch.float64):
             m = m.to(torch.float64)
         mdt = _lib.F32 if m.dtype == torch.float32 else _lib.F64
-        loc_t, npts, layout = _loc_args(to_device(loc, "loc", torch.float64))
+        loc_t, npts, layout = _loc_args(to_device(loc, "loc", torch.float64, contiguous=False))
         if spin == 0:
             m = m.reshape(-1)
             assert m.numel() == npts, (m.numel(), npts)
@@ -286,7 +288,7 @@ class GPU_cufinufft_transformer:
         mi = torch.repeat_interleave(torch.arange(self.lmax + 1, device="cuda"),
                                      torch.arange(self.lmax + 1, 0, -1, device="cuda"))
         li = torch.arange(self.nalm, device="cuda") - (mi * (2 * self.lmax + 1 - mi)) // 2
-        return self.synthesis((a * fl[li])[None], spin=1)
+        return GPU_cufinufft_transformer.synthesis(self, (a * fl[li])[None], spin=1)
 
     def set_pts(self, ptg):
         self.ptg = to_device(ptg, "ptg", torch.float64)
@@ -443,8 +445,11 @@ class GPU_cufinufft_transformer:
         spin = self._spin_of(gclm, spin)
         ptg, gamma = self._timed("dlm2pointing", lambda: self._pointing(ptg, dlm_scaled, dclm_scaled, lmax, verbose))
         g = gamma if (spin and polrot) else None
+        # complex64 alm give float32 maps (the single-precision configuration),
+        # complex128 alm float64 maps
+        odt = torch.float32 if (isinstance(gclm, torch.Tensor) and gclm.dtype == torch.complex64) else torch.float64
         res = self._timed("nusht2d2", lambda: self.nusht2d2(lmax, mmax, gclm, ptg.t(), epsilon=epsilon, spin=spin,
-                                                            gamma=g))
+                                                            gamma=g, out_dtype=odt))
         if execmode == "debug":
             self.ret = {"dlm2pointing": ptg, "gamma": gamma, "nusht2d2": res}
             return self.ret
@@ -533,8 +538,120 @@ class GPU_cufinufft_transformer:
 
 
 class GPU_SHT_transformer(GPU_cufinufft_transformer):
-    """SHT-only mode on the (GL) geometry: synthesis / adjoint_synthesis /
-    synthesis_der1 (cunusht.py:75-76, GPU_sht_transformer.py:11-127)."""
+    """SHT-only mode (cunusht.py:75-76) with the surface of the reference's
+    ``GPU_SHTns_transformer`` (cunusht/sht/GPU_sht_transformer.py:11-127):
+    synthesis / synthesis_cupy, adjoint_synthesis_cupy, synthesis_der1 /
+    synthesis_der1_cupy, analysis, adjoint_synthesis, map2alm, alm2map, with
+    the reference's argument order.
+
+    Maps follow SHTns's theta-contiguous grid as the reference sets it up
+    (SHT_THETA_CONTIGUOUS, GPU_sht_transformer.py:21-37): spatial shape
+    (nphi, nlat), flattened by ``synthesis``; ``synthesis_der1_cupy``
+    returns ring-major planes as the reference's ``.T.flatten()`` does
+    (:106-107).  Geometries whose rings differ in length (HEALPix, thinned
+    grids) have no such grid and use ring-major (npix,) maps throughout.
+    ``analysis`` / ``adjoint_synthesis`` / ``map2alm`` are SHTns ``analys``:
+    the quadrature-weighted adjoint (exact inverse of the synthesis on a
+    Gauss-Legendre grid at the band limit).  ``spin`` (default 0, the
+    reference's scalar SHTns transforms) extends every method to spin 1, 2.
+    Compute runs in the library (cunusht_synthesis, cunusht_analysis); the
+    layout change is a device transpose."""
 
     def __init__(self, geominfo, nthreads=None, max_spin: int = 2):
         super().__init__(geominfo, nuFFTtype=None, epsilon=1e-7, max_spin=max_spin)
+        nph = np.asarray(self.geom.nph, dtype=np.int64)
+        self.nlat = int(nph.size)
+        self.nphi = int(nph[0])
+        self.theta_contiguous = bool(np.all(nph == nph[0]))
+        self.spat_shape = (self.nphi, self.nlat) if self.theta_contiguous else (self.npix(),)
+        self._ring_w = torch.as_tensor(np.ascontiguousarray(self.geom.weight, dtype=np.float64), device="cuda")
+
+    # ring-major (..., npix) <-> the transformer's spatial layout
+    def _to_spat(self, ring: torch.Tensor) -> torch.Tensor:
+        if not self.theta_contiguous:
+            return ring
+        lead = ring.shape[:-1]
+        return ring.reshape(*lead, self.nlat, self.nphi).transpose(-1, -2).contiguous()
+
+    def _from_spat(self, m: torch.Tensor, spin: int) -> torch.Tensor:
+        npix = self.npix()
+        ncomp = 2 if spin else 1
+        m = m.reshape(ncomp, npix) if spin else m.reshape(1, npix)
+        if self.theta_contiguous:
+            m = m.reshape(ncomp, self.nphi, self.nlat).transpose(-1, -2).reshape(ncomp, npix)
+        return (m if spin else m[0]).contiguous()
+
+    def synthesis_cupy(self, gclm, out=None, lmax=None, mmax=None, mode=None, nthreads=None, spin=0):
+        """gclm -> map(s) of spatial shape (GPU_sht_transformer.py:56-62).
+        ``out`` (optional, spatial shape) receives the result and is returned."""
+        ring = GPU_cufinufft_transformer.synthesis(self, gclm, None, lmax, mmax, spin=spin)
+        res = self._to_spat(ring)
+        if out is not None:
+            o = out if isinstance(out, torch.Tensor) else torch.as_tensor(out, device="cuda")
+            if o.numel() == res.numel():
+                o.copy_(res.reshape(o.shape))
+                return o
+        return res
+
+    def synthesis(self, gclm, lmax=None, mmax=None, mode=None, nthreads=None, spin=0):
+        """gclm -> flattened map(s) (GPU_sht_transformer.py:47-54): (npix,)
+        for spin 0, (2, npix) for spin s."""
+        res = self.synthesis_cupy(gclm, None, lmax, mmax, spin=spin)
+        return res.reshape(2, -1) if spin else res.reshape(-1)
+
+    def alm2map(self, gclm, **kwargs):
+        return self.synthesis(gclm, **kwargs)
+
+    def analysis(self, map, lmax=None, mmax=None, nthreads=None, alm=None, mode=None, spin=0, ncomp=None):
+        """Quadrature-weighted adjoint, SHTns analys (GPU_sht_transformer.py:
+        99-105): map(s) in spatial shape or flattened -> (1, nalm) for spin 0
+        (np.atleast_2d of the reference), (ncomp, nalm) for spin s."""
+        lmax = self.lmax if lmax is None else lmax
+        self._check_lm(lmax, self.lmax if mmax is None else mmax)
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        m = self._from_spat(to_device(map, "map", torch.float64), spin)
+        ncomp = (1 if spin == 0 else 2) if ncomp is None else ncomp
+        res = torch.empty((ncomp, self.nalm), dtype=torch.complex128, device="cuda")
+        _lib.check(self._lib.cunusht_analysis(self._plan, spin, ncomp, m.data_ptr(), self._ring_w.data_ptr(),
+                                              res.data_ptr(), _lib.F64, _stream()))
+        return res
+
+    def adjoint_synthesis(self, map, **kwargs):
+        """As the reference's SHT mode (GPU_sht_transformer.py:108-118): the
+        map reshaped to the spatial shape, then ``analysis``."""
+        return self.analysis(map, **kwargs)
+
+    def map2alm(self, m, **kwargs):
+        return self.analysis(m, **kwargs)
+
+    def adjoint_synthesis_cupy(self, synthmap, gclm=None, lmax=None, mmax=None, mode=None, nthreads=None, iw=None,
+                               spin=0):
+        """SHTns analys of synthmap * iw (GPU_sht_transformer.py:65-73):
+        (nalm,) for spin 0, (ncomp, nalm) for spin s.  With iw = 1 / w (the
+        inverse quadrature weights) this is the unweighted adjoint synthesis
+        the nuFFT adjoint uses (GPU_nufft_transformer.py:265-269)."""
+        m = to_device(synthmap, "synthmap", torch.float64)
+        if iw is not None:
+            w = to_device(iw, "iw", torch.float64, warn=False)
+            m = (m.reshape(*((2,) if spin else ()), *self.spat_shape) * w).contiguous()
+        res = self.analysis(m, lmax, mmax, spin=spin)
+        return res if spin else res[0]
+
+    def synthesis_der1(self, gclm, out=None, nthreads=None):
+        """(d/dtheta, 1/sin(theta) d/dphi) of a scalar field, SHTns
+        synth_grad, as flattened spatial maps (GPU_sht_transformer.py:76-86):
+        (2, npix)."""
+        ring = GPU_cufinufft_transformer.synthesis_der1(self, gclm)
+        return self._to_spat(ring).reshape(2, -1)
+
+    def synthesis_der1_cupy(self, gclm, out_theta=None, out_phi=None, nthreads=None):
+        """The gradient of synthesis_der1 as ring-major planes (2, npix), the
+        reference's ``.T.flatten()`` of the theta-contiguous grid
+        (GPU_sht_transformer.py:88-97); out_theta / out_phi (optional)
+        receive the planes."""
+        ring = GPU_cufinufft_transformer.synthesis_der1(self, gclm)
+        for o, r in ((out_theta, ring[0]), (out_phi, ring[1])):
+            if isinstance(o, torch.Tensor) and o.is_contiguous() and o.numel() == r.numel():
+                o.view(-1).copy_(r)
+        return ring

@@ -137,9 +137,12 @@ int cunusht_plan_device_status(cunusht_plan_t *plan, int *status);
  * below 2^24) through the descriptors, tensor-memory accumulation and
  * read-back path of the tensor-core Legendre kernel, on the current device.
  * mode 0: entries of both signs; 1: entries in [64, 128]; 2: one large
- * product per output among small ones.  *maxerr = largest |result - exact|
- * (0 when the accumulation is exact), *timeout = 1 if the completion wait ran
- * out.  No reference counterpart.
+ * product per output among small ones; 3: no product is issued and the
+ * completion wait is limited to 64 polls, so it runs out on purpose (the
+ * kernel's timeout path: status set, tensor memory released, nothing read;
+ * the context stays usable).  *maxerr = largest |result - exact| (0 when the
+ * accumulation is exact), *timeout = 1 if the completion wait ran out.  No
+ * reference counterpart.
  */
 int cunusht_tc_selftest(int n, int reps, int mode, double *maxerr, int *timeout);
 
@@ -300,6 +303,21 @@ int cunusht_adjoint_synthesis(cunusht_plan_t *plan, int spin, int ncomp, const d
                               void *alm_out, int alm_dtype, void *stream);
 
 /*
+ * Analysis on the plan's ring geometry: the adjoint synthesis of the map
+ * weighted per ring by ring_weight (DEVICE array, nring entries: the
+ * quadrature weight of one pixel of that ring, e.g. Gauss-Legendre weight x
+ * 2 pi / nphi), so that on a Gauss-Legendre grid with nring >= lmax + 1 and
+ * nphi >= 2 lmax + 1 it inverts cunusht_synthesis exactly.  Replaces the
+ * SHTns analys of the reference's SHT-only mode (GPU_SHTns_transformer.
+ * analysis / adjoint_synthesis_cupy / map2alm, GPU_sht_transformer.py:65-73,
+ * :99-127; with iw = 1 / w the weighted adjoint of GPU_nufft_transformer.py:
+ * 265-269 is cunusht_adjoint_synthesis).  Maps as cunusht_adjoint_synthesis.
+ */
+int cunusht_analysis(cunusht_plan_t *plan, int spin, int ncomp, const double *map, const double *ring_weight,
+                     void *alm_out, int alm_dtype, void *stream);
+
+/*
+ * Raw pointing rotation/*
  * Raw pointing rotation (compute_pointing_1Dto1D_lowmem, pointing.cu:197-226):
  * per pixel of a ring geometry, deflected (theta', phi') from the spin-1
  * deflection maps (d_theta, d_phi) in ring-major pixel order; gamma optional.
@@ -334,15 +352,19 @@ int cunusht_adjoint_doubling(const void *dmap, int64_t ntheta, int64_t nphi, int
  * that give a plugin no allocator.  The caller passes the alm (complex128,
  * device, ncomp x nalm) and the output map (device, npix or 2 x npix float64,
  * ring i at pixels [i nphi, (i + 1) nphi)); ring colatitudes and first
- * longitudes are host arrays and the rings must be north/south symmetric.
+ * longitudes are host arrays and the rings must be north/south symmetric;
+ * they are read on the host and reach the device as a kernel parameter, so
+ * the call makes no host-to-device copy and does not block the host.
  * Every intermediate lives in one file-scope device array of
  * CUNUSHT_NOALLOC_SCRATCH_BYTES that each GPU loading the library holds until
  * the process exits; sizes beyond the CUNUSHT_NOALLOC_MAX_* limits are
  * rejected with CUNUSHT_ERR_ARG.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture.  All calls share the one array,
- * so calls that overlap on the GPU (different streams or host threads) race.
- * Same math as cunusht_synthesis; nothing is allocated and nothing freed.
+ * that first call before any stream capture.  The address is kept per device
+ * for the life of the process: a cudaDeviceReset between calls is not
+ * supported.  All calls share the one array, so calls that overlap on the GPU
+ * (different streams or host threads) race.  Same math as cunusht_synthesis;
+ * nothing is allocated and nothing freed.
  */
 #define CUNUSHT_NOALLOC_SCRATCH_BYTES (4u * 1024u * 1024u)
 #define CUNUSHT_NOALLOC_MAX_LMAX 255

@@ -329,3 +329,13 @@ def test_lensing_adjointness_spin2_with_rotation(cu, precision):
     # mixed: the forward carries ~1e-7 arithmetic error (eps 1e-7) while the
     # adjoint runs in FP64, so the two agree to a few eps, not to FP64 rounding
     np.testing.assert_allclose(lhs, rhs, rtol=5e-7 if precision == "mixed" else 1e-9)
+
+
+def test_planar_pointing_reaches_the_library_without_a_copy(built_lib):
+    """gclm2lenmap passes ptg.t() as loc (GPU_nufft_transformer.py:569): the
+    planar (2, npix) device buffer reaches the C ABI as layout 1, not as a
+    strided copy."""
+    from cunusht_gb300.transformer import _loc_args, to_device
+    ptg = torch.arange(20, dtype=torch.float64, device="cuda").reshape(2, 10)
+    t, n, lay = _loc_args(to_device(ptg.t(), "loc", torch.float64, contiguous=False))
+    assert (n, lay) == (10, 1) and t.data_ptr() == ptg.data_ptr()
