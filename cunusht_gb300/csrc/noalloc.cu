@@ -24,6 +24,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[CUNUSHT_NOALLOC
 // Device address of g_noalloc_scratch per device.  In host code the symbol
 // name is only a host-side stand-in, never a device address, so it is looked
 // up with cudaGetSymbolAddress once per device, with that device current.
+// The cached address outlives nothing but the process's CUDA context: after a
+// cudaDeviceReset the module is loaded again and the cached address would be
+// stale, so a device reset between calls is not supported.
 static std::mutex g_scratch_mu;
 static void *g_scratch_ptr[256] = {};
 
@@ -56,18 +59,89 @@ struct ScratchLayout {
     }
 };
 
-static double lg0_start(int m, int s) {
-    const int l0 = m > s ? m : s;
-    const double v = std::log((2.0 * l0 + 1.0) / (4.0 * PI)) + std::lgamma(2.0 * l0 + 1.0) -
-                     std::lgamma(m + s + 1.0) - std::lgamma(std::fabs((double)(m - s)) + 1.0);
-    return 0.5 * v / std::log(2.0);
-}
+// Ring tables of one call, passed BY VALUE as a kernel parameter (under the
+// classic 4 KB parameter limit), so that the call copies nothing from host
+// memory: no pageable transfer that could block the host.  Ring pairs
+// (theta, pi - theta) are sorted on the host; everything else is computed on
+// the device into the scratch array.
+struct NoallocRings {
+    double theta_n[(CUNUSHT_NOALLOC_MAX_NRING + 1) / 2];  // north ring of each pair
+    short rn[(CUNUSHT_NOALLOC_MAX_NRING + 1) / 2];        // ring index, north / south member
+    short rs[(CUNUSHT_NOALLOC_MAX_NRING + 1) / 2];
+    double phi0[CUNUSHT_NOALLOC_MAX_NRING];
+    int npairs, nring, nphi, lmax, spin, Mb;
+};
+static_assert(sizeof(NoallocRings) <= 4000, "no-alloc ring tables must fit a 4 KB kernel parameter");
 
-template <typename T>
-static int put(void *base, size_t off, const std::vector<T> &h, cudaStream_t st) {
-    if (h.empty()) return CUNUSHT_OK;
-    CU_TRY(cudaMemcpyAsync((char *)base + off, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
-    return CUNUSHT_OK;
+struct NoallocTables {
+    double *lg, *px, *psh, *pch, *phi0;
+    int *prn, *prs;
+    long long *nph, *ofs;
+    double2 *chirp, *bk, *tw;
+};
+
+// One thread per table entry over the concatenated index ranges:
+// pairs | rings | m = 0..lmax | chirp (nphi) | Bluestein kernel (Mb) | twiddles (Mb)
+__global__ void k_noalloc_tables(const NoallocRings R, NoallocTables T) {
+    const long long n_pairs = R.npairs, n_rings = R.nring, n_m = R.lmax + 1, n_ch = R.nphi, n_bk = R.Mb;
+    const long long total = n_pairs + n_rings + n_m + n_ch + 2 * n_bk;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        long long k = i;
+        if (k < n_pairs) {
+            const double t = R.theta_n[k];
+            T.px[k] = cos(t);
+            T.psh[k] = sin(0.5 * t);
+            T.pch[k] = cos(0.5 * t);
+            T.prn[k] = R.rn[k];
+            T.prs[k] = R.rs[k];
+            continue;
+        }
+        k -= n_pairs;
+        if (k < n_rings) {
+            T.phi0[k] = R.phi0[k];
+            T.nph[k] = R.nphi;
+            T.ofs[k] = k * (long long)R.nphi;
+            continue;
+        }
+        k -= n_rings;
+        if (k < n_m) {  // log2 of the recursion start's normalisation (as the plan's lg0 table)
+            const int m = (int)k, s = R.spin, l0 = m > s ? m : s;
+            const double v = log((2.0 * l0 + 1.0) / (4.0 * PI)) + lgamma(2.0 * l0 + 1.0) - lgamma(m + s + 1.0) -
+                             lgamma(fabs((double)(m - s)) + 1.0);
+            T.lg[m] = 0.5 * v / log(2.0);
+            continue;
+        }
+        k -= n_m;
+        if (k < n_ch) {  // chirp_q = exp(i pi q^2 / nphi), q^2 reduced mod 2 nphi
+            const long long qq = (k * k) % (2LL * R.nphi);
+            double sn, cs;
+            sincospi((double)qq / R.nphi, &sn, &cs);
+            T.chirp[k] = make_double2(cs, sn);
+            continue;
+        }
+        k -= n_ch;
+        if (k < n_bk) {  // conj(chirp) / Mb at k and Mb - k (k < nphi), zero between
+            long long q = -1;
+            if (k < R.nphi) q = k;
+            else if (k > R.Mb - R.nphi) q = R.Mb - k;
+            double2 b = make_double2(0.0, 0.0);
+            if (q >= 0) {
+                const long long qq = (q * q) % (2LL * R.nphi);
+                double sn, cs;
+                sincospi((double)qq / R.nphi, &sn, &cs);
+                b = make_double2(cs / R.Mb, -sn / R.Mb);
+            }
+            T.bk[k] = b;
+            continue;
+        }
+        k -= n_bk;
+        {  // twiddles exp(-2 pi i t / Mb)
+            double sn, cs;
+            sincospi(-2.0 * (double)k / R.Mb, &sn, &cs);
+            T.tw[k] = make_double2(cs, sn);
+        }
+    }
 }
 
 }  // namespace cunusht
@@ -92,7 +166,7 @@ extern "C" int cunusht_synthesis_noalloc(int lmax, int spin, int ncomp, const vo
     ARG_CHECK(alm && map && ring_theta && ring_phi0, "NULL array argument");
     cudaStream_t st = (cudaStream_t)stream;
 
-    // host tables: ring pairs (theta, pi - theta), start normalisations, Bluestein chirp
+    // ring pairs (theta, pi - theta) sorted on the host; the device builds the rest
     cunusht_plan_s P;  // host-side view; all device pointers point into the scratch array
     P.lmax = lmax;
     P.nalm = (long long)(lmax + 1) * (lmax + 2) / 2;
@@ -107,53 +181,40 @@ extern "C" int cunusht_synthesis_noalloc(int lmax, int spin, int ncomp, const vo
         idx[i] = i;
     }
     std::sort(idx.begin(), idx.end(), [&](int a, int b) { return ring_theta[a] < ring_theta[b]; });
-    std::vector<double> px, psh, pch;
-    std::vector<int> prn, prs;
+    NoallocRings R;
+    int np = 0;
     for (int i = 0, j = nring - 1; i <= j; ++i, --j) {
         const double tn = ring_theta[idx[i]], ts = ring_theta[idx[j]];
         ARG_CHECK(std::fabs(tn + ts - PI) <= 1e-9, "no-alloc synthesis: rings must be north/south symmetric");
-        px.push_back(std::cos(tn));
-        psh.push_back(std::sin(0.5 * tn));
-        pch.push_back(std::cos(0.5 * tn));
-        prn.push_back(idx[i]);
-        prs.push_back(idx[j]);
+        R.theta_n[np] = tn;
+        R.rn[np] = (short)idx[i];
+        R.rs[np] = (short)idx[j];
+        ++np;
     }
-    P.gl_npairs = (int)px.size();
-    std::vector<double> lg(lmax + 1), phi0(ring_phi0, ring_phi0 + nring);
-    for (int m = 0; m <= lmax; ++m) lg[m] = lg0_start(m, spin);
-    std::vector<long long> nph(nring, nphi), ofs(nring);
-    for (int i = 0; i < nring; ++i) ofs[i] = (long long)i * nphi;
+    for (int i = 0; i < nring; ++i) R.phi0[i] = ring_phi0[i];
+    P.gl_npairs = np;
     int Mb = 1;
     while (Mb < 2 * nphi - 1) Mb <<= 1;
     P.Mb = Mb;
     P.TW = Mb;
-    std::vector<double2> chirp(nphi), bk(Mb, make_double2(0.0, 0.0)), tw(Mb);
-    for (int q = 0; q < nphi; ++q) {
-        const long long qq = ((long long)q * q) % (2LL * nphi);
-        const double a = PI * (double)qq / nphi;
-        chirp[q] = make_double2(std::cos(a), std::sin(a));
-    }
-    for (int k = 0; k < nphi; ++k) {
-        const double2 b = make_double2(chirp[k].x / Mb, -chirp[k].y / Mb);
-        bk[k] = b;
-        if (k > 0) bk[Mb - k] = b;
-    }
-    for (int t = 0; t < Mb; ++t) {
-        const long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)t / (long double)Mb;
-        tw[t] = make_double2((double)std::cos(a), (double)std::sin(a));
-    }
+    R.npairs = np;
+    R.nring = nring;
+    R.nphi = nphi;
+    R.lmax = lmax;
+    R.spin = spin;
+    R.Mb = Mb;
 
     // scratch layout (the limits above keep it below CUNUSHT_NOALLOC_SCRATCH_BYTES)
     ScratchLayout Lo;
     const size_t o_coef = Lo.take<double>(3 * (size_t)P.nalm);
-    const size_t o_lg = Lo.take<double>(lg.size());
-    const size_t o_px = Lo.take<double>(px.size()), o_psh = Lo.take<double>(psh.size());
-    const size_t o_pch = Lo.take<double>(pch.size());
-    const size_t o_prn = Lo.take<int>(prn.size()), o_prs = Lo.take<int>(prs.size());
-    const size_t o_phi0 = Lo.take<double>(phi0.size());
-    const size_t o_nph = Lo.take<long long>(nph.size()), o_ofs = Lo.take<long long>(ofs.size());
-    const size_t o_chirp = Lo.take<double2>(chirp.size()), o_bk = Lo.take<double2>(bk.size());
-    const size_t o_tw = Lo.take<double2>(tw.size());
+    const size_t o_lg = Lo.take<double>(lmax + 1);
+    const size_t o_px = Lo.take<double>(np), o_psh = Lo.take<double>(np);
+    const size_t o_pch = Lo.take<double>(np);
+    const size_t o_prn = Lo.take<int>(np), o_prs = Lo.take<int>(np);
+    const size_t o_phi0 = Lo.take<double>(nring);
+    const size_t o_nph = Lo.take<long long>(nring), o_ofs = Lo.take<long long>(nring);
+    const size_t o_chirp = Lo.take<double2>(nphi), o_bk = Lo.take<double2>(Mb);
+    const size_t o_tw = Lo.take<double2>(Mb);
     const size_t o_H = Lo.take<double2>((size_t)(2 * lmax + 1) * nring);
     if (Lo.off > CUNUSHT_NOALLOC_SCRATCH_BYTES) {
         set_error("no-alloc synthesis needs %zu bytes of scratch, above the %u-byte array", Lo.off,
@@ -163,18 +224,6 @@ extern "C" int cunusht_synthesis_noalloc(int lmax, int spin, int ncomp, const vo
     void *base = nullptr;
     RC_TRY(scratch_address(&base));
     char *b = (char *)base;
-    RC_TRY(put(base, o_lg, lg, st));
-    RC_TRY(put(base, o_px, px, st));
-    RC_TRY(put(base, o_psh, psh, st));
-    RC_TRY(put(base, o_pch, pch, st));
-    RC_TRY(put(base, o_prn, prn, st));
-    RC_TRY(put(base, o_prs, prs, st));
-    RC_TRY(put(base, o_phi0, phi0, st));
-    RC_TRY(put(base, o_nph, nph, st));
-    RC_TRY(put(base, o_ofs, ofs, st));
-    RC_TRY(put(base, o_chirp, chirp, st));
-    RC_TRY(put(base, o_bk, bk, st));
-    RC_TRY(put(base, o_tw, tw, st));
     P.d_coef[spin] = (double *)(b + o_coef);
     P.d_lg0[spin] = (double *)(b + o_lg);
     P.d_gl_x = (double *)(b + o_px);
@@ -189,6 +238,10 @@ extern "C" int cunusht_synthesis_noalloc(int lmax, int spin, int ncomp, const vo
     P.d_bker = (double2 *)(b + o_bk);
     P.d_tw64 = (double2 *)(b + o_tw);
     double2 *H = (double2 *)(b + o_H);
+    NoallocTables Tb{P.d_lg0[spin], P.d_gl_x, P.d_gl_sh, P.d_gl_ch, P.d_ring_phi0, P.d_gl_rn, P.d_gl_rs,
+                     P.d_ring_nph, P.d_ring_ofs, P.d_chirp, P.d_bker, P.d_tw64};
+    k_noalloc_tables<<<64, 256, 0, st>>>(R, Tb);
+    CU_LAUNCH_CHECK();
 
     // every scratch piece read below is fully rewritten by this call
     RC_TRY(build_coef_tables_spin(&P, spin, P.d_coef[spin], st));

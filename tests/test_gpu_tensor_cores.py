@@ -42,6 +42,22 @@ def test_tc_selftest_exact(built_lib, n, reps, mode):
     assert err.value == 0.0
 
 
+def test_tc_wait_timeout_path_returns_and_leaves_the_context_usable(built_lib):
+    """A bounded mbarrier wait that nothing arrives on (self test mode 3: no
+    MMA issued, limit 64 polls) runs out: the kernel reports the timeout,
+    releases its tensor memory and returns; an ordinary self test right after
+    it in the same process is exact."""
+    from cunusht_gb300 import _lib
+    lib = _lib.load()
+    err, to = ctypes.c_double(-1.0), ctypes.c_int(-1)
+    _lib.check(lib.cunusht_tc_selftest(64, 1, 3, ctypes.byref(err), ctypes.byref(to)))
+    assert to.value == 1
+    for _ in range(2):
+        err, to = ctypes.c_double(-1.0), ctypes.c_int(-1)
+        _lib.check(lib.cunusht_tc_selftest(64, 16, 0, ctypes.byref(err), ctypes.byref(to)))
+        assert to.value == 0 and err.value == 0.0
+
+
 def _transformers(cu, lmax, mmax=None):
     geo = ("gl", {"lmax": lmax})
     mk = lambda prec: cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=1e-7, precision=prec, max_spin=2)

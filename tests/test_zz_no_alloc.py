@@ -61,6 +61,24 @@ def test_noalloc_synthesis_matches_plan_synthesis_two_calls_in_a_row(built_lib):
         assert _rel(got.reshape(want.shape), want) < 1e-11
 
 
+@pytest.mark.parametrize("lmax,nphi", [(255, 1024), (62, 125)])
+def test_noalloc_at_the_limits_and_with_an_odd_ring_count(built_lib, lmax, nphi):
+    """The largest documented case (lmax 255, 256 rings, 1024 pixels per
+    ring: the scratch layout at its bound) and an odd ring count (the
+    equator ring pairs with itself), spin 2 then spin 0, against the
+    plan-based synthesis."""
+    import cunusht_gb300 as cu
+    T = cu.get_transformer("GPU")(("gl", {"lmax": lmax, "nphi": nphi}), nuFFTtype=2, epsilon=1e-10,
+                                  precision="fp64")
+    assert T.geom.theta.size == lmax + 1
+    for spin, ncomp, seed in [(2, 2, 5), (0, 1, 6)]:
+        a = _alm(lmax, ncomp, spin, seed)
+        want = T.synthesis(torch.as_tensor(a[0] if spin == 0 else a, device="cuda"), spin=spin).cpu().numpy()
+        got = _noalloc(built_lib, lmax, spin, a, T.geom)
+        assert np.all(np.isfinite(got))
+        assert _rel(got.reshape(want.shape), want) < 1e-11
+
+
 def test_noalloc_rejects_sizes_beyond_the_scratch_limit(built_lib):
     a = torch.zeros((1, 300 * 301 // 2), dtype=torch.complex128, device="cuda")
     out = torch.zeros(4, dtype=torch.float64, device="cuda")
