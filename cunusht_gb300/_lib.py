@@ -35,6 +35,7 @@ SIGNATURES = {
     "cunusht_plan_force_split": (_i, [_vp, _i]),
     "cunusht_plan_set_mmax": (_i, [_vp, _i]),
     "cunusht_plan_set_tensor_cores": (_i, [_vp, _i]),
+    "cunusht_plan_set_spreading": (_i, [_vp, _i, _i, _i64]),
     "cunusht_plan_device_status": (_i, [_vp, ctypes.POINTER(_i)]),
     "cunusht_tc_selftest": (_i, [_i, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_i)]),
     "cunusht_dlm2A": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),

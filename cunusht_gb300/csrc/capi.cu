@@ -121,9 +121,13 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_ring_cls, P->d_cls_N, P->d_cls_Mb, P->d_cls_SP,
                     P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
-                    P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[1], P->d_tc_woff[2], P->d_tc_rec};
+                    P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[0], P->d_tc_woff[1], P->d_tc_woff[2],
+                    P->d_tc_rec};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (P->d_bin) cudaFree(P->d_bin);
+    if (P->d_ufix) cudaFree(P->d_ufix);
+    if (P->d_vmax) cudaFree(P->d_vmax);
     for (int g = 0; g < 2; ++g)
         for (int s = 0; s < 3; ++s) {
             if (P->d_tc_stv[g][s]) cudaFree(P->d_tc_stv[g][s]);
@@ -451,6 +455,7 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
         P->d_F = f;
         RC_TRY(dalloc(P, &u, usz * (size_t)P->nrows * P->Npf));
         P->d_U = u;
+        P->u_bytes = usz * (size_t)P->nrows * P->Npf;
         if (P->sp_theta == 2 && (size_t)ncols * P->Nt * gsz > usz * (size_t)P->nrows * P->Npf) {
             set_error("internal: split theta adjoint scratch does not fit the fine-grid workspace");
             return CUNUSHT_ERR_UNSUPPORTED;
@@ -600,7 +605,7 @@ int cunusht_tc_selftest(int n, int reps, int mode, double *maxerr, int *timeout)
     ARG_CHECK(maxerr != nullptr && timeout != nullptr, "maxerr and timeout must not be NULL");
     ARG_CHECK(n == 16 || n == 32 || n == 64, "n must be 16, 32 or 64, got %d", n);
     ARG_CHECK(reps >= 1 && reps <= 16, "reps must be in [1, 16], got %d", reps);
-    ARG_CHECK(mode >= 0 && mode <= 3, "mode must be 0, 1, 2 or 3, got %d", mode);
+    ARG_CHECK(mode >= 0 && mode <= 6, "mode must be in [0, 6], got %d", mode);
     return tc_selftest(n, reps, mode, maxerr, timeout);
 }
 
@@ -636,6 +641,43 @@ int cunusht_plan_stage_times(cunusht_plan_t *P, double *ms, int64_t *count, int 
 static size_t f_elem(const cunusht_plan_s *P) { return P->grid_fp32 ? sizeof(float2) : 16; }
 static size_t adj_scalar(const cunusht_plan_s *P) { return P->grid_fp32 ? sizeof(float) : sizeof(double); }
 
+// workspace of the spreading options for max(batch capacity, 1) requests
+static int spread_alloc(cunusht_plan_s *P) {
+    if (P->d_bin || P->d_ufix) CU_TRY(cudaDeviceSynchronize());  // queued work may still use them
+    if (P->d_bin) {
+        cudaFree(P->d_bin);
+        P->d_bin = nullptr;
+    }
+    if (P->d_ufix) {
+        cudaFree(P->d_ufix);
+        P->ws_bytes -= P->ufix_bytes;
+        P->d_ufix = nullptr;
+        P->ufix_bytes = 0;
+    }
+    const int nreq = P->batch_cap > 1 ? P->batch_cap : 1;
+    if (P->spread_method == 1) RC_TRY(dalloc(P, &P->d_bin, (size_t)nreq * bin_workspace_ints(P, P->bin_npts)));
+    if (P->spread_det) {
+        const size_t n = (size_t)nreq * (P->max_spin ? 2 : 1) * P->nrows * P->Npf;
+        RC_TRY(dalloc(P, &P->d_ufix, n));
+        P->ufix_bytes = n * sizeof(unsigned long long);
+        if (!P->d_vmax) RC_TRY(dalloc(P, &P->d_vmax, 64));
+    }
+    P->spread_nreq = nreq;
+    return CUNUSHT_OK;
+}
+
+int cunusht_plan_set_spreading(cunusht_plan_t *P, int method, int deterministic, int64_t max_points) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(method == 0 || method == 1, "method must be 0 (warp strips) or 1 (bin-sorted), got %d", method);
+    ARG_CHECK(deterministic == 0 || deterministic == 1, "deterministic must be 0 or 1");
+    ARG_CHECK(max_points >= 0 && max_points < (1LL << 31), "max_points must be in [0, 2^31)");
+    P->spread_method = method;
+    P->spread_det = deterministic;
+    P->bin_npts = max_points > 0 ? max_points : P->npix;
+    return spread_alloc(P);
+}
+
 int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     clear_error();
     RC_TRY(check_plan(P));
@@ -647,6 +689,7 @@ int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
         if (q) cudaFree(q);
     P->d_Hb = nullptr;
     P->d_Fb = P->d_Ub = nullptr;
+    P->ub_bytes = 0;
     P->d_Hglb = nullptr;
     P->d_glmapb = P->d_ptgb = P->d_gamb = nullptr;
     P->batch_cap = 0;
@@ -661,12 +704,14 @@ int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     RC_TRY(dalloc(P, &u, B * adj_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf));
     P->d_Fb = f;
     P->d_Ub = u;
+    P->ub_bytes = B * adj_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf;
     RC_TRY(dalloc(P, &P->d_Hglb, B * (2 * (size_t)L + 1) * P->nring));
     RC_TRY(dalloc(P, &P->d_glmapb, B * 2 * (size_t)P->npix));
     RC_TRY(dalloc(P, &P->d_ptgb, B * 2 * (size_t)P->npix));
     RC_TRY(dalloc(P, &P->d_gamb, B * (size_t)P->npix));
     if (P->prec == CUNUSHT_PREC_MIXED) RC_TRY(tc_reserve(P, max_batch));
     P->batch_cap = max_batch;
+    if (P->spread_method == 1 || P->spread_det) RC_TRY(spread_alloc(P));
     return CUNUSHT_OK;
 }
 
@@ -779,8 +824,10 @@ int cunusht_delensing_batch(cunusht_plan_t *P, int nreq, int spin, int ncomp, co
     {
         StageScope sc(P, CUNUSHT_STAGE_LEG_ADJ, st);
         double2 *G = (double2 *)alm_out;
+        // the fine grids are free once the theta pass is done: the tensor-core
+        // adjoint keeps its fixed-point sums there
         RC_TRY(leg_adjoint_batch(P, nreq, spin, ncomp, P->d_Hb, ncols * P->ncc, false, true, G, G + nalm,
-                                 ncomp * nalm, st));
+                                 ncomp * nalm, st, P->d_Ub, P->ub_bytes));
     }
     return CUNUSHT_OK;
 }
@@ -829,7 +876,7 @@ int cunusht_nusht2d1(cunusht_plan_t *P, int spin, int ncomp, const void *map, in
     { StageScope sc(P, CUNUSHT_STAGE_THETA_ADJ, st); RC_TRY(theta_adj(P, spin, P->d_F, P->d_H, st)); }
     double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
     double2 *C = G + P->nalm;
-    { StageScope sc(P, CUNUSHT_STAGE_LEG_ADJ, st); RC_TRY(leg_adjoint(P, spin, ncomp, P->d_H, false, true, G, C, st)); }
+    { StageScope sc(P, CUNUSHT_STAGE_LEG_ADJ, st); RC_TRY(leg_adjoint(P, spin, ncomp, P->d_H, false, true, G, C, st, P->d_U, P->u_bytes)); }
     if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
     return CUNUSHT_OK;
 }
@@ -956,7 +1003,7 @@ int cunusht_lensing_vjp_dlm(cunusht_plan_t *P, int spin, const void *gclm, int a
     // per-pixel pull-back, then the adjoint spin-1 synthesis (scaled by sqrt(l(l+1)))
     RC_TRY(lens_vjp_launch(P, ptg, grad_map, gd, st));
     RC_TRY(ring_adjoint(P, 1, gd, gd + P->npix, P->d_Hgl, st));
-    RC_TRY(leg_adjoint(P, 1, 1, P->d_Hgl, true, false, (double2 *)grad_dlm, nullptr, st));
+    RC_TRY(leg_adjoint(P, 1, 1, P->d_Hgl, true, false, (double2 *)grad_dlm, nullptr, st, P->d_U, P->u_bytes));
     return CUNUSHT_OK;
 }
 
@@ -993,7 +1040,7 @@ int cunusht_adjoint_synthesis(cunusht_plan_t *P, int spin, int ncomp, const doub
     cudaStream_t st = (cudaStream_t)stream;
     RC_TRY(ring_adjoint(P, spin, map, spin ? map + P->npix : nullptr, P->d_Hgl, st));
     double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
-    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st));
+    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st, P->d_U, P->u_bytes));
     if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
     return CUNUSHT_OK;
 }
@@ -1010,7 +1057,7 @@ int cunusht_analysis(cunusht_plan_t *P, int spin, int ncomp, const double *map, 
     cudaStream_t st = (cudaStream_t)stream;
     RC_TRY(ring_adjoint(P, spin, map, spin ? map + P->npix : nullptr, P->d_Hgl, st, ring_weight));
     double2 *G = alm_dtype == CUNUSHT_F64 ? (double2 *)alm_out : P->d_alm;
-    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st));
+    RC_TRY(leg_adjoint(P, spin, ncomp, P->d_Hgl, false, false, G, G + P->nalm, st, P->d_U, P->u_bytes));
     if (alm_dtype != CUNUSHT_F64) RC_TRY(store_alm(P->d_alm, ncomp * P->nalm, alm_dtype, alm_out, st));
     return CUNUSHT_OK;
 }

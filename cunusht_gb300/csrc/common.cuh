@@ -177,7 +177,7 @@ struct cunusht_plan_s {
     double *d_lg0[3] = {nullptr, nullptr, nullptr};  // per m: log2 start normalisation
     double *d_lfac = nullptr;                        // sqrt(l(l+1)), l = 0..L
     float2 *d_coef_df[3] = {nullptr, nullptr, nullptr};  // the same tables as (hi, lo) FP32 pairs
-    bool use_tc = true;       // mixed precision: spin > 0 Legendre synthesis on the tensor cores
+    bool use_tc = true;       // mixed precision: Legendre synthesis (every spin) on the tensor cores
     int *d_status = nullptr;  // device status word: bit 0 = a bounded wait of a tensor-core kernel ran out
     // tensor-core synthesis: per spin 1, 2 the first window record of each m (m = 0..lmax+1),
     // and the record buffer (alm digit planes and scales per (m, l-window), written per call)
@@ -216,6 +216,7 @@ struct cunusht_plan_s {
     double2 *d_H = nullptr;    // Legendre columns on the CC rings  [ncols][ncc]
     void *d_F = nullptr;       // theta-pass output                 [nrows][ncols]
     void *d_U = nullptr;       // fine grid                          [nrows][Npf](x2)
+    size_t u_bytes = 0;        // its size (free scratch of the adjoint Legendre stage)
     double2 *d_Hgl = nullptr;  // Legendre columns on pointing rings [ncols][nring]
     double2 *d_ring = nullptr; // Bluestein buffers (unused: in smem)
     double *d_glmap = nullptr; // spin-1 maps on pointing grid       [2][npix]
@@ -227,10 +228,20 @@ struct cunusht_plan_s {
     double2 *d_Hb = nullptr;    // [cap][ncols][ncc]
     void *d_Fb = nullptr;       // [cap][nrows][ncols]
     void *d_Ub = nullptr;       // [cap][nrows][Npf] (x2 for spin)
+    size_t ub_bytes = 0;        // its size
     double2 *d_Hglb = nullptr;  // [cap][2L+1][nring]
     double *d_glmapb = nullptr; // [cap][2][npix]
     double *d_ptgb = nullptr;   // [cap][2][npix]
     double *d_gamb = nullptr;   // [cap][npix]
+    // spreading options (cunusht_plan_set_spreading): 0 warp strips, 1 bin-sorted
+    int spread_method = 0;
+    int spread_det = 0;          // int64 fixed-point accumulation
+    int spread_nreq = 0;         // requests the option workspace holds
+    long long bin_npts = 0;      // points per request the bin workspace holds
+    int *d_bin = nullptr;        // [nreq][npts] bins | [nreq][npts] order | [nreq][nbins + 1] x 2 counts
+    unsigned long long *d_ufix = nullptr;  // [nreq][grid scalars] fixed-point grid
+    size_t ufix_bytes = 0;
+    float *d_vmax = nullptr;     // [64] largest |value| per request
     size_t ws_bytes = 0;
 
     // per-stage CUDA-event timing (cunusht_plan_set_profiling)

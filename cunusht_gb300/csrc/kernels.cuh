@@ -21,12 +21,28 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
                        long long astride, const double *fl, bool cc, double2 *H, long long hstride, cudaStream_t st);
 int synth_points(const cunusht_plan_s *P, int spin, const double2 *G, const double2 *C, long long npts,
                  const double *loc, int layout, const double *gamma, double *out, cudaStream_t st);
+// scratch (may be NULL): free device workspace of scratch_bytes; the tensor-core
+// adjoint keeps its fixed-point sums there (adj_tc_scratch_bytes), else the
+// CUDA-core kernels run
 int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
-                bool cc, double2 *G, double2 *C, cudaStream_t st);
+                bool cc, double2 *G, double2 *C, cudaStream_t st, void *scratch = nullptr, size_t scratch_bytes = 0);
 int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
-                      bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st);
+                      bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st,
+                      void *scratch = nullptr, size_t scratch_bytes = 0);
+int leg_adj_pole_pair_spin(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                           int ld, const double *lf, int rn, int rs, double2 *G, double2 *C, long long astride,
+                           cudaStream_t st);
+int leg_adj_df_pairs(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                     int ld, int npairs, const double *x, const double *sh, const double *ch, const int *rn,
+                     const int *rs, const double *lf, double2 *G, double2 *C, long long astride, cudaStream_t st);
+// legendre_tc_adj.cu: tensor-core adjoint (mixed precision, every spin)
+size_t adj_tc_scratch_bytes(const cunusht_plan_s *P, int nreq);
+int leg_adjoint_tc(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                   int ld, int npairs, const double *x, const double *sh, const double *ch, const int *rn,
+                   const int *rs, int pole, int pole_rn, int pole_rs, const float2 *stv, const short *ste,
+                   const double *lf, double2 *G, double2 *C, long long astride, void *scratch, cudaStream_t st);
 
-// legendre_tc.cu: tensor-core synthesis (spin > 0, mixed precision), nb in {1, 2, 4, 8};
+// legendre_tc.cu: tensor-core synthesis (mixed precision, every spin), nb in {1, 2, 4, 8};
 // stv / ste: the plan's recursion-start table of the grid and spin (row stride npairs), or NULL
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
                       const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
@@ -75,6 +91,14 @@ int magnification_det(long long npix, const double *k, const double *g1, const d
                       const double *d2, const double *w, double *A, cudaStream_t st);
 int pointing_batch(const cunusht_plan_s *P, int nreq, const double *d, long long dbs, double *ptg, long long pbs,
                    double *gamma, cudaStream_t st);
+// spread_bins.cu: the plan's spreading options (bin-sorted path, deterministic
+// fixed-point accumulation) around the warp-strip kernels of nufft_spread_batch
+size_t bin_workspace_ints(const cunusht_plan_s *P, long long npts);
+int spread_options_begin(const cunusht_plan_s *P, int nreq, int spin, void *U, long long ubs, const double *loc,
+                         long long lbs, long long npts, int layout, const double *gamma, const void *in,
+                         long long ibs, int in_dtype, int *done, cudaStream_t st);
+int spread_options_end(const cunusht_plan_s *P, int nreq, int spin, void *U, long long ubs, long long npts,
+                       cudaStream_t st);
 int nufft_spread_batch(const cunusht_plan_s *P, int nreq, int spin, void *U, long long ubs, const double *loc,
                        long long lbs, long long npts, int layout, const double *gamma, const void *in, long long ibs,
                        int in_dtype, cudaStream_t st);

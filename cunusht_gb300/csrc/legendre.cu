@@ -1139,7 +1139,7 @@ int leg_synth_batch_fl(const cunusht_plan_s *P, int nreq, int spin, const double
             const int left = nreq - r0;
             const double2 *Gr = G + r0 * astride, *Cr = C ? C + r0 * astride : nullptr;
             double2 *Hr = H + r0 * hstride;
-            if (spin > 0 && P->use_tc) {
+            if (P->use_tc) {
                 // as many requests per launch as the window records were reserved for
                 const int cap = left < P->tc_rec_nb ? left : P->tc_rec_nb;
                 const int nb = cap >= 8 ? 8 : cap >= 4 ? 4 : cap >= 2 ? 2 : 1;
@@ -1229,13 +1229,55 @@ static void launch_adj_df(const cunusht_plan_s *P, const RingPairs &R, dim3 grid
                                                         R.rs, (double *)G, (double *)C, astride);
 }
 
+// the pole pair (theta = 0, pi) of a spin s >= 1 adjoint, added to the alm
+int leg_adj_pole_pair_spin(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                           int ld, const double *lf, int rn, int rs, double2 *G, double2 *C, long long astride,
+                           cudaStream_t st) {
+    const int L = P->lmax;
+    k_pole_pair_adj_spin<<<dim3((L - spin + 256) / 256, nreq), 256, 0, st>>>(
+        L, spin, ncomp, P->mmax, H, hstride, ld, lf, rn, rs, (double *)G, (spin > 0 && ncomp > 1) ? (double *)C : nullptr,
+        astride);
+    CU_LAUNCH_CHECK();
+    return CUNUSHT_OK;
+}
+
+// npairs ring pairs of a grid through the double-float CUDA-core adjoint,
+// added to the alm (up to four requests share a recursion)
+int leg_adj_df_pairs(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
+                     int ld, int npairs, const double *x, const double *sh, const double *ch, const int *rn,
+                     const int *rs, const double *lf, double2 *G, double2 *C, long long astride, cudaStream_t st) {
+    const RingPairs R{npairs, x, sh, ch, rn, rs, ld};
+    const dim3 grid((npairs + LEG_TPB - 1) / LEG_TPB, P->mmax + 1);
+    for (int r0 = 0; r0 < nreq;) {
+        const int left = nreq - r0;
+        const double2 *Hr = H + r0 * hstride;
+        double2 *Gr = G + r0 * astride, *Cr = (spin > 0 && ncomp > 1) ? C + r0 * astride : nullptr;
+        const int nb = left >= 4 ? 4 : left >= 2 ? 2 : 1;
+        if (nb == 4) launch_adj_df<4>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+        else if (nb == 2) launch_adj_df<2>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+        else launch_adj_df<1>(P, R, grid, spin, ncomp, Hr, hstride, lf, Gr, Cr, astride, st);
+        CU_LAUNCH_CHECK();
+        r0 += nb;
+    }
+    return CUNUSHT_OK;
+}
+
 // nreq requests: columns at H + r * hstride, alm written at G + r * astride
-// (and C + r * astride); the mixed-precision kernels share one recursion
-// between up to four requests, the FP64 kernels run one request per launch.
+// (and C + r * astride).  Mixed precision: on the tensor cores when the plan
+// uses them and scratch (the caller's free workspace, scratch_bytes) holds the
+// fixed-point sums, else double-float CUDA-core kernels sharing one recursion
+// between up to four requests; the FP64 kernels run one request per launch.
 int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
-                      bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st) {
+                      bool use_lfac, bool cc, double2 *G, double2 *C, long long astride, cudaStream_t st,
+                      void *scratch, size_t scratch_bytes) {
     const RingPairs R = pairs_of(P, cc);
     const int L = P->lmax;
+    if (P->prec == CUNUSHT_PREC_MIXED && P->use_tc && P->d_coef_df[spin] && scratch &&
+        scratch_bytes >= adj_tc_scratch_bytes(P, nreq)) {
+        return leg_adjoint_tc(P, nreq, spin, ncomp, H, hstride, R.ld, R.npairs, R.x, R.sh, R.ch, R.rn, R.rs, R.pole,
+                              R.pole_rn, R.pole_rs, R.stv ? R.stv[spin] : nullptr, R.ste ? R.ste[spin] : nullptr,
+                              use_lfac ? P->d_lfac : nullptr, G, C, astride, scratch, st);
+    }
     for (int r = 0; r < nreq; ++r) {
         CU_TRY(cudaMemsetAsync(G + r * astride, 0, sizeof(double2) * P->nalm, st));
         if (spin > 0 && ncomp > 1) CU_TRY(cudaMemsetAsync(C + r * astride, 0, sizeof(double2) * P->nalm, st));
@@ -1289,8 +1331,8 @@ int leg_adjoint_batch(const cunusht_plan_s *P, int nreq, int spin, int ncomp, co
 }
 
 int leg_adjoint(const cunusht_plan_s *P, int spin, int ncomp, const double2 *H, bool use_lfac,
-                bool cc, double2 *G, double2 *C, cudaStream_t st) {
-    return leg_adjoint_batch(P, 1, spin, ncomp, H, 0, use_lfac, cc, G, C, 0, st);
+                bool cc, double2 *G, double2 *C, cudaStream_t st, void *scratch, size_t scratch_bytes) {
+    return leg_adjoint_batch(P, 1, spin, ncomp, H, 0, use_lfac, cc, G, C, 0, st, scratch, scratch_bytes);
 }
 
 }  // namespace cunusht

@@ -29,9 +29,9 @@
 // which round every product to FP32.
 //
 // Block: one order m and 256 ring pairs as four 128-row MMA tiles (544
-// threads) for launches of up to 4 requests, 128 ring pairs as two tiles (288
-// threads) for 8 requests, whose 160 tensor-memory columns per tile fit 512
-// only twice.  Each ring thread holds one ring (the first half of them the
+// threads) for launches of up to 4 requests, 192 ring pairs as three tiles
+// (416 threads) for 8 requests, whose 160 tensor-memory columns per tile fit
+// 512 three times.  Each ring thread holds one ring (the first half of them the
 // rings theta, the second half pi - theta); per chunk of 16 l it writes its
 // four digit rows (two 16-byte K-cores per digit) into the A tile, and the
 // ring threads together write the B' digits.  The last warp issues tiles x 4
@@ -44,163 +44,13 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.cuh"
+#include "tcgen05.cuh"
 
 #include <algorithm>
 #include <type_traits>
 #include <vector>
 
 namespace cunusht {
-
-// ---------------------------------------------------------------- tcgen05 / mbarrier helpers
-constexpr int MBAR_SPIN_LIMIT = 1 << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Shared-memory matrix descriptor, no swizzle, K-major: core matrices of
-// 8 rows x 16 bytes (rows 16 bytes apart); lbo = byte distance between core
-// matrices adjacent in K, sbo = between 8-row groups; descriptor version 1.
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-
-// Instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16
-// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
-        : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// generic-proxy shared-memory writes made visible to the tensor cores
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-// Wait for the completion of the barrier phase with the given parity; false
-// when the iteration limit runs out first.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit = MBAR_SPIN_LIMIT) {
-    for (int it = 0; it < limit; ++it) {
-        uint32_t ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-
-// bytes from global to shared memory by the bulk-copy engine, completion counted on bar
-// (both addresses 16-byte aligned, bytes a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
-}
-
-// barrier 1 over the first nthr threads of the block (the others never wait on it)
-__device__ __forceinline__ void bar_sync_1(int nthr) { asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory"); }
-// barrier 1 that also returns whether any participating thread passed v != 0
-__device__ __forceinline__ int bar_or_1(int nthr, int v) {
-    uint32_t r;
-    asm volatile(
-        "{\n\t.reg .pred p, q;\n\t"
-        "setp.ne.u32 q, %1, 0;\n\t"
-        "bar.red.or.pred p, 1, %2, q;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(r)
-        : "r"(v), "r"(nthr)
-        : "memory");
-    return (int)r;
-}
-
-// one warp, converged
-__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-
-// 16 consecutive 32-bit columns of the calling thread's lane (warp-collective)
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-    uint32_t r[8];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr)
-                 : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// ---------------------------------------------------------------- digit split
-// x = (h + l) sc for a power of two sc (|h sc| <= 128) as d0 + d1/256 +
-// d2/256^2 + d3/256^3 + O(2^-25), integer digits |d_i| <= 128.  The integer
-// part of h sc by one FMA with the rounding constant 1.5 x 2^23, its exact
-// remainder by another; l sc (l below half an ulp of h) is added to the
-// remainder, which stays within 0.5 (plus an ulp), so the next digit rounds to
-// at most 128 in magnitude.
-__device__ __forceinline__ void digits4s(float h, float l, float sc, float (&d)[4]) {
-    const float RND = 12582912.f;
-    d[0] = __fsub_rn(__fmaf_rn(h, sc, RND), RND);
-    float r = __fmaf_rn(l, sc, __fmaf_rn(h, sc, -d[0]));
-#pragma unroll
-    for (int k = 1; k < 4; ++k) {
-        d[k] = __fsub_rn(__fmaf_rn(r, 256.f, RND), RND);
-        r = __fmaf_rn(r, 256.f, -d[k]);
-    }
-}
-
-// two integer-valued floats (|v| <= 256) as packed bf16 (exact: their low 16 bits are zero)
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
-}
-
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // -126 <= e <= 127
-// 2^e, or 0 below the normal range (terms scaled that low are below 2^-102 of the sums)
-__device__ __forceinline__ float pow2f_or0(int e) { return e < -126 ? 0.f : pow2f(e); }
 
 // ---------------------------------------------------------------- self test
 // A 128 x n x 32 product of integer matrices (|entries| <= 128) accumulated
@@ -292,12 +142,99 @@ __global__ void __launch_bounds__(128) k_tc_selftest(int nn, int reps, int mode,
     if (bad && tid == 0) out[1] = 1.f;
 }
 
+// Operands stored MN-major (the transpose bits 15 / 16 of the instruction
+// descriptor): no-swizzle core matrices of 8 K-rows x 16 bytes (8 elements
+// along M or N), SBO = byte distance between core matrices adjacent along
+// M / N, LBO = along K.  A (128 x 32) and B (nn x 32) hold the integer
+// entries of k_tc_selftest; amn / bmn choose the layout of each operand
+// (K-major as in k_tc_selftest otherwise).  Both buffers are sized so that a
+// reading of the descriptor with LBO and SBO exchanged still stays inside
+// them (A 48 KB, B 16 KB of dynamic shared memory).
+constexpr int TST_ABYTES = 48 * 1024, TST_BBYTES = 16 * 1024;
+__global__ void __launch_bounds__(128) k_tc_selftest_mn(int nn, int amn, int bmn, float *out) {
+    extern __shared__ __align__(1024) unsigned char dsm[];
+    unsigned char *sA = dsm, *sB = dsm + TST_ABYTES;
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_base), 64);
+    if (tid == 0) {
+        mbar_init(smem_u32(&bar), 1);
+        mbar_init_fence();
+    }
+    for (int i = tid; i < (TST_ABYTES + TST_BBYTES) / 16; i += 128)
+        reinterpret_cast<uint4 *>(dsm)[i] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    // element (r, k) of A and (n, k) of B, one 2-byte store each
+    const int a_lbo = amn ? 16 * 128 : 128, a_sbo = amn ? 128 : 512;
+    const int b_lbo = bmn ? (nn / 8) * 128 : 128, b_sbo = bmn ? 128 : 512;
+    for (int k = 0; k < 32; ++k) {
+        const float av = (float)st_a(tid, k, 0);
+        const int ao = amn ? (k >> 3) * a_lbo + (tid >> 3) * a_sbo + (k & 7) * 16 + (tid & 7) * 2
+                           : (tid >> 3) * a_sbo + (k >> 3) * a_lbo + (tid & 7) * 16 + (k & 7) * 2;
+        *reinterpret_cast<unsigned short *>(sA + ao) = (unsigned short)(__float_as_uint(av) >> 16);
+        if (tid < nn) {
+            const float bv = (float)st_b(tid, k, 0);
+            const int bo = bmn ? (k >> 3) * b_lbo + (tid >> 3) * b_sbo + (k & 7) * 16 + (tid & 7) * 2
+                               : (tid >> 3) * b_sbo + (k >> 3) * b_lbo + (tid & 7) * 16 + (k & 7) * 2;
+            *reinterpret_cast<unsigned short *>(sB + bo) = (unsigned short)(__float_as_uint(bv) >> 16);
+        }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tb = tmem_base;
+    if (tid == 0) {
+        const uint32_t id = idesc_bf16_f32(128, nn) | (amn ? (1u << 15) : 0u) | (bmn ? (1u << 16) : 0u);
+#pragma unroll
+        for (int k = 0; k < 2; ++k)  // K-step k: K-cores 2k, 2k + 1
+            tc_mma(tb, sdesc(smem_u32(sA) + 2 * k * a_lbo, a_lbo, a_sbo),
+                   sdesc(smem_u32(sB) + 2 * k * b_lbo, b_lbo, b_sbo), id, k > 0 ? 1u : 0u);
+        tc_commit(smem_u32(&bar));
+    }
+    const bool ok = mbar_wait(smem_u32(&bar), 0);
+    const int bad = __syncthreads_or(!ok);
+    tc_fence_after();
+    float err = 0.f;
+    if (!bad) {
+        for (int c0 = 0; c0 < nn; c0 += 16) {
+            float v[16];
+            tmem_ld16(tb + ((uint32_t)(warp * 32) << 16) + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                int ref = 0;
+                for (int k = 0; k < 32; ++k) ref += st_a(tid, k, 0) * st_b(c0 + i, k, 0);
+                err = fmaxf(err, fabsf(v[i] - (float)ref));
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tb, 64);
+    }
+    atomicMax(reinterpret_cast<int *>(out), __float_as_int(err));
+    if (bad && tid == 0) out[1] = 1.f;
+}
+
 int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout) {
-    if ((nn != 16 && nn != 32 && nn != 64) || reps < 1 || reps > 16 || mode < 0 || mode > 3) return CUNUSHT_ERR_ARG;
+    if ((nn != 16 && nn != 32 && nn != 64) || reps < 1 || reps > 16 || mode < 0 || mode > 6) return CUNUSHT_ERR_ARG;
     float *d = nullptr;
     CU_TRY(cudaMalloc(&d, 2 * sizeof(float)));
     CU_TRY(cudaMemset(d, 0, 2 * sizeof(float)));
-    k_tc_selftest<<<1, 128>>>(nn, reps, mode, d);
+    if (mode >= 4) {
+        // 4: A and B MN-major; 5: A MN-major, B K-major; 6: A K-major, B MN-major
+        const int amn = mode != 6, bmn = mode != 5;
+        const int bytes = TST_ABYTES + TST_BBYTES;
+        cudaError_t ea = cudaFuncSetAttribute(k_tc_selftest_mn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (ea == cudaSuccess) k_tc_selftest_mn<<<1, 128, bytes>>>(nn, amn, bmn, d);
+        else cudaFree(d), d = nullptr;
+        CU_TRY(ea);
+    } else {
+        k_tc_selftest<<<1, 128>>>(nn, reps, mode, d);
+    }
     cudaError_t e = cudaGetLastError();
     float h[2] = {0.f, 0.f};
     if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
@@ -318,10 +255,11 @@ constexpr int TCL_MIN_TAIL = 32;          // fewer leftover ring pairs than this
 
 // Launches of NB <= 4 requests run blocks of four 128-ring tiles (256 ring
 // pairs); NB = 8 needs 5 x 32 = 160 tensor-memory columns per tile and runs
-// blocks of two tiles (128 ring pairs) so that they fit the 512 columns.
+// blocks of three tiles (192 ring pairs, 480 of the 512 columns; a tile may
+// hold rings of both sides).
 template <int NB>
 struct TclLayout {
-    static constexpr int NT = NB >= 8 ? 2 : 4;           // 128-row MMA tiles per block
+    static constexpr int NT = NB >= 8 ? 3 : 4;           // 128-row MMA tiles per block
     static constexpr int T = 128 * NT;                   // ring threads (one ring each)
     static constexpr int BLOCK = T + 32;                 // + the MMA warp
     static constexpr int ABUF = NT * TCL_TILE;           // A buffer: NT tiles
@@ -364,7 +302,12 @@ __device__ __forceinline__ void tcl_pair(int pr, int &g, int &di) {
 // epilogue scales 2^(El + Ea - 14 - 8g) and the lambda digit scale
 // 2^(7 - El).  All FP64 work of the tensor-core synthesis happens here, in
 // parallel over every window, rather than between the ring warps' chunks.
-template <int NB>
+//
+// Spin 0 (S0): one recursion per ring pair at theta serves both rings, since
+// lambda_lm(pi - theta) = (-1)^(l+m) lambda_lm(theta); the four columns of a
+// request are the alm split by the parity of l + m, (E re, E im, O re, O im),
+// and the rings receive E + O (theta) and E - O (pi - theta).
+template <int NB, bool S0>
 __global__ void __launch_bounds__(TCL_W)
     k_tc_records(int L, int spin, const double2 *__restrict__ G, const double2 *__restrict__ C, long long astride,
                  const double *__restrict__ lfac, const float2 *__restrict__ coef, long long nalm,
@@ -406,6 +349,14 @@ __global__ void __launch_bounds__(TCL_W)
 #pragma unroll
         for (int r = 0; r < NB; ++r) {
             const double2 g = G[r * astride + ix];
+            if (S0) {
+                const bool odd = (l + m) & 1;
+                v[4 * r + 0] = df_from(odd ? 0.0 : f * g.x);
+                v[4 * r + 1] = df_from(odd ? 0.0 : f * g.y);
+                v[4 * r + 2] = df_from(odd ? f * g.x : 0.0);
+                v[4 * r + 3] = df_from(odd ? f * g.y : 0.0);
+                continue;
+            }
             const double2 c = C ? C[r * astride + ix] : make_double2(0.0, 0.0);
             v[4 * r + 0] = df_from(f * (g.x - c.y));
             v[4 * r + 1] = df_from(f * (g.y + c.x));
@@ -459,7 +410,11 @@ __global__ void __launch_bounds__(TCL_W)
 // apart instead of meeting at a block barrier every chunk.  The window
 // records arrive by bulk copy, the next one prefetched while the current
 // window runs; block-wide steps use barrier 1 over the ring warps only.
-template <int NB>
+//
+// S0 (spin 0): every ring thread holds one ring PAIR at theta (no second
+// side), so a block covers T pairs instead of T / 2, and the columns (E, O)
+// give theta E + O and pi - theta E - O.
+template <int NB, bool S0>
 __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
     k_leg_synth_spin_tc(int L, int spin, const unsigned char *__restrict__ rec, const int *__restrict__ woff,
                         const double *__restrict__ lg0, int npairs,
@@ -541,9 +496,9 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
         __syncwarp();
     } else {
         // ---------------- ring warps
-        const int side = tid / (T / 2);  // 0: ring theta, 1: ring pi - theta
+        const int side = S0 ? 0 : tid / (T / 2);  // 0: ring theta, 1: ring pi - theta
         const int tile = tid >> 7, row = tid & 127;
-        const int p = blockIdx.x * (T / 2) + (tid & (T / 2 - 1));
+        const int p = S0 ? blockIdx.x * T + tid : blockIdx.x * (T / 2) + tid % (T / 2);
         const bool act = p < npairs;
         const double x = act ? px[p] : 0.0;
         const dfl xd = df_from(side ? -x : x);
@@ -700,6 +655,16 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
                 // the record copy of the window after the last one entered may still be in flight
                 if (l0 + (kw + 1) * TCL_W <= L) mbar_wait(rbar0 + 8 * ((kw + 1) & 1), ((kw + 1) >> 1) & 1);
             }
+        } else if (act && S0) {
+            const int n = prn[p], s = prs[p];
+#pragma unroll
+            for (int r = 0; r < NB; ++r) {
+                double2 *Hr = H + r * hstride;
+                const double er = acc[4 * r].value(), ei = acc[4 * r + 1].value();
+                const double orr = acc[4 * r + 2].value(), oi = acc[4 * r + 3].value();
+                Hr[(long long)m * ldH + n] = make_double2(er + orr, ei + oi);
+                if (s != n) Hr[(long long)m * ldH + s] = make_double2(er - orr, ei - oi);
+            }
         } else if (act) {
             const int n = prn[p], s = prs[p];
             const double sgs = (spin & 1) ? -1.0 : 1.0;
@@ -726,7 +691,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
     }
 }
 
-template <int NB>
+template <int NB, bool S0>
 static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double *x, const double *sh,
                               const double *ch, const int *rn, const int *rs, const float2 *stv, const short *ste,
                               int st_ld, int ld, int spin, const double2 *G,
@@ -740,12 +705,14 @@ static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double 
         return CUNUSHT_ERR_ARG;
     }
     const dim3 rgrid((L - spin + 1 + TCL_W - 1) / TCL_W, P->mmax + 1);  // m <= spin has the most windows
-    k_tc_records<NB><<<rgrid, TCL_W, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm_tab,
-                                              P->d_tc_woff[spin], P->d_tc_rec);
+    k_tc_records<NB, S0><<<rgrid, TCL_W, 0, st>>>(L, spin, G, C, astride, lf, P->d_coef_df[spin], P->nalm_tab,
+                                                  P->d_tc_woff[spin], P->d_tc_rec);
     CU_LAUNCH_CHECK();
-    CU_TRY(cudaFuncSetAttribute(k_leg_synth_spin_tc<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::BYTES));
-    dim3 grid((npairs + LY::T / 2 - 1) / (LY::T / 2), P->mmax + 1);
-    k_leg_synth_spin_tc<NB><<<grid, LY::BLOCK, LY::BYTES, st>>>(L, spin, P->d_tc_rec, P->d_tc_woff[spin],
+    CU_TRY(cudaFuncSetAttribute(k_leg_synth_spin_tc<NB, S0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                LY::BYTES));
+    constexpr int PER = S0 ? LY::T : LY::T / 2;  // ring pairs per block
+    dim3 grid((npairs + PER - 1) / PER, P->mmax + 1);
+    k_leg_synth_spin_tc<NB, S0><<<grid, LY::BLOCK, LY::BYTES, st>>>(L, spin, P->d_tc_rec, P->d_tc_woff[spin],
                                                                 P->d_lg0[spin], npairs, x, sh, ch, rn, rs, stv, ste,
                                                                 st_ld, H, hstride, ld, P->d_status);
     CU_LAUNCH_CHECK();
@@ -807,12 +774,12 @@ __global__ void k_tc_starts(int L, int spin, const double *__restrict__ lg0, int
 
 int tc_plan_init(cunusht_plan_s *P) {
     const int L = P->lmax;
-    // start tables: GL spin 1 (the pointing's synthesis) and spins up to max_spin on both grids
+    // start tables: GL spin 1 (the pointing's synthesis) and spins 0 up to max_spin on both grids
     for (int g = 0; g < 2; ++g) {
         const int np = g ? P->cc_npairs : P->gl_npairs;
         const double *sh = g ? P->d_cc_sh : P->d_gl_sh, *ch = g ? P->d_cc_ch : P->d_gl_ch;
         const int smax = g ? P->max_spin : std::max(P->max_spin, 1);
-        for (int s = 1; s <= smax && s <= L && np > 0; ++s) {
+        for (int s = 0; s <= smax && s <= L && np > 0; ++s) {
             const size_t n = 2 * (size_t)np * (L + 1);
             CU_TRY(cudaMalloc(&P->d_tc_stv[g][s], n * sizeof(float2)));
             CU_TRY(cudaMalloc(&P->d_tc_ste[g][s], n * sizeof(short)));
@@ -824,7 +791,7 @@ int tc_plan_init(cunusht_plan_s *P) {
     }
     CU_TRY(cudaDeviceSynchronize());  // the tables are read from any stream
     size_t nrec = 0;
-    for (int s = 1; s <= 2 && s <= L; ++s) {
+    for (int s = 0; s <= 2 && s <= L; ++s) {
         std::vector<int> wo(L + 2, 0);
         for (int m = 0; m <= L; ++m) wo[m + 1] = wo[m] + (L - std::max(m, s) + 1 + TCL_W - 1) / TCL_W;
         CU_TRY(cudaMalloc(&P->d_tc_woff[s], wo.size() * sizeof(int)));
@@ -897,7 +864,55 @@ __global__ void __launch_bounds__(POLE_TPB)
     }
 }
 
-// Ring pairs in full blocks (256 pairs, 128 for NB = 8) on the tensor cores; a
+// The pole pair of a spin-0 synthesis: lambda_lm(0) = delta_m0 sqrt((2l+1)/(4 pi))
+// and lambda_lm(pi) = (-1)^l lambda_lm(0), so both rings get zeros for m > 0
+// and one FP64 sum over l for m = 0; block r handles request r.
+__global__ void __launch_bounds__(POLE_TPB)
+    k_pole_pair_s0(int L, int mmax, const double2 *__restrict__ G, long long astride,
+                   const double *__restrict__ lfac, int rn, int rs, double2 *__restrict__ H, long long hstride,
+                   int ldH) {
+    __shared__ double s_red[4][POLE_TPB / 32];
+    const int r = blockIdx.x, tid = threadIdx.x;
+    double2 *Hr = H + r * hstride;
+    for (int m = 1 + tid; m <= mmax; m += POLE_TPB) {
+        Hr[(long long)m * ldH + rn] = make_double2(0.0, 0.0);
+        Hr[(long long)m * ldH + rs] = make_double2(0.0, 0.0);
+    }
+    const double2 *Gr = G + r * astride;  // m = 0: (l, 0) at index l
+    double n_re = 0.0, n_im = 0.0, s_re = 0.0, s_im = 0.0;
+    for (int l = tid; l <= L; l += POLE_TPB) {
+        const double lam = sqrt((2.0 * l + 1.0) / (4.0 * PI)) * (lfac ? lfac[l] : 1.0);
+        const double2 a = Gr[l];
+        const double sg = (l & 1) ? -lam : lam;
+        n_re += a.x * lam;
+        n_im += a.y * lam;
+        s_re += a.x * sg;
+        s_im += a.y * sg;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_re += __shfl_xor_sync(0xffffffffu, n_re, o);
+        n_im += __shfl_xor_sync(0xffffffffu, n_im, o);
+        s_re += __shfl_xor_sync(0xffffffffu, s_re, o);
+        s_im += __shfl_xor_sync(0xffffffffu, s_im, o);
+    }
+    if ((tid & 31) == 0) {
+        s_red[0][tid >> 5] = n_re;
+        s_red[1][tid >> 5] = n_im;
+        s_red[2][tid >> 5] = s_re;
+        s_red[3][tid >> 5] = s_im;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = 0; k < 4; ++k)
+            for (int w = 0; w < POLE_TPB / 32; ++w) t[k] += s_red[k][w];
+        Hr[rn] = make_double2(t[0], t[1]);
+        Hr[rs] = make_double2(t[2], t[3]);
+    }
+}
+
+// Ring pairs in full blocks (256 pairs, 128 for NB = 8; spin 0: 512 and 256) on the tensor cores; a
 // tail of fewer than TCL_MIN_TAIL pairs after at least one full block goes to
 // the double-float CUDA-core kernel instead of a nearly empty block per order m.
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
@@ -908,19 +923,26 @@ int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double 
     if (pole == 0 && npairs > 1) {
         // the pole pair in closed form; the tensor cores take the other pairs
         // (a Clenshaw-Curtis grid of 2^k + 1 rings then fills whole blocks)
-        k_pole_pair_spin<<<nb, POLE_TPB, 0, st>>>(P->lmax, spin, P->mmax, G, C, astride, lf, pole_rn, pole_rs, H,
-                                                  hstride, ld);
+        if (spin == 0)
+            k_pole_pair_s0<<<nb, POLE_TPB, 0, st>>>(P->lmax, P->mmax, G, astride, lf, pole_rn, pole_rs, H, hstride,
+                                                    ld);
+        else
+            k_pole_pair_spin<<<nb, POLE_TPB, 0, st>>>(P->lmax, spin, P->mmax, G, C, astride, lf, pole_rn, pole_rs,
+                                                      H, hstride, ld);
         CU_LAUNCH_CHECK();
         ++x, ++sh, ++ch, ++rn, ++rs;
         if (stv) ++stv, ++ste;
         --npairs;
     }
-    const int per = (nb == 8 ? TclLayout<8>::T : TclLayout<4>::T) / 2, tail = npairs % per;
+    const int per = (nb == 8 ? TclLayout<8>::T : TclLayout<4>::T) / (spin == 0 ? 1 : 2), tail = npairs % per;
     const int ntc = (npairs > per && tail < TCL_MIN_TAIL) ? npairs - tail : npairs;
     auto launch = [&](auto nbc) {
         constexpr int NBV = decltype(nbc)::value;
-        return launch_synth_tc_nb<NBV>(P, ntc, x, sh, ch, rn, rs, stv, ste, st_ld, ld, spin, G, C, astride, lf, H,
-                                       hstride, st);
+        if (spin == 0)
+            return launch_synth_tc_nb<NBV, true>(P, ntc, x, sh, ch, rn, rs, stv, ste, st_ld, ld, spin, G, nullptr,
+                                                 astride, lf, H, hstride, st);
+        return launch_synth_tc_nb<NBV, false>(P, ntc, x, sh, ch, rn, rs, stv, ste, st_ld, ld, spin, G, C, astride,
+                                              lf, H, hstride, st);
     };
     if (nb == 8) RC_TRY(launch(std::integral_constant<int, 8>{}));
     else if (nb == 4) RC_TRY(launch(std::integral_constant<int, 4>{}));

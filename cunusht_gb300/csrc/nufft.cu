@@ -15,57 +15,9 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.cuh"
+#include "nufft_pts.cuh"
 
 namespace cunusht {
-
-constexpr int NU_TPB = 256;
-constexpr int MAXW = 16;
-
-template <typename T> __device__ __forceinline__ T es_kernel(T z, T beta) {
-    const T q = (T)1 - z * z;
-    return q > (T)0 ? exp(beta * (sqrt(q) - (T)1)) : (T)0;
-}
-
-struct PointCoords {
-    int r0;  // first fine row (relative to n_lo)
-    int p0;  // first fine column (may be negative / >= Npf: wrap)
-    double ft, fp;  // (n0 - t), (p0 - p): offsets of the first tap
-};
-
-__device__ __forceinline__ PointCoords point_coords(double th, double ph, int Ntf, int Npf, int n_lo,
-                                                    int nrows, int w) {
-    PointCoords pc;
-    // non-finite or far out-of-range coordinates are clamped so every index
-    // below stays inside the grid (the result for such points is garbage-in)
-    if (!isfinite(th)) th = 0.0;
-    if (!isfinite(ph) || fabs(ph) > 1e12) ph = 0.0;
-    double t = th * ((double)Ntf / TWOPI);
-    t = fmin(fmax(t, -1.0), 0.5 * Ntf + 1.0);
-    double p = ph * ((double)Npf / TWOPI);
-    p -= floor(p / (double)Npf) * (double)Npf;
-    p = fmin(fmax(p, 0.0), (double)Npf);
-    const double hw = 0.5 * w;
-    const int n0 = (int)ceil(t - hw);
-    const int p0 = (int)ceil(p - hw);
-    pc.ft = (double)n0 - t;
-    pc.fp = (double)p0 - p;
-    int r0 = n0 - n_lo;
-    r0 = r0 < 0 ? 0 : (r0 > nrows - w ? nrows - w : r0);  // stays in bounds for any input
-    pc.r0 = r0;
-    pc.p0 = p0;
-    return pc;
-}
-
-__device__ __forceinline__ void load_point(const double *loc, long long j, long long npts, int layout,
-                                           double &th, double &ph) {
-    if (layout == 0) {
-        th = loc[2 * j];
-        ph = loc[2 * j + 1];
-    } else {
-        th = loc[j];
-        ph = loc[npts + j];
-    }
-}
 
 template <typename T, int W = MAXW>
 __device__ __forceinline__ void weights(const PointCoords &pc, int w, T beta, T *kt, T *kp) {
@@ -157,15 +109,6 @@ __global__ void __launch_bounds__(NU_TPB)
     }
 }
 
-// FP32 kernel value from the cancellation-free exponent
-// beta (sqrt(1 - z^2) - 1) = -beta z^2 / (1 + sqrt(1 - z^2))
-__device__ __forceinline__ float es_kernel_acc(float z, float beta) {
-    const float q = 1.f - z * z;
-    if (q <= 0.f) return 0.f;
-    const float r = sqrtf(q);
-    return expf(-beta * (z * z) / (1.f + r));
-}
-
 // ------------------------------------------------------------ warp-strip spreading (type 1)
 // Each warp spreads 32 consecutive points (for lensing: neighbouring pixels of
 // one ring, whose w x w footprints overlap) into a private shared-memory strip
@@ -183,11 +126,14 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp(T *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, T beta,
                   const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
                   int spin, const void *__restrict__ in, int in_f32, int SR, int SC, long long ubs, long long lbs,
-                  long long ibs) {
+                  long long ibs, unsigned long long *__restrict__ Ufix, const float *__restrict__ vmax, int lgn) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NC = CPLX ? 2 : 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     T *strip = reinterpret_cast<T *>(smem_raw) + (size_t)wid * SR * SC * NC;
+    // deterministic plans add to the int64 fixed-point grid instead (exact, order-free)
+    const int E = Ufix ? fix_exp(vmax[blockIdx.y], lgn) : 0;
+    if (Ufix) Ufix += blockIdx.y * ubs;
     U += blockIdx.y * ubs;  // request of a batch
     loc += blockIdx.y * lbs;
     if (gamma) gamma += blockIdx.y * npts;
@@ -237,6 +183,12 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
             for (int b = 0; b < W; ++b) {
                 int c = pc.p0 + b;
                 c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+                if (Ufix) {
+                    unsigned long long *fc = Ufix + (rowoff + c) * NC;
+                    atomicAdd(fc, (unsigned long long)to_fix(kp[b] * fr, E));
+                    if constexpr (CPLX) atomicAdd(fc + 1, (unsigned long long)to_fix(kp[b] * fi, E));
+                    continue;
+                }
                 T *cell = U + (rowoff + c) * NC;
                 atomicAdd(cell, kp[b] * fr);
                 if constexpr (CPLX) atomicAdd(cell + 1, kp[b] * fi);
@@ -275,11 +227,13 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
         const int lr = i / ncl, lc = i - lr * ncl;
         int c = pmin + lc;
         c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
-        T *cell = U + ((long long)(rmin + lr) * Npf + c) * NC;
+        const long long ci = ((long long)(rmin + lr) * Npf + c) * NC;
 #pragma unroll
         for (int q = 0; q < NC; ++q) {
             const T v = strip[i * NC + q];
-            if (v != (T)0) atomicAdd(cell + q, v);
+            if (v == (T)0) continue;
+            if (Ufix) atomicAdd(Ufix + ci + q, (unsigned long long)to_fix(v, E));
+            else atomicAdd(U + ci + q, v);
         }
     }
 }
@@ -288,6 +242,8 @@ template <typename T, bool CPLX>
 static int launch_spread_warp(const cunusht_plan_s *P, int nreq, T *U, long long ubs, const double *loc, long long lbs,
                               long long npts, int layout, const double *gamma, int spin, const void *in,
                               long long ibs, int f32i, cudaStream_t st) {
+    int lgn = 0;
+    while ((1LL << lgn) < npts + 1) ++lgn;
     // strip: the footprint of 32 neighbouring ring pixels at about 2 fine
     // cells per pixel, plus row jitter from the deflection
     const int SR = P->w + 4, SC = 80 + P->w;
@@ -302,7 +258,7 @@ static int launch_spread_warp(const cunusht_plan_s *P, int nreq, T *U, long long
         if (e == cudaSuccess)
             k_spread_warp<T, CPLX, W><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(
                 U, P->nrows, P->Npf, P->Ntf, P->n_lo, W, (T)P->beta, loc, npts, layout, gamma, spin, in, f32i, SR, SC,
-                ubs, lbs, ibs);
+                ubs, lbs, ibs, P->spread_det ? P->d_ufix : nullptr, P->d_vmax, lgn);
     });
     CU_TRY(e);
     return CUNUSHT_OK;
@@ -332,11 +288,14 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp_mixed(double *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                         const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
                         int spin, const void *__restrict__ in, int in_f32, int SR, int SC, long long ubs,
-                        long long lbs, long long ibs) {
+                        long long lbs, long long ibs, unsigned long long *__restrict__ Ufix,
+                        const float *__restrict__ vmax, int lgn) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NC = CPLX ? 2 : 1;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float2 *strip = reinterpret_cast<float2 *>(smem_raw) + (size_t)wid * SR * SC * NC;  // (sum, compensation)
+    const int E = Ufix ? fix_exp(vmax[blockIdx.y], lgn) : 0;
+    if (Ufix) Ufix += blockIdx.y * ubs;
     U += blockIdx.y * ubs;  // request of a batch
     loc += blockIdx.y * lbs;
     if (gamma) gamma += blockIdx.y * npts;
@@ -400,6 +359,12 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
                 int c = pc.p0 + b;
                 c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
                 const double kw = (double)kt[a] * (double)kp[b];
+                if (Ufix) {
+                    unsigned long long *fc = Ufix + (rowoff + c) * NC;
+                    atomicAdd(fc, (unsigned long long)to_fix(kw * vr, E));
+                    if constexpr (CPLX) atomicAdd(fc + 1, (unsigned long long)to_fix(kw * vi, E));
+                    continue;
+                }
                 double *cell = U + (rowoff + c) * NC;
                 atomicAdd(cell, kw * vr);
                 if constexpr (CPLX) atomicAdd(cell + 1, kw * vi);
@@ -447,12 +412,18 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
         const int lr = i / ncl, lc = i - lr * ncl;
         int c = pmin + lc;
         c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
-        double *cell = U + ((long long)(rmin + lr) * Npf + c) * NC;
+        const long long ci = ((long long)(rmin + lr) * Npf + c) * NC;
+        double *cell = U + ci;
 #pragma unroll
         for (int q = 0; q < NC; ++q) {
             // Kahan value x - c as two exact FP64 atomic adds (the additions
             // happen in L2, the conversions on the integer pipe)
             const float2 v = strip[i * NC + q];
+            if (Ufix) {
+                if (v.x != 0.f || v.y != 0.f)
+                    atomicAdd(Ufix + ci + q, (unsigned long long)(to_fix(v.x, E) - to_fix(v.y, E)));
+                continue;
+            }
             if (v.x != 0.f) atomicAdd(cell + q, f2d_exact_int(v.x));
             if (v.y != 0.f) atomicAdd(cell + q, -f2d_exact_int(v.y));
         }
@@ -463,6 +434,8 @@ template <bool CPLX>
 static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U, long long ubs, const double *loc,
                                     long long lbs, long long npts, int layout, const double *gamma, int spin,
                                     const void *in, long long ibs, int f32i, cudaStream_t st) {
+    int lgn = 0;
+    while ((1LL << lgn) < npts + 1) ++lgn;
     const int SR = P->w + 4, SC = 80 + P->w;
     const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(float2);
     const long long nwarps = (npts + 31) / 32;
@@ -476,7 +449,7 @@ static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U
         if (e == cudaSuccess)
             k_spread_warp_mixed<CPLX, W><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(
                 U, P->nrows, P->Npf, P->Ntf, P->n_lo, W, (float)P->beta, loc, npts, layout, gamma, spin, in, f32i, SR,
-                SC, ubs, lbs, ibs);
+                SC, ubs, lbs, ibs, P->spread_det ? P->d_ufix : nullptr, P->d_vmax, lgn);
     });
     CU_TRY(e);
     return CUNUSHT_OK;
@@ -631,6 +604,10 @@ int nufft_spread_batch(const cunusht_plan_s *P, int nreq, int spin, void *U, lon
         CU_TRY(cudaMemsetAsync((char *)U + r * ubs * scal, 0, cell * (size_t)P->nrows * P->Npf, st));
     if (npts == 0) return CUNUSHT_OK;
     const int f32i = in_dtype == CUNUSHT_F32;
+    // the plan's spreading options: bin-sorted path, fixed-point accumulation
+    int done = 0;
+    RC_TRY(spread_options_begin(P, nreq, spin, U, ubs, loc, lbs, npts, layout, gamma, in, ibs, in_dtype, &done, st));
+    if (done) return spread_options_end(P, nreq, spin, U, ubs, npts, st);
     if (P->grid_fp32) {
         if (spin == 0) RC_TRY((launch_spread_warp<float, false>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
         else RC_TRY((launch_spread_warp<float, true>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
@@ -642,7 +619,7 @@ int nufft_spread_batch(const cunusht_plan_s *P, int nreq, int spin, void *U, lon
         else RC_TRY((launch_spread_warp<double, true>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
     }
     CU_LAUNCH_CHECK();
-    return CUNUSHT_OK;
+    return spread_options_end(P, nreq, spin, U, ubs, npts, st);
 }
 
 int nufft_spread(const cunusht_plan_s *P, int spin, const double *loc, long long npts, int layout,

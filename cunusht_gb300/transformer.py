@@ -307,6 +307,20 @@ class GPU_cufinufft_transformer:
         _lib.check(self._lib.cunusht_plan_stage_times(self._plan, ms, cnt, _lib.NSTAGE))
         return {n: (ms[i], cnt[i]) for i, n in enumerate(_lib.STAGES) if cnt[i]}
 
+    def set_spreading(self, method: str = "strips", deterministic: bool = False, max_points: int | None = None):
+        """Spreading of the type-1 nuFFT (nusht2d1, lenmap2gclm), the choice of
+        cuFINUFFT's gpu_method / gpu_sort in the reference's plan
+        (GPU_nufft_transformer.py:242-246): "strips" (default; points in ring
+        order, the lensing pointing) or "bins" (bin-sorted shared-memory
+        spreading, points in any order, up to max_points per request,
+        default the pixel count); deterministic=True accumulates in exact
+        int64 fixed point, so results do not depend on the order of atomics."""
+        if self._plan is None:
+            self._ensure_plan(self.epsilon if self.epsilon is not None else 1e-7)
+        m = {"strips": 0, "bins": 1}[method]
+        _lib.check(self._lib.cunusht_plan_set_spreading(self._plan, m, int(bool(deterministic)),
+                                                        int(max_points or 0)))
+
     def reserve_batch(self, max_batch: int):
         """Allocate the per-request workspace for lensing_batch (once)."""
         if self._plan is None:

@@ -113,15 +113,35 @@ int cunusht_plan_set_mmax(cunusht_plan_t *plan, int mmax);
 int cunusht_plan_force_split(cunusht_plan_t *plan, int force);
 
 /*
- * Mixed precision: the Legendre synthesis of spin > 0 (CC synthesis of spin
- * 1 / 2 maps, the deflection synthesis of dlm2pointing) runs on the tensor
- * cores (exact integer-digit bf16 products accumulated in tensor memory,
- * enable = 1, the default) or on the CUDA cores in double-float (enable = 0).
+ * Mixed precision: the Legendre synthesis (CC synthesis of spin 0 / 1 / 2
+ * maps, the deflection synthesis of dlm2pointing, the ring synthesis of the
+ * SHT-only mode) runs on the tensor cores (exact integer-digit bf16 products
+ * accumulated in tensor memory, enable = 1, the default) or on the CUDA
+ * cores in double-float (enable = 0).
  * Both replace the SHTns synthesis of the reference
  * (cunusht/sht/GPU_sht_transformer.py:56-62, :88-97); the switch exists so
  * that the two can be checked against each other.
  */
 int cunusht_plan_set_tensor_cores(cunusht_plan_t *plan, int enable);
+
+/*
+ * Spreading of the type-1 nuFFT (nusht2d1, lenmap2gclm, the delensing batch),
+ * the options cuFINUFFT's gpu_method / gpu_sort set in the reference's plan
+ * (GPU_nufft_transformer.py:242-246):
+ *   method 0  warp strips (default): neighbouring points in neighbouring
+ *             threads share shared-memory strips -- the ring-ordered pointing
+ *             of a lensing solve; scattered points fall back to global atomics;
+ *   method 1  bin-sorted: points counted into 32 x 32-cell bins of the fine
+ *             grid, scattered into bin order, one block per bin accumulating
+ *             a shared-memory tile -- points in any order (up to max_points per
+ *             request, 0 = the plan's pixel count; more points use method 0);
+ *   deterministic 1: the grid sums are accumulated in int64 fixed point (exact,
+ *             so independent of the order of the atomics) and converted after;
+ *             the same inputs then give bit-identical grids run after run,
+ *             alone or batched.
+ * Allocates the option's workspace (grown by cunusht_plan_reserve_batch).
+ */
+int cunusht_plan_set_spreading(cunusht_plan_t *plan, int method, int deterministic, int64_t max_points);
 
 /*
  * Device status word of the plan, read after the plan's work so far has
@@ -140,7 +160,9 @@ int cunusht_plan_device_status(cunusht_plan_t *plan, int *status);
  * product per output among small ones; 3: no product is issued and the
  * completion wait is limited to 64 polls, so it runs out on purpose (the
  * kernel's timeout path: status set, tensor memory released, nothing read;
- * the context stays usable).  *maxerr = largest |result - exact| (0 when the
+ * the context stays usable); 4, 5, 6: one 128 x n x 32 product (reps unused)
+ * with A and B, A only, or B only stored MN-major (transposed operands, the
+ * layout of the tensor-core adjoint).  *maxerr = largest |result - exact| (0 when the
  * accumulation is exact), *timeout = 1 if the completion wait ran out.  No
  * reference counterpart.
  */

@@ -42,6 +42,21 @@ def test_tc_selftest_exact(built_lib, n, reps, mode):
     assert err.value == 0.0
 
 
+@pytest.mark.parametrize("n", [16, 32, 64])
+@pytest.mark.parametrize("mode", [4, 5, 6])
+def test_tc_selftest_mn_major_operands(built_lib, n, mode):
+    """Operands stored MN-major (transposed, the tensor-core adjoint's layout:
+    core matrices of 8 K-rows x 16 bytes, SBO along M / N, LBO along K) give
+    the exact integer product."""
+    from cunusht_gb300 import _lib
+    lib = _lib.load()
+    err, to = ctypes.c_double(-1.0), ctypes.c_int(-1)
+    _lib.check(lib.cunusht_tc_selftest(n, 1, mode, ctypes.byref(err), ctypes.byref(to)))
+    print(f"selftest MN-major mode {mode} n {n}: max error {err.value}")
+    assert to.value == 0
+    assert err.value == 0.0
+
+
 def test_tc_wait_timeout_path_returns_and_leaves_the_context_usable(built_lib):
     """A bounded mbarrier wait that nothing arrives on (self test mode 3: no
     MMA issued, limit 64 polls) runs out: the kernel reports the timeout,
@@ -68,7 +83,7 @@ def _transformers(cu, lmax, mmax=None):
 
 
 @pytest.mark.parametrize("lmax", [40, 127, 300, 2047])
-@pytest.mark.parametrize("spin", [1, 2])
+@pytest.mark.parametrize("spin", [0, 1, 2])
 def test_tc_synthesis_matches_fp64(built_lib, lmax, spin):
     """lmax 2047 runs the recursion over 2048 steps and 16 windows: an error
     that grows with the number of steps (an unnormalised double-float step
@@ -76,7 +91,7 @@ def test_tc_synthesis_matches_fp64(built_lib, lmax, spin):
     import cunusht_gb300 as cu
     tc, cc, f64 = _transformers(cu, lmax)
     gclm, _ = orc.make_inputs(lmax, 2, seed=40 + lmax + spin)
-    alm = torch.as_tensor(gclm, device="cuda")
+    alm = torch.as_tensor(gclm[0] if spin == 0 else gclm, device="cuda")
     m_tc = tc.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
     m_cc = cc.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
     m_64 = f64.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
@@ -104,20 +119,20 @@ def test_tc_synthesis_mmax(built_lib):
     assert _status(tc) == 0
 
 
-@pytest.mark.parametrize("nreq", [1, 3, 4, 6, 8, 11])
-def test_tc_lensing_batch_equals_single(built_lib, nreq):
+@pytest.mark.parametrize("nreq,spin", [(1, 2), (3, 2), (4, 2), (6, 2), (8, 2), (11, 2), (3, 0), (8, 0)])
+def test_tc_lensing_batch_equals_single(built_lib, nreq, spin):
     """Batched launches (8, 4, 2, 1 requests sharing the recursion; 8 in blocks
     of two tiles) give each request exactly its single-request result: the
     digit products are summed exactly and each column's exponent depends on
     its own data only."""
     import cunusht_gb300 as cu
-    lmax, spin = 127, 2
+    lmax = 127
     t = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=1e-7, precision="mixed",
                                   max_spin=2)
     G, D = [], []
     for r in range(nreq):
         gclm, dls = orc.make_inputs(lmax, spin, seed=500 + r)
-        G.append(gclm)
+        G.append(gclm if spin else gclm[0])
         D.append(dls[0])
     Gt = torch.as_tensor(np.stack(G), device="cuda")
     Dt = torch.as_tensor(np.stack(D), device="cuda")
@@ -128,7 +143,7 @@ def test_tc_lensing_batch_equals_single(built_lib, nreq):
     assert _status(t) == 0
 
 
-@pytest.mark.parametrize("spin", [1, 2])
+@pytest.mark.parametrize("spin", [0, 1, 2])
 def test_tc_lensing_against_cuda_cores(built_lib, spin):
     """End to end (dlm2pointing + nusht2d2): tensor-core and CUDA-core Legendre
     stages agree well within epsilon, and both agree with the FP64 plan."""
@@ -136,7 +151,7 @@ def test_tc_lensing_against_cuda_cores(built_lib, spin):
     lmax = 255
     tc, cc, f64 = _transformers(cu, lmax)
     gclm, dls = orc.make_inputs(lmax, spin, seed=90 + spin)
-    g = torch.as_tensor(gclm, device="cuda")
+    g = torch.as_tensor(gclm if spin else gclm[0], device="cuda")
     d = torch.as_tensor(dls[0], device="cuda")
     r_tc = tc.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0).cpu().numpy()
     r_cc = cc.gclm2lenmap(g, lmax, lmax, dlm_scaled=d, spin=spin, verbose=0).cpu().numpy()
@@ -168,4 +183,74 @@ def test_tc_lensing_batch8_matches_fp64(built_lib):
         err = _rel(batch[r], ref)
         print(f"request {r}: {err:.2e} vs FP64")
         assert err < 1e-7
+    assert _status(t) == 0
+
+
+@pytest.mark.parametrize("lmax", [40, 127, 300, 2047])
+@pytest.mark.parametrize("spin", [0, 1, 2])
+def test_tc_adjoint_synthesis_matches_fp64(built_lib, lmax, spin):
+    """The adjoint Legendre stage on the tensor cores (integer-digit products
+    summed exactly over 256 rings per block, exact int64 sums across blocks)
+    against the FP64 plan and the double-float CUDA-core kernels, through
+    the ring adjoint synthesis on the Gauss-Legendre grid."""
+    import cunusht_gb300 as cu
+    tc, cc, f64 = _transformers(cu, lmax)
+    th, _ = tc.geom.pixels()
+    rng = np.random.default_rng(900 + lmax + spin)
+    y = torch.as_tensor(rng.standard_normal(th.size if spin == 0 else (2, th.size)), device="cuda")
+    ncomp = 1 if spin == 0 else 2
+    a_tc = tc.adjoint_synthesis(y, spin=spin, ncomp=ncomp).cpu().numpy()
+    a_cc = cc.adjoint_synthesis(y, spin=spin, ncomp=ncomp).cpu().numpy()
+    a_64 = f64.adjoint_synthesis(y, spin=spin, ncomp=ncomp).cpu().numpy()
+    e_tc, e_cc = _rel(a_tc, a_64), _rel(a_cc, a_64)
+    print(f"adjoint lmax {lmax} spin {spin}: tensor cores {e_tc:.2e}, CUDA cores {e_cc:.2e} vs FP64")
+    # digit truncation at 2^-32 of lambda's bound sqrt((2l+1)/(4 pi)), while a
+    # typical |lambda| is about bound / sqrt(l): 2.3e-9 at lmax 40, 1.2e-8 at
+    # lmax 2047 (the double-float CUDA-core adjoint reaches 1e-11)
+    assert e_tc < 2e-8
+    assert e_cc < 1e-7
+    assert _status(tc) == 0
+
+
+@pytest.mark.parametrize("spin", [0, 2])
+def test_tc_delensing_matches_fp64_and_is_deterministic(built_lib, spin):
+    """lenmap2gclm (spread, adjoint FFTs, adjoint Legendre on the tensor cores
+    over the Clenshaw-Curtis rings, pole pair in closed form) against the FP64
+    plan; the adjoint Legendre stage sums exactly, so two runs agree to the
+    spreading's atomics order only."""
+    import cunusht_gb300 as cu
+    lmax = 255
+    tc, cc, f64 = _transformers(cu, lmax)
+    gclm, dls = orc.make_inputs(lmax, spin, seed=95 + spin)
+    th, _ = tc.geom.pixels()
+    rng = np.random.default_rng(96 + spin)
+    m = torch.as_tensor(rng.standard_normal(th.size if spin == 0 else (2, th.size)), device="cuda")
+    d = torch.as_tensor(dls[0], device="cuda")
+    r_tc = tc.lenmap2gclm(m, d, None, lmax, lmax, spin=spin, verbose=0).cpu().numpy()
+    r_cc = cc.lenmap2gclm(m, d, None, lmax, lmax, spin=spin, verbose=0).cpu().numpy()
+    r_64 = f64.lenmap2gclm(m, d, None, lmax, lmax, spin=spin, verbose=0).cpu().numpy()
+    print(f"delensing spin {spin}: tensor cores {_rel(r_tc, r_64):.2e}, CUDA cores {_rel(r_cc, r_64):.2e}")
+    assert _rel(r_tc, r_64) < 1e-7
+    assert _rel(r_cc, r_64) < 1e-7
+    assert _rel(r_tc, r_cc) < 1e-7
+    assert _status(tc) == 0
+
+
+@pytest.mark.parametrize("nreq,spin", [(3, 2), (8, 2), (11, 2), (8, 0)])
+def test_tc_delensing_batch_equals_single(built_lib, nreq, spin):
+    """Batched delensing (8, 4, 2, 1 requests per tensor-core launch) gives each
+    request its single-request result within the spreading's atomics order."""
+    import cunusht_gb300 as cu
+    lmax = 127
+    t = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=1, epsilon=1e-7, precision="mixed",
+                                  max_spin=2)
+    npix = t.npix()
+    rng = np.random.default_rng(1200 + nreq)
+    M = torch.as_tensor(rng.standard_normal((nreq, npix) if spin == 0 else (nreq, 2, npix)), device="cuda")
+    D = torch.as_tensor(np.stack([orc.make_inputs(lmax, spin, seed=1300 + r)[1][0] for r in range(nreq)]),
+                        device="cuda")
+    batch = t.delensing_batch(M, D, spin).cpu().numpy()
+    for r in (0, nreq - 1):
+        single = np.atleast_2d(t.lenmap2gclm(M[r], D[r], None, lmax, lmax, spin=spin, verbose=0).cpu().numpy())
+        assert _rel(batch[r], single) < 1e-6
     assert _status(t) == 0
