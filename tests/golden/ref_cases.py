@@ -23,14 +23,15 @@ def _healpix(nside: int):
 # reference kernel (pointing.cu:213-222), 0.05 rad puts rings on its exact
 # branch (:204-211)
 POINTING = {
-    "gl63_small": (lambda: _gl(63, 127), 7e-4, 11),
+    "gl47_small": (lambda: _gl(47, 95), 7e-4, 11),
     "gl31_large": (lambda: _gl(31, 63), 5e-2, 12),
     "healpix8_small": (lambda: _healpix(8), 7e-4, 13),
 }
 
 # theta / phi sizes of the Clenshaw-Curtis grid at lmax 31 ((good_size(lmax + 2)
-# + 3) // 4 * 4, 2 good_size(lmax + 1); test_doublingGPU.py:100-101)
-DOUBLING = {"cc_l31": (36, 64, 21), "cc_l63": (68, 128, 22)}
+# + 3) // 4 * 4, 2 good_size(lmax + 1); test_doublingGPU.py:100-101) and a small
+# grid whose phi half-length is odd
+DOUBLING = {"cc_l31": (36, 64, 21), "cc_small": (12, 20, 22)}
 
 
 def pointing_inputs(name: str):

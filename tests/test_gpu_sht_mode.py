@@ -53,7 +53,8 @@ def _theta_contig(S, ring_major):
 
 def test_layout_attributes(S):
     assert S.theta_contiguous
-    assert S.spat_shape == (S.nphi, S.nlat) == (2 * LMAX + 1, LMAX + 1)
+    assert S.nlat == LMAX + 1 and S.nphi == int(S.geom.nph[0]) >= 2 * LMAX + 1
+    assert S.spat_shape == (S.nphi, S.nlat)
 
 
 def test_synthesis_positional(S):
