@@ -15,17 +15,17 @@
 // sqrt((2l+1)/(4 pi)), Ea per block and column from the block's largest |X|.
 // Per chunk of 16 l and lambda digit i one tensor-memory accumulator holds
 //     D_i[(j, col)][l] = sum_ring t_j(ring, col) d_i(ring, l)
-// (M = 128 rows (digit j, column), N = 16 l, K = the block's 256 rings in 16
-// K-steps): integer products below 2^14 summed 256 times stay below 2^22, so
-// the FP32 accumulation is exact.  Both operands are stored MN-major: the A
-// tile (map digits, fixed for the block) and the B tiles (lambda digits of 16
-// l, one per digit i) are written by each ring thread as 16-byte rows of 8
-// consecutive values, as in the synthesis.
+// (M = 128 rows (digit j, column), N = (digit i, l) = 4 x 16, K = the block's
+// 256 rings in 16 K-steps of one MMA each): integer products below 2^14
+// summed 256 times stay below 2^22, so the FP32 accumulation is exact.  Both
+// operands are stored MN-major: the A tile (map digits, fixed for the block)
+// and the B tile (lambda digits of 16 l) are written by each ring thread as
+// 16-byte rows of 8 consecutive values, as in the synthesis.
 //
 // Block: one order m and 256 rings (spin s: 128 ring pairs, both sides; spin
 // 0: 256 ring pairs, the theta side only), 8 ring warps (one ring per
-// thread, double-float recursion, digit split, B rows), 1 MMA warp (4 x 16
-// MMAs of 128 x 16 x 16 per chunk) and 4 epilogue warps (one TMEM lane
+// thread, double-float recursion, digit split, B rows), 1 MMA warp (16 MMAs
+// of 128 x 64 x 16 per chunk) and 4 epilogue warps (one TMEM lane
 // quarter each).  Two B buffers (full / empty mbarriers) and four
 // tensor-memory chunk buffers (full / empty) let the three roles run apart.
 // The epilogue folds the digit sums of a row, hi = v_0 (exact) and lo =
@@ -53,10 +53,11 @@ constexpr int TCA_THREADS = (TCA_RW + 5) * 32;  // 416
 constexpr int TCA_A_LBO = 16 * 128;             // A: [K-core 32][M-core 16][8 K-rows][16 B]
 constexpr int TCA_A_SBO = 128;
 constexpr int TCA_ABYTES = (TCA_R / 8) * TCA_A_LBO;    // 64 KB
-constexpr int TCA_B_LBO = 2 * 128;              // B per digit: [K-core 32][N-core 2][8 K-rows][16 B]
-constexpr int TCA_B_SBO = 128;
-constexpr int TCA_BDIG = (TCA_R / 8) * TCA_B_LBO;      // 8 KB
-constexpr int TCA_BBUF = 4 * TCA_BDIG;                 // 32 KB per chunk
+// B of a chunk: N = (lambda digit i, l) = 4 x 16, [K-core 32][N-core 8 = (i, l half)][8 K-rows][16 B],
+// so that one MMA of N = 64 per K-step forms all four digit sums
+constexpr int TCA_B_SBO = 128;                  // N-core stride
+constexpr int TCA_B_LBO = 8 * TCA_B_SBO;        // K-core stride
+constexpr int TCA_BBUF = (TCA_R / 8) * TCA_B_LBO;      // 32 KB per chunk
 constexpr int TCA_XBYTES = TCA_KC * 128 * 8;           // exchange [l][row] float2
 constexpr int TCA_OFF_B = TCA_ABYTES;
 constexpr int TCA_OFF_X = TCA_OFF_B + 2 * TCA_BBUF;
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
 
     if (warp == TCA_MMA) {
         // ---------------- MMA warp
-        constexpr uint32_t IDESC = idesc_bf16_f32(128, TCA_KC) | (1u << 15) | (1u << 16);  // A, B MN-major
+        constexpr uint32_t IDESC = idesc_bf16_f32(128, 4 * TCA_KC) | (1u << 15) | (1u << 16);  // A, B MN-major
         int gc = 0;
         bool ok = true;
         for (int lb = l0; lb <= L; lb += TCA_KC, ++gc) {
@@ -250,13 +251,10 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
             if (lane == 0) {
                 tc_fence_after();
                 const uint32_t bb = sbase + TCA_OFF_B + buf * TCA_BBUF;
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
 #pragma unroll 4
-                    for (int ks = 0; ks < TCA_R / 16; ++ks)
-                        tc_mma(tbase + tb * 64 + i * 16, sdesc(sbase + 2 * ks * TCA_A_LBO, TCA_A_LBO, TCA_A_SBO),
-                               sdesc(bb + i * TCA_BDIG + 2 * ks * TCA_B_LBO, TCA_B_LBO, TCA_B_SBO), IDESC,
-                               ks > 0 ? 1u : 0u);
+                for (int ks = 0; ks < TCA_R / 16; ++ks)  // columns i 16 + l: the sums of lambda digit i
+                    tc_mma(tbase + tb * 64, sdesc(sbase + 2 * ks * TCA_A_LBO, TCA_A_LBO, TCA_A_SBO),
+                           sdesc(bb + 2 * ks * TCA_B_LBO, TCA_B_LBO, TCA_B_SBO), IDESC, ks > 0 ? 1u : 0u);
                 tc_commit(bempty0 + 8 * buf);
                 tc_commit(tfull0 + 8 * tb);
             }
@@ -375,8 +373,8 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
                     for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
                 }
 #pragma unroll
-                for (int k = 0; k < 4; ++k)  // digit k of lambda -> B tile k, N-core lh
-                    *reinterpret_cast<uint4 *>(sB + k * TCA_BDIG + lh * TCA_B_SBO) =
+                for (int k = 0; k < 4; ++k)  // digit k of lambda -> N-core (k, lh)
+                    *reinterpret_cast<uint4 *>(sB + (2 * k + lh) * TCA_B_SBO) =
                         make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
                 REC_RESCALE_DF(cur, prev, e);
             }
