@@ -393,11 +393,34 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
     }
 }
 
+// v 2^e2 as a double, on the integer pipe (GB300 runs integer-to-FP64
+// conversions at the FP64 rate): the leading-zero count normalises |v|, the
+// top 53 bits round to nearest even, and e2 goes into the exponent field.
+// Requires |v| < 2^63 and a result in the normal range.
+__device__ __forceinline__ double i64_ldexp(long long v, int e2) {
+    if (v == 0) return 0.0;
+    const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
+    const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+    const int lz = __clzll((long long)u);
+    const unsigned long long m = u << lz;  // leading one at bit 63
+    unsigned long long mant = m >> 11;      // 53 bits, leading one at bit 52
+    const unsigned long long rem = m & 0x7FFull;
+    mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+    int ex = 63 - lz + e2;
+    if (mant >> 53) {  // rounding carried into bit 53
+        mant >>= 1;
+        ++ex;
+    }
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 // D(l, col) from the fixed-point sums -> alm, the combinations of the
 // double-float kernels (legendre.cu k_leg_adj_s0_df / k_leg_adj_spin_df):
 // spin 0: a = f (E or O by the parity of l + m); spin s: P = (D0, D1),
 // Q = sgn (D2, -D3) for even l + m and sgn (-D2, D3) for odd (sgn = -1 for
 // odd s), G = -f (P + Q) / 2 and C = f (-(P im - Q im), P re - Q re) / 2.
+// The sums and differences are exact in int64 (|D| < 2^61), so each output
+// takes one conversion (i64_ldexp) and, with a per-l factor f, one product.
 // Every alm of the orders m <= mmax is written (=); the pole pair and the
 // leftover ring pairs are added afterwards.
 __global__ void k_leg_adj_tc_finish(int L, int spin, int ncomp, const unsigned long long *__restrict__ acc,
@@ -409,26 +432,31 @@ __global__ void k_leg_adj_tc_finish(int L, int spin, int ncomp, const unsigned l
     if (l > L) return;
     const long long ix = almidx(L, m, m) - m + l;
     const unsigned long long *a = acc + ((long long)r * nalm_tab + ix) * 4;
-    const double u = ldexp(1.0, adj_unit_exp(npairs_all, l, hm[r]));
-    const double d0 = (double)(long long)a[0] * u, d1 = (double)(long long)a[1] * u;
-    const double d2 = (double)(long long)a[2] * u, d3 = (double)(long long)a[3] * u;
-    const double f = lfac ? lfac[l] : 1.0;
+    const long long d0 = (long long)a[0], d1 = (long long)a[1], d2 = (long long)a[2], d3 = (long long)a[3];
+    const int U = adj_unit_exp(npairs_all, l, hm[r]);
     const bool odd = (l + m) & 1;
     double *Gr = G + 2 * r * astride;
+    double f0, f1;
     if (spin == 0) {
-        Gr[2 * ix] = f * (odd ? d2 : d0);
-        Gr[2 * ix + 1] = f * (odd ? d3 : d1);
-        return;
+        f0 = i64_ldexp(odd ? d2 : d0, U);
+        f1 = i64_ldexp(odd ? d3 : d1, U);
+    } else {
+        const bool neg = (spin & 1) != 0;
+        long long qr = odd ? -d2 : d2, qi = odd ? d3 : -d3;
+        if (neg) qr = -qr, qi = -qi;
+        f0 = i64_ldexp(-(d0 + qr), U - 1);
+        f1 = i64_ldexp(-(d1 + qi), U - 1);
+        if (ncomp > 1) {
+            double c0 = i64_ldexp(-(d1 - qi), U - 1), c1 = i64_ldexp(d0 - qr, U - 1);
+            if (lfac) c0 *= lfac[l], c1 *= lfac[l];
+            double *Cr = C + 2 * r * astride;
+            Cr[2 * ix] = c0;
+            Cr[2 * ix + 1] = c1;
+        }
     }
-    const double sgs = (spin & 1) ? -1.0 : 1.0;
-    const double Qr = sgs * (odd ? -d2 : d2), Qi = sgs * (odd ? d3 : -d3);
-    Gr[2 * ix] = -0.5 * f * (d0 + Qr);
-    Gr[2 * ix + 1] = -0.5 * f * (d1 + Qi);
-    if (ncomp > 1) {
-        double *Cr = C + 2 * r * astride;
-        Cr[2 * ix] = -0.5 * f * (d1 - Qi);
-        Cr[2 * ix + 1] = 0.5 * f * (d0 - Qr);
-    }
+    if (lfac) f0 *= lfac[l], f1 *= lfac[l];
+    Gr[2 * ix] = f0;
+    Gr[2 * ix + 1] = f1;
 }
 
 // The pole pair of a spin-0 adjoint: lambda_lm(0) = delta_m0 sqrt((2l+1)/(4 pi))
