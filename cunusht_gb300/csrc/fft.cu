@@ -493,9 +493,11 @@ __global__ void __launch_bounds__(FFT_TPB)
     }
 }
 
-template <typename T>
+// TU: the grid's scalar type (double for the double-float transforms of the
+// mixed plan, whose spread accumulates in FP64)
+template <typename T, typename TU = T>
 __global__ void __launch_bounds__(FFT_TPB)
-    k_phi_adj_s0(const T *__restrict__ U, int nrows, int Npf, cplx<T> *__restrict__ F, int ncols,
+    k_phi_adj_s0(const TU *__restrict__ U, int nrows, int Npf, cplx<T> *__restrict__ F, int ncols,
                  const cplx<T> *__restrict__ tw, int TW, int SP, int q, long long ubs, long long fbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
@@ -505,13 +507,13 @@ __global__ void __launch_bounds__(FFT_TPB)
     F += blockIdx.y * fbs;
     const int r1 = 2 * blockIdx.x, r2 = r1 + 1;
     const bool has2 = r2 < nrows;
-    const T *u1 = U + (long long)r1 * Npf;
-    const T *u2 = U + (long long)r2 * Npf;
+    const TU *u1 = U + (long long)r1 * Npf;
+    const TU *u2 = U + (long long)r2 * Npf;
     const int Nb = Npf / SP;
     const int tstep = TW / Npf;
     for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
         const int p = SP * j + q;
-        buf[j] = mk<T>(u1[p], has2 ? u2[p] : cvt<T>(0.0));
+        buf[j] = mk<T>(cvt<T>(to_d(u1[p])), cvt<T>(has2 ? to_d(u2[p]) : 0.0));
     }
     __syncthreads();
     fft_smem<T>(buf, Nb, -1, stw, MTW);
@@ -562,9 +564,9 @@ __global__ void __launch_bounds__(FFT_TPB)
     for (int j = threadIdx.x; j < Nb; j += blockDim.x) U[(long long)r * Npf + SP * j + q] = ccast<TU>(buf[j]);
 }
 
-template <typename T>
+template <typename T, typename TU = T>
 __global__ void __launch_bounds__(FFT_TPB)
-    k_phi_adj_spin(const cplx<T> *__restrict__ U, int L, int Npf, cplx<T> *__restrict__ F,
+    k_phi_adj_spin(const cplx<TU> *__restrict__ U, int L, int Npf, cplx<T> *__restrict__ F,
                    const cplx<T> *__restrict__ tw, int TW, int SP, int q, long long ubs, long long fbs) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *buf = reinterpret_cast<cplx<T> *>(smem_raw);
@@ -576,7 +578,10 @@ __global__ void __launch_bounds__(FFT_TPB)
     const int ncols = 2 * L + 1;
     const int Nb = Npf / SP;
     const int tstep = TW / Npf;
-    for (int j = threadIdx.x; j < Nb; j += blockDim.x) buf[j] = U[(long long)r * Npf + SP * j + q];
+    for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
+        const cplx<TU> u = U[(long long)r * Npf + SP * j + q];
+        buf[j] = mk<T>(cvt<T>(to_d(u.x)), cvt<T>(to_d(u.y)));
+    }
     __syncthreads();
     fft_smem<T>(buf, Nb, -1, stw, MTW);
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
@@ -938,6 +943,11 @@ int theta_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, 
             k_theta_adj2<float><<<g2, FFT_TPB, sm, st>>>((const float2 *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
                                                          spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32,
                                                          P->TW, fbs, hbs);
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_theta_adj2<dfl>, sm));
+            k_theta_adj2<dfl><<<g2, FFT_TPB, sm, st>>>((const dcplx *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
+                                                       spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc,
+                                                       (const dcplx *)P->d_twdf, P->TW, fbs, hbs);
         } else {
             RC_TRY(set_smem(k_theta_adj2<double>, sm));
             k_theta_adj2<double><<<g2, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt,
@@ -954,6 +964,12 @@ int theta_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, 
                                                           spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc, P->d_tw32,
                                                           P->TW, SP, q, (float2 *)U, fbs, hbs,
                                                           ubs_bytes / (long long)sizeof(float2));
+        } else if (P->fft_df) {
+            RC_TRY(set_smem(k_theta_adj<dfl>, sm));
+            k_theta_adj<dfl><<<grid, FFT_TPB, sm, st>>>((const dcplx *)F, ncols, P->n_lo, P->nrows, P->Nt, P->Ntf,
+                                                        spin, mofs, L, P->d_Dth, P->d_Dph, H, P->ncc,
+                                                        (const dcplx *)P->d_twdf, P->TW, SP, q, (dcplx *)U, fbs, hbs,
+                                                        ubs_bytes / (long long)sizeof(dcplx));
         } else {
             RC_TRY(set_smem(k_theta_adj<double>, sm));
             k_theta_adj<double><<<grid, FFT_TPB, sm, st>>>((const double2 *)F, ncols, P->n_lo, P->nrows, P->Nt,
@@ -1034,6 +1050,11 @@ int phi_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, lo
                 RC_TRY(set_smem(k_phi_adj_s0<float>, sm));
                 k_phi_adj_s0<float><<<grid, FFT_TPB, sm, st>>>((const float *)U, P->nrows, P->Npf, (float2 *)F, L + 1,
                                                                P->d_tw32, P->TW, SP, q, ubs, fbs);
+            } else if (P->fft_df) {  // FP64 grid, double-float transforms
+                RC_TRY(set_smem(k_phi_adj_s0<dfl, double>, sm));
+                k_phi_adj_s0<dfl, double><<<grid, FFT_TPB, sm, st>>>((const double *)U, P->nrows, P->Npf, (dcplx *)F,
+                                                                     L + 1, (const dcplx *)P->d_twdf, P->TW, SP, q,
+                                                                     ubs, fbs);
             } else {
                 RC_TRY(set_smem(k_phi_adj_s0<double>, sm));
                 k_phi_adj_s0<double><<<grid, FFT_TPB, sm, st>>>((const double *)U, P->nrows, P->Npf, (double2 *)F,
@@ -1045,6 +1066,11 @@ int phi_adj_batch(const cunusht_plan_s *P, int nreq, int spin, const void *U, lo
                 RC_TRY(set_smem(k_phi_adj_spin<float>, sm));
                 k_phi_adj_spin<float><<<grid, FFT_TPB, sm, st>>>((const float2 *)U, L, P->Npf, (float2 *)F,
                                                                  P->d_tw32, P->TW, SP, q, ubs / 2, fbs);
+            } else if (P->fft_df) {
+                RC_TRY(set_smem(k_phi_adj_spin<dfl, double>, sm));
+                k_phi_adj_spin<dfl, double><<<grid, FFT_TPB, sm, st>>>((const double2 *)U, L, P->Npf, (dcplx *)F,
+                                                                       (const dcplx *)P->d_twdf, P->TW, SP, q,
+                                                                       ubs / 2, fbs);
             } else {
                 RC_TRY(set_smem(k_phi_adj_spin<double>, sm));
                 k_phi_adj_spin<double><<<grid, FFT_TPB, sm, st>>>((const double2 *)U, L, P->Npf, (double2 *)F,
