@@ -70,8 +70,10 @@ def parse():
                    help="served mixed workload instead: Poisson arrivals of mixed lmax / spin / direction / eps")
     p.add_argument("--serve-requests", type=int, default=2000)
     p.add_argument("--serve-rate", type=float, default=200.0, help="mean arrival rate, requests/s")
-    p.add_argument("--serve-budget-gb", type=float, default=150.0)
+    p.add_argument("--serve-budget-gb", type=float, default=200.0)
     p.add_argument("--serve-native", action="store_true", help="drive the library's C++ server (cunusht_server_*)")
+    p.add_argument("--serve-lazy-graphs", action="store_true",
+                   help="capture each (direction, batch size) graph on first use instead of before the stream")
     p.add_argument("--serve-fp64-sample", type=int, default=60,
                    help="requests of the same mix run as serial plain FP64 calls for the comparison")
     return p.parse_args()
@@ -710,10 +712,11 @@ def serve_main(args):
     if args.serve_native:
         srv = NativeLensingServer(precision="mixed", hbm_budget_bytes=args.serve_budget_gb * 1e9,
                                   policy={L: serve_policy(L) for L in SERVE_LMAX})
-        admitted = keys  # buckets are admitted on first use; the warm-up below creates them
     else:
         srv = LensingServer(precision="mixed", hbm_budget_bytes=args.serve_budget_gb * 1e9, policy=serve_policy)
-        admitted = srv.prewarm(keys)
+    # buckets admitted and, unless --serve-lazy-graphs, every (direction, batch
+    # size) graph captured before the stream starts
+    admitted = srv.prewarm(keys, graphs=not args.serve_lazy_graphs)
     setup_s = time.perf_counter() - t0
     for L in SERVE_LMAX:
         inputs.tables(int(L))
@@ -725,6 +728,8 @@ def serve_main(args):
     torch.cuda.synchronize()
     srv.completed.clear()
     launches0 = srv.stats()["launches"] if args.serve_native else srv.launches
+    evict0 = srv.stats()["evictions"] if args.serve_native else srv.evictions
+    refuse0 = srv.stats()["refusals"] if args.serve_native else srv.rejected_admissions
 
     # timed run: Poisson arrivals on the server clock
     clk = ClockSampler(torch.cuda.current_device())
@@ -732,13 +737,20 @@ def serve_main(args):
     srv.t0 = time.perf_counter()
     nxt = 0
     seen = 0
+    step_max, slow_n, slow_s = 0.0, 0, 0.0   # host time inside the scheduler's step()
     while True:
         now = srv.now()
         while nxt < n and arrivals[nxt] <= now:
             L, sp, kd, ep = int(lmaxs[nxt]), int(spins[nxt]), str(kinds[nxt]), float(epss[nxt])
             srv.submit(kd, L, sp, ep, inputs.make(kd, L, sp, nxt, npix_of[L]), None, arrival=float(arrivals[nxt]))
             nxt += 1
+        ts = time.perf_counter()
         pending = srv.step()
+        dt = time.perf_counter() - ts
+        step_max = max(step_max, dt)
+        if dt > 0.02:
+            slow_n += 1
+            slow_s += dt
         for r in srv.completed[seen:]:
             r.result = None                     # results are consumed (dropped) as they complete
         seen = len(srv.completed)
@@ -750,6 +762,9 @@ def serve_main(args):
     wall = srv.now()
     clocks = clk.stop()
     nlaunch = (srv.stats()["launches"] if args.serve_native else srv.launches) - launches0
+    used_gb = (srv.stats()["bytes"] if args.serve_native else srv.used_bytes()) / 1e9
+    evictions = (srv.stats()["evictions"] if args.serve_native else srv.evictions) - evict0
+    refusals = (srv.stats()["refusals"] if args.serve_native else srv.rejected_admissions) - refuse0
     if args.serve_native:
         admitted = [None] * int(srv.stats()["buckets"])
     lat = np.array(srv.latencies_ms())
@@ -803,7 +818,10 @@ def serve_main(args):
                                    for L, v in sorted(by.items())},
             "launches": nlaunch, "requests_per_launch": done / max(1, nlaunch),
             "fp64_serial": fp64, "buckets_admitted": len(admitted), "buckets": len(keys),
-            "plan_setup_s": setup_s, "hbm_budget_gb": args.serve_budget_gb,
+            "plan_setup_s": setup_s, "hbm_budget_gb": args.serve_budget_gb, "hbm_in_use_gb": used_gb,
+            "graphs": "captured on first use" if args.serve_lazy_graphs else "captured before the stream",
+            "host_step": {"max_ms": 1e3 * step_max, "calls_over_20ms": slow_n, "s_in_calls_over_20ms": slow_s,
+                          "evictions": evictions, "refusals": refusals},
             "server": "native (cunusht_server_*)" if args.serve_native else "python (serving.LensingServer)",
             "config": {"workload": f"{n} Poisson requests at {args.serve_rate}/s, lmax {list(SERVE_LMAX)} "
                                    f"p={list(SERVE_P)}, spin {{0,2}}, gclm2lenmap / lenmap2gclm, eps {{1e-5,1e-7}}",

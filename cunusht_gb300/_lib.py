@@ -33,6 +33,8 @@ SIGNATURES = {
     "cunusht_plan_info": (_i, [_vp, _vp, _i]),
     "cunusht_plan_set_profiling": (_i, [_vp, _i]),
     "cunusht_plan_force_split": (_i, [_vp, _i]),
+    "cunusht_plan_set_ring_transform": (_i, [_vp, _i]),
+    "cunusht_plan_ring_transform": (_i, [_vp]),
     "cunusht_plan_set_mmax": (_i, [_vp, _i]),
     "cunusht_plan_set_tensor_cores": (_i, [_vp, _i]),
     "cunusht_plan_set_spreading": (_i, [_vp, _i, _i, _i64]),
@@ -44,6 +46,7 @@ SIGNATURES = {
     "cunusht_server_submit": (_i, [_vp, _i, _i, _i, _d, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_i64)]),
     "cunusht_server_poll": (_i, [_vp, _vp, _i, ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "cunusht_server_stats": (_i, [_vp, _vp, _i]),
+    "cunusht_server_prewarm": (_i, [_vp, _i, _i, _d, _i, ctypes.POINTER(_i)]),
     "cunusht_server_destroy": (_i, [_vp]),
     "cunusht_delensing_batch": (_i, [_vp, _i, _i, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cunusht_synth_points": (_i, [_vp, _i, _i, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp]),

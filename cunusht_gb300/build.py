@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcunusht_gb300.so")
-SOURCES = ["capi.cu", "legendre.cu", "legendre_tc.cu", "legendre_tc_adj.cu", "fft.cu", "nufft.cu", "spread_bins.cu",
+SOURCES = ["capi.cu", "legendre.cu", "legendre_tc.cu", "legendre_tc_adj.cu", "fft.cu", "ring_mr.cu", "nufft.cu", "spread_bins.cu",
            "noalloc.cu", "server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

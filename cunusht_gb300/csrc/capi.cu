@@ -107,6 +107,13 @@ template <typename T> static int dalloc(cunusht_plan_s *P, T **p, size_t n) {
     return CUNUSHT_OK;
 }
 
+int plan_alloc(cunusht_plan_s *P, void **p, size_t bytes) {
+    char *c = nullptr;
+    RC_TRY(dalloc(P, &c, bytes));
+    *p = c;
+    return CUNUSHT_OK;
+}
+
 template <typename T> static int upload(cunusht_plan_s *P, T **p, const std::vector<T> &h) {
     RC_TRY(dalloc(P, p, h.size()));
     if (!h.empty()) CU_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
@@ -122,7 +129,7 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_ring_cls, P->d_cls_N, P->d_cls_Mb, P->d_cls_SP,
                     P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
                     P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[0], P->d_tc_woff[1], P->d_tc_woff[2],
-                    P->d_tc_rec};
+                    P->d_tc_rec, P->d_mr_pos, P->d_mr_tw64, P->d_mr_twdf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (P->d_bin) cudaFree(P->d_bin);
@@ -405,6 +412,7 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
             RC_TRY(upload(P, &P->d_cls_boff, cls_boff));
         }
     }
+    RC_TRY(ring_mr_init(P));
     // twiddles
     {
         P->TW = std::max(std::max(P->Ntf, P->Npf), P->Mb);
@@ -578,7 +586,22 @@ int cunusht_plan_force_split(cunusht_plan_t *P, int force) {
     P->sp_theta = (force || P->Ntf > emax) ? 2 : 1;
     P->sp_phi = (force || P->Npf > emax) ? 2 : 1;
     P->sp_ring = (force || P->Mb > emax) ? 2 : 1;
+    P->ring_bluestein = force != 0;
     return CUNUSHT_OK;
+}
+
+int cunusht_plan_set_ring_transform(cunusht_plan_t *P, int method) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(method == 0 || method == 1, "ring transform method must be 0 (mixed radix where possible) or 1 "
+              "(Bluestein), got %d", method);
+    P->ring_bluestein = method == 1;
+    return CUNUSHT_OK;
+}
+
+int cunusht_plan_ring_transform(const cunusht_plan_t *P) {
+    if (!P) return -1;
+    return ring_mr_available(P) ? 0 : 1;
 }
 
 int cunusht_plan_set_tensor_cores(cunusht_plan_t *P, int enable) {

@@ -128,6 +128,11 @@ constexpr double TWOPI = 6.283185307179586476925286766559005768;
 }  // namespace cunusht
 
 // ---------------------------------------------------------------- plan
+// mixed-radix ring transforms: longest ring, most stages, radix constants
+constexpr int MR_NMAX = 8192;
+constexpr int MR_MAXST = 16;
+constexpr int MR_KMAX = 128;
+
 struct cunusht_plan_s {
     int lmax = 0;
     int max_spin = 0;
@@ -211,6 +216,15 @@ struct cunusht_plan_s {
     long long nchirp = 0, nbker = 0;
     int *d_ring_cls = nullptr, *d_cls_N = nullptr, *d_cls_Mb = nullptr, *d_cls_SP = nullptr;
     long long *d_cls_coff = nullptr, *d_cls_boff = nullptr;
+    // mixed-radix ring transform (ring_mr.cu) of uniform rings whose length
+    // factors into radices <= 13: stages (radix, sub-transform length, offset
+    // of the radix constants), output positions and e^{+2 pi i t / N} tables
+    int mr_nst = 0;
+    int mr_R[MR_MAXST] = {}, mr_Ls[MR_MAXST] = {}, mr_coff[MR_MAXST] = {};
+    int *d_mr_pos = nullptr;
+    double2 *d_mr_tw64 = nullptr;
+    void *d_mr_twdf = nullptr;  // dcplx
+    bool ring_bluestein = false;  // cunusht_plan_set_ring_transform(plan, 1): Bluestein for every ring length
 
     // workspace
     double2 *d_H = nullptr;    // Legendre columns on the CC rings  [ncols][ncc]

@@ -1092,6 +1092,7 @@ static int ring_buffer_len(const cunusht_plan_s *P) { return P->ncls > 1 ? P->ri
 
 int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,
                      double *out1, long long obs, cudaStream_t st) {
+    if (ring_mr_available(P)) return ring_synth_mr_batch(P, nreq, spin, Hgl, hbs, out0, out1, obs, st);
     size_t sm = fft_smem_bytes(ring_buffer_len(P), false);
     dim3 grid(P->nring, nreq);
     const RingCls rc = ring_cls_of(P);

@@ -6,6 +6,15 @@ namespace cunusht {
 
 constexpr int FFT_TPB = 512;
 
+// capi.cu: device allocation counted in the plan's workspace bytes
+int plan_alloc(cunusht_plan_s *P, void **p, size_t bytes);
+
+// ring_mr.cu: mixed-radix ring transforms of uniform rings
+int ring_mr_init(cunusht_plan_s *P);
+bool ring_mr_available(const cunusht_plan_s *P);
+int ring_synth_mr_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 *Hgl, long long hbs, double *out0,
+                        double *out1, long long obs, cudaStream_t st);
+
 // capi.cu: Gauss-Legendre nodes x (descending cos theta) and weights, Newton iteration
 void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w);
 

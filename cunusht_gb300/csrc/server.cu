@@ -23,6 +23,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <set>
 #include <tuple>
 #include <vector>
 
@@ -79,10 +80,12 @@ struct cunusht_server_s {
     std::map<int, std::pair<int, int>> policy;  // lmax -> (requests per launch, slots)
     std::map<Key, Bucket> buckets;
     std::map<Key, std::deque<Req>> queues;
-    std::map<Key, size_t> blocked;  // bytes in use when the bucket was refused
+    std::map<Key, size_t> sizes;       // measured device bytes of each bucket's slots
+    std::map<Key, long long> last_use;  // launch counter at each bucket's last launch
+    std::set<Key> refused;              // buckets waiting for room
     std::vector<int64_t> done;
     int64_t next_id = 1;
-    long long launches = 0, completed = 0, refusals = 0;
+    long long launches = 0, completed = 0, refusals = 0, evictions = 0;
 
     size_t used() const {
         size_t u = 0;
@@ -103,6 +106,18 @@ size_t free_bytes() {
     size_t f = 0, t = 0;
     cudaMemGetInfo(&f, &t);
     return f;
+}
+
+// Stream priority of a bucket's slots: the smaller the transform, the higher
+// the priority, so that a short launch takes the SMs that free up while long
+// launches of larger lmax are resident instead of waiting behind their
+// thousands of blocks (lmax <= 1023: highest, 2047: one below, larger: the
+// default).
+int slot_priority(int lmax) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
+    const int rank = lmax <= 1023 ? 2 : lmax <= 2047 ? 1 : 0;  // levels above the default
+    return std::max(greatest, least - rank);
 }
 
 // GL pointing geometry with nphi pixels per ring (geometry.py:267-284)
@@ -133,7 +148,11 @@ int make_slot(cunusht_server_s *S, const Key &k, int cap, std::unique_ptr<Slot> 
     CU_TRY(cudaMalloc(&sl->aout, sizeof(double2) * cap * sl->ncomp * sl->nalm));
     CU_TRY(cudaMalloc(&sl->mout, sizeof(double) * cap * ncm * sl->npix));
     CU_TRY(cudaMalloc(&sl->lin, sizeof(double) * cap * ncm * sl->npix));
-    CU_TRY(cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking));
+    // zeroed inputs: a prewarm run (graph capture ahead of traffic) reads them
+    CU_TRY(cudaMemset(sl->gin, 0, sizeof(double2) * cap * sl->ncomp * sl->nalm));
+    CU_TRY(cudaMemset(sl->din, 0, sizeof(double2) * cap * sl->nalm));
+    CU_TRY(cudaMemset(sl->lin, 0, sizeof(double) * cap * ncm * sl->npix));
+    CU_TRY(cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, slot_priority(lmax)));
     CU_TRY(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming));
     CU_TRY(cudaDeviceSynchronize());
     const size_t f1 = free_bytes();
@@ -150,28 +169,32 @@ int run_batch(Slot *sl, int dir, int n) {
                                    nullptr, sl->aout, sl->st);
 }
 
+// capture the (direction, n) graph of a slot if it has none yet
+int capture_graph(Slot *sl, int dir, int n) {
+    auto key = std::make_pair(dir, n);
+    if (sl->graphs.count(key)) return CUNUSHT_OK;
+    RC_TRY(run_batch(sl, dir, n));  // eager first run: kernel attributes, module loading
+    cudaGraph_t g = nullptr;
+    CU_TRY(cudaStreamBeginCapture(sl->st, cudaStreamCaptureModeThreadLocal));
+    const int rc = run_batch(sl, dir, n);
+    const cudaError_t e = cudaStreamEndCapture(sl->st, &g);
+    if (rc != CUNUSHT_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    CU_TRY(e);
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    CU_TRY(ei);
+    sl->graphs.emplace(key, ex);
+    return CUNUSHT_OK;
+}
+
 // replay the (direction, n) graph, capturing it on first use
 int launch_graph(Slot *sl, int dir, int n) {
-    auto key = std::make_pair(dir, n);
-    auto it = sl->graphs.find(key);
-    if (it == sl->graphs.end()) {
-        RC_TRY(run_batch(sl, dir, n));  // eager first run: kernel attributes, module loading
-        cudaGraph_t g = nullptr;
-        CU_TRY(cudaStreamBeginCapture(sl->st, cudaStreamCaptureModeThreadLocal));
-        const int rc = run_batch(sl, dir, n);
-        const cudaError_t e = cudaStreamEndCapture(sl->st, &g);
-        if (rc != CUNUSHT_OK) {
-            if (g) cudaGraphDestroy(g);
-            return rc;
-        }
-        CU_TRY(e);
-        cudaGraphExec_t ex = nullptr;
-        const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
-        cudaGraphDestroy(g);
-        CU_TRY(ei);
-        it = sl->graphs.emplace(key, ex).first;
-    }
-    CU_TRY(cudaGraphLaunch(it->second, sl->st));
+    RC_TRY(capture_graph(sl, dir, n));
+    CU_TRY(cudaGraphLaunch(sl->graphs.at(std::make_pair(dir, n)), sl->st));
     return CUNUSHT_OK;
 }
 
@@ -213,33 +236,54 @@ int launch(cunusht_server_s *S, Slot *sl, std::deque<Req> &q) {
     return CUNUSHT_OK;
 }
 
-// Release the buckets other than keep whose queue is empty and whose slots
-// have nothing in flight; true if any was released.
-bool release_idle(cunusht_server_s *S, const Key &keep) {
-    bool released = false;
-    for (auto it = S->buckets.begin(); it != S->buckets.end();) {
-        bool idle = S->queues[it->first].empty();
-        for (auto &s : it->second.slots) idle = idle && s->busy.empty();
-        if (idle && it->first != keep) {
-            it = S->buckets.erase(it);
-            released = true;
-        } else {
-            ++it;
-        }
+// Release idle buckets other than keep (empty queue, nothing in flight),
+// least recently used first, until at least free bytes are released; release
+// nothing and return false if all the idle buckets together hold less.
+bool release_lru(cunusht_server_s *S, const Key &keep, size_t free) {
+    std::vector<std::pair<long long, Key>> idle;
+    for (auto &b : S->buckets) {
+        if (b.first == keep || !S->queues[b.first].empty()) continue;
+        bool busy = false;
+        for (auto &s : b.second.slots) busy = busy || !s->busy.empty();
+        if (!busy) idle.emplace_back(S->last_use[b.first], b.first);
     }
-    return released;
+    std::sort(idle.begin(), idle.end());
+    std::vector<Key> chosen;
+    size_t got = 0;
+    for (auto &c : idle) {
+        if (got >= free) break;
+        chosen.push_back(c.second);
+        for (auto &s : S->buckets[c.second].slots) got += s->bytes;
+    }
+    if (got < free) return false;
+    for (auto &k : chosen) {
+        S->buckets.erase(k);
+        S->evictions += 1;
+    }
+    return true;
 }
 
-int admit(cunusht_server_s *S, const Key &k, bool &ok) {
+void refuse(cunusht_server_s *S, const Key &k) {
+    if (S->refused.insert(k).second) S->refusals += 1;  // one count per refused episode
+}
+
+// Slots for bucket k within the budget.  Once a bucket's size is known
+// (measured when its slots were first made), a bucket that does not fit
+// releases idle buckets, least recently used first and only as many as it
+// needs, or none when all the idle ones together would not make room, and
+// waits; the size check comes before any allocation.  evict = false
+// (prewarm) releases nothing.
+int admit(cunusht_server_s *S, const Key &k, bool &ok, bool evict = true) {
     ok = S->buckets.count(k) > 0;
     if (ok) return CUNUSHT_OK;
     size_t used = S->used();
-    auto bl = S->blocked.find(k);
-    if (bl != S->blocked.end() && used >= bl->second) {
-        // nothing released since the last refusal: release the buckets that
-        // have gone idle since then (a refusal while they were busy released
-        // nothing), or keep waiting if none has
-        if (!release_idle(S, k)) return CUNUSHT_OK;
+    auto sz = S->sizes.find(k);
+    if (sz != S->sizes.end() && (double)(used + sz->second) > S->budget) {
+        const size_t free = (size_t)((double)(used + sz->second) - S->budget) + 1;
+        if (!evict || !release_lru(S, k, free)) {
+            refuse(S, k);
+            return CUNUSHT_OK;
+        }
         used = S->used();
     }
     const auto pol = S->policy_of(std::get<0>(k));
@@ -251,17 +295,20 @@ int admit(cunusht_server_s *S, const Key &k, bool &ok) {
             cudaGetLastError();  // an allocation failure is a refusal, not an error
             break;
         }
-        if ((double)(used + add + sl->bytes) > S->budget) break;
+        if ((double)(used + add + sl->bytes) > S->budget) {
+            S->sizes[k] = (size_t)pol.second * sl->bytes;  // known for the next attempt
+            break;
+        }
         add += sl->bytes;
         b.slots.push_back(std::move(sl));
     }
     if (b.slots.empty()) {
-        S->refusals += 1;
-        S->blocked[k] = used;
-        release_idle(S, k);
+        refuse(S, k);
         return CUNUSHT_OK;
     }
-    S->blocked.erase(k);
+    S->refused.erase(k);
+    S->sizes[k] = add;
+    S->last_use[k] = S->launches;
     S->buckets.emplace(k, std::move(b));
     ok = true;
     return CUNUSHT_OK;
@@ -334,7 +381,10 @@ int cunusht_server_poll(cunusht_server_t *S, int64_t *done_ids, int max_ids, int
         RC_TRY(admit(S, kq.first, ok));
         if (!ok) continue;
         for (auto &sl : S->buckets[kq.first].slots)
-            if (!q.empty() && sl->busy.empty()) RC_TRY(launch(S, sl.get(), q));
+            if (!q.empty() && sl->busy.empty()) {
+                RC_TRY(launch(S, sl.get(), q));
+                S->last_use[kq.first] = S->launches;
+            }
     }
     for (auto &kq : S->queues) npend += (int)kq.second.size();
     for (auto &b : S->buckets)
@@ -355,9 +405,29 @@ int cunusht_server_stats(cunusht_server_t *S, double *stats, int n) {
     ARG_CHECK(S != nullptr && stats != nullptr, "NULL argument");
     int nslots = 0;
     for (auto &b : S->buckets) nslots += (int)b.second.slots.size();
-    const double v[6] = {(double)S->launches, (double)S->completed, (double)S->used(), (double)S->buckets.size(),
-                         (double)nslots, (double)S->refusals};
-    for (int i = 0; i < n && i < 6; ++i) stats[i] = v[i];
+    const double v[7] = {(double)S->launches, (double)S->completed, (double)S->used(), (double)S->buckets.size(),
+                         (double)nslots, (double)S->refusals, (double)S->evictions};
+    for (int i = 0; i < n && i < 7; ++i) stats[i] = v[i];
+    return CUNUSHT_OK;
+}
+
+int cunusht_server_prewarm(cunusht_server_t *S, int lmax, int spin, double eps, int nphi, int *admitted) {
+    clear_error();
+    ARG_CHECK(S != nullptr, "server is NULL");
+    ARG_CHECK(lmax >= 1 && lmax <= 4095, "lmax must be in [1, 4095], got %d", lmax);
+    ARG_CHECK(spin >= 0 && spin <= 2, "spin must be 0, 1 or 2");
+    if (nphi <= 0) nphi = 2 * lmax + 1;
+    const Key k(lmax, spin, eps, nphi);
+    bool ok = false;
+    RC_TRY(admit(S, k, ok, false));
+    if (admitted) *admitted = ok ? 1 : 0;
+    if (!ok) return CUNUSHT_OK;
+    for (auto &sl : S->buckets[k].slots) {
+        if (!sl->busy.empty()) continue;  // a slot with work in flight keeps capturing lazily
+        for (int dir = 0; dir < 2; ++dir)
+            for (int n = 1; n <= sl->cap; ++n) RC_TRY(capture_graph(sl.get(), dir, n));
+    }
+    CU_TRY(cudaDeviceSynchronize());
     return CUNUSHT_OK;
 }
 

@@ -9,19 +9,23 @@ call of :meth:`LensingServer.step` retires the launches whose completion
 events have fired and fills every idle slot with the requests waiting in its
 bucket's queue, so requests that arrive while others are on the GPU are
 admitted as soon as a slot frees up, and launches of different slots and
-buckets overlap on the device.
+buckets overlap on the device.  Slots of smaller lmax run on streams of
+higher priority (slot_priority), so short launches are not queued behind the
+blocks of long ones.
 
 A launch is one CUDA-graph replay: lensing requests of a bucket go up to
 ``max_batch`` per launch through cunusht_lensing_batch, delensing requests
 through cunusht_delensing_batch (on the mixed path one shared Legendre
-recursion per launch of up to eight requests forward, on the tensor cores,
-and up to four in the adjoint).  The graph of each (slot, direction, batch
-size) is captured on first use; the request's inputs are copied into the
-slot's static buffers before the replay and its result copied out after.
+recursion per launch of up to eight requests, on the tensor cores, in both
+directions).  The graph of each (slot, direction, batch size) is captured on
+first use, or for every batch size ahead of traffic by prewarm(graphs=True);
+the request's inputs are copied into the slot's static buffers before the
+replay and its result copied out after.
 
-Admission: a bucket's slots are created when the bucket first has work and
-only if the device memory they take (measured) stays within the HBM budget;
-otherwise idle buckets are released and the bucket waits.
+Admission: a bucket's slots are created when the bucket first has work (or
+by prewarm) and only if the device memory they take (measured) stays within
+the HBM budget; otherwise idle buckets are released, least recently used
+first and only as many as it needs, or the bucket waits.
 
 The reference has no serving layer: its transformers process one call at a
 time with device-wide synchronisation (cunusht/helper_GPU.py:27-51).
@@ -58,13 +62,23 @@ class Request:
     t_done: Optional[float] = None
 
 
+def slot_priority(lmax: int) -> int:
+    """CUDA stream priority of a bucket's slots (lower is higher): the smaller
+    the transform, the higher the priority, so that a short launch takes the
+    SMs that free up while long launches of larger lmax are resident instead of
+    waiting behind their thousands of blocks.  lmax <= 1023: two levels above
+    the default, 2047: one, larger: the default.  torch maps values outside
+    the device's range to its nearest end."""
+    return -2 if lmax <= 1023 else (-1 if lmax <= 2047 else 0)
+
+
 class _Slot:
     """Plan + batch workspace + static buffers + stream; one launch in flight."""
 
     def __init__(self, lmax, spin, eps, max_batch, nphi, precision, graphs):
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]
-        self.stream = torch.cuda.Stream()
+        self.stream = torch.cuda.Stream(priority=slot_priority(lmax))
         self.spin = spin
         self.max_batch = max_batch
         self.use_graphs = graphs
@@ -101,12 +115,34 @@ class _Slot:
             return
         g = self.graphs.get((kind, n))
         if g is None:
-            self._work(kind, n)             # eager run first: kernel attributes, lazy module loading
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-                self._work(kind, n)
-            self.graphs[(kind, n)] = g
+            g = self.capture(kind, n)
         g.replay()
+
+    def capture(self, kind, n):
+        """Capture the (kind, n) graph on the slot's stream (the caller holds
+        torch.cuda.stream(self.stream)).  An eager run comes first (kernel
+        attributes, lazy module loading).  capture_begin / capture_end rather
+        than the torch.cuda.graph context: that one synchronises the whole
+        device on entry, which would stall every other slot's launches."""
+        self._work(kind, n)
+        g = torch.cuda.CUDAGraph()
+        g.capture_begin(capture_error_mode="thread_local")
+        try:
+            self._work(kind, n)
+        finally:
+            g.capture_end()
+        self.graphs[(kind, n)] = g
+        return g
+
+    def prewarm_graphs(self):
+        """Capture the graphs of both directions and every batch size."""
+        if not self.use_graphs:
+            return
+        with torch.cuda.stream(self.stream):
+            for kind in ("g2l", "l2g"):
+                for n in range(1, self.max_batch + 1):
+                    if (kind, n) not in self.graphs:
+                        self.capture(kind, n)
 
 
 class LensingServer:
@@ -127,7 +163,10 @@ class LensingServer:
         self.completed: list[Request] = []
         self.launches = 0
         self.rejected_admissions = 0
-        self._blocked: dict[tuple, int] = {}
+        self.evictions = 0
+        self._sizes: dict[tuple, int] = {}       # measured device bytes of each bucket's slots
+        self._last_use: dict[tuple, float] = {}  # server clock of each bucket's last launch
+        self._refused: set = set()
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -136,14 +175,21 @@ class LensingServer:
     def used_bytes(self) -> int:
         return sum(sl.bytes for slots in self.buckets.values() for sl in slots)
 
-    def _admit(self, key) -> bool:
+    def _admit(self, key, evict: bool = True) -> bool:
+        """Slots for bucket key within the HBM budget.  Once a bucket's size is
+        known (measured when its slots were first made), a bucket that does
+        not fit releases idle buckets (empty queue, nothing in flight), least
+        recently used first and only as many as it needs, or none when all the
+        idle ones together would not make room; it then waits and retries on
+        later steps, where the size check comes before any allocation.  With
+        evict=False (prewarm) nothing is released."""
         if key in self.buckets:
             return True
         used = self.used_bytes()
-        if key in self._blocked and used >= self._blocked[key]:
-            # nothing was released since the last refusal: release the buckets
-            # that have gone idle since then, or keep waiting if none has
-            if not self._evict_idle(keep=key):
+        need = self._sizes.get(key)
+        if need is not None and used + need > self.budget:
+            if not (evict and self._evict_lru(keep=key, free=used + need - self.budget)):
+                self._refuse(key)
                 return False
             torch.cuda.empty_cache()
             used = self.used_bytes()
@@ -157,33 +203,62 @@ class LensingServer:
                 break
             slots.append(sl)
             if used + sum(s.bytes for s in slots) > self.budget:
+                self._sizes[key] = nslots * sl.bytes  # known for the next attempt
                 slots.pop()
                 del sl
                 break
         if not slots:
-            self.rejected_admissions += 1
-            self._blocked[key] = used
-            self._evict_idle(keep=key)
+            self._refuse(key)
             torch.cuda.empty_cache()
             return False
-        self._blocked.pop(key, None)
+        self._refused.discard(key)
+        self._sizes[key] = sum(s.bytes for s in slots)
+        self._last_use[key] = self.now()
         self.buckets[key] = slots
         return True
 
-    def _evict_idle(self, keep) -> bool:
-        """Release the buckets other than keep with an empty queue and no launch
-        in flight; True if any was released."""
-        released = False
-        for k in list(self.buckets):
-            if k != keep and not self.queues[k] and all(not sl.busy for sl in self.buckets[k]):
-                del self.buckets[k]
-                released = True
-        return released
+    def _refuse(self, key):
+        if key not in self._refused:  # one count per refused episode, not per step
+            self._refused.add(key)
+            self.rejected_admissions += 1
 
-    def prewarm(self, keys) -> list:
-        """Create the slots of these buckets ahead of traffic (within the
-        budget); returns the keys admitted."""
-        return [k for k in keys if self._admit(tuple(k))]
+    def _evict_lru(self, keep, free: int) -> bool:
+        """Release idle buckets other than keep, least recently used first,
+        until at least free bytes are released; release nothing and return
+        False if all the idle buckets together hold less."""
+        idle = [k for k in self.buckets
+                if k != keep and not self.queues[k] and all(not sl.busy for sl in self.buckets[k])]
+        idle.sort(key=lambda k: self._last_use.get(k, 0.0))
+        chosen, got = [], 0
+        for k in idle:
+            if got >= free:
+                break
+            chosen.append(k)
+            got += sum(sl.bytes for sl in self.buckets[k])
+        if got < free:
+            return False
+        for k in chosen:
+            del self.buckets[k]
+            self.evictions += 1
+        return True
+
+    def prewarm(self, keys, graphs: bool = False) -> list:
+        """Create the slots of these buckets ahead of traffic, in order, while
+        they fit the budget (releasing none), and with graphs capture every
+        (direction, batch size) graph of their slots; returns the keys
+        admitted.  The others are admitted on first use."""
+        admitted = []
+        for k in keys:
+            k = tuple(k)
+            if not self._admit(k, evict=False):
+                continue
+            admitted.append(k)
+            if graphs:
+                for sl in self.buckets[k]:
+                    sl.prewarm_graphs()
+        if graphs:
+            torch.cuda.synchronize()
+        return admitted
 
     # ------------------------------------------------------------------ API
     def submit(self, kind, lmax, spin, epsilon, data, dlm_scaled, arrival=None) -> Request:
@@ -222,6 +297,7 @@ class LensingServer:
             for sl in self.buckets[key]:
                 if q and not sl.busy:
                     self._launch(sl, q)
+                    self._last_use[key] = self.now()
         return pending or self.busy()
 
     def _launch(self, sl: _Slot, q: collections.deque):
@@ -303,6 +379,24 @@ class NativeLensingServer:
         # requests with callable payloads wait here until their bucket has room
         self.waiting: dict[tuple, collections.deque] = collections.defaultdict(collections.deque)
         self.inflight: dict[tuple, int] = collections.defaultdict(int)
+
+    def prewarm(self, keys, graphs: bool = True) -> list:
+        """Admit these buckets (lmax, spin, epsilon) ahead of traffic on the
+        package's default GL geometry and capture every (direction, batch
+        size) graph of their slots (cunusht_server_prewarm); returns the keys
+        admitted.  Without graphs the buckets are admitted on first use."""
+        from . import _lib
+        if not graphs:
+            return list(keys)
+        out = []
+        for k in keys:
+            lmax, spin, eps = int(k[0]), int(k[1]), float(k[2])
+            ok = self._c.c_int()
+            _lib.check(self._lib.cunusht_server_prewarm(self._srv, lmax, spin, eps, _default_nphi(lmax),
+                                                        self._c.byref(ok)))
+            if ok.value:
+                out.append(tuple(k))
+        return out
 
     def _cap(self, lmax: int) -> int:
         """Requests of one bucket handed to the library at a time: two full
@@ -389,9 +483,9 @@ class NativeLensingServer:
 
     def stats(self) -> dict:
         from . import _lib
-        v = (self._c.c_double * 6)()
-        _lib.check(self._lib.cunusht_server_stats(self._srv, v, 6))
-        return dict(zip(["launches", "completed", "bytes", "buckets", "slots", "refusals"], list(v)))
+        v = (self._c.c_double * 7)()
+        _lib.check(self._lib.cunusht_server_stats(self._srv, v, 7))
+        return dict(zip(["launches", "completed", "bytes", "buckets", "slots", "refusals", "evictions"], list(v)))
 
     def close(self):
         if getattr(self, "_srv", None):

@@ -106,11 +106,24 @@ int cunusht_plan_set_mmax(cunusht_plan_t *plan, int mmax);
  * Bluestein ring transforms above 4096 pixels per ring) run as two
  * half-length transforms split by output parity.  force = 1 selects that
  * split form for every transform of the plan, so that it can be checked
- * against the direct form at small sizes; force = 0 restores the automatic
+ * against the direct form at small sizes (the ring transforms then run
+ * Bluestein, the form that has a split); force = 0 restores the automatic
  * choice.  No reference counterpart (the reference delegates its FFTs to
  * cuFFT / cuFINUFFT).
  */
 int cunusht_plan_force_split(cunusht_plan_t *plan, int force);
+
+/*
+ * Ring transform of the pointing geometry (the phi FFT inside SHTns
+ * synth_grad, GPU_sht_transformer.py:95).  method 0 (default): rings of one
+ * length N <= 8192 whose prime factors are at most 13 (e.g. the 4095-pixel
+ * Gauss-Legendre rings of lmax 2047, power-of-two rings) run a mixed-radix
+ * FFT of N points; every other geometry runs Bluestein.  method 1: Bluestein
+ * for every ring length (for comparisons).  cunusht_plan_ring_transform
+ * returns 0 when the plan's rings run the mixed-radix form, 1 for Bluestein.
+ */
+int cunusht_plan_set_ring_transform(cunusht_plan_t *plan, int method);
+int cunusht_plan_ring_transform(const cunusht_plan_t *plan);
 
 /*
  * Mixed precision: the Legendre synthesis (CC synthesis of spin 0 / 1 / 2
@@ -265,7 +278,15 @@ int cunusht_dlm2pointing(cunusht_plan_t *plan, const void *dlm_scaled, const voi
  * One host thread drives a server.  Default policy: lmax >= 4095: 1 request
  * per launch, 1 slot; >= 2047: 4, 2; else 8, 2 (cunusht_server_set_policy).
  * cunusht_server_stats: [launches, completed, bytes in use, buckets, slots,
- * refused admissions].
+ * refused admissions, evicted buckets].  A bucket that does not fit releases
+ * idle buckets (empty queue, nothing in flight), least recently used first
+ * and only as many as it needs once its size is known, or none, and waits.
+ * cunusht_server_prewarm: admits the bucket (lmax, spin, eps, nphi) ahead of
+ * traffic and captures the graphs of both directions and every batch size up
+ * to its requests per launch on each of its slots (one eager run and one
+ * capture each, on zeroed inputs), so that no launch of the served stream
+ * pays for a capture; *admitted = 0 when the bucket does not fit the budget.
+ * Returns after the device has finished the warm-up work.
  */
 typedef struct cunusht_server_s cunusht_server_t;
 int cunusht_server_create(cunusht_server_t **server, double hbm_budget_bytes, int precision);
@@ -275,6 +296,7 @@ int cunusht_server_submit(cunusht_server_t *server, int direction, int lmax, int
                           int64_t *request_id);
 int cunusht_server_poll(cunusht_server_t *server, int64_t *done_ids, int max_ids, int *ndone, int *pending);
 int cunusht_server_stats(cunusht_server_t *server, double *stats, int n);
+int cunusht_server_prewarm(cunusht_server_t *server, int lmax, int spin, double eps, int nphi, int *admitted);
 int cunusht_server_destroy(cunusht_server_t *server);
 
 /*

@@ -237,3 +237,52 @@ def test_server_admits_after_refusal_while_busy(built_lib, native):
     assert refusals >= 1  # the second bucket was refused while the first ran
     if native:
         srv.close()
+
+
+@pytest.mark.parametrize("native", [False, True])
+def test_server_prewarmed_graphs_match_lazy_capture(built_lib, native):
+    """Buckets prewarmed with every (direction, batch size) graph captured
+    ahead of traffic (zeroed inputs) give the results of a server that
+    captures on first use: lensing to 1e-12, delensing (floating-point
+    spreading atomics) to a tenth of epsilon."""
+    import cunusht_gb300 as cu
+    from cunusht_gb300.serving import LensingServer, NativeLensingServer
+    lmax, eps = 63, 1e-7
+    keys = [(lmax, 0, eps), (lmax, 2, eps)]
+
+    def make():
+        if native:
+            return NativeLensingServer(precision="mixed", policy={lmax: (3, 2)})
+        return LensingServer(max_batch=3, precision="mixed")
+
+    rng = np.random.default_rng(21)
+    npix = cu.get_geom(("gl", {"lmax": lmax})).npix()
+    work = []
+    for i in range(8):
+        spin = keys[i % 2][1]
+        kind = "l2g" if i % 3 == 2 else "g2l"
+        gc, dl = orc.make_inputs(lmax, spin, seed=500 + i)
+        d = torch.as_tensor(dl[0], device="cuda")
+        data = torch.as_tensor(gc if spin else gc[0], device="cuda") if kind == "g2l" else \
+            torch.as_tensor(rng.standard_normal((2, npix) if spin else npix), device="cuda")
+        work.append((kind, spin, data, d))
+    results = []
+    for pre in (False, True):
+        srv = make()
+        if pre:
+            assert srv.prewarm(keys, graphs=True) == keys
+            if not native:
+                for k in keys:
+                    for sl in srv.buckets[k]:
+                        assert len(sl.graphs) == 2 * sl.max_batch
+        reqs = [srv.submit(kind, lmax, spin, eps, data, d) for kind, spin, data, d in work]
+        srv.run_until_idle()
+        torch.cuda.synchronize()
+        results.append([r.result.clone() for r in reqs])
+        if native:
+            srv.close()
+        del srv
+    for (kind, spin, data, d), a, b in zip(work, *results):
+        scale = float(torch.max(torch.abs(a)))
+        tol = 1e-12 if kind == "g2l" else 0.1 * eps
+        assert float(torch.max(torch.abs(a - b))) <= tol * scale, (kind, spin)

@@ -123,3 +123,30 @@ def test_submit_rejects_unknown_direction(fake_server):
     srv = fake_server(100, lambda lmax: (1, 1))
     with pytest.raises(ValueError):
         srv.submit("both", 511, 0, 1e-5, None, None)
+
+
+def test_lru_release_frees_only_what_the_new_bucket_needs(fake_server):
+    """Four idle lmax-511 buckets (20 each) hold 80 of a 100 budget; an
+    lmax-1023 bucket (2 slots of 40) does not fit even one slot, is refused
+    once (its size becomes known), then releases the three least recently
+    used 511 buckets (60 >= 60 needed) and no more."""
+    srv = fake_server(100, lambda lmax: (4, 2))
+    small = [(511, 0, 1e-5), (511, 2, 1e-7), (511, 0, 1e-7), (511, 2, 1e-5)]
+    for k in small:                            # used in this order
+        srv.submit("g2l", *k, None, None)
+        _drain(srv)
+    srv.submit("g2l", 1023, 2, 1e-7, None, None)
+    _drain(srv)
+    assert len(srv.completed) == 5
+    assert srv.rejected_admissions == 1
+    assert srv.evictions == 3
+    assert set(srv.buckets) == {small[3], (1023, 2, 1e-7)}
+    assert srv.used_bytes() <= 100
+
+
+def test_prewarm_admits_in_order_and_releases_nothing(fake_server):
+    srv = fake_server(100, lambda lmax: (4, 2))
+    keys = [(1023, 0, 1e-5), (511, 0, 1e-5), (1023, 2, 1e-7)]
+    assert srv.prewarm(keys) == keys[:2]       # 80 + 20; the second 1023 bucket waits
+    assert srv.evictions == 0
+    assert set(srv.buckets) == set(keys[:2])
