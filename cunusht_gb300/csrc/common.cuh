@@ -194,8 +194,8 @@ struct cunusht_plan_s {
     // recursion starts of the tensor-core synthesis per [grid: 0 GL, 1 CC][spin]: for every
     // (m, side, pair) the start value (hi, lo) and its exponent / 96, built at plan creation
     // (NULL: the kernel evaluates the start itself)
-    float2 *d_tc_stv[2][3] = {};
-    short *d_tc_ste[2][3] = {};
+    float4 *d_tc_stv[2][3] = {};
+    short2 *d_tc_ste[2][3] = {};
 
     // FFT twiddles e^{-2 pi i t / TW}
     int TW = 0;

@@ -48,14 +48,16 @@ int leg_adj_df_pairs(const cunusht_plan_s *P, int nreq, int spin, int ncomp, con
 size_t adj_tc_scratch_bytes(const cunusht_plan_s *P, int nreq);
 int leg_adjoint_tc(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
                    int ld, int npairs, const double *x, const double *sh, const double *ch, const int *rn,
-                   const int *rs, int pole, int pole_rn, int pole_rs, const float2 *stv, const short *ste,
+                   const int *rs, int pole, int pole_rn, int pole_rs, const float4 *stv, const short2 *ste,
                    const double *lf, double2 *G, double2 *C, long long astride, void *scratch, cudaStream_t st);
 
+// first chunk of a ring that never reaches the accumulated range (start tables, k_tc_starts)
+constexpr short TC_NEVER = 32767;
 // legendre_tc.cu: tensor-core synthesis (mixed precision, every spin), nb in {1, 2, 4, 8};
 // stv / ste: the plan's recursion-start table of the grid and spin (row stride npairs), or NULL
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
                       const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
-                      const float2 *stv, const short *ste, int spin, const double2 *G,
+                      const float4 *stv, const short2 *ste, int spin, const double2 *G,
                       const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
                       cudaStream_t st);
 int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout);

@@ -1075,8 +1075,8 @@ struct RingPairs {
     int ld;
     int pole = -1;  // pair (theta = 0, pi), or -1
     int pole_rn = 0, pole_rs = 0;  // its ring indices
-    const float2 *const *stv = nullptr;  // tensor-core recursion starts per spin (or NULL)
-    const short *const *ste = nullptr;
+    const float4 *const *stv = nullptr;  // tensor-core recursion starts per spin (or NULL)
+    const short2 *const *ste = nullptr;
 };
 
 static RingPairs pairs_of(const cunusht_plan_s *P, bool cc) {

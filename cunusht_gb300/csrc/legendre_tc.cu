@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
                         const double *__restrict__ lg0, int npairs,
                         const double *__restrict__ px, const double *__restrict__ psh,
                         const double *__restrict__ pch, const int *__restrict__ prn, const int *__restrict__ prs,
-                        const float2 *__restrict__ stv, const short *__restrict__ ste, int st_ld,
+                        const float4 *__restrict__ stv, const short2 *__restrict__ ste, int st_ld,
                         double2 *__restrict__ H, long long hstride, int ldH, int *status) {
     using LY = TclLayout<NB>;
     constexpr int NO = LY::NO, NN = LY::NN, NG = LY::NG, T = LY::T, NT = LY::NT;
@@ -441,6 +441,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
     const int l0 = max(m, spin);
     const unsigned char *recm = rec + (size_t)woff[m] * LY::RSZ;  // this order's window records
 
+    int *s_c0 = reinterpret_cast<int *>(sm + LY::OFF_TM + 8);
     if (warp == T / 32) tmem_alloc(sbase + LY::OFF_TM, LY::NCOLS);
     if (tid == 0) {
         mbar_init(full0, T / 32);
@@ -450,17 +451,55 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
         mbar_init(rbar0, 1);
         mbar_init(rbar0 + 8, 1);
         *s_bad = 0;
+        *s_c0 = TC_NEVER;
         mbar_init_fence();
     }
     // B' positions with g - i outside [0, 3] and the padding rows stay zero for the whole kernel
     for (int i = tid; i < 2 * LY::BBUF / 16; i += LY::BLOCK)
         reinterpret_cast<uint4 *>(sm + LY::OFF_B)[i] = make_uint4(0u, 0u, 0u, 0u);
+
+    // ring threads: this ring's recursion state at its first accumulated chunk c_me
+    // (the plan's table), or the start at l0 (c_me = 0)
+    const bool ring_thread = warp < T / 32;
+    const int side = S0 ? 0 : tid / (T / 2);  // 0: ring theta, 1: ring pi - theta
+    const int p = S0 ? blockIdx.x * T + tid : blockIdx.x * (T / 2) + tid % (T / 2);
+    const bool act = ring_thread && p < npairs;
+    dfl cur{0.f, 0.f}, prev{0.f, 0.f};
+    int e = 0, c_me = TC_NEVER;
+    if (act) {
+        if (stv) {
+            const size_t ix = ((size_t)m * 2 + side) * st_ld + p;
+            const float4 v = stv[ix];
+            const short2 ec = ste[ix];
+            cur = dfl{v.x, v.y};
+            prev = dfl{v.z, v.w};
+            e = 96 * (int)ec.x;
+            c_me = ec.y;
+        } else {
+            const double sh = psh[p], ch = pch[p];
+            if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
+            else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
+            c_me = 0;
+        }
+    }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *s_tm;
-    if (tid == 0 && l0 <= L) bulk_g2s(sbase + LY::OFF_R, recm, LY::RSZ, rbar0);  // record of window 0
+    {
+        const int cm = __reduce_min_sync(0xffffffffu, c_me);
+        if (lane == 0 && ring_thread && cm < TC_NEVER) atomicMin(s_c0, cm);
+    }
+    __syncthreads();
+    // the block starts at the first chunk in which any of its rings accumulates:
+    // window kw0, chunk cs0 of it; nothing to do when no ring ever does
+    const int nchk = l0 <= L ? (L - l0 + 1 + TCL_KC - 1) / TCL_KC : 0;
+    const int cb = *s_c0;
+    const bool work = cb < nchk;
+    constexpr int CPW = TCL_W / TCL_KC;  // chunks per window
+    const int kw0 = work ? cb / CPW : 0, cs0 = cb - kw0 * CPW;
+    if (tid == 0 && work) bulk_g2s(sbase + LY::OFF_R, recm + (size_t)kw0 * LY::RSZ, LY::RSZ, rbar0);
 
     if (warp == T / 32) {
         // ---------------- MMA warp: the whole warp follows the chunk sequence (its
@@ -468,9 +507,11 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
         constexpr uint32_t IDESC = idesc_bf16_f32(128, NN);
         int gc = 0;
         bool ok = true;
-        for (int wb = l0; wb <= L && ok; wb += TCL_W) {
+        for (int kw = kw0; work && l0 + kw * TCL_W <= L && ok; ++kw) {
+            const int wb = l0 + kw * TCL_W;
             const int nch = (min(TCL_W, L - wb + 1) + TCL_KC - 1) / TCL_KC;
-            for (int c = 0; c < nch; ++c, ++gc) {
+            const int cs = kw == kw0 ? cs0 : 0;
+            for (int c = cs; c < nch; ++c, ++gc) {
                 const int buf = gc & 1;
                 const bool got = !*s_bad && mbar_wait(full0 + 8 * buf, (gc >> 1) & 1);
                 if (!__all_sync(0xffffffffu, got)) {
@@ -486,7 +527,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
 #pragma unroll
                         for (int k = 0; k < 4; ++k)  // K-step k: digit k of lambda, 16 l
                             tc_mma(tbase + t * NN, sdesc(aa + t * TCL_TILE + k * 256, 128, TCL_SBO),
-                                   sdesc(ba + k * 256, 128, TCL_SBO), IDESC, (c > 0 || k > 0) ? 1u : 0u);
+                                   sdesc(ba + k * 256, 128, TCL_SBO), IDESC, (c > cs || k > 0) ? 1u : 0u);
                     tc_commit(empty0 + 8 * buf);
                 }
                 __syncwarp();
@@ -496,45 +537,27 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
         __syncwarp();
     } else {
         // ---------------- ring warps
-        const int side = S0 ? 0 : tid / (T / 2);  // 0: ring theta, 1: ring pi - theta
         const int tile = tid >> 7, row = tid & 127;
-        const int p = S0 ? blockIdx.x * T + tid : blockIdx.x * (T / 2) + tid % (T / 2);
-        const bool act = p < npairs;
         const double x = act ? px[p] : 0.0;
         const dfl xd = df_from(side ? -x : x);
-        dfl cur{0.f, 0.f}, prev{0.f, 0.f};
-        int e = 0;
-        if (stv) {
-            // the plan's table: the same values as rec_start_df, without its FP64
-            // logarithms and powers (one block per SM would wait for them)
-            if (act) {
-                const size_t ix = ((size_t)m * 2 + side) * st_ld + p;
-                const float2 v = stv[ix];
-                cur = dfl{v.x, v.y};
-                e = 96 * (int)ste[ix];
-            }
-        } else {
-            const double sh = act ? psh[p] : 0.0, ch = act ? pch[p] : 1.0;
-            if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
-            else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
-        }
         sum2 acc[NO];
         const uint32_t t_lane = tbase + ((uint32_t)((warp & 3) * 32) << 16) + tile * NN;  // this thread's row
         const uint32_t a_row = (uint32_t)tile * TCL_TILE + (row >> 3) * TCL_SBO + (row & 7) * 16;
-        int gc = 0, kw = 0;
+        int gc = 0, kw = kw0, kl = 0;  // kl: windows processed (record buffer and barrier phase)
         int bad = 0;
 
-        for (int wb = l0; wb <= L; wb += TCL_W, ++kw) {
+        for (; work && l0 + kw * TCL_W <= L; ++kw, ++kl) {
+            const int wb = l0 + kw * TCL_W;
             const int cnt = min(TCL_W, L - wb + 1);
             // prefetch the next window's record into the other buffer (its readers
             // finished at the previous window's closing barrier)
             if (tid == 0 && wb + TCL_W <= L) {
                 fence_async_smem();
-                bulk_g2s(sbase + LY::OFF_R + ((kw + 1) & 1) * LY::RSZ, recm + (size_t)(kw + 1) * LY::RSZ, LY::RSZ,
-                         rbar0 + 8 * ((kw + 1) & 1));
+                bulk_g2s(sbase + LY::OFF_R + ((kl + 1) & 1) * LY::RSZ, recm + (size_t)(kw + 1) * LY::RSZ, LY::RSZ,
+                         rbar0 + 8 * ((kl + 1) & 1));
             }
-            bad |= !mbar_wait(rbar0 + 8 * (kw & 1), (kw >> 1) & 1);  // this window's record has landed
-            const unsigned char *Rw = sm + LY::OFF_R + (kw & 1) * LY::RSZ;
+            bad |= !mbar_wait(rbar0 + 8 * (kl & 1), (kl >> 1) & 1);  // this window's record has landed
+            const unsigned char *Rw = sm + LY::OFF_R + (kl & 1) * LY::RSZ;
             const unsigned short *s_tp = reinterpret_cast<const unsigned short *>(Rw);
             const float *s_sc = reinterpret_cast<const float *>(Rw + LY::RSC);
             const float lsc = *reinterpret_cast<const float *>(Rw + LY::RLS);
@@ -543,10 +566,10 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
             const float2 *s_be = reinterpret_cast<const float2 *>(Rw + LY::RBE);
 
             const int nch = (cnt + TCL_KC - 1) / TCL_KC;
-            float4 agn = s_ag[0];  // coefficients of the next step, loaded one step ahead
-            float2 ben = s_be[0];
-            for (int c = 0; c < nch; ++c, ++gc) {
+            for (int c = kw == kw0 ? cs0 : 0; c < nch; ++c, ++gc) {
                 const int buf = gc & 1;
+                // before its first chunk a ring holds its table state and writes zero digits
+                const bool live = kw * CPW + c >= c_me;
                 if (gc >= 2) bad |= !mbar_wait(empty0 + 8 * buf, ((gc - 2) >> 1) & 1);
                 unsigned char *sA = sm + buf * LY::ABUF;
                 unsigned char *sB = sm + LY::OFF_B + buf * LY::BBUF;
@@ -572,36 +595,44 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
                 // most (alpha + beta) < 2^8.5 (alpha_m ~ sqrt(2m) <= 181 for lmax <= 16383),
                 // so from below 2^40 eight steps stay below 2^108, inside the FP32
                 // range, and e (hence the digit mask) stays fixed within the half.
+                float4 agn = s_ag[c * TCL_KC];  // coefficients of the next step, loaded one step ahead
+                float2 ben = s_be[c * TCL_KC];
+                if (live) {
 #pragma unroll
-                for (int lh = 0; lh < 2; ++lh) {
-                    uint32_t pk[4][4];
-                    const float scg = (act && e == 0) ? lsc : 0.f;
+                    for (int lh = 0; lh < 2; ++lh) {
+                        uint32_t pk[4][4];
+                        const float scg = (act && e == 0) ? lsc : 0.f;
 #pragma unroll
-                    for (int j2 = 0; j2 < 4; ++j2) {
-                        float d0[4], d1[4];
-                        // digits of lambda_l (zero unless accumulated), then one recursion step l -> l + 1
-                        auto step = [&](int i, float(&d)[4]) {
-                            digits4s(cur.h, cur.l, i < cnt ? scg : 0.f, d);
-                            const float4 ag = agn;
-                            const float2 b2 = ben;
-                            agn = s_ag[i + 1];
-                            ben = s_be[i + 1];
-                            const dfl t = df_fma_u(dfl{ag.x, ag.y}, xd, dfl{ag.z, ag.w});
-                            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
-                            prev = cur;
-                            cur = nxt;
-                        };
-                        const int i0 = c * TCL_KC + 8 * lh + 2 * j2;
-                        step(i0, d0);
-                        step(i0 + 1, d1);
+                        for (int j2 = 0; j2 < 4; ++j2) {
+                            float d0[4], d1[4];
+                            // digits of lambda_l (zero unless accumulated), then one recursion step l -> l + 1
+                            auto step = [&](int i, float(&d)[4]) {
+                                digits4s(cur.h, cur.l, i < cnt ? scg : 0.f, d);
+                                const float4 ag = agn;
+                                const float2 b2 = ben;
+                                agn = s_ag[i + 1];
+                                ben = s_be[i + 1];
+                                const dfl t = df_fma_u(dfl{ag.x, ag.y}, xd, dfl{ag.z, ag.w});
+                                const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                                prev = cur;
+                                cur = nxt;
+                            };
+                            const int i0 = c * TCL_KC + 8 * lh + 2 * j2;
+                            step(i0, d0);
+                            step(i0 + 1, d1);
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+                            for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+                        }
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            *reinterpret_cast<uint4 *>(sA + a_row + (2 * k + lh) * 128) =
+                                make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
+                        REC_RESCALE_DF(cur, prev, e);
                     }
+                } else {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        *reinterpret_cast<uint4 *>(sA + a_row + (2 * k + lh) * 128) =
-                            make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
-                    REC_RESCALE_DF(cur, prev, e);
+                    for (int k = 0; k < 8; ++k)
+                        *reinterpret_cast<uint4 *>(sA + a_row + k * 128) = make_uint4(0u, 0u, 0u, 0u);
                 }
                 fence_async_smem();
                 __syncwarp();
@@ -653,7 +684,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
             if (tid == 0) {
                 if (status) atomicOr(status, 1);
                 // the record copy of the window after the last one entered may still be in flight
-                if (l0 + (kw + 1) * TCL_W <= L) mbar_wait(rbar0 + 8 * ((kw + 1) & 1), ((kw + 1) >> 1) & 1);
+                if (l0 + (kw + 1) * TCL_W <= L) mbar_wait(rbar0 + 8 * ((kl + 1) & 1), ((kl + 1) >> 1) & 1);
             }
         } else if (act && S0) {
             const int n = prn[p], s = prs[p];
@@ -693,7 +724,7 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
 
 template <int NB, bool S0>
 static int launch_synth_tc_nb(const cunusht_plan_s *P, int npairs, const double *x, const double *sh,
-                              const double *ch, const int *rn, const int *rs, const float2 *stv, const short *ste,
+                              const double *ch, const int *rn, const int *rs, const float4 *stv, const short2 *ste,
                               int st_ld, int ld, int spin, const double2 *G,
                               const double2 *C, long long astride, const double *lf, double2 *H, long long hstride,
                               cudaStream_t st) {
@@ -751,25 +782,67 @@ int tc_reserve(cunusht_plan_s *P, int nb) {
     return CUNUSHT_OK;
 }
 
-// Recursion starts of every (m, side, pair) of one grid and spin: the values
-// rec_start_df gives at the start of the synthesis kernels, evaluated once per
-// plan so that the synthesis blocks (one per SM) do not wait for FP64
-// logarithms and powers.  Entry ((m * 2 + side) * npairs + p); e / 96 is
-// clamped to the short range: a start below 2^(-96 * 32767) grows by less than
-// 2^8.5 per step and so never reaches the accumulated range within lmax steps.
-__global__ void k_tc_starts(int L, int spin, const double *__restrict__ lg0, int npairs, const double *__restrict__ sh,
-                            const double *__restrict__ ch, float2 *__restrict__ v, short *__restrict__ e96) {
+// Recursion start states of every (m, side, pair) of one grid and spin, built
+// once per plan.  A ring whose functions are still below the accumulated range
+// (the evanescent region sin(theta) < m / l, where lambda_lm decays like
+// exp(-l ...) towards the pole) contributes zero digits to every chunk before
+// the one where its exponent e reaches 0.  The table holds, per ring, that
+// first chunk c0 (16 l from l0 = max(m, s)) and the recursion state (cur,
+// prev, e) at its start, obtained by running the kernels' own double-float
+// steps (same coefficients, same operations, the exponent check after every 8
+// l) from rec_start_df.  The kernels start each ring there and each block at
+// the smallest c0 of its rings, so chunks in which no ring of a block
+// accumulates are neither recursed nor multiplied (about a fifth of the
+// (l, m, ring) volume at lmax 2047), with the same digits for the chunks that
+// are.  A ring whose start is exactly zero (a pole) gets c0 = 32767 (never).
+// Entry ((m * 2 + side) * npairs + p): v = (cur.h, cur.l, prev.h, prev.l),
+// ec = (e / 96, c0); e is 0 or -96 at a ring's first chunk.
+__device__ __forceinline__ void tc_rec_step(dfl &cur, dfl &prev, dfl xd, const float2 *__restrict__ coef,
+                                            long long nalm, long long ix) {
+    const float2 a2 = coef[ix], g2 = coef[nalm + ix], b2 = coef[2 * nalm + ix];
+    const dfl t = df_fma_u(dfl{a2.x, a2.y}, xd, dfl{g2.x, g2.y});
+    const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+    prev = cur;
+    cur = nxt;
+}
+
+__global__ void k_tc_starts(int L, int spin, const double *__restrict__ lg0, int npairs, const double *__restrict__ x,
+                            const double *__restrict__ sh, const double *__restrict__ ch,
+                            const float2 *__restrict__ coef, long long nalm, float4 *__restrict__ v,
+                            short2 *__restrict__ ec) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 2LL * npairs * (L + 1)) return;
     const int p = (int)(i % npairs);
     const long long ms = i / npairs;
     const int side = (int)(ms & 1), m = (int)(ms >> 1);
+    const int l0 = max(m, spin);
     dfl cur, prev;
     int e;
     if (side) rec_start_df(lg0[m], m, spin, ch[p], sh[p], cur, prev, e);
     else rec_start_df(lg0[m], m, spin, sh[p], ch[p], cur, prev, e);
-    v[i] = make_float2(cur.h, cur.l);
-    e96[i] = (short)max(e / 96, -32767);
+    const dfl xd = df_from(side ? -x[p] : x[p]);
+    const long long b = almidx(L, m, m) - m;  // (l, m) at b + l
+    const int nchk = l0 <= L ? (L - l0 + 1 + TCL_KC - 1) / TCL_KC : 0;
+    int c = 0;
+    for (; c < nchk && e != 0; ++c) {
+        // the chunk's first half accumulates only if e is 0 at its start; its
+        // second half if the check after the first 8 steps brings e to 0
+        const dfl c0 = cur, p0 = prev;
+        const int e0 = e, lb = l0 + TCL_KC * c;
+        for (int j = 0; j < 8; ++j)
+            if (lb + j <= L) tc_rec_step(cur, prev, xd, coef, nalm, b + lb + j);
+        REC_RESCALE_DF(cur, prev, e);
+        if (e == 0) {
+            cur = c0, prev = p0, e = e0;
+            break;
+        }
+        for (int j = 8; j < TCL_KC; ++j)
+            if (lb + j <= L) tc_rec_step(cur, prev, xd, coef, nalm, b + lb + j);
+        REC_RESCALE_DF(cur, prev, e);
+    }
+    const bool never = c >= nchk || (cur.h == 0.f && prev.h == 0.f);
+    v[i] = make_float4(cur.h, cur.l, prev.h, prev.l);
+    ec[i] = make_short2((short)(e / 96), never ? TC_NEVER : (short)c);
 }
 
 int tc_plan_init(cunusht_plan_s *P) {
@@ -777,15 +850,16 @@ int tc_plan_init(cunusht_plan_s *P) {
     // start tables: GL spin 1 (the pointing's synthesis) and spins 0 up to max_spin on both grids
     for (int g = 0; g < 2; ++g) {
         const int np = g ? P->cc_npairs : P->gl_npairs;
+        const double *x = g ? P->d_cc_x : P->d_gl_x;
         const double *sh = g ? P->d_cc_sh : P->d_gl_sh, *ch = g ? P->d_cc_ch : P->d_gl_ch;
         const int smax = g ? P->max_spin : std::max(P->max_spin, 1);
         for (int s = 0; s <= smax && s <= L && np > 0; ++s) {
             const size_t n = 2 * (size_t)np * (L + 1);
-            CU_TRY(cudaMalloc(&P->d_tc_stv[g][s], n * sizeof(float2)));
-            CU_TRY(cudaMalloc(&P->d_tc_ste[g][s], n * sizeof(short)));
-            P->ws_bytes += n * (sizeof(float2) + sizeof(short));
-            k_tc_starts<<<(unsigned)((n + 255) / 256), 256>>>(L, s, P->d_lg0[s], np, sh, ch, P->d_tc_stv[g][s],
-                                                             P->d_tc_ste[g][s]);
+            CU_TRY(cudaMalloc(&P->d_tc_stv[g][s], n * sizeof(float4)));
+            CU_TRY(cudaMalloc(&P->d_tc_ste[g][s], n * sizeof(short2)));
+            P->ws_bytes += n * (sizeof(float4) + sizeof(short2));
+            k_tc_starts<<<(unsigned)((n + 255) / 256), 256>>>(L, s, P->d_lg0[s], np, x, sh, ch, P->d_coef_df[s],
+                                                             P->nalm_tab, P->d_tc_stv[g][s], P->d_tc_ste[g][s]);
             CU_LAUNCH_CHECK();
         }
     }
@@ -917,7 +991,7 @@ __global__ void __launch_bounds__(POLE_TPB)
 // the double-float CUDA-core kernel instead of a nearly empty block per order m.
 int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,
                       const double *ch, const int *rn, const int *rs, int ld, int pole, int pole_rn, int pole_rs,
-                      const float2 *stv, const short *ste, int spin, const double2 *G, const double2 *C,
+                      const float4 *stv, const short2 *ste, int spin, const double2 *G, const double2 *C,
                       long long astride, const double *lf, double2 *H, long long hstride, cudaStream_t st) {
     const int st_ld = npairs;  // row stride of the start table: all pairs of the grid
     if (pole == 0 && npairs > 1) {

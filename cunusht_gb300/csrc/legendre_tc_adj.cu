@@ -77,8 +77,8 @@ struct TcAdjArgs {
     int st_ld = 0;       // row stride of the start tables
     const double *x = nullptr, *sh = nullptr, *ch = nullptr;
     const int *rn = nullptr, *rs = nullptr;
-    const float2 *stv = nullptr;
-    const short *ste = nullptr;
+    const float4 *stv = nullptr;
+    const short2 *ste = nullptr;
     float *hm = nullptr;
     unsigned long long *acc = nullptr;
 };
@@ -124,8 +124,8 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
     k_leg_adj_tc(int L, int spin, const double2 *__restrict__ H, long long hstride, int ldH,
                  const float2 *__restrict__ coef, long long nalm, const double *__restrict__ lg0, int npairs,
                  const double *__restrict__ px, const double *__restrict__ psh, const double *__restrict__ pch,
-                 const int *__restrict__ prn, const int *__restrict__ prs, const float2 *__restrict__ stv,
-                 const short *__restrict__ ste, int st_ld, const float *__restrict__ hm, int npairs_all,
+                 const int *__restrict__ prn, const int *__restrict__ prs, const float4 *__restrict__ stv,
+                 const short2 *__restrict__ ste, int st_ld, const float *__restrict__ hm, int npairs_all,
                  unsigned long long *__restrict__ acc, int *status) {
     constexpr int NO = 4 * NB;       // columns per ring
     constexpr int NROW = 4 * NO;     // used rows (digit j, column) of the 128
@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
     extern __shared__ __align__(1024) unsigned char sm[];
     uint32_t *s_tm = reinterpret_cast<uint32_t *>(sm + TCA_OFF_MISC);
     volatile int *s_bad = reinterpret_cast<volatile int *>(sm + TCA_OFF_MISC + 4);
+    int *s_c0 = reinterpret_cast<int *>(sm + TCA_OFF_MISC + 8);
     int *s_ea = reinterpret_cast<int *>(sm + TCA_OFF_MISC + 16);
     float *s_mx = reinterpret_cast<float *>(sm + TCA_OFF_MISC + 16 + 32 * 4);  // [ring warp][col]
     const uint32_t sbase = smem_u32(sm);
@@ -156,6 +157,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
             mbar_init(tempty0 + 8 * k, 4);
         }
         *s_bad = 0;
+        *s_c0 = TC_NEVER;
         mbar_init_fence();
     }
     // A rows >= NROW stay zero
@@ -167,6 +169,26 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
     const int side = S0 ? 0 : tid / (TCA_R / 2);  // 0: ring theta, 1: ring pi - theta
     const int p = S0 ? blockIdx.x * TCA_R + tid : blockIdx.x * (TCA_R / 2) + (tid & (TCA_R / 2 - 1));
     const bool act = ring_thread && p < npairs;
+    // this ring's recursion state at its first accumulated chunk c_me (the plan's
+    // table, legendre_tc.cu k_tc_starts), or the start at l0 (c_me = 0)
+    dfl cur{0.f, 0.f}, prev{0.f, 0.f};
+    int e = 0, c_me = TC_NEVER;
+    if (act) {
+        if (stv) {
+            const size_t ix = ((size_t)m * 2 + side) * st_ld + p;
+            const float4 v = stv[ix];
+            const short2 ec = ste[ix];
+            cur = dfl{v.x, v.y};
+            prev = dfl{v.z, v.w};
+            e = 96 * (int)ec.x;
+            c_me = ec.y;
+        } else {
+            const double sh = psh[p], ch = pch[p];
+            if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
+            else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
+            c_me = 0;
+        }
+    }
     // column col = 4 r + c of request r (see the file comment)
     auto column = [&](int r, int c) -> double {
         if (!act) return 0.0;
@@ -194,6 +216,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
         const double2 v = Hr[(long long)(L - m) * ldH + rm];
         return c == 2 ? v.x : v.y;
     };
+    const int c_warp = __reduce_min_sync(0xffffffffu, c_me);  // this warp's first chunk
     if (ring_thread) {
 #pragma unroll
         for (int col = 0; col < NO; ++col) {
@@ -203,7 +226,8 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
             if (lane == 0) s_mx[warp * 32 + col] = a;
         }
     }
-    __syncthreads();
+    __syncthreads();  // s_c0 initialised
+    if (ring_thread && lane == 0 && c_warp < TC_NEVER) atomicMin(s_c0, c_warp);
     if (tid < NO) {
         float cm = 0.f;
         for (int w = 0; w < TCA_RW; ++w) cm = fmaxf(cm, s_mx[w * 32 + tid]);
@@ -233,13 +257,18 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = *s_tm;
+    // the block starts at the first chunk in which any of its rings accumulates
+    // (earlier chunks would add zero digit products); none when no ring ever does
+    const int nchk = l0 <= L ? (L - l0 + 1 + TCA_KC - 1) / TCA_KC : 0;
+    const int cb = *s_c0;
+    const int lstart = cb < nchk ? l0 + TCA_KC * cb : L + 1;
 
     if (warp == TCA_MMA) {
         // ---------------- MMA warp
         constexpr uint32_t IDESC = idesc_bf16_f32(128, 4 * TCA_KC) | (1u << 15) | (1u << 16);  // A, B MN-major
         int gc = 0;
         bool ok = true;
-        for (int lb = l0; lb <= L; lb += TCA_KC, ++gc) {
+        for (int lb = lstart; lb <= L; lb += TCA_KC, ++gc) {
             const int buf = gc & 1, tb = gc % TCA_NTB;
             bool got = !*s_bad && mbar_wait(bfull0 + 8 * buf, (gc >> 1) & 1);
             if (got && gc >= TCA_NTB) got = mbar_wait(tempty0 + 8 * tb, ((gc / TCA_NTB) - 1) & 1);
@@ -270,7 +299,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
 #pragma unroll
         for (int r = 0; r < NB; ++r) hmr[r] = hm[r];
         int gc = 0;
-        for (int lb = l0; lb <= L; lb += TCA_KC, ++gc) {
+        for (int lb = lstart; lb <= L; lb += TCA_KC, ++gc) {
             const int tb = gc % TCA_NTB;
             const bool got = !*s_bad && mbar_wait(tfull0 + 8 * tb, (gc / TCA_NTB) & 1);
             if (bar_or_n(2, 128, !__all_sync(0xffffffffu, got))) {
@@ -320,63 +349,57 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
         // ---------------- ring warps
         const double x = act ? px[p] : 0.0;
         const dfl xd = df_from(side ? -x : x);
-        dfl cur{0.f, 0.f}, prev{0.f, 0.f};
-        int e = 0;
-        if (stv) {
-            if (act) {
-                const size_t ix = ((size_t)m * 2 + side) * st_ld + p;
-                const float2 v = stv[ix];
-                cur = dfl{v.x, v.y};
-                e = 96 * (int)ste[ix];
-            }
-        } else {
-            const double sh = act ? psh[p] : 0.0, ch = act ? pch[p] : 1.0;
-            if (side) rec_start_df(lg0[m], m, spin, ch, sh, cur, prev, e);
-            else rec_start_df(lg0[m], m, spin, sh, ch, cur, prev, e);
-        }
         const float2 *al = coef, *ga = coef + nalm, *be = coef + 2 * nalm;
         const uint32_t boff = (tid >> 3) * TCA_B_LBO + (tid & 7) * 16;
         int gc = 0, bad = 0;
-        for (int lb = l0; lb <= L; lb += TCA_KC, ++gc) {
+        for (int lb = lstart; lb <= L; lb += TCA_KC, ++gc) {
             const int buf = gc & 1;
             if (gc >= 2) bad |= !mbar_wait(bempty0 + 8 * buf, ((gc - 2) >> 1) & 1);
             bad = __any_sync(0xffffffffu, bad | *s_bad);
             if (bad) break;
             const float lsc = pow2f(7 - adj_chunk_el(min(lb + TCA_KC - 1, L)));
             unsigned char *sB = sm + TCA_OFF_B + buf * TCA_BBUF + boff;
-            // two halves of 8 l; the exponent check runs once per half (a step grows the
-            // mantissa by less than 2^8.5: eight steps from below 2^40 stay inside FP32)
+            // before its first chunk a ring holds its table state and writes zero digits
+            const bool live = (lb - l0) / TCA_KC >= c_me;
+            if (live) {
+                // two halves of 8 l; the exponent check runs once per half (a step grows the
+                // mantissa by less than 2^8.5: eight steps from below 2^40 stay inside FP32)
 #pragma unroll
-            for (int lh = 0; lh < 2; ++lh) {
-                uint32_t pk[4][4];
-                const float scg = (act && e == 0) ? lsc : 0.f;
+                for (int lh = 0; lh < 2; ++lh) {
+                    uint32_t pk[4][4];
+                    const float scg = (act && e == 0) ? lsc : 0.f;
 #pragma unroll
-                for (int j2 = 0; j2 < 4; ++j2) {
-                    float d0[4], d1[4];
-                    auto step = [&](int l, float(&d)[4]) {
-                        digits4s(cur.h, cur.l, l <= L ? scg : 0.f, d);
-                        float2 a2 = make_float2(0.f, 0.f), g2 = a2, b2 = a2;
-                        if (l < L) {
-                            a2 = __ldg(al + b + l);
-                            g2 = __ldg(ga + b + l);
-                            b2 = __ldg(be + b + l);
-                        }
-                        const dfl t = df_fma_u(dfl{a2.x, a2.y}, xd, dfl{g2.x, g2.y});
-                        const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
-                        prev = cur;
-                        cur = nxt;
-                    };
-                    const int l = lb + 8 * lh + 2 * j2;
-                    step(l, d0);
-                    step(l + 1, d1);
+                    for (int j2 = 0; j2 < 4; ++j2) {
+                        float d0[4], d1[4];
+                        auto step = [&](int l, float(&d)[4]) {
+                            digits4s(cur.h, cur.l, l <= L ? scg : 0.f, d);
+                            float2 a2 = make_float2(0.f, 0.f), g2 = a2, b2 = a2;
+                            if (l < L) {
+                                a2 = __ldg(al + b + l);
+                                g2 = __ldg(ga + b + l);
+                                b2 = __ldg(be + b + l);
+                            }
+                            const dfl t = df_fma_u(dfl{a2.x, a2.y}, xd, dfl{g2.x, g2.y});
+                            const dfl nxt = df_mul_sub(t, cur, dfl{b2.x, b2.y}, prev);
+                            prev = cur;
+                            cur = nxt;
+                        };
+                        const int l = lb + 8 * lh + 2 * j2;
+                        step(l, d0);
+                        step(l + 1, d1);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+                        for (int k = 0; k < 4; ++k) pk[k][j2] = pack_bf16(d0[k], d1[k]);
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)  // digit k of lambda -> N-core (k, lh)
+                        *reinterpret_cast<uint4 *>(sB + (2 * k + lh) * TCA_B_SBO) =
+                            make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
+                    REC_RESCALE_DF(cur, prev, e);
                 }
+            } else {
 #pragma unroll
-                for (int k = 0; k < 4; ++k)  // digit k of lambda -> N-core (k, lh)
-                    *reinterpret_cast<uint4 *>(sB + (2 * k + lh) * TCA_B_SBO) =
-                        make_uint4(pk[k][0], pk[k][1], pk[k][2], pk[k][3]);
-                REC_RESCALE_DF(cur, prev, e);
+                for (int k = 0; k < 8; ++k)
+                    *reinterpret_cast<uint4 *>(sB + k * TCA_B_SBO) = make_uint4(0u, 0u, 0u, 0u);
             }
             fence_async_smem();
             __syncwarp();
@@ -499,7 +522,7 @@ size_t adj_tc_scratch_bytes(const cunusht_plan_s *P, int nreq) {
 // the pole pair and the leftover pairs (double-float CUDA cores).
 int leg_adjoint_tc(const cunusht_plan_s *P, int nreq, int spin, int ncomp, const double2 *H, long long hstride,
                    int ld, int npairs, const double *x, const double *sh, const double *ch, const int *rn,
-                   const int *rs, int pole, int pole_rn, int pole_rs, const float2 *stv, const short *ste,
+                   const int *rs, int pole, int pole_rn, int pole_rs, const float4 *stv, const short2 *ste,
                    const double *lf, double2 *G, double2 *C, long long astride, void *scratch, cudaStream_t st) {
     const int L = P->lmax;
     TcAdjArgs A;

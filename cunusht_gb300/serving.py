@@ -379,6 +379,17 @@ class NativeLensingServer:
         # requests with callable payloads wait here until their bucket has room
         self.waiting: dict[tuple, collections.deque] = collections.defaultdict(collections.deque)
         self.inflight: dict[tuple, int] = collections.defaultdict(int)
+        self._streams: dict[int, "torch.cuda.Stream"] = {}  # input streams by slot priority
+
+    def _input_stream(self, lmax: int):
+        """Stream on which a request's inputs are materialised and converted:
+        the priority of its bucket's slots, so that the inputs of a short
+        request are not queued behind the blocks of long launches running at
+        a lower priority (on the caller's stream they would be)."""
+        pr = slot_priority(lmax)
+        if pr not in self._streams:
+            self._streams[pr] = torch.cuda.Stream(priority=pr)
+        return self._streams[pr]
 
     def prewarm(self, keys, graphs: bool = True) -> list:
         """Admit these buckets (lmax, spin, epsilon) ahead of traffic on the
@@ -426,25 +437,31 @@ class NativeLensingServer:
         from . import _lib
         from .utils import Alm
         kind, lmax, spin, epsilon, nphi, out = r.kind, r.lmax, r.spin, r.epsilon, r.nphi, r.out_arg
-        data, dlm_scaled = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
         if not nphi:  # the package's default GL geometry (geometry.get_gl_geometry)
             nphi = _default_nphi(lmax)
         nalm = Alm.getsize(lmax, lmax)
         ncm = 2 if spin else 1
         npix = (lmax + 1) * nphi
-        if kind == "g2l":
-            inp = data.reshape(ncm, nalm).to(torch.complex128).contiguous()
-            res = out if out is not None else torch.empty((ncm, npix) if spin else (npix,), dtype=torch.float64,
-                                                          device="cuda")
+        # the result on the caller's stream (its earlier work on the memory comes first)
+        if out is not None:
+            res = out
+        elif kind == "g2l":
+            res = torch.empty((ncm, npix) if spin else (npix,), dtype=torch.float64, device="cuda")
         else:
-            inp = data.reshape(ncm, npix).to(torch.float64).contiguous()
-            res = out if out is not None else torch.empty((ncm, nalm) if spin else (nalm,), dtype=torch.complex128,
-                                                          device="cuda")
-        d = dlm_scaled.reshape(-1).to(torch.complex128).contiguous()
+            res = torch.empty((ncm, nalm) if spin else (nalm,), dtype=torch.complex128, device="cuda")
+        st = self._input_stream(lmax)
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):
+            data, dlm_scaled = r.data() if callable(r.data) else (r.data, r.dlm_scaled)
+            if kind == "g2l":
+                inp = data.reshape(ncm, nalm).to(torch.complex128).contiguous()
+            else:
+                inp = data.reshape(ncm, npix).to(torch.float64).contiguous()
+            d = dlm_scaled.reshape(-1).to(torch.complex128).contiguous()
         rid = self._c.c_int64()
         _lib.check(self._lib.cunusht_server_submit(self._srv, 0 if kind == "g2l" else 1, lmax, spin, float(epsilon),
                                                    int(nphi), inp.data_ptr(), d.data_ptr(), res.data_ptr(),
-                                                   torch.cuda.current_stream().cuda_stream, self._c.byref(rid)))
+                                                   st.cuda_stream, self._c.byref(rid)))
         r.data, r.dlm_scaled, r.result, r.rid, r.key = inp, d, res, rid.value, key
         self.live[rid.value] = r
         self.inflight[key] += 1
