@@ -60,12 +60,12 @@ template <typename T> __device__ __forceinline__ T cvt(double x) { return (T)x; 
 template <> __device__ __forceinline__ dfl cvt<dfl>(double x) { return df_from(x); }
 __device__ __forceinline__ double to_d(float x) { return (double)x; }
 __device__ __forceinline__ double to_d(double x) { return x; }
-__device__ __forceinline__ double to_d(dfl x) { return (double)x.h + (double)x.l; }
+__device__ __forceinline__ double to_d(dfl x) { return df_to(x); }  // integer pipe, bit-exact
 template <typename To> __device__ __forceinline__ To to_t(float x) { return (To)x; }
 template <typename To> __device__ __forceinline__ To to_t(double x) { return (To)x; }
 template <typename To> __device__ __forceinline__ To to_t(dfl x);
 template <> __device__ __forceinline__ float to_t<float>(dfl x) { return x.h + x.l; }
-template <> __device__ __forceinline__ double to_t<double>(dfl x) { return (double)x.h + (double)x.l; }
+template <> __device__ __forceinline__ double to_t<double>(dfl x) { return df_to(x); }
 template <typename T> using cplx = typename cplx_t<T>::type;
 
 template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T re, T im) {

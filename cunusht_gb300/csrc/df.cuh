@@ -12,14 +12,73 @@ struct dfl {
     float h, l;
 };
 
-__device__ __forceinline__ dfl df_from(double x) {
+// Conversions between FP64 and double-float.  GB300 issues FP64 arithmetic
+// and FP64 conversions (DADD, F2F.F64) at about 1.6 lanes per SM and clock,
+// 1/80 of FP32 (measured), so the FP64 forms ((float)x, x - (double)hi,
+// (double)h + (double)l: 4 and 3 FP64-pipe instructions) made the conversions
+// at stage boundaries an FP64-pipe bottleneck (the interpolation kernel ran
+// its FP64 pipe at 85 %).  df_from splits on the integer pipe: hi = x rounded
+// to nearest even in 24 bits, lo = the exact 29-bit remainder converted by
+// I2F.F32 (integer and FMA pipes); bit for bit what the FP64 form gives.
+// df_to builds the exact doubles of h and l from their bits and adds them
+// with one DADD (the same correctly rounded sum).  Operands outside the
+// ranges handled (|x| >= 2^127 or < 2^-74, subnormal or non-finite floats)
+// take the FP64 forms through a call, so the common path carries no
+// predicated FP64 instructions.
+static __device__ __noinline__ dfl df_from_fp64(double x) {
     dfl r;
     r.h = (float)x;
     r.l = (float)(x - (double)r.h);
     return r;
 }
+static __device__ __noinline__ double df_to_fp64(float h, float l) { return (double)h + (double)l; }
 
-__device__ __forceinline__ double df_to(dfl a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ bool df_split_i(double x, float &hi, float &lo) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned uh = (unsigned)(u >> 32);
+    const unsigned sgn = uh >> 31;
+    if ((u << 1) == 0) {  // +-0
+        hi = __uint_as_float(sgn << 31);
+        lo = 0.f;
+        return true;
+    }
+    const int E = (int)((uh >> 20) & 0x7FF) - 1023;
+    if (E < -74 || E > 126) return false;
+    const unsigned long long m = (u & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    unsigned mh = (unsigned)(m >> 29);
+    const unsigned rem = (unsigned)u & 0x1FFFFFFFu;
+    if (rem > 0x10000000u || (rem == 0x10000000u && (mh & 1u))) mh += 1u;
+    const int r = (int)rem - ((int)(mh - (unsigned)(m >> 29)) << 29);  // m - mh 2^29, |r| <= 2^28
+    // hi = mh 2^(E - 23): the implicit bit of mh (or its carry to 2^24) lands in the exponent field
+    hi = __uint_as_float((sgn << 31) + ((unsigned)(E + 126) << 23) + mh);
+    // lo = r 2^(E - 52), r rounded to 24 bits by the conversion, 2^(E - 52) a normal float
+    lo = __int2float_rn(sgn ? -r : r) * __uint_as_float((unsigned)(E - 52 + 127) << 23);
+    return true;
+}
+
+// the exact double of a normal float or zero from its bits
+__device__ __forceinline__ bool df_f2d_i(float f, double &d) {
+    const unsigned u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+    if (a == 0u) {
+        d = __hiloint2double((int)u, 0);
+        return true;
+    }
+    if (a - 0x00800000u >= 0x7F000000u) return false;  // subnormal, inf, nan
+    d = __hiloint2double((int)(((a >> 3) + 0x38000000u) | (u & 0x80000000u)), (int)(u << 29));
+    return true;
+}
+
+__device__ __forceinline__ dfl df_from(double x) {
+    dfl r;
+    if (!df_split_i(x, r.h, r.l)) r = df_from_fp64(x);
+    return r;
+}
+
+__device__ __forceinline__ double df_to(dfl a) {
+    double h, l;
+    if (!df_f2d_i(a.h, h) || !df_f2d_i(a.l, l)) return df_to_fp64(a.h, a.l);
+    return h + l;
+}
 
 // hi/lo renormalisation, |a| >= |b| assumed (Fast2Sum)
 __device__ __forceinline__ dfl df_fast(float a, float b) {
@@ -61,7 +120,7 @@ struct kahan {
         c = (t - s) - y;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ double value() const { return df_to(dfl{s, -c}); }
 };
 
 // Compensated FP32 sum with the exact error of every addition (Knuth's
@@ -76,7 +135,8 @@ struct sum2 {
         c += (s - (t - bb)) + (x - bb);
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+    __device__ __forceinline__ double value() const { return df_to(dfl{s, c}); }
+    __device__ __forceinline__ dfl df() const { return dfl{s, c}; }
 };
 
 // a * lam with both operands as df, rounded once to FP32

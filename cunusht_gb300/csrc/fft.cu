@@ -243,6 +243,10 @@ __device__ __forceinline__ cplx<T> twk(const cplx<T> *__restrict__ tw, int k, in
     return w;
 }
 
+// a * b in the transform's type; double-float from the split factors (no FP64 product)
+template <typename T> __device__ __forceinline__ T scale_of(double a, double b) { return cvt<T>(a * b); }
+template <> __device__ __forceinline__ dfl scale_of<dfl>(double a, double b) { return df_mul(df_from(a), df_from(b)); }
+
 __device__ __forceinline__ int wrapi(int n, int N) {
     n %= N;
     return n < 0 ? n + N : n;
@@ -287,16 +291,16 @@ __global__ void __launch_bounds__(FFT_TPB)
     if (SP == 1) {
         for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
             const int src = Nt - 1 - i;  // kappa = -(i+1)
-            buf[Ntf - 1 - i] = cscale(buf[src], cvt<T>(Dth[src] * dm));
+            buf[Ntf - 1 - i] = cscale(buf[src], scale_of<T>(Dth[src], dm));
         }
-        for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
+        for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], scale_of<T>(Dth[i], dm));
         __syncthreads();
         for (int i = half + threadIdx.x; i <= Ntf - half; i += blockDim.x) buf[i] = czero<T>();
     } else {
         const int tstep = TW / Ntf;
         for (int i = threadIdx.x; i < Nt; i += blockDim.x) {
             // Dth[half] = 0 drops the Nyquist term
-            cplx<T> v = cscale(buf[i], cvt<T>(Dth[i] * dm));
+            cplx<T> v = cscale(buf[i], scale_of<T>(Dth[i], dm));
             if (q) v = cmul(v, twk<T>(tw, i < half ? i : i - Nt, tstep, +1));
             buf[i] = v;
         }
@@ -341,11 +345,21 @@ __global__ void __launch_bounds__(FFT_TPB)
         const bool lo = k <= half;
         const int kk = lo ? k : Nt - k;
         double2 v1 = col1[kk], v2 = two ? col2[kk] : make_double2(0.0, 0.0);
-        if (!lo) {
-            v1 = make_double2(s1 * v1.x, s1 * v1.y);
-            v2 = make_double2(s2 * v2.x, s2 * v2.y);
+        if constexpr (std::is_same<T, dfl>::value) {
+            // split first, combine in double-float: no FP64 arithmetic (s2 = -s1)
+            dfl ax = df_from(v1.x), ay = df_from(v1.y), bx = df_from(v2.x), by = df_from(v2.y);
+            if (!lo) {
+                if (s1 < 0.0) ax = df_neg(ax), ay = df_neg(ay);
+                else bx = df_neg(bx), by = df_neg(by);
+            }
+            buf[k] = mk<T>(df_add(ax, df_neg(by)), df_add(ay, bx));  // x1 + i x2
+        } else {
+            if (!lo) {
+                v1 = make_double2(s1 * v1.x, s1 * v1.y);
+                v2 = make_double2(s2 * v2.x, s2 * v2.y);
+            }
+            buf[k] = mk<T>(cvt<T>(v1.x - v2.y), cvt<T>(v1.y + v2.x));  // x1 + i x2
         }
-        buf[k] = mk<T>(cvt<T>(v1.x - v2.y), cvt<T>(v1.y + v2.x));  // x1 + i x2
     }
     __syncthreads();
     fft_smem<T>(buf, Nt, -1, stw, Ntf);
@@ -359,7 +373,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         const C x1 = cscale(cadd(zp, zn), hf);
         const C d = cscale(csub(zp, zn), hf);
         const C x2 = mk<T>(d.y, -d.x);  // d / i
-        const C y1 = cscale(x1, cvt<T>(Dth[j] * dm1)), y2 = cscale(x2, cvt<T>(Dth[j] * dm2));
+        const C y1 = cscale(x1, scale_of<T>(Dth[j], dm1)), y2 = cscale(x2, scale_of<T>(Dth[j], dm2));
         buf[j] = mk<T>(y1.x - y2.y, y1.y + y2.x);  // y1 + i y2
         if (j) {
             const C y1n = cscale(y1, ts1), y2n = cscale(y2, ts2);  // Y_{-j} = s Y_j (D even)
@@ -417,9 +431,9 @@ __global__ void __launch_bounds__(FFT_TPB)
     if (SP == 1) {
         for (int i = threadIdx.x; i < half - 1; i += blockDim.x) {
             const int dst = Nt - 1 - i;  // kappa = -(i+1)
-            buf[dst] = cscale(buf[Ntf - 1 - i], cvt<T>(Dth[dst] * dm));
+            buf[dst] = cscale(buf[Ntf - 1 - i], scale_of<T>(Dth[dst], dm));
         }
-        for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], cvt<T>(Dth[i] * dm));
+        for (int i = threadIdx.x; i < half; i += blockDim.x) buf[i] = cscale(buf[i], scale_of<T>(Dth[i], dm));
         if (threadIdx.x == 0) buf[half] = czero<T>();
     } else {
         const int tstep = TW / Ntf;
@@ -430,7 +444,7 @@ __global__ void __launch_bounds__(FFT_TPB)
             return;
         }
         for (int i = threadIdx.x; i < Nt; i += blockDim.x)
-            buf[i] = cscale(cadd(buf[i], sc[i]), cvt<T>(Dth[i] * dm));  // Dth[half] = 0
+            buf[i] = cscale(cadd(buf[i], sc[i]), scale_of<T>(Dth[i], dm));  // Dth[half] = 0
     }
     __syncthreads();
     fft_smem<T>(buf, Nt, +1, stw, MTW);
@@ -904,7 +918,7 @@ __global__ void __launch_bounds__(FFT_TPB)
         const C x1 = cscale(cadd(zp, zn), hf);
         const C d = cscale(csub(zp, zn), hf);
         const C x2 = mk<T>(d.y, -d.x);
-        const C y1 = cscale(x1, cvt<T>(Dth[j] * dm1)), y2 = cscale(x2, cvt<T>(Dth[j] * dm2));
+        const C y1 = cscale(x1, scale_of<T>(Dth[j], dm1)), y2 = cscale(x2, scale_of<T>(Dth[j], dm2));
         buf[j] = mk<T>(y1.x - y2.y, y1.y + y2.x);
         if (j) {
             const C y1n = cscale(y1, ts1), y2n = cscale(y2, ts2);

@@ -342,26 +342,33 @@ __global__ void __launch_bounds__(TCL_W)
 #pragma unroll
     for (int o = 0; o < NO; ++o) v[o] = dfl{0.f, 0.f};
     if (i < cnt) {
+        // the combinations in double-float from the split inputs: no FP64
+        // arithmetic (GB300 issues FP64 at 1/64 of the FP32 rate); 2^-47 of
+        // each value, far below the 2^-32 digit truncation
         const int l = wb + i;
         const long long ix = almidx(L, m, m) - m + l;
-        const double f = lfac ? lfac[l] : 1.0;
-        const double par = ((l + m) & 1) ? -f : f;
+        const dfl f = lfac ? df_from(lfac[l]) : dfl{1.f, 0.f};
+        const dfl par = ((l + m) & 1) ? df_neg(f) : f;
+        const dfl z{0.f, 0.f};
 #pragma unroll
         for (int r = 0; r < NB; ++r) {
             const double2 g = G[r * astride + ix];
+            const dfl gx = df_from(g.x), gy = df_from(g.y);
             if (S0) {
                 const bool odd = (l + m) & 1;
-                v[4 * r + 0] = df_from(odd ? 0.0 : f * g.x);
-                v[4 * r + 1] = df_from(odd ? 0.0 : f * g.y);
-                v[4 * r + 2] = df_from(odd ? f * g.x : 0.0);
-                v[4 * r + 3] = df_from(odd ? f * g.y : 0.0);
+                const dfl ex = df_mul(f, gx), ey = df_mul(f, gy);
+                v[4 * r + 0] = odd ? z : ex;
+                v[4 * r + 1] = odd ? z : ey;
+                v[4 * r + 2] = odd ? ex : z;
+                v[4 * r + 3] = odd ? ey : z;
                 continue;
             }
             const double2 c = C ? C[r * astride + ix] : make_double2(0.0, 0.0);
-            v[4 * r + 0] = df_from(f * (g.x - c.y));
-            v[4 * r + 1] = df_from(f * (g.y + c.x));
-            v[4 * r + 2] = df_from(par * (g.x + c.y));
-            v[4 * r + 3] = df_from(par * (c.x - g.y));
+            const dfl cx = df_from(c.x), cy = df_from(c.y);
+            v[4 * r + 0] = df_mul(f, df_add(gx, df_neg(cy)));
+            v[4 * r + 1] = df_mul(f, df_add(gy, cx));
+            v[4 * r + 2] = df_mul(par, df_add(gx, cy));
+            v[4 * r + 3] = df_mul(par, df_add(cx, df_neg(gy)));
         }
     }
 #pragma unroll
@@ -371,9 +378,11 @@ __global__ void __launch_bounds__(TCL_W)
         for (int sft = 16; sft > 0; sft >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, sft));
         if (lane == 0) s_mx[warp][o] = mx;
     }
-    // lambda exponent: 2^El > sqrt((2 lhi + 1) / (4 pi)) >= |lambda_l| for l <= lhi
+    // lambda exponent: 2^El > sqrt((2 lhi + 1) / (4 pi)) >= |lambda_l| for l <= lhi;
+    // in FP32: (2 lhi + 1) / (4 pi) is at least 1 / (2 lhi + 1) (relative) away
+    // from every power of two, far beyond the FP32 rounding
     int El;
-    frexp(sqrt((2.0 * (wb + cnt - 1) + 1.0) / (4.0 * PI)), &El);
+    frexpf(sqrtf((2.f * (wb + cnt - 1) + 1.f) * 0.0795774715459476679f), &El);
     __syncthreads();
     if (i < NO) {
         float cm = 0.f;
@@ -690,20 +699,25 @@ __global__ void __launch_bounds__(TclLayout<NB>::BLOCK, 1)
             const int n = prn[p], s = prs[p];
 #pragma unroll
             for (int r = 0; r < NB; ++r) {
+                // E + O, E - O in double-float, one integer-pipe conversion each (no FP64 arithmetic)
                 double2 *Hr = H + r * hstride;
-                const double er = acc[4 * r].value(), ei = acc[4 * r + 1].value();
-                const double orr = acc[4 * r + 2].value(), oi = acc[4 * r + 3].value();
-                Hr[(long long)m * ldH + n] = make_double2(er + orr, ei + oi);
-                if (s != n) Hr[(long long)m * ldH + s] = make_double2(er - orr, ei - oi);
+                const dfl er = acc[4 * r].df(), ei = acc[4 * r + 1].df();
+                const dfl orr = acc[4 * r + 2].df(), oi = acc[4 * r + 3].df();
+                Hr[(long long)m * ldH + n] = make_double2(df_to(df_add(er, orr)), df_to(df_add(ei, oi)));
+                if (s != n)
+                    Hr[(long long)m * ldH + s] =
+                        make_double2(df_to(df_add(er, df_neg(orr))), df_to(df_add(ei, df_neg(oi))));
             }
         } else if (act) {
             const int n = prn[p], s = prs[p];
-            const double sgs = (spin & 1) ? -1.0 : 1.0;
 #pragma unroll
             for (int r = 0; r < NB; ++r) {
+                // signs applied to the pairs before the conversion (no FP64 products)
                 double2 *Hr = H + r * hstride;
-                const double2 A = make_double2(-acc[4 * r].value(), -acc[4 * r + 1].value());
-                const double2 B = make_double2(-sgs * acc[4 * r + 2].value(), -sgs * acc[4 * r + 3].value());
+                const double2 A = make_double2(df_to(df_neg(acc[4 * r].df())), df_to(df_neg(acc[4 * r + 1].df())));
+                const dfl b2 = acc[4 * r + 2].df(), b3 = acc[4 * r + 3].df();
+                const double2 B = (spin & 1) ? make_double2(df_to(b2), df_to(b3))
+                                             : make_double2(df_to(df_neg(b2)), df_to(df_neg(b3)));
                 if (side == 0) {
                     Hr[(long long)(L + m) * ldH + n] = A;
                     if (m > 0 && s != n) Hr[(long long)(L - m) * ldH + s] = B;

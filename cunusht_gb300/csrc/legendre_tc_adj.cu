@@ -111,7 +111,7 @@ __global__ void k_adj_hmax(const double2 *__restrict__ H, long long hstride, int
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const long long c = c0 + i / nring, ring = i % nring;
         const double2 v = Hr[c * ldH + ring];
-        mx = fmaxf(mx, fmaxf(fabsf((float)v.x), fabsf((float)v.y)));
+        mx = fmaxf(mx, fmaxf(fabsf(df_from(v.x).h), fabsf(df_from(v.y).h)));  // no FP64 conversion
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -190,37 +190,40 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
         }
     }
     // column col = 4 r + c of request r (see the file comment)
-    auto column = [&](int r, int c) -> double {
-        if (!act) return 0.0;
+    // columns as double-floats (split on the integer pipe, sums in FP32 pairs: no
+    // FP64 arithmetic)
+    auto column = [&](int r, int c) -> dfl {
+        const dfl z{0.f, 0.f};
+        if (!act) return z;
         const double2 *Hr = H + r * hstride;
         const int n = prn[p], s = prs[p];
         if (S0) {
             // E = h(theta) + h(pi - theta), O = h(theta) - h(pi - theta); a self-paired
             // ring gives E = O = h
             const double2 hn = Hr[(long long)m * ldH + n];
-            const double a = (c & 1) ? hn.y : hn.x;
+            const dfl a = df_from((c & 1) ? hn.y : hn.x);
             if (s == n) return a;
             const double2 hs = Hr[(long long)m * ldH + s];
-            const double bs = (c & 1) ? hs.y : hs.x;
-            return c < 2 ? a + bs : a - bs;
+            const dfl bs = df_from((c & 1) ? hs.y : hs.x);
+            return df_add(a, c < 2 ? bs : df_neg(bs));
         }
         // side 0: (h(+m) at n, h(-m) at s); side 1: (h(+m) at s, h(-m) at n); the S
         // ring of a self-paired ring carries nothing
         const int rp = side ? s : n, rm = side ? n : s;
         if (c < 2) {
-            if (side && s == n) return 0.0;
+            if (side && s == n) return z;
             const double2 v = Hr[(long long)(L + m) * ldH + rp];
-            return c == 0 ? v.x : v.y;
+            return df_from(c == 0 ? v.x : v.y);
         }
-        if (!side && s == n) return 0.0;
+        if (!side && s == n) return z;
         const double2 v = Hr[(long long)(L - m) * ldH + rm];
-        return c == 2 ? v.x : v.y;
+        return df_from(c == 2 ? v.x : v.y);
     };
     const int c_warp = __reduce_min_sync(0xffffffffu, c_me);  // this warp's first chunk
     if (ring_thread) {
 #pragma unroll
         for (int col = 0; col < NO; ++col) {
-            float a = fabsf((float)column(col >> 2, col & 3));
+            float a = fabsf(column(col >> 2, col & 3).h);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, o));
             if (lane == 0) s_mx[warp * 32 + col] = a;
@@ -241,7 +244,7 @@ __global__ void __launch_bounds__(TCA_THREADS, 1)
         unsigned char *aK = sm + (tid >> 3) * TCA_A_LBO + (tid & 7) * 16;
 #pragma unroll 4
         for (int col = 0; col < NO; ++col) {
-            const dfl x = df_from(column(col >> 2, col & 3));
+            const dfl x = column(col >> 2, col & 3);
             float t[4];
             digits4s(x.h, x.l, pow2f(7 - s_ea[col]), t);
 #pragma unroll

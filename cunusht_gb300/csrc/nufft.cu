@@ -304,36 +304,38 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const bool act = j < npts;
     const unsigned amask = __ballot_sync(0xffffffffu, act);
     if (amask == 0) return;
-    PointCoords pc{0, 0, 0.0, 0.0};
-    double vr = 0.0, vi = 0.0;
+    // coordinates, values and the rotation in double-float: no FP64 instruction
+    // on this path (GB300 issues FP64 at 1/64 of the FP32 rate)
+    PointCoordsDf pc{0, 0, dfl{0.f, 0.f}, dfl{0.f, 0.f}};
+    dfl vr{0.f, 0.f}, vi{0.f, 0.f};
     if (act) {
         double th, ph;
         load_point(loc, j, npts, layout, th, ph);
-        pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, W);
+        pc = point_coords_df(th, ph, Ntf, Npf, n_lo, nrows, W);
         if (in_f32) {
-            vr = ((const float *)in)[j];
-            if (CPLX) vi = ((const float *)in)[npts + j];
+            vr = dfl{((const float *)in)[j], 0.f};
+            if (CPLX) vi = dfl{((const float *)in)[npts + j], 0.f};
         } else {
-            vr = ((const double *)in)[j];
-            if (CPLX) vi = ((const double *)in)[npts + j];
+            vr = df_from(((const double *)in)[j]);
+            if (CPLX) vi = df_from(((const double *)in)[npts + j]);
         }
         if (CPLX && gamma) {
             // multiply by e^{-i spin gamma}; 1 - cos from 2 sin^2(x/2) keeps
-            // the error relative to the angle
-            const float x = (float)(spin * gamma[j]);
+            // the FP32 error of the small correction terms relative to the angle
+            const float x = (float)spin * df_from(gamma[j]).h;
             const float sh = sinf(0.5f * x);
-            const double d = 2.0 * (double)sh * (double)sh;
-            const double sn = (double)sinf(x);
-            const double t2 = vr - vr * d + vi * sn;
-            vi = vi - vi * d - vr * sn;
-            vr = t2;
+            const float d = 2.f * sh * sh;
+            const float sn = sinf(x);
+            const float cr = fmaf(vr.h, d, -vi.h * sn), ci = fmaf(vi.h, d, vr.h * sn);
+            vr = df_add(vr, dfl{-cr, 0.f});
+            vi = df_add(vi, dfl{-ci, 0.f});
         }
     }
     float kt[W], kp[W];
     {
         const float sc = 2.f / (float)W;
-        const float fth = (float)pc.ft, ftl = (float)(pc.ft - (double)fth);
-        const float fph = (float)pc.fp, fpl = (float)(pc.fp - (double)fph);
+        const float fth = pc.ft.h, ftl = pc.ft.l;
+        const float fph = pc.fp.h, fpl = pc.fp.l;
 #pragma unroll
         for (int a = 0; a < W; ++a) {
             kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
@@ -346,11 +348,12 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const int pmin = __reduce_min_sync(0xffffffffu, act ? pc.p0 : big);
     const int pmax = __reduce_max_sync(0xffffffffu, act ? pc.p0 : -big);
     const int nr = rmax - rmin + W, ncl = pmax - pmin + W;
-    // the value split once into hi + lo floats (FP64 work per point, not per tap)
-    const float vrh = (float)vr, vrl = (float)(vr - (double)vrh);
-    const float vih = (float)vi, vil = (float)(vi - (double)vih);
+    const float vrh = vr.h, vrl = vr.l;
+    const float vih = vi.h, vil = vi.l;
     if (nr > SR || ncl > SC) {
         if (!act) return;
+        // footprint wider than the strip (scattered points): FP64 products and atomics
+        const double vrd = df_to(vr), vid = df_to(vi);
 #pragma unroll 1
         for (int a = 0; a < W; ++a) {
             const long long rowoff = (long long)(pc.r0 + a) * Npf;
@@ -361,13 +364,13 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
                 const double kw = (double)kt[a] * (double)kp[b];
                 if (Ufix) {
                     unsigned long long *fc = Ufix + (rowoff + c) * NC;
-                    atomicAdd(fc, (unsigned long long)to_fix(kw * vr, E));
-                    if constexpr (CPLX) atomicAdd(fc + 1, (unsigned long long)to_fix(kw * vi, E));
+                    atomicAdd(fc, (unsigned long long)to_fix(kw * vrd, E));
+                    if constexpr (CPLX) atomicAdd(fc + 1, (unsigned long long)to_fix(kw * vid, E));
                     continue;
                 }
                 double *cell = U + (rowoff + c) * NC;
-                atomicAdd(cell, kw * vr);
-                if constexpr (CPLX) atomicAdd(cell + 1, kw * vi);
+                atomicAdd(cell, kw * vrd);
+                if constexpr (CPLX) atomicAdd(cell + 1, kw * vid);
             }
         }
         return;
@@ -475,15 +478,15 @@ __global__ void __launch_bounds__(NU_TPB)
     out = out_f32 ? (void *)((float *)out + blockIdx.y * obs) : (void *)((double *)out + blockIdx.y * obs);
     double th, ph;
     load_point(loc, j, npts, layout, th, ph);
-    const PointCoords pc = point_coords(th, ph, Ntf, Npf, n_lo, nrows, W);
+    const PointCoordsDf pc = point_coords_df(th, ph, Ntf, Npf, n_lo, nrows, W);
     float kt[W], kp[W];
-    // tap offsets (n0 + a - t) from the FP64 offset split into hi + lo floats:
-    // (a + ft_h) is exact in FP32, so each tap argument carries only its own
-    // final rounding (a single FP32 rounding of ft would shift every tap of
-    // the point by up to 2.4e-7 grid cells, a coherent position error)
+    // tap offsets (n0 + a - t) from the double-float offset: (a + ft_h) is
+    // exact in FP32, so each tap argument carries only its own final rounding
+    // (a single FP32 rounding of ft would shift every tap of the point by up
+    // to 2.4e-7 grid cells, a coherent position error)
     const float sc = 2.f / (float)W;
-    const float fth = (float)pc.ft, ftl = (float)(pc.ft - (double)fth);
-    const float fph = (float)pc.fp, fpl = (float)(pc.fp - (double)fph);
+    const float fth = pc.ft.h, ftl = pc.ft.l;
+    const float fph = pc.fp.h, fpl = pc.fp.l;
 #pragma unroll
     for (int a = 0; a < W; ++a) {
         kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
@@ -522,28 +525,31 @@ __global__ void __launch_bounds__(NU_TPB)
             zi.add(-kt[a] * ri.c);
         }
     }
+    // the compensated sums as double-floats (value s - c); no FP64 instruction below
     if constexpr (CPLX) {
-        double vr = zr.value(), vi = zi.value();
+        dfl vr = df_fast(zr.s, -zr.c), vi = df_fast(zi.s, -zi.c);
         if (gamma) {
-            const float x = (float)(spin * gamma[j]);
+            // (vr + i vi) e^{i x}: 1 - cos x = 2 sin^2(x / 2) keeps the FP32
+            // error of the small correction terms relative to the angle
+            const float x = (float)spin * df_from(gamma[j]).h;
             const float sh = sinf(0.5f * x);
-            const double d = 2.0 * (double)sh * (double)sh;  // 1 - cos x
-            const double s = (double)sinf(x);
-            const double tr = vr - vr * d - vi * s;
-            vi = vi - vi * d + vr * s;
-            vr = tr;
+            const float d = 2.f * sh * sh;  // 1 - cos x
+            const float s = sinf(x);
+            const float cr = fmaf(vi.h, s, vr.h * d), ci = fmaf(vr.h, -s, vi.h * d);
+            vr = df_add(vr, dfl{-cr, 0.f});
+            vi = df_add(vi, dfl{-ci, 0.f});
         }
         if (out_f32) {
-            ((float *)out)[j] = (float)vr;
-            ((float *)out)[npts + j] = (float)vi;
+            ((float *)out)[j] = vr.h + vr.l;
+            ((float *)out)[npts + j] = vi.h + vi.l;
         } else {
-            ((double *)out)[j] = vr;
-            ((double *)out)[npts + j] = vi;
+            ((double *)out)[j] = df_to(vr);
+            ((double *)out)[npts + j] = df_to(vi);
         }
     } else {
-        const double v = zr.value();
-        if (out_f32) ((float *)out)[j] = (float)v;
-        else ((double *)out)[j] = v;
+        const dfl v = df_fast(zr.s, -zr.c);
+        if (out_f32) ((float *)out)[j] = v.h + v.l;
+        else ((double *)out)[j] = df_to(v);
     }
 }
 
@@ -730,7 +736,8 @@ __global__ void __launch_bounds__(256)
     if (ogam) ogam += blockIdx.y * npix;
     int ring;
     if (nph_uniform > 0) {
-        ring = (int)(j / nph_uniform);
+        // 32-bit division when it fits (64-bit division is a long software sequence)
+        ring = j < 0x7FFFFFFFLL ? (int)((unsigned)j / (unsigned)nph_uniform) : (int)(j / nph_uniform);
     } else {
         int lo = 0, hi = nring - 1;
         while (lo < hi) {
@@ -740,9 +747,11 @@ __global__ void __launch_bounds__(256)
         }
         ring = lo;
     }
-    const double theta = rth[ring];
-    const long long nph = rnph[ring];
-    const double phi = rph0[ring] + (double)(j - rofs[ring]) * (TWOPI / (double)nph);
+    // ring angles and the pixel's longitude as double-floats (no FP64 division)
+    const dfl twopi{0x1.921fb6p+2f, -0x1.777a5cp-23f};  // 2 pi
+    const dfl theta = df_from(rth[ring]);
+    const float nph = (float)rnph[ring];
+    const dfl phi = df_add(df_from(rph0[ring]), df_mul(dfl{(float)(j - rofs[ring]), 0.f}, df_div(twopi, dfl{nph, 0.f})));
     const double t64 = dth[j], p64 = dph[j];
     const dfl t = df_from(t64), p = df_from(p64);
     const float d2 = t.h * t.h + p.h * p.h;
@@ -767,29 +776,31 @@ __global__ void __launch_bounds__(256)
     const dfl ctt = df_mul(ct, t), two_st_ct_C = df_scale(df_mul(df_mul(st, ct), C), 2.f);
     const dfl num = df_add(df_mul(two_st_ct_C, tS), df_mul(df_add(df_mul(ctt, ctt), df_mul(p, p)), df_mul(S, S)));
     const dfl sdt = df_add(df_mul(ct, df_div(num, df_add(rho, stC))), df_mul(df_mul(st, st), tS));
-    double dtheta;
+    // series branches in double-float (deflections of a few arcmin); FP64 asin /
+    // atan2 only for large angles
+    dfl dtheta;
     if (fabsf(sdt.h) < 0.02f) {
         const float x = sdt.h, x2 = x * x;
-        dtheta = df_to(df_add(sdt, dfl{x * x2 * (1.f / 6.f + 0.075f * x2), 0.f}));
+        dtheta = df_add(sdt, dfl{x * x2 * (1.f / 6.f + 0.075f * x2), 0.f});
     } else {
-        dtheta = asin(fmin(fmax(df_to(sdt), -1.0), 1.0));
+        dtheta = df_from(asin(fmin(fmax(df_to(sdt), -1.0), 1.0)));
     }
-    oth[j] = theta + dtheta;
-    double dphi;
+    oth[j] = df_to(df_add(theta, dtheta));
+    dfl dphi;
     const dfl q = nx.h > 0.f ? df_div(pS, nx) : dfl{1e30f, 0.f};
     if (fabsf(q.h) < 0.02f) {
         const float x = q.h, x2 = x * x;
-        dphi = df_to(df_add(q, dfl{x * x2 * (-1.f / 3.f + 0.2f * x2), 0.f}));
+        dphi = df_add(q, dfl{x * x2 * (-1.f / 3.f + 0.2f * x2), 0.f});
     } else {
-        dphi = atan2(df_to(pS), df_to(nx));
+        dphi = df_from(atan2(df_to(pS), df_to(nx)));
     }
-    double php = phi + dphi;
-    if (php >= TWOPI) php -= TWOPI;
-    oph[j] = php;
+    dfl php = df_add(phi, dphi);
+    if (php.h > twopi.h || (php.h == twopi.h && php.l >= twopi.l)) php = df_add(php, df_neg(twopi));
+    oph[j] = df_to(php);
     if (ogam) {
         const float x2m = d2 * (1.f + s1) * (sc.z / sc.x) + t.h * c1;  // x2 - d_t
         const float x2 = t.h + x2m;
-        ogam[j] = d2 > 0.f ? (double)atan2f(p.h * x2m, t.h * x2 + p.h * p.h) : 0.0;
+        ogam[j] = d2 > 0.f ? df_to(dfl{atan2f(p.h * x2m, t.h * x2 + p.h * p.h), 0.f}) : 0.0;
     }
 }
 

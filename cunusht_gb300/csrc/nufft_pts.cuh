@@ -3,6 +3,7 @@
 // kernels (nufft.cu, spread_bins.cu).
 #pragma once
 #include "common.cuh"
+#include "df.cuh"
 
 namespace cunusht {
 
@@ -41,6 +42,59 @@ __device__ __forceinline__ PointCoords point_coords(double th, double ph, int Nt
     r0 = r0 < 0 ? 0 : (r0 > nrows - w ? nrows - w : r0);  // stays in bounds for any input
     pc.r0 = r0;
     pc.p0 = p0;
+    return pc;
+}
+
+// The same coordinates in double-float arithmetic, for the mixed-precision
+// kernels: no FP64 instruction (GB300 issues FP64 at 1/64 of the FP32 rate,
+// and point_coords' FP64 products, division, rounding and clamps made the
+// interpolation kernel FP64-pipe bound).  theta and phi become double-floats
+// on the integer pipe (df_from), are scaled by Ntf / 2 pi and Npf / 2 pi
+// (1 / 2 pi as a double-float constant, Ntf and Npf powers of two), and the
+// first taps and offsets follow as in point_coords: ceil of a normalised
+// double-float is ceilf(h) unless h is an integer and l > 0, and the offsets
+// n0 - t, p0 - p are formed exactly (|n0 - t.h| <= w / 2 + 1 is a multiple of
+// ulp(t.h)) and renormalised.  Positions carry about 2^-47 of the grid size
+// (6e-11 cells at 8192) instead of 2^-53.
+struct PointCoordsDf {
+    int r0;      // first fine row (relative to n_lo), clamped into the grid
+    int p0;      // first fine column (may be negative / >= Npf: wrap)
+    dfl ft, fp;  // (n0 - t), (p0 - p)
+};
+
+__device__ __forceinline__ float df_ceil(dfl x) {
+    const float c = ceilf(x.h);
+    return (c == x.h && x.l > 0.f) ? c + 1.f : c;
+}
+
+__device__ __forceinline__ PointCoordsDf point_coords_df(double th, double ph, int Ntf, int Npf, int n_lo,
+                                                         int nrows, int w) {
+    const dfl inv2pi{0x1.45f306p-3f, 0x1.b93910p-28f};  // 1 / 2 pi
+    dfl a = df_from(th), b = df_from(ph);
+    // non-finite or far out-of-range coordinates are clamped so every index
+    // below stays inside the grid (the result for such points is garbage-in)
+    if (!isfinite(a.h) || !isfinite(a.l)) a = dfl{0.f, 0.f};
+    if (!isfinite(b.h) || !isfinite(b.l) || fabsf(b.h) > 1e12f) b = dfl{0.f, 0.f};
+    dfl t = df_scale(df_mul(a, inv2pi), (float)Ntf);
+    const float thi = 0.5f * (float)Ntf + 1.f;
+    if (t.h < -1.f) t = dfl{-1.f, 0.f};
+    else if (t.h > thi) t = dfl{thi, 0.f};
+    dfl p = df_scale(df_mul(b, inv2pi), (float)Npf);
+    const float k = floorf(p.h / (float)Npf);  // Npf a power of two: exact quotient
+    p = df_add(p, dfl{-k * (float)Npf, 0.f});
+    if (p.h < 0.f) p = df_add(p, dfl{(float)Npf, 0.f});  // p.h an integer multiple of Npf with p.l < 0
+    if (p.h < 0.f) p = dfl{0.f, 0.f};
+    else if (p.h > (float)Npf) p = dfl{(float)Npf, 0.f};
+    const float hw = 0.5f * (float)w;
+    const float n0 = df_ceil(df_add(t, dfl{-hw, 0.f}));
+    const float q0 = df_ceil(df_add(p, dfl{-hw, 0.f}));
+    PointCoordsDf pc;
+    pc.ft = df_fast(n0 - t.h, -t.l);  // |n0 - t.h| >= w / 2 - 1 > |t.l|
+    pc.fp = df_fast(q0 - p.h, -p.l);
+    int r0 = (int)n0 - n_lo;
+    r0 = r0 < 0 ? 0 : (r0 > nrows - w ? nrows - w : r0);  // stays in bounds for any input
+    pc.r0 = r0;
+    pc.p0 = (int)q0;
     return pc;
 }
 

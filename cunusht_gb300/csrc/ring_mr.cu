@@ -224,7 +224,9 @@ __global__ void __launch_bounds__(MR_TPB, 2)
         for (int m = threadIdx.x; m < st.R[i]; m += blockDim.x) K[st.coff[i] + m] = tw[m * (N / st.R[i])];
     const double ph0 = phi0[ring];
     for (int qi = threadIdx.x; qi < N; qi += blockDim.x) {
-        double2 acc = make_double2(0.0, 0.0);
+        // bin qi gathers every m = qi (mod N); with N >= 2L + 1 (no aliasing) one term.
+        // Double-float sums for the mixed path: no FP64 arithmetic unless phi0 != 0
+        T ax = cvt<T>(0.0), ay = cvt<T>(0.0);
         for (int m = qi - N * ((qi + L) / N); m <= L; m += N) {
             double2 h;
             if (spin == 0) {
@@ -238,10 +240,10 @@ __global__ void __launch_bounds__(MR_TPB, 2)
                 sincos(m * ph0, &sn, &cs);
                 h = cmul(h, make_double2(cs, sn));
             }
-            acc.x += h.x;
-            acc.y += h.y;
+            ax = ax + cvt<T>(h.x);
+            ay = ay + cvt<T>(h.y);
         }
-        buf[qi] = mk<T>(cvt<T>(acc.x), cvt<T>(acc.y));
+        buf[qi] = mk<T>(ax, ay);
     }
     __syncthreads();
     mr_fft<T>(buf, N, st, K, tw);
