@@ -465,8 +465,11 @@ static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U
 // from d = 1 - cos(x) = 2 sin^2(x/2) and sin(x) evaluated in FP32 (errors
 // relative to the small angle, not to 1).
 
+// Five 256-thread blocks per SM for kernel widths up to 9 (48 registers, an
+// 8-byte spill at width 9): the kernel waits on its tap loads, and 40 warps
+// per SM hide more of that latency than the 32 of four blocks.
 template <bool CPLX, int W>
-__global__ void __launch_bounds__(NU_TPB)
+__global__ void __launch_bounds__(NU_TPB, W <= 9 ? 5 : 4)
     k_interp_mixed(const float *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                    const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
                    int spin, void *__restrict__ out, int out_f32, long long ubs, long long lbs, long long obs) {
@@ -479,52 +482,48 @@ __global__ void __launch_bounds__(NU_TPB)
     double th, ph;
     load_point(loc, j, npts, layout, th, ph);
     const PointCoordsDf pc = point_coords_df(th, ph, Ntf, Npf, n_lo, nrows, W);
-    float kt[W], kp[W];
     // tap offsets (n0 + a - t) from the double-float offset: (a + ft_h) is
     // exact in FP32, so each tap argument carries only its own final rounding
     // (a single FP32 rounding of ft would shift every tap of the point by up
-    // to 2.4e-7 grid cells, a coherent position error)
+    // to 2.4e-7 grid cells, a coherent position error).  The theta weights are
+    // evaluated row by row and the columns wrap only for points whose taps
+    // cross phi = 0 (a separate path), which keeps the live registers low.
     const float sc = 2.f / (float)W;
     const float fth = pc.ft.h, ftl = pc.ft.l;
     const float fph = pc.fp.h, fpl = pc.fp.l;
+    float kp[W];
 #pragma unroll
-    for (int a = 0; a < W; ++a) {
-        kt[a] = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
-        kp[a] = es_kernel_acc((((float)a + fph) + fpl) * sc, beta);
-    }
-    int cols[W];
-#pragma unroll
-    for (int b = 0; b < W; ++b) {
-        int c = pc.p0 + b;
-        c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
-        cols[b] = c;
-    }
+    for (int b = 0; b < W; ++b) kp[b] = es_kernel_acc((((float)b + fph) + fpl) * sc, beta);
     kahan zr, zi;
+    auto rows = [&](auto wrap) {
 #pragma unroll
-    for (int a = 0; a < W; ++a) {
-        const long long rowoff = (long long)(pc.r0 + a) * Npf;
-        kahan rr, ri;
-        if constexpr (CPLX) {
-            const float2 *row = reinterpret_cast<const float2 *>(U) + rowoff;
+        for (int a = 0; a < W; ++a) {
+            const float kta = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
+            const long long rowoff = (long long)(pc.r0 + a) * Npf;
+            kahan rr, ri;
 #pragma unroll
             for (int b = 0; b < W; ++b) {
-                const float2 v = row[cols[b]];
-                rr.add(kp[b] * v.x);
-                ri.add(kp[b] * v.y);
+                int c = pc.p0 + b;
+                if constexpr (decltype(wrap)::value) c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
+                if constexpr (CPLX) {
+                    const float2 v = reinterpret_cast<const float2 *>(U)[rowoff + c];
+                    rr.add(kp[b] * v.x);
+                    ri.add(kp[b] * v.y);
+                } else {
+                    rr.add(kp[b] * U[rowoff + c]);
+                }
             }
-        } else {
-            const float *row = U + rowoff;
-#pragma unroll
-            for (int b = 0; b < W; ++b) rr.add(kp[b] * row[cols[b]]);
+            // row sums carry their compensation into the outer sum
+            zr.add(kta * rr.s);
+            zr.add(-kta * rr.c);
+            if constexpr (CPLX) {
+                zi.add(kta * ri.s);
+                zi.add(-kta * ri.c);
+            }
         }
-        // row sums carry their compensation into the outer sum
-        zr.add(kt[a] * rr.s);
-        zr.add(-kt[a] * rr.c);
-        if constexpr (CPLX) {
-            zi.add(kt[a] * ri.s);
-            zi.add(-kt[a] * ri.c);
-        }
-    }
+    };
+    if (pc.p0 >= 0 && pc.p0 + W <= Npf) rows(std::false_type{});
+    else rows(std::true_type{});
     // the compensated sums as double-floats (value s - c); no FP64 instruction below
     if constexpr (CPLX) {
         dfl vr = df_fast(zr.s, -zr.c), vi = df_fast(zi.s, -zi.c);
@@ -750,8 +749,9 @@ __global__ void __launch_bounds__(256)
     // ring angles and the pixel's longitude as double-floats (no FP64 division)
     const dfl twopi{0x1.921fb6p+2f, -0x1.777a5cp-23f};  // 2 pi
     const dfl theta = df_from(rth[ring]);
-    const float nph = (float)rnph[ring];
-    const dfl phi = df_add(df_from(rph0[ring]), df_mul(dfl{(float)(j - rofs[ring]), 0.f}, df_div(twopi, dfl{nph, 0.f})));
+    const float nph = (float)(int)rnph[ring];  // 32-bit integer conversions
+    const dfl phi =
+        df_add(df_from(rph0[ring]), df_mul(dfl{(float)(int)(j - rofs[ring]), 0.f}, df_div(twopi, dfl{nph, 0.f})));
     const double t64 = dth[j], p64 = dph[j];
     const dfl t = df_from(t64), p = df_from(p64);
     const float d2 = t.h * t.h + p.h * p.h;
