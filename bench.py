@@ -42,7 +42,7 @@ METRIC = "lensing solves/s at lmax=2047 spin-2 eps=1e-7 (served mixed vs plain F
 # DRAM bytes (read + write) of the Legendre stages (records + pole + tensor-core
 # kernels) per launch of 8 requests at lmax 2047: one ncu capture at lmax 1023
 # (a few GB on the device) scaled by 4.0, the ratio of (l, m) pairs
-LEG_TRAFFIC = {"batch": 8, "leg_synth": 2686.0e6, "ptg_leg": 2414.0e6}
+LEG_TRAFFIC = {"batch": 8, "leg_synth": 2750.0e6, "ptg_leg": 2474.0e6}
 
 
 def parse():

@@ -720,6 +720,11 @@ __device__ __forceinline__ dfl df_sqrt(dfl a) {
     return df_fast(r0, e / (2.f * r0));
 }
 
+// the large-angle branches of k_pointing_mixed in FP64, out of line so that
+// the common (series) path carries no predicated FP64 instruction
+static __device__ __noinline__ dfl df_asin_fp64(dfl s) { return df_from(asin(fmin(fmax(df_to(s), -1.0), 1.0))); }
+static __device__ __noinline__ dfl df_atan2_fp64(dfl y, dfl x) { return df_from(atan2(df_to(y), df_to(x))); }
+
 __global__ void __launch_bounds__(256)
     k_pointing_mixed(int nring, int nph_uniform, const double *__restrict__ rth,
                      const float4 *__restrict__ rsc, const double *__restrict__ rph0,
@@ -783,7 +788,7 @@ __global__ void __launch_bounds__(256)
         const float x = sdt.h, x2 = x * x;
         dtheta = df_add(sdt, dfl{x * x2 * (1.f / 6.f + 0.075f * x2), 0.f});
     } else {
-        dtheta = df_from(asin(fmin(fmax(df_to(sdt), -1.0), 1.0)));
+        dtheta = df_asin_fp64(sdt);
     }
     oth[j] = df_to(df_add(theta, dtheta));
     dfl dphi;
@@ -792,7 +797,7 @@ __global__ void __launch_bounds__(256)
         const float x = q.h, x2 = x * x;
         dphi = df_add(q, dfl{x * x2 * (-1.f / 3.f + 0.2f * x2), 0.f});
     } else {
-        dphi = df_from(atan2(df_to(pS), df_to(nx)));
+        dphi = df_atan2_fp64(pS, nx);
     }
     dfl php = df_add(phi, dphi);
     if (php.h > twopi.h || (php.h == twopi.h && php.l >= twopi.l)) php = df_add(php, df_neg(twopi));
