@@ -92,6 +92,24 @@ template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
     r.y = a.x * b.y + a.y * b.x;
     return r;
 }
+// Complex double-float product: each real part a b +- c d from the two
+// unnormalised products (df_mul_u) and one full TwoSum of their leading parts,
+// left unnormalised like every double-float addition of the butterflies
+// (32 FP32 operations instead of the 44 of four renormalised products and
+// two additions).
+__device__ __forceinline__ dfl df_dot2_u(dfl a, dfl b, dfl c, dfl d) {  // a b + c d
+    const dfl p = df_mul_u(a, b), q = df_mul_u(c, d);
+    const float s = p.h + q.h;
+    const float bb = s - p.h;
+    const float t = (p.h - (s - bb)) + (q.h - bb);
+    return dfl{s, (p.l + q.l) + t};
+}
+__device__ __forceinline__ dcplx cmul(dcplx a, dcplx b) {
+    dcplx r;
+    r.x = df_dot2_u(a.x, b.x, df_neg(a.y), b.y);
+    r.y = df_dot2_u(a.x, b.y, a.y, b.x);
+    return r;
+}
 template <typename C> __host__ __device__ __forceinline__ C cconj(C a) {
     C r;
     r.x = a.x;
