@@ -566,8 +566,8 @@ __global__ void __launch_bounds__(FFT_TPB)
     const int ncols = 2 * L + 1;
     const int Nb = Npf / SP;
     const int tstep = TW / Npf;
-    for (int i = threadIdx.x; i < Nb; i += blockDim.x) buf[i] = czero<T>();
-    __syncthreads();
+    // modes m in [-L, L] land in [0, L] and [Nb - L, Nb); only the gap between is zeroed
+    for (int i = L + 1 + threadIdx.x; i < Nb - L; i += blockDim.x) buf[i] = czero<T>();
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
         cplx<T> v = F[(long long)r * ncols + c];
         if (q) v = cmul(v, twk<T>(tw, c - L, tstep, +1));
