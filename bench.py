@@ -70,7 +70,7 @@ def parse():
                    help="served mixed workload instead: Poisson arrivals of mixed lmax / spin / direction / eps")
     p.add_argument("--serve-requests", type=int, default=2000)
     p.add_argument("--serve-rate", type=float, default=200.0, help="mean arrival rate, requests/s")
-    p.add_argument("--serve-budget-gb", type=float, default=200.0)
+    p.add_argument("--serve-budget-gb", type=float, default=150.0)
     p.add_argument("--serve-native", action="store_true", help="drive the library's C++ server (cunusht_server_*)")
     p.add_argument("--serve-lazy-graphs", action="store_true",
                    help="capture each (direction, batch size) graph on first use instead of before the stream")
@@ -635,8 +635,11 @@ SERVE_P = (0.4, 0.3, 0.2, 0.1)
 
 def serve_policy(lmax):
     """(requests per launch, slots) per bucket: sized so that all 16 buckets
-    (4 lmax x 2 spins x 2 accuracies) fit a 150 GB budget together."""
-    return {511: (8, 2), 1023: (8, 2), 2047: (4, 2), 4095: (1, 1)}.get(lmax, (2, 1))
+    (4 lmax x 2 spins x 2 accuracies) fit the 150 GB budget together.  One
+    slot per bucket (at a sustained load a bucket's slot is seldom busy when
+    its next request arrives), so lmax 4095 can reserve two requests per
+    launch, whose Legendre recursion they then share under overload."""
+    return {511: (8, 1), 1023: (8, 1), 2047: (4, 1), 4095: (2, 1)}.get(lmax, (2, 1))
 
 
 class DeviceInputs:
