@@ -1,7 +1,7 @@
 // Double-float ("df") arithmetic: a value is hi + lo with two FP32 numbers,
 // about 48 significant bits.  Error-free transformations (Knuth TwoSum,
 // FMA-based TwoProduct; Dekker 1971) on the FP32 pipe, which on GB300 runs
-// about 60 times the FP64 instruction rate.  Only additions, subtractions and
+// about 80 times the FP64 instruction rate.  Only additions, subtractions and
 // explicit fmaf are used, so FMA contraction cannot change the error terms.
 #pragma once
 #include <cuda_runtime.h>

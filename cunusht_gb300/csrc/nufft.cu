@@ -282,7 +282,7 @@ __device__ __forceinline__ double f2d_exact_int(float f) {
 // kernel weights in FP32 from the FP64 tap offset split into hi + lo floats
 // (as k_interp_mixed), FP32 products, Kahan-compensated FP32 strip sums, FP64
 // global accumulation.  The FP64 variant is bound by its FP64 exponentials and
-// products (GB300 runs FP64 at 1/60 of the FP32 rate).
+// products (GB300 runs FP64 at about 1/80 of the FP32 rate).
 template <bool CPLX, int W>
 __global__ void __launch_bounds__(SPW_WARPS * 32)
     k_spread_warp_mixed(double *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
