@@ -37,6 +37,7 @@ SIGNATURES = {
     "cunusht_plan_ring_transform": (_i, [_vp]),
     "cunusht_plan_set_mmax": (_i, [_vp, _i]),
     "cunusht_plan_set_tensor_cores": (_i, [_vp, _i]),
+    "cunusht_plan_set_start_states": (_i, [_vp, _i, _i, _i]),
     "cunusht_plan_set_spreading": (_i, [_vp, _i, _i, _i64]),
     "cunusht_plan_device_status": (_i, [_vp, ctypes.POINTER(_i)]),
     "cunusht_tc_selftest": (_i, [_i, _i, _i, ctypes.POINTER(_d), ctypes.POINTER(_i)]),

@@ -127,8 +127,8 @@ static void free_plan(cunusht_plan_s *P) {
                     P->d_cc_rs, P->d_Dth, P->d_Dph, P->d_coef[0], P->d_coef[1], P->d_coef[2], P->d_lg0[0],
                     P->d_lg0[1], P->d_lg0[2], P->d_lfac, P->d_coef_df[0], P->d_coef_df[1], P->d_coef_df[2], P->d_tw64, P->d_tw32, P->d_twdf, P->d_chirp_df, P->d_bker_df, P->d_chirp, P->d_bker,
                     P->d_H, P->d_F, P->d_U, P->d_Hgl, P->d_ring, P->d_glmap, P->d_alm, P->d_vjp, P->d_lfac_g, P->d_ring_cls, P->d_cls_N, P->d_cls_Mb, P->d_cls_SP,
-                    P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb,
-                    P->d_glmapb, P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[0], P->d_tc_woff[1], P->d_tc_woff[2],
+                    P->d_cls_coff, P->d_cls_boff, P->d_Hb, P->d_Fb, P->d_Ub,  // d_Hglb, d_glmapb alias d_Hb, d_Fb
+                    P->d_ptgb, P->d_gamb, P->d_status, P->d_tc_woff[0], P->d_tc_woff[1], P->d_tc_woff[2],
                     P->d_tc_rec, P->d_mr_pos, P->d_mr_tw64, P->d_mr_twdf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -604,6 +604,17 @@ int cunusht_plan_ring_transform(const cunusht_plan_t *P) {
     return ring_mr_available(P) ? 0 : 1;
 }
 
+int cunusht_plan_set_start_states(cunusht_plan_t *P, int grid, int spin, int enable) {
+    clear_error();
+    RC_TRY(check_plan(P));
+    ARG_CHECK(P->prec == CUNUSHT_PREC_MIXED, "start states belong to mixed-precision plans");
+    ARG_CHECK(grid == 0 || grid == 1, "grid must be 0 (Gauss-Legendre pointing rings) or 1 (Clenshaw-Curtis), got %d",
+              grid);
+    const int smax = grid ? P->max_spin : std::max(P->max_spin, 1);
+    ARG_CHECK(spin >= 0 && spin <= smax, "spin %d outside [0, %d] for this grid", spin, smax);
+    return tc_start_states(P, grid, spin, enable != 0);
+}
+
 int cunusht_plan_set_tensor_cores(cunusht_plan_t *P, int enable) {
     clear_error();
     RC_TRY(check_plan(P));
@@ -706,7 +717,7 @@ int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     RC_TRY(check_plan(P));
     ARG_CHECK(max_batch >= 1 && max_batch <= 64, "max_batch must be in [1, 64], got %d", max_batch);
     if (max_batch <= P->batch_cap) return CUNUSHT_OK;
-    void *old[] = {P->d_Hb, P->d_Fb, P->d_Ub, P->d_Hglb, P->d_glmapb, P->d_ptgb, P->d_gamb};
+    void *old[] = {P->d_Hb, P->d_Fb, P->d_Ub, P->d_ptgb, P->d_gamb};  // d_Hglb, d_glmapb are aliases
     CU_TRY(cudaDeviceSynchronize());
     for (void *q : old)
         if (q) cudaFree(q);
@@ -720,16 +731,23 @@ int cunusht_plan_reserve_batch(cunusht_plan_t *P, int max_batch) {
     const size_t B = max_batch;
     const size_t ncols = P->max_spin ? 2 * (size_t)L + 1 : (size_t)L + 1;
     char *f = nullptr, *u = nullptr;
-    RC_TRY(dalloc(P, &P->d_Hb, B * ncols * P->ncc));
-    RC_TRY(dalloc(P, &f, B * f_elem(P) * ncols * P->nrows));
+    // The pointing's GL columns and maps are dead before the synthesis (adjoint)
+    // writes the CC columns and the theta-pass rows, so they share memory:
+    // d_Hglb lives in d_Hb and d_glmapb in d_Fb (lensing: Hglb, glmapb in the
+    // pointing stages, then Hb, Fb; delensing: the pointing stages first, then
+    // Fb from the phi adjoint on and Hb from the theta adjoint on).
+    const size_t hb = std::max(ncols * P->ncc, (2 * (size_t)L + 1) * P->nring);      // double2 per request
+    const size_t fb = std::max(f_elem(P) * ncols * P->nrows, 2 * sizeof(double) * (size_t)P->npix);  // bytes
+    RC_TRY(dalloc(P, &P->d_Hb, B * hb));
+    RC_TRY(dalloc(P, &f, B * fb));
     // sized for the adjoint (FP64 grid unless eps > 1e-6); the forward's FP32
     // grid uses the first half of each request's slot
     RC_TRY(dalloc(P, &u, B * adj_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf));
     P->d_Fb = f;
     P->d_Ub = u;
     P->ub_bytes = B * adj_scalar(P) * (P->max_spin ? 2 : 1) * (size_t)P->nrows * P->Npf;
-    RC_TRY(dalloc(P, &P->d_Hglb, B * (2 * (size_t)L + 1) * P->nring));
-    RC_TRY(dalloc(P, &P->d_glmapb, B * 2 * (size_t)P->npix));
+    P->d_Hglb = P->d_Hb;
+    P->d_glmapb = reinterpret_cast<double *>(f);
     RC_TRY(dalloc(P, &P->d_ptgb, B * 2 * (size_t)P->npix));
     RC_TRY(dalloc(P, &P->d_gamb, B * (size_t)P->npix));
     if (P->prec == CUNUSHT_PREC_MIXED) RC_TRY(tc_reserve(P, max_batch));

@@ -62,6 +62,7 @@ int leg_synth_spin_tc(const cunusht_plan_s *P, int nb, int npairs, const double 
                       cudaStream_t st);
 int tc_selftest(int nn, int reps, int mode, double *maxerr, int *timeout);
 int tc_plan_init(cunusht_plan_s *P);  // window tables and record buffer of a mixed-precision plan
+int tc_start_states(cunusht_plan_s *P, int grid, int spin, bool enable);  // build / release one start-state table
 int tc_reserve(cunusht_plan_s *P, int nb);  // record buffer for launches of up to nb requests
 // legendre.cu: double-float CUDA-core synthesis (spin > 0) of npairs ring pairs given by their tables
 int leg_synth_spin_df_pairs(const cunusht_plan_s *P, int nb, int npairs, const double *x, const double *sh,

@@ -859,25 +859,51 @@ __global__ void k_tc_starts(int L, int spin, const double *__restrict__ lg0, int
     ec[i] = make_short2((short)(e / 96), never ? TC_NEVER : (short)c);
 }
 
+// Build (enable) or release the start states of one grid (0 GL, 1 CC) and
+// spin; without them the tensor-core kernels start every ring at l0 from
+// rec_start_df (no chunk is skipped).  Synchronises the device.
+int tc_start_states(cunusht_plan_s *P, int g, int s, bool enable) {
+    const int L = P->lmax;
+    const int np = g ? P->cc_npairs : P->gl_npairs;
+    const size_t n = 2 * (size_t)np * (L + 1);
+    const size_t bytes = n * (sizeof(float4) + sizeof(short2));
+    CU_TRY(cudaDeviceSynchronize());  // earlier work may still read the tables
+    if (!enable) {
+        if (P->d_tc_stv[g][s]) {
+            cudaFree(P->d_tc_stv[g][s]);
+            cudaFree(P->d_tc_ste[g][s]);
+            P->d_tc_stv[g][s] = nullptr;
+            P->d_tc_ste[g][s] = nullptr;
+            P->ws_bytes -= bytes;
+        }
+        return CUNUSHT_OK;
+    }
+    if (P->d_tc_stv[g][s] || np == 0 || s > L) return CUNUSHT_OK;
+    const double *x = g ? P->d_cc_x : P->d_gl_x;
+    const double *sh = g ? P->d_cc_sh : P->d_gl_sh, *ch = g ? P->d_cc_ch : P->d_gl_ch;
+    CU_TRY(cudaMalloc(&P->d_tc_stv[g][s], n * sizeof(float4)));
+    const cudaError_t e = cudaMalloc(&P->d_tc_ste[g][s], n * sizeof(short2));
+    if (e != cudaSuccess) {
+        cudaFree(P->d_tc_stv[g][s]);
+        P->d_tc_stv[g][s] = nullptr;
+        P->d_tc_ste[g][s] = nullptr;
+        CU_TRY(e);
+    }
+    P->ws_bytes += bytes;
+    k_tc_starts<<<(unsigned)((n + 255) / 256), 256>>>(L, s, P->d_lg0[s], np, x, sh, ch, P->d_coef_df[s],
+                                                     P->nalm_tab, P->d_tc_stv[g][s], P->d_tc_ste[g][s]);
+    CU_LAUNCH_CHECK();
+    CU_TRY(cudaDeviceSynchronize());  // the tables are read from any stream
+    return CUNUSHT_OK;
+}
+
 int tc_plan_init(cunusht_plan_s *P) {
     const int L = P->lmax;
     // start tables: GL spin 1 (the pointing's synthesis) and spins 0 up to max_spin on both grids
     for (int g = 0; g < 2; ++g) {
-        const int np = g ? P->cc_npairs : P->gl_npairs;
-        const double *x = g ? P->d_cc_x : P->d_gl_x;
-        const double *sh = g ? P->d_cc_sh : P->d_gl_sh, *ch = g ? P->d_cc_ch : P->d_gl_ch;
         const int smax = g ? P->max_spin : std::max(P->max_spin, 1);
-        for (int s = 0; s <= smax && s <= L && np > 0; ++s) {
-            const size_t n = 2 * (size_t)np * (L + 1);
-            CU_TRY(cudaMalloc(&P->d_tc_stv[g][s], n * sizeof(float4)));
-            CU_TRY(cudaMalloc(&P->d_tc_ste[g][s], n * sizeof(short2)));
-            P->ws_bytes += n * (sizeof(float4) + sizeof(short2));
-            k_tc_starts<<<(unsigned)((n + 255) / 256), 256>>>(L, s, P->d_lg0[s], np, x, sh, ch, P->d_coef_df[s],
-                                                             P->nalm_tab, P->d_tc_stv[g][s], P->d_tc_ste[g][s]);
-            CU_LAUNCH_CHECK();
-        }
+        for (int s = 0; s <= smax && s <= L; ++s) RC_TRY(tc_start_states(P, g, s, true));
     }
-    CU_TRY(cudaDeviceSynchronize());  // the tables are read from any stream
     size_t nrec = 0;
     for (int s = 0; s <= 2 && s <= L; ++s) {
         std::vector<int> wo(L + 2, 0);

@@ -126,6 +126,19 @@ int cunusht_plan_set_ring_transform(cunusht_plan_t *plan, int method);
 int cunusht_plan_ring_transform(const cunusht_plan_t *plan);
 
 /*
+ * Recursion start states of the tensor-core Legendre kernels (mixed plans):
+ * per ring, its first 16-l chunk outside the evanescent region and the
+ * recursion state there, so that chunks in which no ring of a block
+ * accumulates are skipped.  Built by cunusht_plan_create for the Gauss-Legendre
+ * grid (grid 0: spins 0 .. max(max_spin, 1)) and the Clenshaw-Curtis grid
+ * (grid 1: spins 0 .. max_spin), 84 MB each at lmax 2047.  enable = 0
+ * releases one table: its kernels then start every ring at l = max(m, s)
+ * (the same result, no chunk skipped); enable = 1 builds it again
+ * (allocates).  Synchronises the device.  No reference counterpart.
+ */
+int cunusht_plan_set_start_states(cunusht_plan_t *plan, int grid, int spin, int enable);
+
+/*
  * Mixed precision: the Legendre synthesis (CC synthesis of spin 0 / 1 / 2
  * maps, the deflection synthesis of dlm2pointing, the ring synthesis of the
  * SHT-only mode) runs on the tensor cores (exact integer-digit bf16 products

@@ -254,3 +254,45 @@ def test_tc_delensing_batch_equals_single(built_lib, nreq, spin):
         single = np.atleast_2d(t.lenmap2gclm(M[r], D[r], None, lmax, lmax, spin=spin, verbose=0).cpu().numpy())
         assert _rel(batch[r], single) < 1e-6
     assert _status(t) == 0
+
+
+@pytest.mark.parametrize("lmax", [300, 2047])
+def test_tc_start_states_give_the_full_recursion_result(built_lib, lmax):
+    """The per-ring start states (each ring's first chunk outside the
+    evanescent region and its recursion state there; blocks skip the chunks
+    none of their rings accumulates) give what the recursion from
+    l = max(m, s) gives: the synthesis on the Gauss-Legendre grid (spins 0, 1,
+    2) and a lensing batch (Clenshaw-Curtis spin 2, pointing GL spin 1) agree
+    to 1e-12 with their tables released (cunusht_plan_set_start_states) and
+    again once the tables are rebuilt."""
+    import cunusht_gb300 as cu
+    from cunusht_gb300 import _lib
+    t = cu.get_transformer("GPU")(("gl", {"lmax": lmax}), nuFFTtype=2, epsilon=1e-7, precision="mixed", max_spin=2)
+    gclm, dls = orc.make_inputs(lmax, 2, seed=90 + lmax)
+    states = lambda grid, spin, on: _lib.check(t._lib.cunusht_plan_set_start_states(t._plan, grid, spin, on))
+    for spin in (0, 1, 2):
+        alm = torch.as_tensor(gclm[0] if spin == 0 else gclm, device="cuda")
+        a = t.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
+        states(0, spin, 0)
+        b = t.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
+        states(0, spin, 1)
+        c = t.synthesis(alm, spin=spin, lmax=lmax, mmax=lmax).cpu().numpy()
+        print(f"lmax {lmax} GL spin {spin}: tables vs none {_rel(a, b):.2e}")
+        assert _rel(a, b) < 1e-12, spin
+        assert np.array_equal(a, c), spin
+    G = torch.as_tensor(np.stack([gclm, gclm]), device="cuda")
+    D = torch.as_tensor(np.stack([dls[0], dls[0]]), device="cuda")
+    a = t.lensing_batch(G, D, spin=2).cpu().numpy()
+    states(1, 2, 0)
+    states(0, 1, 0)
+    b = t.lensing_batch(G, D, spin=2).cpu().numpy()
+    states(1, 2, 1)
+    states(0, 1, 1)
+    c = t.lensing_batch(G, D, spin=2).cpu().numpy()
+    print(f"lmax {lmax} lensing: tables vs none {_rel(a, b):.2e}")
+    assert _rel(a, b) < 1e-12
+    assert np.array_equal(a, c)
+    assert _status(t) == 0
+    from cunusht_gb300._lib import CunushtError
+    with pytest.raises(CunushtError):
+        states(1, 3, 0)  # spin above the plan's maximum
