@@ -637,9 +637,9 @@ def serve_policy(lmax):
     """(requests per launch, slots) per bucket: sized so that all 16 buckets
     (4 lmax x 2 spins x 2 accuracies) fit the 150 GB budget together.  One
     slot per bucket (at a sustained load a bucket's slot is seldom busy when
-    its next request arrives), so lmax 4095 can reserve two requests per
+    its next request arrives), so lmax 4095 can reserve four requests per
     launch, whose Legendre recursion they then share under overload."""
-    return {511: (8, 1), 1023: (8, 1), 2047: (4, 1), 4095: (2, 1)}.get(lmax, (2, 1))
+    return {511: (8, 1), 1023: (8, 1), 2047: (4, 1), 4095: (4, 1)}.get(lmax, (2, 1))
 
 
 class DeviceInputs:

@@ -57,7 +57,7 @@ struct Slot {
 
     ~Slot() {
         for (auto &g : graphs) cudaGraphExecDestroy(g.second);
-        void *bufs[] = {gin, din, aout, mout, lin};
+        void *bufs[] = {gin, din, mout};  // aout, lin alias gin, mout
         for (void *b : bufs)
             if (b) cudaFree(b);
         if (ev) cudaEventDestroy(ev);
@@ -137,6 +137,14 @@ int make_slot(cunusht_server_s *S, const Key &k, int cap, std::unique_ptr<Slot> 
     RC_TRY(cunusht_plan_create(&sl->plan, lmax, eps, S->precision, std::max(spin, 1), nring, th.data(), p0.data(),
                                nph.data(), ofs.data()));
     RC_TRY(cunusht_plan_reserve_batch(sl->plan, cap));
+    if (sl->plan->prec == CUNUSHT_PREC_MIXED) {
+        // the batched solves read the start states of the CC grid at the bucket's
+        // spin and of the pointing grid at spin 1 only
+        for (int s = 0; s <= std::max(spin, 1); ++s) {
+            if (s != 1) RC_TRY(cunusht_plan_set_start_states(sl->plan, 0, s, 0));
+            if (s != spin) RC_TRY(cunusht_plan_set_start_states(sl->plan, 1, s, 0));
+        }
+    }
     sl->spin = spin;
     sl->ncomp = spin ? 2 : 1;
     sl->cap = cap;
@@ -145,9 +153,11 @@ int make_slot(cunusht_server_s *S, const Key &k, int cap, std::unique_ptr<Slot> 
     const long long ncm = spin ? 2 : 1;
     CU_TRY(cudaMalloc(&sl->gin, sizeof(double2) * cap * sl->ncomp * sl->nalm));
     CU_TRY(cudaMalloc(&sl->din, sizeof(double2) * cap * sl->nalm));
-    CU_TRY(cudaMalloc(&sl->aout, sizeof(double2) * cap * sl->ncomp * sl->nalm));
     CU_TRY(cudaMalloc(&sl->mout, sizeof(double) * cap * ncm * sl->npix));
-    CU_TRY(cudaMalloc(&sl->lin, sizeof(double) * cap * ncm * sl->npix));
+    // a launch runs one direction: the delensing maps in share the lensing maps
+    // out, the delensing alm out the lensing alm in
+    sl->lin = sl->mout;
+    sl->aout = sl->gin;
     // zeroed inputs: a prewarm run (graph capture ahead of traffic) reads them
     CU_TRY(cudaMemset(sl->gin, 0, sizeof(double2) * cap * sl->ncomp * sl->nalm));
     CU_TRY(cudaMemset(sl->din, 0, sizeof(double2) * cap * sl->nalm));

@@ -72,6 +72,21 @@ def slot_priority(lmax: int) -> int:
     return -2 if lmax <= 1023 else (-1 if lmax <= 2047 else 0)
 
 
+def release_unused_start_states(T, spin: int):
+    """A served slot's batched solves read the tensor-core start states of the
+    Clenshaw-Curtis grid at the bucket's spin and of the pointing grid at spin
+    1 only; the plan's other tables are released (mixed plans)."""
+    from . import _lib
+    if T.info["precision"] != _lib.PREC_MIXED:
+        return
+    top = max(spin, 1)
+    for s in range(top + 1):
+        if s != 1:
+            _lib.check(T._lib.cunusht_plan_set_start_states(T._plan, 0, s, 0))
+        if s != spin:
+            _lib.check(T._lib.cunusht_plan_set_start_states(T._plan, 1, s, 0))
+
+
 class _Slot:
     """Plan + batch workspace + static buffers + stream; one launch in flight."""
 
@@ -87,14 +102,17 @@ class _Slot:
             self.T = GPU_cufinufft_transformer(("gl", gi), nuFFTtype=2, epsilon=eps, precision=precision,
                                                max_spin=max(spin, 1))
             self.T.reserve_batch(max_batch)
+            release_unused_start_states(self.T, spin)
             nalm, npix = self.T.nalm, self.T.npix()
             self.ncomp = 2 if spin else 1
             f64, c128 = torch.float64, torch.complex128
             self.gin = torch.zeros((max_batch, self.ncomp, nalm), dtype=c128, device="cuda")
             self.din = torch.zeros((max_batch, nalm), dtype=c128, device="cuda")
             self.out = torch.zeros((max_batch, 2, npix) if spin else (max_batch, npix), dtype=f64, device="cuda")
-            self.lin = torch.zeros((max_batch, 2, npix) if spin else (max_batch, npix), dtype=f64, device="cuda")
-            self.aout = torch.zeros((max_batch, self.ncomp, nalm), dtype=c128, device="cuda")
+            # a launch runs one direction, so the delensing buffers share the
+            # lensing ones: maps in = lensing maps out, alm out = lensing alm in
+            self.lin = self.out
+            self.aout = self.gin
         torch.cuda.synchronize()
         self.bytes = max(0, free0 - torch.cuda.mem_get_info()[0])
         self.graphs: dict[tuple, torch.cuda.CUDAGraph] = {}
