@@ -168,13 +168,16 @@ __device__ __forceinline__ void fft_pass_e(cplx<T> *buf, int N, int Ns, int dir,
 
 // Whole transform with E elements per thread; radices up to min(E, RMAX) with
 // RMAX = 16 for float and 8 for double / double-float (register budget).
+// l0 > 0: the first passes, of 2^l0 points in all, are already done (buf
+// holds the output of a radix-2^l0 pass with Ns = 1).
 template <typename T, int E, int LMAX = (std::is_same<T, float>::value ? 4 : 3)>
-__device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ stw, int M) {
+__device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ stw, int M,
+                                           int l0 = 0) {
     constexpr int LE = (E >= 16) ? 4 : (E >= 8) ? 3 : (E >= 4) ? 2 : 1;
     constexpr int LR = LE < LMAX ? LE : LMAX;
     const int nthr = N / E;
-    int rem = __ffs(N) - 1;
-    int Ns = 1;
+    int rem = __ffs(N) - 1 - l0;
+    int Ns = 1 << l0;
     while (rem > 0) {
         const int r = rem < LR ? rem : LR;
         if (r == 4) {
@@ -197,21 +200,38 @@ __device__ __forceinline__ void fft_smem_e(cplx<T> *buf, int N, int dir, const c
 // shared memory (load_twiddles).  Longer transforms are split by output parity
 // in the callers (sp_* of the plan).
 template <typename T>
-__device__ __forceinline__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ stw, int M) {
+__device__ __forceinline__ void fft_smem(cplx<T> *buf, int N, int dir, const cplx<T> *__restrict__ stw, int M,
+                                         int l0 = 0) {
     const int B = blockDim.x;
     if (N > 8 * B) {
         // 16 elements per thread: radix <= 8 for float, <= 4 for double and
         // double-float keeps the pass within the 128-register budget of a
         // 512-thread block
-        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 16, 3>(buf, N, dir, stw, M);
-        else fft_smem_e<T, 16, 2>(buf, N, dir, stw, M);
+        if constexpr (std::is_same<T, float>::value) fft_smem_e<T, 16, 3>(buf, N, dir, stw, M, l0);
+        else fft_smem_e<T, 16, 2>(buf, N, dir, stw, M, l0);
     } else if (N > 4 * B) {
-        fft_smem_e<T, 8, 3>(buf, N, dir, stw, M);
+        fft_smem_e<T, 8, 3>(buf, N, dir, stw, M, l0);
     } else if (N > 2 * B) {
-        fft_smem_e<T, 4>(buf, N, dir, stw, M);
+        fft_smem_e<T, 4>(buf, N, dir, stw, M, l0);
     } else {
-        fft_smem_e<T, 2>(buf, N, dir, stw, M);
+        fft_smem_e<T, 2>(buf, N, dir, stw, M, l0);
     }
+}
+
+// First radix-4 Stockham pass (Ns = 1) of a transform of N >= 4 points whose
+// inputs x[j + N/4] and x[j + N/2] are zero for every j < N/4 (a zero-padded
+// spectrum: modes |k| < N/4 at [0, N/4) and (3N/4, N)).  Butterfly j takes
+// v0 = x[j], v3 = x[j + 3N/4] and stores its four outputs at 4j .. 4j + 3,
+// which is what fft_pass_e<T, 4> writes for it; the transform then continues
+// with fft_smem(..., l0 = 2).  Half the pass's additions, and the zero middle
+// of the input is neither stored nor read.
+template <typename T>
+__device__ __forceinline__ void r4_first_pruned(cplx<T> *buf, int j, cplx<T> v0, cplx<T> v3, int dir) {
+    const cplx<T> t = cmul_idir(v3, dir);
+    buf[4 * j] = cadd(v0, v3);
+    buf[4 * j + 1] = csub(v0, t);
+    buf[4 * j + 2] = csub(v0, v3);
+    buf[4 * j + 3] = cadd(v0, t);
 }
 
 // Shared memory of a transform kernel with an N-element buffer: the buffer
@@ -381,9 +401,28 @@ __global__ void __launch_bounds__(FFT_TPB)
         }
     }
     __syncthreads();
-    for (int i = half + threadIdx.x; i <= Ntf - half; i += blockDim.x) buf[i] = czero<T>();
+    // the inverse's input is zero in [half, Ntf - half] (Ntf / 4 = half): its
+    // first radix-4 pass reads only x[j] and x[j + 3 Ntf / 4] (zero for j = 0),
+    // up to four butterflies per thread (Ntf <= 16 blockDim)
+    {
+        C a[4], b[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int j = threadIdx.x + c * blockDim.x;
+            if (j < half) {
+                a[c] = buf[j];
+                b[c] = j ? buf[j + 3 * half] : czero<T>();
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int j = threadIdx.x + c * blockDim.x;
+            if (j < half) r4_first_pruned<T>(buf, j, a[c], b[c], +1);
+        }
+    }
     __syncthreads();
-    fft_smem<T>(buf, Ntf, +1, stw, Ntf);
+    fft_smem<T>(buf, Ntf, +1, stw, Ntf, 2);
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
         const int n = wrap2(r + n_lo, Ntf);
         const C wp = buf[n], wn = cscale(buf[wrap2(-n, Ntf)], ts1);
@@ -550,8 +589,11 @@ __global__ void __launch_bounds__(FFT_TPB)
     }
 }
 
-// spin s: one complex row per block, columns c = m + L for m in [-L, L]
-template <typename T, typename TU>
+// spin s: one complex row per block, columns c = m + L for m in [-L, L].
+// PRUNE (SP = 1, where Nb / 4 > L): the modes fill at most [0, Nb/4) and
+// (3 Nb / 4, Nb), so the first radix-4 pass is done as the row is read
+// (r4_first_pruned) and the zero middle of the row is never written.
+template <typename T, typename TU, bool PRUNE = false>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_fwd_spin(const cplx<T> *__restrict__ F, int L, int Npf, cplx<TU> *__restrict__ U,
                    const cplx<T> *__restrict__ tw, int TW, long long fbs, long long ubs, int SP) {
@@ -566,6 +608,20 @@ __global__ void __launch_bounds__(FFT_TPB)
     const int ncols = 2 * L + 1;
     const int Nb = Npf / SP;
     const int tstep = TW / Npf;
+    if constexpr (PRUNE) {
+        const cplx<T> *row = F + (long long)r * ncols + L;  // mode m at row[m]
+        const int nb = Nb / 4;
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+            const cplx<T> v0 = j <= L ? row[j] : czero<T>();
+            const int m3 = j - nb;  // the mode at x[j + 3 Nb / 4]
+            const cplx<T> v3 = m3 >= -L ? row[m3] : czero<T>();
+            r4_first_pruned<T>(buf, j, v0, v3, +1);
+        }
+        __syncthreads();
+        fft_smem<T>(buf, Nb, +1, stw, MTW, 2);
+        for (int j = threadIdx.x; j < Nb; j += blockDim.x) U[(long long)r * Npf + j] = ccast<TU>(buf[j]);
+        return;
+    }
     // modes m in [-L, L] land in [0, L] and [Nb - L, Nb); only the gap between is zeroed
     for (int i = L + 1 + threadIdx.x; i < Nb - L; i += blockDim.x) buf[i] = czero<T>();
     for (int c = threadIdx.x; c < ncols; c += blockDim.x) {
@@ -1000,6 +1056,25 @@ int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cuda
     return theta_adj_batch(P, 1, spin, F, 0, H, 0, P->d_U, 0, st);
 }
 
+// spin phi pass of nreq requests; unsplit rows (SP = 1, Npf >= 4 (L + 1))
+// take the pruned first pass
+template <typename T, typename TU>
+static int phi_fwd_spin_launch(const cunusht_plan_s *P, int nreq, const void *F, long long fbs, void *U, long long ubs,
+                               const cplx<T> *tw, size_t sm, cudaStream_t st) {
+    const int L = P->lmax, SP = P->sp_phi;
+    const dim3 grid(P->nrows, nreq, SP);
+    if (SP == 1 && P->Npf / 4 > L) {
+        RC_TRY(set_smem(k_phi_fwd_spin<T, TU, true>, sm));
+        k_phi_fwd_spin<T, TU, true><<<grid, FFT_TPB, sm, st>>>((const cplx<T> *)F, L, P->Npf, (cplx<TU> *)U, tw,
+                                                                P->TW, fbs, ubs, SP);
+    } else {
+        RC_TRY(set_smem(k_phi_fwd_spin<T, TU, false>, sm));
+        k_phi_fwd_spin<T, TU, false><<<grid, FFT_TPB, sm, st>>>((const cplx<T> *)F, L, P->Npf, (cplx<TU> *)U, tw,
+                                                                 P->TW, fbs, ubs, SP);
+    }
+    return CUNUSHT_OK;
+}
+
 int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, long long fbs, void *U, long long ubs,
                   cudaStream_t st) {
     const int L = P->lmax;
@@ -1026,21 +1101,13 @@ int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, lo
         }
     } else {
         if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_fwd_spin<float, float>, sm));
-            k_phi_fwd_spin<float, float><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const float2 *)F, L, P->Npf,
-                                                                        (float2 *)U, P->d_tw32, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_spin_launch<float, float>(P, nreq, F, fbs, U, ubs, P->d_tw32, sm, st)));
         } else if (P->fft_df) {
-            RC_TRY(set_smem(k_phi_fwd_spin<dfl, float>, sm));
-            k_phi_fwd_spin<dfl, float><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const dcplx *)F, L, P->Npf, (float2 *)U,
-                                                                      (const dcplx *)P->d_twdf, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_spin_launch<dfl, float>(P, nreq, F, fbs, U, ubs, (const dcplx *)P->d_twdf, sm, st)));
         } else if (P->fwd_u32) {
-            RC_TRY(set_smem(k_phi_fwd_spin<double, float>, sm));
-            k_phi_fwd_spin<double, float><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
-                                                                         (float2 *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_spin_launch<double, float>(P, nreq, F, fbs, U, ubs, P->d_tw64, sm, st)));
         } else {
-            RC_TRY(set_smem(k_phi_fwd_spin<double, double>, sm));
-            k_phi_fwd_spin<double, double><<<dim3(P->nrows, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L, P->Npf,
-                                                                          (double2 *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_spin_launch<double, double>(P, nreq, F, fbs, U, ubs, P->d_tw64, sm, st)));
         }
     }
     CU_LAUNCH_CHECK();
