@@ -522,8 +522,44 @@ __global__ void __launch_bounds__(NU_TPB, W <= 9 ? 5 : 4)
             }
         }
     };
-    if (pc.p0 >= 0 && pc.p0 + W <= Npf) rows(std::false_type{});
-    else rows(std::true_type{});
+    // complex grid away from phi = 0: each row's taps come as NQ aligned
+    // 16-byte loads (two taps each) from the even column pa <= p0, with the
+    // weights shifted by p0 - pa and zero on the extra tap(s): about half the
+    // load instructions of one 8-byte load per tap (Npf is even, so every
+    // row of every request starts 16-byte aligned)
+    constexpr int NQ = (W + 2) / 2;
+    const int pa = pc.p0 & ~1;
+    if (CPLX && pc.p0 >= 0 && pa + 2 * NQ <= Npf) {
+        const bool odd = pc.p0 & 1;
+        float kq[2 * NQ];
+#pragma unroll
+        for (int i = 0; i < 2 * NQ; ++i) {
+            const float ke = i < W ? kp[i] : 0.f, ko = (i >= 1 && i - 1 < W) ? kp[i - 1] : 0.f;
+            kq[i] = odd ? ko : ke;
+        }
+#pragma unroll
+        for (int a = 0; a < W; ++a) {
+            const float kta = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
+            const float4 *row = reinterpret_cast<const float4 *>(U + 2 * ((long long)(pc.r0 + a) * Npf + pa));
+            kahan rr, ri;
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const float4 v = row[q];
+                rr.add(kq[2 * q] * v.x);
+                ri.add(kq[2 * q] * v.y);
+                rr.add(kq[2 * q + 1] * v.z);
+                ri.add(kq[2 * q + 1] * v.w);
+            }
+            zr.add(kta * rr.s);
+            zr.add(-kta * rr.c);
+            zi.add(kta * ri.s);
+            zi.add(-kta * ri.c);
+        }
+    } else if (pc.p0 >= 0 && pc.p0 + W <= Npf) {
+        rows(std::false_type{});
+    } else {
+        rows(std::true_type{});
+    }
     // the compensated sums as double-floats (value s - c); no FP64 instruction below
     if constexpr (CPLX) {
         dfl vr = df_fast(zr.s, -zr.c), vi = df_fast(zi.s, -zi.c);
