@@ -198,6 +198,10 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
     P->grid_fp32 = (P->prec != CUNUSHT_PREC_FP64) && eps > 1e-6;
     P->fwd_u32 = (P->prec == CUNUSHT_PREC_MIXED) && !P->grid_fp32;
     P->fft_df = P->fwd_u32;
+    // the ring transforms stay double-float at every eps: in FP64 they were the
+    // largest FP64-pipe stage of the eps > 1e-6 plans (GB300 issues FP64 at
+    // 1/80 of the FP32 rate)
+    P->ring_df = P->prec == CUNUSHT_PREC_MIXED;
 
     // ---- pointing geometry, sorted by first pixel (Geom, geometry.py:47-52)
     std::vector<int> order(nring);
@@ -440,7 +444,7 @@ static int build_plan(cunusht_plan_s *P, int lmax, double eps, int precision, in
             CU_TRY(cudaMemcpy(b, bk.data(), Mb * sizeof(double2), cudaMemcpyHostToDevice));
         }
     }
-    if (P->fft_df) {
+    if (P->fft_df || P->ring_df) {
         char *t = nullptr, *c = nullptr, *b = nullptr;
         RC_TRY(dalloc(P, &t, 16 * (size_t)P->TW));
         RC_TRY(dalloc(P, &c, 16 * (size_t)P->nchirp));

@@ -158,6 +158,7 @@ struct cunusht_plan_s {
     bool grid_fp32 = false;        // FFT + nuFFT grids in FP32
     bool fwd_u32 = false;          // forward fine grid stored FP32 (FFTs FP64), mixed-precision interp
     bool fft_df = false;           // forward FFTs (theta, phi, ring) in double-float
+    bool ring_df = false;          // dlm2pointing's ring transforms in double-float (every mixed plan)
     double eps = 1e-7;
     long long nalm = 0;      // alm count of the arrays the calls take: m <= mmax (healpy m-major layout)
     long long nalm_tab = 0;  // size of the recursion tables: every (l, m <= lmax), same index as the alm

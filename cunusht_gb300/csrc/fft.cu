@@ -1178,7 +1178,7 @@ int ring_synth_batch(const cunusht_plan_s *P, int nreq, int spin, const double2 
     dim3 grid(P->nring, nreq);
     const RingCls rc = ring_cls_of(P);
     for (int q = P->sp_ring - 1; q >= 0; --q) {
-        if (P->fft_df && P->d_chirp_df) {
+        if (P->ring_df && P->d_chirp_df) {
             RC_TRY(set_smem(k_ring_synth<dfl>, sm));
             k_ring_synth<dfl><<<grid, FFT_TPB, sm, st>>>(Hgl, P->nring, P->lmax, spin, P->d_ring_phi0, P->d_ring_ofs,
                                                          rc, (const dcplx *)P->d_chirp_df,

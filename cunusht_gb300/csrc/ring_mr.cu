@@ -268,7 +268,7 @@ int ring_synth_mr_batch(const cunusht_plan_s *P, int nreq, int spin, const doubl
     }
     const int N = P->nph_uniform;
     const dim3 grid(P->nring, nreq);
-    if (P->fft_df) {
+    if (P->ring_df) {
         const size_t sm = sizeof(dcplx) * ((size_t)MR_KMAX + N);
         if (sm > 48 * 1024)
             CU_TRY(cudaFuncSetAttribute(k_ring_synth_mr<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
