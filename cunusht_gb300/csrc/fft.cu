@@ -501,7 +501,9 @@ __global__ void __launch_bounds__(FFT_TPB)
 // q = blockIdx.z in the forward kernels; the adjoint kernels are launched for
 // q = 1 (writes F) and then q = 0 (adds to F).
 // spin 0: two real rows per block packed as one complex transform
-template <typename T, typename TU>
+// PRUNE (SP = 1, Nb / 4 > L): first radix-4 pass done as the rows are read,
+// as in k_phi_fwd_spin
+template <typename T, typename TU, bool PRUNE = false>
 __global__ void __launch_bounds__(FFT_TPB)
     k_phi_fwd_s0(const cplx<T> *__restrict__ F, int ncols, int nrows, int Npf, TU *__restrict__ U,
                  const cplx<T> *__restrict__ tw, int TW, long long fbs, long long ubs, int SP) {
@@ -516,6 +518,35 @@ __global__ void __launch_bounds__(FFT_TPB)
     const bool has2 = r2 < nrows;
     const int Nb = Npf / SP;
     const int tstep = TW / Npf;
+    if constexpr (PRUNE) {
+        // x[j] = a_j + i b_j (j <= L), x[j + 3 Nb / 4] = conj a_m + i conj b_m
+        // at m = Nb / 4 - j (m <= L); x[0] = (Re a_0, Re b_0)
+        const cplx<T> *f1 = F + (long long)r1 * ncols, *f2 = F + (long long)r2 * ncols;
+        const int nb = Nb / 4;
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+            cplx<T> v0 = czero<T>(), v3 = czero<T>();
+            if (j < ncols) {
+                const cplx<T> a = f1[j], b = has2 ? f2[j] : czero<T>();
+                v0 = j ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x, b.x);
+            }
+            const int m = nb - j;
+            if (m < ncols) {
+                const cplx<T> a = f1[m], b = has2 ? f2[m] : czero<T>();
+                v3 = mk<T>(a.x + b.y, b.x - a.y);
+            }
+            r4_first_pruned<T>(buf, j, v0, v3, +1);
+        }
+        __syncthreads();
+        fft_smem<T>(buf, Nb, +1, stw, MTW, 2);
+        TU *u1 = U + (long long)r1 * Npf;
+        TU *u2 = U + (long long)r2 * Npf;
+        for (int j = threadIdx.x; j < Nb; j += blockDim.x) {
+            const cplx<T> z = buf[j];
+            u1[j] = to_t<TU>(z.x);
+            if (has2) u2[j] = to_t<TU>(z.y);
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < Nb; i += blockDim.x) buf[i] = czero<T>();
     __syncthreads();
     for (int m = threadIdx.x; m < ncols; m += blockDim.x) {
@@ -1056,6 +1087,25 @@ int theta_adj(const cunusht_plan_s *P, int spin, const void *F, double2 *H, cuda
     return theta_adj_batch(P, 1, spin, F, 0, H, 0, P->d_U, 0, st);
 }
 
+// spin-0 phi pass of nreq requests (two real rows per transform); unsplit
+// rows (SP = 1, Npf >= 4 (L + 1)) take the pruned first pass
+template <typename T, typename TU>
+static int phi_fwd_s0_launch(const cunusht_plan_s *P, int nreq, const void *F, long long fbs, void *U, long long ubs,
+                             const cplx<T> *tw, size_t sm, cudaStream_t st) {
+    const int L = P->lmax, SP = P->sp_phi;
+    const dim3 grid((P->nrows + 1) / 2, nreq, SP);
+    if (SP == 1 && P->Npf / 4 > L) {
+        RC_TRY(set_smem(k_phi_fwd_s0<T, TU, true>, sm));
+        k_phi_fwd_s0<T, TU, true><<<grid, FFT_TPB, sm, st>>>((const cplx<T> *)F, L + 1, P->nrows, P->Npf, (TU *)U, tw,
+                                                              P->TW, fbs, ubs, SP);
+    } else {
+        RC_TRY(set_smem(k_phi_fwd_s0<T, TU, false>, sm));
+        k_phi_fwd_s0<T, TU, false><<<grid, FFT_TPB, sm, st>>>((const cplx<T> *)F, L + 1, P->nrows, P->Npf, (TU *)U,
+                                                               tw, P->TW, fbs, ubs, SP);
+    }
+    return CUNUSHT_OK;
+}
+
 // spin phi pass of nreq requests; unsplit rows (SP = 1, Npf >= 4 (L + 1))
 // take the pruned first pass
 template <typename T, typename TU>
@@ -1081,23 +1131,14 @@ int phi_fwd_batch(const cunusht_plan_s *P, int nreq, int spin, const void *F, lo
     size_t sm = fft_smem_bytes(P->Npf / P->sp_phi, P->grid_fp32);
     const int SP = P->sp_phi;
     if (spin == 0) {
-        const int nb = (P->nrows + 1) / 2;
         if (P->grid_fp32) {
-            RC_TRY(set_smem(k_phi_fwd_s0<float, float>, sm));
-            k_phi_fwd_s0<float, float><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const float2 *)F, L + 1, P->nrows, P->Npf,
-                                                                (float *)U, P->d_tw32, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_s0_launch<float, float>(P, nreq, F, fbs, U, ubs, P->d_tw32, sm, st)));
         } else if (P->fft_df) {
-            RC_TRY(set_smem(k_phi_fwd_s0<dfl, float>, sm));
-            k_phi_fwd_s0<dfl, float><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const dcplx *)F, L + 1, P->nrows, P->Npf,
-                                                              (float *)U, (const dcplx *)P->d_twdf, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_s0_launch<dfl, float>(P, nreq, F, fbs, U, ubs, (const dcplx *)P->d_twdf, sm, st)));
         } else if (P->fwd_u32) {
-            RC_TRY(set_smem(k_phi_fwd_s0<double, float>, sm));
-            k_phi_fwd_s0<double, float><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
-                                                                 (float *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_s0_launch<double, float>(P, nreq, F, fbs, U, ubs, P->d_tw64, sm, st)));
         } else {
-            RC_TRY(set_smem(k_phi_fwd_s0<double, double>, sm));
-            k_phi_fwd_s0<double, double><<<dim3(nb, nreq, SP), FFT_TPB, sm, st>>>((const double2 *)F, L + 1, P->nrows, P->Npf,
-                                                                  (double *)U, P->d_tw64, P->TW, fbs, ubs, SP);
+            RC_TRY((phi_fwd_s0_launch<double, double>(P, nreq, F, fbs, U, ubs, P->d_tw64, sm, st)));
         }
     } else {
         if (P->grid_fp32) {
