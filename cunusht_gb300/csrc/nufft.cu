@@ -278,22 +278,26 @@ __device__ __forceinline__ double f2d_exact_int(float f) {
     return __longlong_as_double((long long)bits);
 }
 
-// Mixed-precision variant for an FP64 grid (eps <= 1e-6 on the mixed path):
-// kernel weights in FP32 from the FP64 tap offset split into hi + lo floats
-// (as k_interp_mixed), FP32 products, Kahan-compensated FP32 strip sums, FP64
-// global accumulation.  The FP64 variant is bound by its FP64 exponentials and
+// Mixed-precision variant: kernel weights in FP32 from the FP64 tap offset
+// split into hi + lo floats (as k_interp_mixed), FP32 products, global
+// accumulation in the grid's type TG.  FP64 grid (eps <= 1e-6):
+// Kahan-compensated FP32 strip sums, each added as two exact FP64 atomics.
+// FP32 grid (eps > 1e-6): plain FP32 strip sums (half the shared memory, so
+// twice the resident blocks) and one FP32 atomic per strip cell.  The FP64 variant is bound by its FP64 exponentials and
 // products (GB300 runs FP64 at about 1/80 of the FP32 rate).
-template <bool CPLX, int W>
+template <typename TG, bool CPLX, int W>
 __global__ void __launch_bounds__(SPW_WARPS * 32)
-    k_spread_warp_mixed(double *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
+    k_spread_warp_mixed(TG *__restrict__ U, int nrows, int Npf, int Ntf, int n_lo, int w, float beta,
                         const double *__restrict__ loc, long long npts, int layout, const double *__restrict__ gamma,
                         int spin, const void *__restrict__ in, int in_f32, int SR, int SC, long long ubs,
                         long long lbs, long long ibs, unsigned long long *__restrict__ Ufix,
                         const float *__restrict__ vmax, int lgn) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NC = CPLX ? 2 : 1;
+    constexpr bool KAHAN = std::is_same<TG, double>::value;
+    using SE = typename std::conditional<KAHAN, float2, float>::type;  // (sum, compensation) or sum
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    float2 *strip = reinterpret_cast<float2 *>(smem_raw) + (size_t)wid * SR * SC * NC;  // (sum, compensation)
+    SE *strip = reinterpret_cast<SE *>(smem_raw) + (size_t)wid * SR * SC * NC;
     const int E = Ufix ? fix_exp(vmax[blockIdx.y], lgn) : 0;
     if (Ufix) Ufix += blockIdx.y * ubs;
     U += blockIdx.y * ubs;  // request of a batch
@@ -352,7 +356,8 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
     const float vih = vi.h, vil = vi.l;
     if (nr > SR || ncl > SC) {
         if (!act) return;
-        // footprint wider than the strip (scattered points): FP64 products and atomics
+        // footprint wider than the strip (scattered points): FP64 products and
+        // atomics (FP32 ones into an FP32 grid)
         const double vrd = df_to(vr), vid = df_to(vi);
 #pragma unroll 1
         for (int a = 0; a < W; ++a) {
@@ -368,14 +373,20 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
                     if constexpr (CPLX) atomicAdd(fc + 1, (unsigned long long)to_fix(kw * vid, E));
                     continue;
                 }
-                double *cell = U + (rowoff + c) * NC;
-                atomicAdd(cell, kw * vrd);
-                if constexpr (CPLX) atomicAdd(cell + 1, kw * vid);
+                TG *cell = U + (rowoff + c) * NC;
+                if constexpr (std::is_same<TG, double>::value) {
+                    atomicAdd(cell, kw * vrd);
+                    if constexpr (CPLX) atomicAdd(cell + 1, kw * vid);
+                } else {
+                    const float kf = kt[a] * kp[b];
+                    atomicAdd(cell, kf * (vrh + vrl));
+                    if constexpr (CPLX) atomicAdd(cell + 1, kf * (vih + vil));
+                }
             }
         }
         return;
     }
-    for (int i = lane; i < nr * ncl * NC; i += 32) strip[i] = make_float2(0.f, 0.f);
+    for (int i = lane; i < nr * ncl * NC; i += 32) strip[i] = SE{};
     __syncwarp();
     const int key = act ? (pc.r0 - rmin) * SC + (pc.p0 - pmin) : -1 - lane;
     const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -390,23 +401,34 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
             // the split value): each tap product then carries one FP32 rounding
             const float frh = kt[a] * vrh, frl = fmaf(kt[a], vrh, -frh) + kt[a] * vrl;
             const float fih = kt[a] * vih, fil = fmaf(kt[a], vih, -fih) + kt[a] * vil;
-            float2 *row = strip + (size_t)(base + a * ncl) * NC;
+            SE *row = strip + (size_t)(base + a * ncl) * NC;
+            if constexpr (!KAHAN) {
 #pragma unroll
-            for (int b = 0; b < W; ++b) {
-                if (go) {
-                    // Kahan: sum = x, comp = c; value = x - c
-                    float2 t = row[b * NC];
-                    float y = fmaf(kp[b], frh, kp[b] * frl) - t.y;
-                    float s2 = t.x + y;
-                    row[b * NC] = make_float2(s2, (s2 - t.x) - y);
-                    if constexpr (CPLX) {
-                        t = row[b * NC + 1];
-                        y = fmaf(kp[b], fih, kp[b] * fil) - t.y;
-                        s2 = t.x + y;
-                        row[b * NC + 1] = make_float2(s2, (s2 - t.x) - y);
+                for (int b = 0; b < W; ++b) {
+                    if (go) {
+                        row[b * NC] += kp[b] * (frh + frl);
+                        if constexpr (CPLX) row[b * NC + 1] += kp[b] * (fih + fil);
                     }
+                    __syncwarp();
                 }
-                __syncwarp();
+            } else {
+#pragma unroll
+                for (int b = 0; b < W; ++b) {
+                    if (go) {
+                        // Kahan: sum = x, comp = c; value = x - c
+                        float2 t = row[b * NC];
+                        float y = fmaf(kp[b], frh, kp[b] * frl) - t.y;
+                        float s2 = t.x + y;
+                        row[b * NC] = make_float2(s2, (s2 - t.x) - y);
+                        if constexpr (CPLX) {
+                            t = row[b * NC + 1];
+                            y = fmaf(kp[b], fih, kp[b] * fil) - t.y;
+                            s2 = t.x + y;
+                            row[b * NC + 1] = make_float2(s2, (s2 - t.x) - y);
+                        }
+                    }
+                    __syncwarp();
+                }
             }
         }
     }
@@ -416,41 +438,49 @@ __global__ void __launch_bounds__(SPW_WARPS * 32)
         int c = pmin + lc;
         c = c < 0 ? c + Npf : (c >= Npf ? c - Npf : c);
         const long long ci = ((long long)(rmin + lr) * Npf + c) * NC;
-        double *cell = U + ci;
+        TG *cell = U + ci;
 #pragma unroll
         for (int q = 0; q < NC; ++q) {
             // Kahan value x - c as two exact FP64 atomic adds (the additions
-            // happen in L2, the conversions on the integer pipe)
-            const float2 v = strip[i * NC + q];
-            if (Ufix) {
-                if (v.x != 0.f || v.y != 0.f)
-                    atomicAdd(Ufix + ci + q, (unsigned long long)(to_fix(v.x, E) - to_fix(v.y, E)));
-                continue;
+            // happen in L2, the conversions on the integer pipe), or as one
+            // FP32 atomic add of x - c into an FP32 grid
+            if constexpr (KAHAN) {
+                const float2 v = strip[i * NC + q];
+                if (Ufix) {
+                    if (v.x != 0.f || v.y != 0.f)
+                        atomicAdd(Ufix + ci + q, (unsigned long long)(to_fix(v.x, E) - to_fix(v.y, E)));
+                    continue;
+                }
+                if (v.x != 0.f) atomicAdd(cell + q, f2d_exact_int(v.x));
+                if (v.y != 0.f) atomicAdd(cell + q, -f2d_exact_int(v.y));
+            } else {
+                const float v = strip[i * NC + q];
+                if (v == 0.f) continue;
+                if (Ufix) atomicAdd(Ufix + ci + q, (unsigned long long)to_fix(v, E));
+                else atomicAdd(cell + q, v);
             }
-            if (v.x != 0.f) atomicAdd(cell + q, f2d_exact_int(v.x));
-            if (v.y != 0.f) atomicAdd(cell + q, -f2d_exact_int(v.y));
         }
     }
 }
 
-template <bool CPLX>
-static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U, long long ubs, const double *loc,
+template <typename TG, bool CPLX>
+static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, TG *U, long long ubs, const double *loc,
                                     long long lbs, long long npts, int layout, const double *gamma, int spin,
                                     const void *in, long long ibs, int f32i, cudaStream_t st) {
     int lgn = 0;
     while ((1LL << lgn) < npts + 1) ++lgn;
     const int SR = P->w + 4, SC = 80 + P->w;
-    const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * sizeof(float2);
+    const size_t sm = (size_t)SPW_WARPS * SR * SC * (CPLX ? 2 : 1) * (std::is_same<TG, double>::value ? 8 : 4);
     const long long nwarps = (npts + 31) / 32;
     const unsigned nb = (unsigned)((nwarps + SPW_WARPS - 1) / SPW_WARPS);
     cudaError_t e = cudaSuccess;
     with_width(P->w, [&](auto WC) {
         constexpr int W = decltype(WC)::value;
         if (sm > 48 * 1024)
-            e = cudaFuncSetAttribute(k_spread_warp_mixed<CPLX, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(k_spread_warp_mixed<TG, CPLX, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm);
         if (e == cudaSuccess)
-            k_spread_warp_mixed<CPLX, W><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(
+            k_spread_warp_mixed<TG, CPLX, W><<<dim3(nb, nreq), SPW_WARPS * 32, sm, st>>>(
                 U, P->nrows, P->Npf, P->Ntf, P->n_lo, W, (float)P->beta, loc, npts, layout, gamma, spin, in, f32i, SR,
                 SC, ubs, lbs, ibs, P->spread_det ? P->d_ufix : nullptr, P->d_vmax, lgn);
     });
@@ -459,11 +489,12 @@ static int launch_spread_warp_mixed(const cunusht_plan_s *P, int nreq, double *U
 }
 
 // ------------------------------------------------------------ interp, mixed precision
-// FP32 fine grid (from FP64 FFTs), FP32 kernel weights from the cancellation-free
+// FP32 fine grid of a mixed plan (from the double-float FFTs at eps <= 1e-6,
+// the FP32 ones above), FP32 kernel weights from the cancellation-free
 // exponent  beta (sqrt(1 - z^2) - 1) = -beta z^2 / (1 + sqrt(1 - z^2)),
-// Kahan-compensated FP32 sums, and the exp(i s gamma) rotation applied in FP64
-// from d = 1 - cos(x) = 2 sin^2(x/2) and sin(x) evaluated in FP32 (errors
-// relative to the small angle, not to 1).
+// Kahan-compensated FP32 sums, and the exp(i s gamma) rotation applied in
+// double-float from d = 1 - cos(x) = 2 sin^2(x/2) and sin(x) evaluated in FP32
+// (errors relative to the small angle, not to 1).
 
 // Five 256-thread blocks per SM for kernel widths up to 9 (48 registers, an
 // 8-byte spill at width 9): the kernel waits on its tap loads, and 40 warps
@@ -500,7 +531,8 @@ __global__ void __launch_bounds__(NU_TPB, W <= 9 ? 5 : 4)
         for (int a = 0; a < W; ++a) {
             const float kta = es_kernel_acc((((float)a + fth) + ftl) * sc, beta);
             const long long rowoff = (long long)(pc.r0 + a) * Npf;
-            kahan rr, ri;
+            kahan rr;
+            [[maybe_unused]] kahan ri;
 #pragma unroll
             for (int b = 0; b < W; ++b) {
                 int c = pc.p0 + b;
@@ -596,7 +628,7 @@ int nufft_interp_batch(const cunusht_plan_s *P, int nreq, int spin, const void *
     const int f32o = out_dtype == CUNUSHT_F32;
     with_width(P->w, [&](auto WC) {
         constexpr int W = decltype(WC)::value;
-        if (P->fwd_u32) {
+        if (P->fwd_u32 || P->grid_fp32) {  // FP32 grid of a mixed plan
             if (spin == 0)
                 k_interp_mixed<false, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
                                                                   W, (float)P->beta, loc, npts, layout, gamma, spin,
@@ -605,15 +637,6 @@ int nufft_interp_batch(const cunusht_plan_s *P, int nreq, int spin, const void *
                 k_interp_mixed<true, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf, P->n_lo,
                                                                  W, (float)P->beta, loc, npts, layout, gamma, spin,
                                                                  out, f32o, ubs, lbs, obs);
-        } else if (P->grid_fp32) {
-            if (spin == 0)
-                k_interp<float, false, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf,
-                                                                   P->n_lo, W, (float)P->beta, loc, npts, layout,
-                                                                   gamma, spin, out, f32o, ubs, lbs, obs);
-            else
-                k_interp<float, true, W><<<grid, NU_TPB, 0, st>>>((const float *)U, P->nrows, P->Npf, P->Ntf,
-                                                                  P->n_lo, W, (float)P->beta, loc, npts, layout,
-                                                                  gamma, spin, out, f32o, ubs, lbs, obs);
         } else {
             if (spin == 0)
                 k_interp<double, false, W><<<grid, NU_TPB, 0, st>>>((const double *)U, P->nrows, P->Npf, P->Ntf,
@@ -649,12 +672,12 @@ int nufft_spread_batch(const cunusht_plan_s *P, int nreq, int spin, void *U, lon
     int done = 0;
     RC_TRY(spread_options_begin(P, nreq, spin, U, ubs, loc, lbs, npts, layout, gamma, in, ibs, in_dtype, &done, st));
     if (done) return spread_options_end(P, nreq, spin, U, ubs, npts, st);
-    if (P->grid_fp32) {
-        if (spin == 0) RC_TRY((launch_spread_warp<float, false>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
-        else RC_TRY((launch_spread_warp<float, true>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+    if (P->grid_fp32) {  // FP32 grid (eps > 1e-6), always a mixed plan
+        if (spin == 0) RC_TRY((launch_spread_warp_mixed<float, false>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+        else RC_TRY((launch_spread_warp_mixed<float, true>(P, nreq, (float *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
     } else if (P->prec == CUNUSHT_PREC_MIXED) {
-        if (spin == 0) RC_TRY((launch_spread_warp_mixed<false>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
-        else RC_TRY((launch_spread_warp_mixed<true>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+        if (spin == 0) RC_TRY((launch_spread_warp_mixed<double, false>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
+        else RC_TRY((launch_spread_warp_mixed<double, true>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
     } else {
         if (spin == 0) RC_TRY((launch_spread_warp<double, false>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
         else RC_TRY((launch_spread_warp<double, true>(P, nreq, (double *)U, ubs, loc, lbs, npts, layout, gamma, spin, in, ibs, f32i, st)));
