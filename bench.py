@@ -69,9 +69,10 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU work of the cpu_baseline leg")
     p.add_argument("--batch", type=int, default=8, help="requests per launch of the served form")
     p.add_argument("--fp64-steps", type=int, default=3, help="timed solves of the plain FP64 single-request form")
-    p.add_argument("--op", default=None, choices=["doubling", "adjoint_doubling", "nusht2d1_scattered"],
-                   help="time one standalone kernel of the C ABI instead (HBM roofline), or nusht2d1 on "
-                        "uniformly scattered points with each spreading method")
+    p.add_argument("--op", default=None, choices=["doubling", "adjoint_doubling", "nusht2d1_scattered", "nusht2d2"],
+                   help="time one standalone kernel of the C ABI instead (HBM roofline), nusht2d1 on "
+                        "uniformly scattered points with each spreading method, or one nusht2d2 call on "
+                        "precomputed deflected points (mixed and FP64 plans)")
     p.add_argument("--direction", default="g2l", choices=["g2l", "l2g"],
                    help="g2l: lensing (headline); l2g: delensing (lenmap2gclm) served form")
     p.add_argument("--serve", action="store_true",
@@ -845,6 +846,60 @@ def serve_main(args):
 
 
 # ----------------------------------------------------------------------------- standalone kernels
+# the reference's one published GPU timing of this path (first_steps/nusht2d2.ipynb,
+# cells 4 and 7): nusht2d2, spin 0, lmax = mmax = 3087 on its GL grid, eps 1e-7,
+# planned type-2 nuFFT, points given, one call 40.9 ms (GPU model not stated)
+PUBLISHED_NUSHT2D2 = {"lmax": 3087, "spin": 0, "eps": 1e-7, "ms": 40.9}
+
+
+def nusht2d2_main(args):
+    """One nusht2d2 call per step (alm -> values at given points; no pointing,
+    no plan set-up in the timed region) on the deflected GL-grid points of the
+    seeded 2.5' deflection, with the mixed and the plain FP64 plans: the form of
+    the reference's only published GPU timing.  CUDA events, median and p99
+    over the steps."""
+    import torch
+    from cunusht_gb300 import build as _b
+    _b.build()
+    import cunusht_gb300 as cu
+    lmax, spin, eps = args.lmax, args.spin, args.eps
+    geo = ("gl", {"lmax": lmax, "nphi": args.nphi or 2 * lmax + 1})
+    g, plm = synth_inputs(lmax, spin, seed=1)
+    alm = torch.as_tensor(g[0] if spin == 0 else g, device="cuda")
+    res, outs = {}, {}
+    for prec in ("mixed", "fp64"):
+        T = cu.get_transformer("GPU")(geo, nuFFTtype=2, epsilon=eps, precision=prec, max_spin=max(spin, 1))
+        loc = T.dlm2pointing(torch.as_tensor(plm, device="cuda"), lmax).T  # (npix, 2) view
+        call = lambda: T.nusht2d2(lmax, lmax, alm, loc, epsilon=eps, spin=spin)
+        for _ in range(args.warmup):
+            call()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+        for k in range(args.steps):
+            ev[2 * k].record()
+            outs[prec] = call()
+            ev[2 * k + 1].record()
+        torch.cuda.synchronize()
+        ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
+        res[prec] = {"ms_per_call": float(np.median(ms)), "p99_ms": float(np.percentile(ms, 99)),
+                     "npts": int(loc.shape[0])}
+        T._destroy()
+    rel = float(torch.linalg.norm(outs["mixed"] - outs["fp64"]) / torch.linalg.norm(outs["fp64"]))
+    pub = None
+    if (lmax, spin, eps) == (PUBLISHED_NUSHT2D2["lmax"], PUBLISHED_NUSHT2D2["spin"], PUBLISHED_NUSHT2D2["eps"]):
+        pub = {"ms_per_call": PUBLISHED_NUSHT2D2["ms"], "hardware": "GPU model not stated",
+               "source": "first_steps/nusht2d2.ipynb (reference notebook output)",
+               "mixed_speedup": PUBLISHED_NUSHT2D2["ms"] / res["mixed"]["ms_per_call"],
+               "fp64_speedup": PUBLISHED_NUSHT2D2["ms"] / res["fp64"]["ms_per_call"]}
+    print(json.dumps({"metric": f"nusht2d2 ms per call at lmax={lmax} spin-{spin} eps={eps:g} (points given)",
+                      "value": res["mixed"]["ms_per_call"], "unit": "ms", "higher_is_better": False,
+                      "steps": args.steps, "warmup": args.warmup,
+                      "config": {"workload": f"nusht2d2 GL {lmax + 1}x{geo[1]['nphi']}, deflected points "
+                                             f"(2.5 arcmin rms), spin {spin}, eps {eps:g}, one call per step"},
+                      "mixed": res["mixed"], "fp64": res["fp64"], "rel_mixed_vs_fp64": rel,
+                      "published_reference": pub}))
+
+
 def scattered_main(args):
     """nusht2d1 (GPU_nufft_transformer.py:439-484) of one spin-2 map sampled at
     npix uniformly scattered points on the sphere (lmax 2047 default: 8.39 M
@@ -1020,6 +1075,8 @@ if __name__ == "__main__":
         serve_main(_args)
     elif _args.op == "nusht2d1_scattered":
         scattered_main(_args)
+    elif _args.op == "nusht2d2":
+        nusht2d2_main(_args)
     elif _args.op:
         op_main(_args)
     elif _args.direction == "l2g" and _args.impl == "gb300":
