@@ -131,7 +131,14 @@ class ClockSampler:
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        pw = []
+        for r in rows:
+            try:
+                pw.append(float(r[3]))
+            except ValueError:
+                pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "sm_min_mhz": min(sm) if sm else None, "power_w_max": max(pw) if pw else None,
                 "reasons": reasons, "samples": len(rows)}
 
 
@@ -556,13 +563,14 @@ def main():
                 for e in ev_out:
                     comp.wait_event(e)
 
-        e_s, e_ms, _, _ = timed(e2e_pipe_step, args.steps, args.warmup)
+        e_s, e_ms, _, e_clk = timed(e2e_pipe_step, args.steps, args.warmup, sample_clocks=True)
         e2e = {"value": world * B * args.steps / e_s, "unit": "solves/s",
                "h2d_bytes_per_step": int(GBh.numel() * GBh.element_size() + DBh.numel() * DBh.element_size()),
                "d2h_bytes_per_step": int(resB.numel() * resB.element_size()),
                "ms_per_step": e_s * 1e3 / args.steps, "api": "GPU_cufinufft_transformer.lensing_batch",
                "requests_per_step": B,
                "copies": "H2D and D2H on their own streams, overlapping the neighbouring steps' launches",
+               "clocks": e_clk, "ms_per_step_max": float(np.max(e_ms)), "ms_per_step_median": float(np.median(e_ms)),
                "serial": {"value": world * B * args.steps / serial_s, "ms_per_step": serial_s * 1e3 / args.steps,
                           "copies": "H2D, launch and D2H in sequence on one stream"}}
         # the reference's own call, one request per call (gclm2lenmap)
